@@ -1,0 +1,415 @@
+"""Benchmark of the transparent pass (one step = one whole frame).
+
+Default workload: Loop64 k-buffer at 1920x1080, OIT_LAYERS=16, 1024 seeded
+spheres (radii 0.03-0.1) with the first 60% transparent over an opaque depth
+pre-pass, tail blending on. Metric: transparent fragments (after early depth)
+per second, in Mfragments/s; ms_per_step is ms/frame.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl gb300|reference]
+
+--impl reference times the CPU restatement of the reference's algorithm (the
+oracle) on every host core: the reference itself is a Vulkan/GLSL program and
+no graphics stack exists on either machine.
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (algorithm, width, height, layers, nodes/px, aa, spheres, rmin, rmax, percent transparent, alpha_min, alpha_width)
+    'loop64_1920x1080_L16_1024spheres_60pct': ('loop64', 1920, 1080, 16, 8, 0, 1024, 0.03, 0.10, 60, 0.2, 0.6),
+    'spinlock_1920x1080_L16_1024spheres_60pct': ('spinlock', 1920, 1080, 16, 8, 0, 1024, 0.03, 0.10, 60, 0.2, 0.6),
+    'linkedlist_640x480_L8_256spheres': ('linkedlist', 640, 480, 8, 8, 0, 256, 0.05, 0.15, 100, 0.2, 0.6),
+    'interlock_2560x1440_msaa8_L8_4096spheres': ('interlock', 2560, 1440, 8, 8, 4, 4096, 0.02, 0.08, 100, 0.2, 0.6),
+    'simple_2560x1440_msaa8_L8_4096spheres': ('simple', 2560, 1440, 8, 8, 4, 4096, 0.02, 0.08, 100, 0.2, 0.6),
+    'weighted_3840x2160_16384spheres': ('weighted', 3840, 2160, 8, 8, 0, 16384, 0.01, 0.05, 100, 0.05, 0.9),
+}
+DEFAULT_WORKLOAD = 'loop64_1920x1080_L16_1024spheres_60pct'
+ALGS = ['simple', 'linkedlist', 'loop', 'loop64', 'spinlock', 'interlock', 'weighted']
+SEED = 2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--workload', default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    return ap.parse_args()
+
+
+def workload_dict(name):
+    alg, W, H, L, npp, aa, n, rmin, rmax, pct, amin, awid = WORKLOADS[name]
+    return dict(workload=name, algorithm=alg, width=W, height=H, oit_layers=L, nodes_per_pixel=npp, aa_type=aa,
+                spheres=n, radius_min=rmin, radius_max=rmax, percent_transparent=pct, alpha_min=amin,
+                alpha_width=awid, seed=SEED)
+
+
+def dtype_of(alg):
+    return {'loop64': 'u64 keys + f32 blend', 'loop': 'u32 depth + f32 blend', 'weighted': 'f16 accum + f32'}.get(
+        alg, 'u32 records + f32 blend')
+
+
+# ---------------------------------------------------------------------------
+# CPU leg (the oracle): a bounded sample of the same workload
+# ---------------------------------------------------------------------------
+def _oracle_frame(args):
+    wd, scale = args
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as orc
+    import vk_order_independent_transparency_gb300 as oit
+    W, H = wd['width'], wd['height']
+    v, i, tpo = oit.make_scene(wd['spheres'], seed=wd['seed'], radius_min=wd['radius_min'],
+                               radius_max=wd['radius_max'])
+    sd = oit.make_camera(W, H)
+    t = time.perf_counter()
+    fr = orc.render(ALGS.index(wd['algorithm']), W, H, sd, v, i, tpo, wd['percent_transparent'],
+                    oit_layers=wd['oit_layers'], nodes_per_pixel=wd['nodes_per_pixel'], aa_type=wd['aa_type'],
+                    alpha_min=wd['alpha_min'], alpha_width=wd['alpha_width'])
+    fr.composite()
+    dt = time.perf_counter() - t
+    return fr.fragment_count(), dt
+
+
+def cpu_baseline(wd, cores=1, frames=None, budget_s=15.0):
+    """Oracle throughput on `cores` processes; each renders whole frames."""
+    import oracle  # noqa: F401  (builds the oracle library if needed)
+    ctx = mp.get_context('spawn')
+    frames = frames or cores
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_oracle_frame, [(wd, 1)] * frames)
+    wall = time.perf_counter() - t0
+    frags = sum(r[0] for r in res)
+    return frags, wall, res
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix='.csv')
+            os.close(fd)
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.dev), '--query-gpu=' + self.Q,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(',')]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = sorted(float(r[1]) for r in rows if r[1].replace('.', '').isdigit())
+        mx = max((float(r[2]) for r in rows if r[2].replace('.', '').isdigit()), default=None)
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith('active')})
+        return {'sm_mhz': sm[len(sm) // 2] if sm else None, 'sm_max_mhz': mx, 'reasons': reasons,
+                'samples': len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+def peaks():
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    return 6800.0, 'fallback'
+
+
+def ncu_traffic(kernel, workload):
+    """dram bytes per launch from a committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, 'profiles', '%s_%s.txt' % (kernel, workload))
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith('dram_bytes_per_launch:'):
+                try:
+                    return float(line.split(':', 1)[1].split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+def kernel_bytes(wd, r, frags, kept_entries, pairs_t, tris_t):
+    """Algorithmic bytes per launch of the transparent raster and the composite."""
+    import vk_order_independent_transparency_gb300 as oit
+    alg = wd['algorithm']
+    msaa, _, ss = oit.aa_settings(wd['aa_type'])
+    P = wd['width'] * wd['height'] * ss * ss
+    S = msaa
+    L = wd['oit_layers']
+    opaque = wd['percent_transparent'] < 100
+    # raster: opaque depth + colour in, colour target out, triangle setup once, tile lists
+    rb = (S * P * 20 if opaque else 0) + P * 16 + tris_t * 136 + pairs_t * 4
+    if alg == 'loop64':
+        rb += P * L * 8
+    elif alg == 'loop':
+        rb += P * L * 8
+    elif alg == 'linkedlist':
+        rb += frags * 16 + P * 4
+    elif alg in ('simple', 'spinlock', 'interlock'):
+        rec = 16 if msaa > 1 else 8
+        rb += kept_entries * rec + P * (4 if alg == 'simple' else 8)
+    elif alg == 'weighted':
+        rb += S * P * 10
+    # composite: A-buffer entries actually read + colour target + output
+    out = wd['width'] * wd['height'] * 4
+    if alg == 'loop64':
+        cb = kept_entries * 8 + P * 16 + out
+    elif alg == 'loop':
+        cb = kept_entries * 8 + P * 16 + out
+    elif alg == 'linkedlist':
+        cb = frags * 16 + P * 4 + P * 16 + out
+    elif alg == 'weighted':
+        cb = S * P * (10 + (16 if opaque else 0)) + out
+    else:
+        rec = 16 if msaa > 1 else 8
+        cb = kept_entries * rec + P * 4 + P * 16 + out
+    return rb, cb
+
+
+def count_kept(wd, r):
+    """A-buffer entries the composite reads (host readback, outside timing)."""
+    import numpy as np
+    import vk_order_independent_transparency_gb300 as oit
+    alg = wd['algorithm']
+    L = wd['oit_layers']
+    msaa, _, ss = oit.aa_settings(wd['aa_type'])
+    P = wd['width'] * wd['height'] * ss * ss
+    if alg == 'loop64':
+        ab = r.read_buffer(oit.OIT_BUF_ABUFFER).reshape(L, P, 2)
+        n = (ab[:, :, 1] != 0xFFFFFFFF).sum(axis=0)
+        return int(n.sum() + (n < L).sum())
+    if alg == 'loop':
+        ab = r.read_buffer(oit.OIT_BUF_ABUFFER).reshape(2 * L, P)
+        n = (ab[:L] != 0xFFFFFFFF).sum(axis=0)
+        return int(2 * n.sum() + (n < L).sum())
+    if alg in ('simple', 'spinlock', 'interlock'):
+        aux = r.read_buffer(oit.OIT_BUF_AUX)[:P]
+        return int(np.minimum(aux, L).sum())
+    return 0
+
+
+def run_gpu(a, wd, rank, world):
+    import numpy as np
+    import torch
+    import vk_order_independent_transparency_gb300 as oit
+    from vk_order_independent_transparency_gb300 import _build
+    if rank == 0 or not os.path.exists(oit.LIB_PATH):
+        _build.build()
+    if world > 1:
+        torch.distributed.barrier()
+    dev = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(dev)
+    alg = ALGS.index(wd['algorithm'])
+    W, H = wd['width'], wd['height']
+    v, i, tpo = oit.make_scene(wd['spheres'], seed=wd['seed'] + rank, radius_min=wd['radius_min'],
+                               radius_max=wd['radius_max'])
+    sd = oit.make_camera(W, H)
+    st = oit.make_state(alg, W, H, oit_layers=wd['oit_layers'], nodes_per_pixel=wd['nodes_per_pixel'],
+                        aa_type=wd['aa_type'], alpha_min=wd['alpha_min'], alpha_width=wd['alpha_width'])
+    r = oit.Renderer(st)
+    mesh = oit.DeviceMesh(v, i)
+    r.update_scene(sd)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def step():
+        r.render_frame(mesh, tpo, wd['percent_transparent'], None, stream)
+
+    for _ in range(max(3, a.warmup)):
+        step()
+    torch.cuda.synchronize()
+    frags = r.fragment_count()
+    assert r.get_error() == 0
+
+    # device-resident timing
+    l0 = r.launch_count()
+    clocks = Clocks(dev)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(a.steps):
+        step()
+    ev1.record()
+    torch.cuda.synchronize()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    launches = r.launch_count() - l0
+
+    # per-pass timing (CUDA events on the launching stream), separate run
+    r.profile_enable(True)
+    for _ in range(a.steps):
+        step()
+    prof = r.profile_read()
+    r.profile_enable(False)
+
+    # end to end through the C ABI with host buffers (pinned), copies inside
+    vh = torch.from_numpy(np.ascontiguousarray(v)).pin_memory().numpy()
+    ih = torch.from_numpy(np.ascontiguousarray(i)).pin_memory().numpy()
+    oh = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory().numpy()
+    for _ in range(2):
+        r.render_frame_host(vh, ih, tpo, wd['percent_transparent'], oh, stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        r.render_frame_host(vh, ih, tpo, wd['percent_transparent'], oh, stream)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+
+    kept = count_kept(wd, r)
+    tris_t = (i.shape[0] // tpo) * wd['percent_transparent'] // 100 * tpo
+    res = dict(elapsed_ms=elapsed_ms, frags=frags, launches=launches, clocks=clk, prof=prof, e2e_s=e2e_s,
+               h2d=int(vh.nbytes + ih.nbytes), d2h=int(oh.nbytes), kept=kept, tris_t=tris_t, r=r)
+    return res
+
+
+def main():
+    a = parse()
+    wd = workload_dict(a.workload)
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+
+    if a.impl == 'reference':
+        if rank != 0:
+            return
+        cores = os.cpu_count() or 1
+        # one step = every core renders one whole frame of the workload
+        for _ in range(max(0, min(a.warmup, 1))):
+            cpu_baseline(wd, cores=cores, frames=cores)
+        frags = 0
+        wall = 0.0
+        for _ in range(a.steps):
+            f, w, _ = cpu_baseline(wd, cores=cores, frames=cores)
+            frags += f
+            wall += w
+        value = frags / wall / 1e6
+        line = {
+            'impl': 'reference', 'metric': 'Mfragments/s', 'value': round(value, 4), 'unit': 'Mfragments/s',
+            'n_gpus': a.gpus, 'steps': a.steps, 'warmup': a.warmup, 'ms_per_step': round(wall / a.steps * 1e3, 3),
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64 blend',
+            'data': 'synthetic: seeded UV-sphere scene', 'config': wd,
+            'cpu_baseline': {'value': round(value, 4), 'unit': 'Mfragments/s', 'cores': cores, 'kind': 'port',
+                             'sample': '%d whole frames per step, one per core' % cores},
+            'e2e': {'value': round(value, 4), 'unit': 'Mfragments/s', 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0},
+            'note': 'reference Vulkan build unavailable on this box (no graphics stack); CPU restatement of the '
+                    'reference shaders (oracle) timed instead',
+        }
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
+    res = run_gpu(a, wd, rank, world)
+    elapsed = torch.tensor([res['elapsed_ms']], dtype=torch.float64, device='cuda')
+    frags_all = torch.tensor([float(res['frags'] * a.steps)], dtype=torch.float64, device='cuda')
+    e2e = torch.tensor([res['e2e_s']], dtype=torch.float64, device='cuda')
+    if world > 1:
+        torch.distributed.all_reduce(elapsed, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(frags_all)
+        torch.distributed.all_reduce(e2e, op=torch.distributed.ReduceOp.MAX)
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return
+    t_ms = float(elapsed.item())
+    value = float(frags_all.item()) / (t_ms * 1e-3) / 1e6
+    e2e_value = float(frags_all.item()) / float(e2e.item()) / 1e6
+
+    peak, peak_kind = peaks()
+    prof = res['prof']
+    rbytes, cbytes = kernel_bytes(wd, res['r'], res['frags'], res['kept'], 0, res['tris_t'])
+    kernels = {}
+    for name, b in (('transparent_raster', rbytes), ('composite', cbytes)):
+        ms, n = prof[name]
+        if n:
+            per = ms / n
+            kernels[name] = {'ms': round(per, 4), 'bytes': int(b), 'gbs': round(b / (per * 1e-3) / 1e9, 1)}
+    for name in ('opaque_bin', 'opaque_raster', 'transparent_bin'):
+        ms, n = prof[name]
+        if n:
+            kernels[name] = {'ms': round(ms / n, 4)}
+    dom = max(kernels, key=lambda k: kernels[k]['ms'])
+    droof = dom if 'gbs' in kernels[dom] else 'transparent_raster'
+    k = kernels[droof]
+    roofline = {'bound': 'hbm', 'kernel': droof, 'achieved': k['gbs'], 'peak': peak, 'unit': 'GB/s',
+                'frac': round(k['gbs'] / peak, 4), 'traffic': ncu_traffic(droof, wd['workload']),
+                'peak_source': peak_kind + ' (MEASURED_PEAKS.json hbm_gbs)' if peak_kind == 'measured' else peak_kind,
+                'dominant_pass': dom}
+    cpu = None
+    if not a.no_cpu_baseline:
+        f, w, runs = cpu_baseline(wd, cores=1, frames=1)
+        n_more = max(0, min(4, int(12.0 / max(w, 1e-3)) - 1))
+        if n_more:
+            f2, w2, _ = cpu_baseline(wd, cores=1, frames=n_more)
+            f += f2
+            w += w2
+        cpu = {'value': round(f / w / 1e6, 4), 'unit': 'Mfragments/s', 'cores': 1, 'kind': 'port',
+               'sample': '%d whole frame(s) of the workload, single-threaded FP64 oracle' % (1 + n_more)}
+    line = {
+        'metric': 'Mfragments/s', 'value': round(value, 3), 'unit': 'Mfragments/s', 'n_gpus': world,
+        'steps': a.steps, 'warmup': a.warmup, 'ms_per_step': round(t_ms / a.steps, 4), 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': dtype_of(wd['algorithm']),
+        'data': 'synthetic: seeded UV-sphere scene (SplitMix64), inputs resident in HBM',
+        'config': dict(wd, fragments_per_frame=res['frags'], parallelism='replicas' if world > 1 else 'single',
+                       l2='working set larger than L2 (A-buffer + triangle setup > 129 MB), no flush'),
+        'e2e': {'value': round(e2e_value, 3), 'unit': 'Mfragments/s', 'h2d_bytes_per_step': res['h2d'],
+                'd2h_bytes_per_step': res['d2h'], 'ms_per_step': round(float(e2e.item()) / a.steps * 1e3, 4)},
+        'roofline': roofline,
+        'kernels': kernels,
+        'cpu_baseline': cpu,
+        'clocks': res['clocks'],
+        'gpu_launches': int(res['launches']),
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,265 @@
+/*
+ * oit_gb300.h - C ABI of the GB300-native order-independent-transparency engine.
+ *
+ * Drop-in for the transparent pass of nvpro-samples/vk_order_independent_transparency:
+ * clearTransparent* -> drawTransparent* (COLOR/DEPTH + COMPOSITE) -> copy to the
+ * back buffer, for the seven algorithms of the reference, on one GB300 (sm_103a).
+ *
+ * Conventions (all functions):
+ *  - return an int status (OIT_OK or a negative OIT_ERR_*), never abort;
+ *  - "stream" is a cudaStream_t passed as void* (NULL = legacy default stream);
+ *    work is stream-ordered and asynchronous unless stated otherwise;
+ *  - device buffers named *_device are CUDA device pointers owned by the caller;
+ *    every other device buffer is owned by the context;
+ *  - one context per host thread (the reference's Sample is single-threaded).
+ */
+#ifndef OIT_GB300_H
+#define OIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Algorithms: shaders/common.h:44-50 (OIT_SIMPLE .. OIT_WEIGHTED). */
+#define OIT_SIMPLE 0
+#define OIT_LINKEDLIST 1
+#define OIT_LOOP 2
+#define OIT_LOOP64 3
+#define OIT_SPINLOCK 4
+#define OIT_INTERLOCK 5
+#define OIT_WEIGHTED 6
+#define OIT_NUM_ALGORITHMS 7
+
+/* Antialiasing modes: shaders/common.h:58-64, expanded by
+ * State::recomputeAntialiasingSettings (oit.h:84-115). */
+#define OIT_AA_NONE 0
+#define OIT_AA_MSAA_4X 1
+#define OIT_AA_SSAA_4X 2
+#define OIT_AA_SUPER_4X 3
+#define OIT_AA_MSAA_8X 4
+#define OIT_AA_SSAA_8X 5
+
+/* Fragment record formats. RGBA8 is the reference's packed sRGB record
+ * (packUnorm4x8, shaders/oitSimple.frag.glsl:70). RGBA32F is the plain FP32
+ * record (unquantised linear colour), used as the precision/throughput
+ * baseline; it is implemented for OIT_LINKEDLIST and OIT_LOOP64. */
+#define OIT_RECORD_RGBA8 0
+#define OIT_RECORD_RGBA32F 1
+
+/* WBOIT accumulation precision: FP16 reproduces the reference's RGBA16F/R16F
+ * targets (oit.h:234-235) by rounding after every blend; FP32 keeps float
+ * accumulators. */
+#define OIT_WEIGHTED_FP16 0
+#define OIT_WEIGHTED_FP32 1
+
+/* oit_state.flags */
+#define OIT_FLAG_LINEAR_OUTPUT 0x1u  /* composite also writes OIT_BUF_OUTPUT_LINEAR */
+
+/* Status codes. */
+#define OIT_OK 0
+#define OIT_ERR_INVALID_ARGUMENT (-1)
+#define OIT_ERR_UNSUPPORTED (-2)
+#define OIT_ERR_OUT_OF_MEMORY (-3)
+#define OIT_ERR_CUDA (-4)
+#define OIT_ERR_DEVICE (-5)      /* a kernel raised a device error bit, see oit_get_error */
+#define OIT_ERR_STATE (-6)       /* call made out of order (e.g. composite before draw) */
+
+/* Device error bits reported by oit_get_error. */
+#define OIT_DEVERR_BIN_OVERFLOW 0x1u  /* triangle/tile pairs exceeded the bin capacity */
+#define OIT_DEVERR_TIMEOUT 0x2u       /* a bounded wait gave up */
+
+/* Renderer settings: State (oit.h:64-116) plus the SceneData scalars
+ * (shaders/common.h:77-92). */
+typedef struct oit_state {
+  uint32_t algorithm;                      /* OIT_SIMPLE .. OIT_WEIGHTED */
+  uint32_t oit_layers;                     /* OIT_LAYERS: 1,2,4,8,16,32 */
+  int32_t linked_list_allocated_per_element; /* A-buffer nodes per pixel/sample (LL) */
+  int32_t tail_blend;                      /* OIT_TAILBLEND */
+  int32_t interlock_is_ordered;            /* OIT_INTERLOCK_IS_ORDERED */
+  uint32_t aa_type;                        /* OIT_AA_* */
+  uint32_t width, height;                  /* viewport size in pixels */
+  float alpha_min, alpha_width;            /* SceneData::alphaMin / alphaWidth */
+  uint32_t record_format;                  /* OIT_RECORD_* */
+  uint32_t weighted_precision;             /* OIT_WEIGHTED_* */
+  float bin_capacity_scale;                /* tile-bin pairs per triangle reserved (0 = default 4) */
+  uint32_t flags;                          /* OIT_FLAG_* */
+} oit_state;
+
+/* Per-frame scene constants: SceneData (shaders/common.h:77-92). Column-major
+ * 4x4 matrices, vectors multiplied on the right (glm convention). */
+typedef struct oit_scene_data {
+  float proj_view_matrix[16];
+  float view_matrix[16];
+} oit_scene_data;
+
+/* A triangle mesh in device memory. Vertex layout = the reference's Vertex
+ * (utilities_vk.h:48-88): pos.xyz, normal.xyz, color.rgba, 40 bytes.
+ * Indices: uint32 triangle list (main.cpp:340-386). */
+typedef struct oit_mesh {
+  const float* vertices_device;
+  const uint32_t* indices_device;
+  uint32_t num_vertices;
+  uint32_t num_triangles;
+} oit_mesh;
+
+typedef struct oit_context oit_context;
+
+/* Which context-owned buffer oit_get_buffer returns. */
+#define OIT_BUF_ABUFFER 0        /* m_oitABuffer (oit.cpp:155-163) */
+#define OIT_BUF_AUX 1            /* m_oitAuxImage: counts or list heads */
+#define OIT_BUF_AUXDEPTH 2       /* m_oitAuxDepthImage (Spinlock/Interlock) */
+#define OIT_BUF_COUNTER 3        /* m_oitCounterImage (Linked List) */
+#define OIT_BUF_DEPTH 4          /* opaque depth, u32 per sample */
+#define OIT_BUF_OPAQUE_COLOR 5   /* opaque colour, float4 per sample */
+#define OIT_BUF_COLOR 6          /* colour target after tail blending, float4 */
+#define OIT_BUF_ACCUM 7          /* WBOIT accumulation, half4 or float4 per sample */
+#define OIT_BUF_REVEAL 8         /* WBOIT revealage, half or float per sample */
+#define OIT_BUF_OUTPUT 9         /* resolved RGBA8 output image (width*height*4) */
+#define OIT_BUF_OUTPUT_LINEAR 10 /* resolved premultiplied linear float4 output */
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* Validates the state, sizes and allocates every per-frame buffer.
+ * Replaces Sample::createFrameImages (oit.cpp:45-220) and the rebuild logic of
+ * Sample::updateRendererFromState (main.cpp:130-250). */
+int oit_create(const oit_state* state, oit_context** out_ctx);
+
+/* Frees the context. Replaces Sample::onDetach / destroyFrameImages (oit.cpp:30-43). */
+int oit_destroy(oit_context* ctx);
+
+/* Uploads the per-frame constants. Replaces Sample::updateUniformBuffer (main.cpp:625-643). */
+int oit_update_scene(oit_context* ctx, const oit_scene_data* scene);
+
+/* ---- per frame (the transparent pass) ---------------------------------- */
+
+/* Clears the colour target to the background (0.2 linear) and depth to 1.0:
+ * the main render pass begin (oitRender.cpp:89-100). */
+int oit_begin_frame(oit_context* ctx, void* stream);
+
+/* Clears the algorithm's auxiliary buffers. Replaces clearTransparentSimple /
+ * LinkedList / Loop / Loop64 / Lock (oitRender.cpp:156-174, 201-216, 242-265,
+ * 303-311, 337-356); WBOIT clears in its own pass (oitRender.cpp:394-397). */
+int oit_clear_transparent(oit_context* ctx, void* stream);
+
+/* Draws triangles [first_triangle, first_triangle + num_triangles) opaque
+ * with depth test LESS and depth write, back faces culled.
+ * Replaces the opaque vkCmdDrawIndexed of Sample::onRender (oitRender.cpp:113-122). */
+int oit_draw_opaque(oit_context* ctx, const oit_mesh* mesh, uint32_t first_triangle,
+                    uint32_t num_triangles, void* stream);
+
+/* COLOR pass (and Loop32's DEPTH pass) of drawTransparent*: rasterises the
+ * triangles, builds the algorithm's A-buffer and tail-blends overflow into the
+ * colour target. Replaces the first draw(s) of drawTransparentSimple /
+ * LinkedList / Loop / Loop64 / Lock / Weighted (oitRender.cpp:176-190, 218-230,
+ * 267-291, 313-325, 358-371, 384-414). */
+int oit_draw_transparent_color(oit_context* ctx, const oit_mesh* mesh, uint32_t first_triangle,
+                               uint32_t num_triangles, void* stream);
+
+/* COMPOSITE pass, fused with copyOffscreenToBackBuffer's MSAA resolve /
+ * supersample downsample (main.cpp:645-774): writes width*height RGBA8 sRGB
+ * pixels to out_rgba8_device (NULL = the context's OIT_BUF_OUTPUT).
+ * Replaces the full-screen composite draws (oitRender.cpp:191-198, 232-239,
+ * 293-300, 327-334, 373-381, 416-424). */
+int oit_composite(oit_context* ctx, uint8_t* out_rgba8_device, void* stream);
+
+/* drawTransparent*(cmd, numObjects) (oit.h:379-425): COLOR + COMPOSITE over the
+ * first num_triangles triangles of the mesh. */
+int oit_draw_transparent(oit_context* ctx, const oit_mesh* mesh, uint32_t num_triangles,
+                         uint8_t* out_rgba8_device, void* stream);
+
+/* One whole frame as Sample::onRender (oitRender.cpp:28-154): begin, clear,
+ * opaque draw of the last (100 - percent_transparent)% of the objects,
+ * transparent draw of the first percent_transparent% and composite. */
+int oit_render_frame(oit_context* ctx, const oit_mesh* mesh, uint32_t triangles_per_object,
+                     int32_t percent_transparent, uint8_t* out_rgba8_device, void* stream);
+
+/* Same frame from host memory: copies the mesh in and the RGBA8 image out
+ * inside the call (synchronous on the stream). Host pointers may be pinned. */
+int oit_render_frame_host(oit_context* ctx, const float* vertices_host, uint32_t num_vertices,
+                          const uint32_t* indices_host, uint32_t num_triangles,
+                          uint32_t triangles_per_object, int32_t percent_transparent,
+                          uint8_t* out_rgba8_host, void* stream);
+
+/* ---- inspection -------------------------------------------------------- */
+
+/* Synchronises the context's last stream and returns the device error bits
+ * (OIT_DEVERR_*) accumulated since the last call, then clears them. */
+int oit_get_error(oit_context* ctx, uint32_t* device_error_bits);
+
+/* Device pointer and size of a context-owned buffer (OIT_BUF_*). */
+int oit_get_buffer(oit_context* ctx, int which, void** device_ptr, size_t* bytes);
+
+/* Number of transparent fragments (after early depth) of the last COLOR pass;
+ * synchronises the stream. */
+int oit_get_fragment_count(oit_context* ctx, uint64_t* fragments);
+
+/* Number of kernels the context launched since creation. */
+int oit_get_launch_count(oit_context* ctx, uint64_t* launches);
+
+/* Per-pass GPU timing with CUDA events recorded on the launching stream: the
+ * role of nvvk::ProfilerGpuTimer::cmdFrameSection (oitRender.cpp:32, 82, 115,
+ * 158, 182, 194, ...). Sections: */
+#define OIT_PROF_OPAQUE_BIN 0        /* opaque setup + binning */
+#define OIT_PROF_OPAQUE_RASTER 1     /* opaque tile raster */
+#define OIT_PROF_TRANSPARENT_BIN 2   /* transparent setup + binning */
+#define OIT_PROF_TRANSPARENT_RASTER 3/* COLOR (+DEPTH) tile raster: A-buffer build */
+#define OIT_PROF_COMPOSITE 4         /* COMPOSITE + resolve */
+#define OIT_PROF_NUM_SECTIONS 5
+
+/* Enables (1) or disables (0) section timing; enabling resets the totals. */
+int oit_profile_enable(oit_context* ctx, int enable);
+
+/* Synchronises and returns, per section, the summed milliseconds and the
+ * number of timed executions since profiling was enabled. */
+int oit_profile_read(oit_context* ctx, double total_ms[OIT_PROF_NUM_SECTIONS],
+                     uint64_t count[OIT_PROF_NUM_SECTIONS]);
+
+/* Human-readable status. */
+const char* oit_status_string(int status);
+
+/* ---- host helpers (no GPU needed) -------------------------------------- */
+
+/* Bytes of the A-buffer and auxiliary buffers for a state: the sizing rules of
+ * Sample::createFrameImages (oit.cpp:100-201). */
+int oit_abuffer_bytes(const oit_state* state, uint64_t* abuffer_bytes, uint64_t* aux_bytes);
+
+/* Seeded synthetic sphere scene (the engine's stand-in for Sample::initScene,
+ * main.cpp:334-417): num_objects UV spheres of `stacks` x `slices`, centres
+ * uniform in [-half_extent, half_extent]^3, radii uniform in [radius_min,
+ * radius_max], colour RGB uniform [0,1] and colour.a uniform [0,1] (mapped to
+ * alpha by alpha_min/alpha_width), flattened into one mesh. */
+typedef struct oit_scene_desc {
+  uint64_t seed;
+  uint32_t num_objects;
+  uint32_t stacks, slices;
+  float half_extent;
+  float radius_min, radius_max;
+} oit_scene_desc;
+
+/* Sizes of the generated mesh. */
+int oit_scene_size(const oit_scene_desc* desc, uint32_t* num_vertices, uint32_t* num_triangles,
+                   uint32_t* triangles_per_object);
+
+/* Fills host arrays of num_vertices*10 floats and num_triangles*3 indices. */
+int oit_scene_generate(const oit_scene_desc* desc, float* vertices_host, uint32_t* indices_host);
+
+/* Camera at `eye` looking at `target` (up +y), vertical fov in degrees,
+ * Vulkan clip space (z in [0,1], y down): the engine's stand-in for
+ * CameraManipulator::getPerspectiveMatrix/getViewMatrix (main.cpp:630-631). */
+int oit_camera(uint32_t width, uint32_t height, const float eye[3], const float target[3],
+               float fov_y_degrees, float z_near, float z_far, oit_scene_data* out);
+
+/* The engine's sRGB quantisation tables: 256 thresholds and 256 decoded
+ * linear values (see gen_srgb_tables.py). */
+int oit_srgb_tables(float* thresholds256, float* decode256);
+
+/* ABI version (major*10000 + minor*100 + patch). */
+int oit_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

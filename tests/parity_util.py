@@ -1,0 +1,119 @@
+"""Shared helpers of the GPU parity tests: render one frame on the engine and
+on the oracle from the same mesh and camera, and compare what the reference
+defines bit for bit (fragment records, kept sets and their order) and what it
+defines as colour (the RGBA8 image, within 1 LSB)."""
+import numpy as np
+
+import oracle as orc
+import vk_order_independent_transparency_gb300 as oit
+
+RECORD_WORDS = {oit.OIT_SIMPLE: None, oit.OIT_SPINLOCK: None, oit.OIT_INTERLOCK: None}
+
+
+def scene(num_objects, width, height, seed=3, radius_min=0.05, radius_max=0.15, half_extent=1.0):
+    v, i, tpo = oit.make_scene(num_objects, seed=seed, radius_min=radius_min, radius_max=radius_max,
+                               half_extent=half_extent)
+    return v, i, tpo, oit.make_camera(width, height)
+
+
+def render_gpu(algorithm, width, height, v, i, tpo, sd, percent=100, **kw):
+    st = oit.make_state(algorithm, width, height, **kw)
+    r = oit.Renderer(st)
+    mesh = oit.DeviceMesh(v, i)
+    r.update_scene(sd)
+    r.render_frame(mesh, tpo, percent)
+    res = {
+        'image': r.output(),
+        'abuf': r.read_buffer(oit.OIT_BUF_ABUFFER),
+        'aux': r.read_buffer(oit.OIT_BUF_AUX),
+        'auxdepth': r.read_buffer(oit.OIT_BUF_AUXDEPTH),
+        'counter': r.read_buffer(oit.OIT_BUF_COUNTER),
+        'color': r.read_buffer(oit.OIT_BUF_COLOR, np.float32).reshape(-1, 4),
+        'depth': r.read_buffer(oit.OIT_BUF_DEPTH),
+        'fragments': r.fragment_count(),
+        'error': r.get_error(),
+        'renderer': r,
+        'mesh': mesh,
+    }
+    if algorithm == oit.OIT_WEIGHTED:
+        if kw.get('weighted_precision', 0) == oit.OIT_WEIGHTED_FP32:
+            res['accum'] = r.read_buffer(oit.OIT_BUF_ACCUM, np.float32).reshape(-1, 4).astype(np.float64)
+            res['reveal'] = r.read_buffer(oit.OIT_BUF_REVEAL, np.float32).astype(np.float64)
+        else:
+            res['accum'] = r.read_buffer(oit.OIT_BUF_ACCUM, np.float16).reshape(-1, 4).astype(np.float64)
+            res['reveal'] = r.read_buffer(oit.OIT_BUF_REVEAL, np.float16).astype(np.float64)
+    return res
+
+
+def render_oracle(algorithm, width, height, v, i, tpo, sd, percent=100, oit_layers=8, nodes_per_pixel=8,
+                  aa_type=0, tail_blend=True, alpha_min=0.2, alpha_width=0.6, **_):
+    fr = orc.render(algorithm, width, height, sd, v, i, tpo, percent, oit_layers=oit_layers,
+                    nodes_per_pixel=nodes_per_pixel, aa_type=aa_type, tail_blend=tail_blend, alpha_min=alpha_min,
+                    alpha_width=alpha_width)
+    state = {
+        'abuf': fr.buffer(orc.BUF_ABUFFER),
+        'aux': fr.buffer(orc.BUF_AUX),
+        'auxdepth': fr.buffer(orc.BUF_AUXDEPTH),
+        'counter': fr.buffer(orc.BUF_COUNTER),
+        'depth': fr.buffer(orc.BUF_DEPTH),
+        'color_samples': fr.buffer(orc.BUF_COLOR, np.float64).reshape(fr.msaa, -1, 4),
+        'accum': fr.buffer(orc.BUF_ACCUM, np.float64).reshape(-1, 4),
+        'reveal': fr.buffer(orc.BUF_REVEAL, np.float64),
+        'fragments': fr.fragment_count(),
+    }
+    out8, lin = fr.composite()
+    state['image'] = out8
+    state['linear'] = lin
+    state['frame'] = fr
+    return state
+
+
+def walk_lists(pool_words, heads):
+    pool = pool_words.reshape(-1, 4)
+    out = []
+    for h in heads:
+        seq = []
+        off = int(h)
+        guard = 0
+        while off:
+            n = pool[off]
+            seq.append((int(n[0]), int(n[1]), int(n[2])))
+            off = int(n[3])
+            guard += 1
+            assert guard <= pool.shape[0], 'cycle in linked list'
+        out.append(seq)
+    return out
+
+
+def compare_abuffer(algorithm, g, o, L, P, coverage):
+    """Bit-exact comparison of the algorithm's A-buffer state."""
+    if algorithm in (oit.OIT_SIMPLE, oit.OIT_SPINLOCK, oit.OIT_INTERLOCK):
+        np.testing.assert_array_equal(g['aux'][:P], o['aux'][:P])
+        words = 4 if coverage else 2
+        ga = g['abuf'][:L * P * words].reshape(L, P, words)
+        oa = o['abuf'][:L * P * words].reshape(L, P, words)
+        n = np.minimum(o['aux'][:P], L)
+        for layer in range(L):
+            sel = n > layer
+            np.testing.assert_array_equal(ga[layer][sel], oa[layer][sel], err_msg='layer %d' % layer)
+        if algorithm != oit.OIT_SIMPLE:
+            np.testing.assert_array_equal(g['auxdepth'][:P], o['auxdepth'][:P])
+    elif algorithm == oit.OIT_LINKEDLIST:
+        assert g['counter'][0] == o['counter'][0]
+        assert walk_lists(g['abuf'], g['aux'][:P]) == walk_lists(o['abuf'], o['aux'][:P])
+    elif algorithm == oit.OIT_LOOP:
+        ga = g['abuf'][:2 * L * P].reshape(2 * L, P)
+        oa = o['abuf'][:2 * L * P].reshape(2 * L, P)
+        np.testing.assert_array_equal(ga[:L], oa[:L])
+        count = (oa[:L] != 0xFFFFFFFF).sum(axis=0)
+        for layer in range(L):
+            sel = count > layer
+            np.testing.assert_array_equal(ga[L + layer][sel], oa[L + layer][sel])
+    elif algorithm == oit.OIT_LOOP64:
+        np.testing.assert_array_equal(g['abuf'][:2 * L * P], o['abuf'][:2 * L * P])
+
+
+def compare_images(g, o, max_lsb=1):
+    d = np.abs(g['image'].astype(np.int32) - o['image'].astype(np.int32))
+    assert d.max() <= max_lsb, 'image differs by %d LSB at %s' % (d.max(), np.argwhere(d == d.max())[:4])
+    return int(d.max()), float((d > 0).mean())

@@ -1,0 +1,153 @@
+"""GPU parity: the CUDA engine against the CPU oracle on the same seeded scenes.
+
+Bit-exact: fragment counts, every algorithm's A-buffer state (Simple /
+Spinlock / Interlock records and counters, linked lists in list order, Loop32
+depth and colour layers, Loop64 keys), the opaque depth buffer.
+Colour: the RGBA8 image within 1 LSB (GPU blends in FP32, the oracle in
+FP64); the tail-blended colour target within 2e-5 absolute.
+"""
+import numpy as np
+import pytest
+
+import parity_util as pu
+
+pytestmark = pytest.mark.gpu
+
+ALGS = [0, 1, 2, 3, 4, 5, 6]
+AA = {'1x': 0, 'msaa4': 1, 'msaa8': 4}
+
+
+def run_pair(engine, alg, W, H, n_obj, percent=100, seed=3, rmin=0.05, rmax=0.2, **kw):
+    v, i, tpo, sd = pu.scene(n_obj, W, H, seed=seed, radius_min=rmin, radius_max=rmax)
+    g = pu.render_gpu(alg, W, H, v, i, tpo, sd, percent, **kw)
+    o = pu.render_oracle(alg, W, H, v, i, tpo, sd, percent, **kw)
+    return g, o
+
+
+def check(engine, alg, g, o, W, H, L, aa=0, ss=1):
+    msaa = {0: 1, 1: 4, 4: 8, 3: 1}[aa]
+    coverage = msaa > 1
+    P = W * H * ss * ss
+    assert g['error'] == 0
+    assert g['fragments'] == o['fragments']
+    if alg != engine.OIT_WEIGHTED:
+        pu.compare_abuffer(alg, g, o, L, P, coverage)
+        ref_col = o['color_samples'].mean(axis=0)
+        np.testing.assert_allclose(g['color'][:P], ref_col, atol=2e-5, rtol=0)
+    pu.compare_images(g, o)
+
+
+@pytest.mark.parametrize('tail', [True, False])
+@pytest.mark.parametrize('aa', list(AA))
+@pytest.mark.parametrize('alg', ALGS)
+def test_algorithm(engine, alg, aa, tail):
+    W, H, L = 128, 96, 4
+    kw = dict(oit_layers=L, nodes_per_pixel=6, aa_type=AA[aa], tail_blend=tail,
+              weighted_precision=engine.OIT_WEIGHTED_FP32)
+    g, o = run_pair(engine, alg, W, H, 40, **kw)
+    check(engine, alg, g, o, W, H, L, AA[aa])
+
+
+@pytest.mark.parametrize('L', [1, 2, 8, 16, 32])
+@pytest.mark.parametrize('alg', [0, 1, 2, 3, 4])
+def test_layers(engine, alg, L):
+    W, H = 96, 80
+    g, o = run_pair(engine, alg, W, H, 48, seed=11, rmin=0.1, rmax=0.3, oit_layers=L, nodes_per_pixel=40)
+    check(engine, alg, g, o, W, H, L)
+
+
+@pytest.mark.parametrize('alg', ALGS)
+def test_opaque_and_transparent(engine, alg):
+    W, H, L = 160, 120, 8
+    g, o = run_pair(engine, alg, W, H, 64, percent=60, seed=21, oit_layers=L, nodes_per_pixel=8,
+                    weighted_precision=engine.OIT_WEIGHTED_FP32)
+    np.testing.assert_array_equal(g['depth'][:W * H], o['depth'][:W * H])
+    check(engine, alg, g, o, W, H, L)
+
+
+@pytest.mark.parametrize('alg', [0, 1, 3, 6])
+def test_supersample(engine, alg):
+    W, H, L = 64, 48, 4
+    g, o = run_pair(engine, alg, W, H, 32, aa_type=3, oit_layers=L, nodes_per_pixel=8,
+                    weighted_precision=engine.OIT_WEIGHTED_FP32)
+    check(engine, alg, g, o, W, H, L, aa=3, ss=2)
+
+
+def test_linked_list_overflow(engine):
+    """A pool smaller than the fragment count: each pixel keeps a primitive-order
+    prefix of its fragments (the counter order decides which); the rest are tail
+    blended. The oracle replays the GPU's per-pixel prefix lengths."""
+    W, H, L = 128, 96, 4
+    v, i, tpo, sd = pu.scene(48, W, H, seed=9, radius_min=0.1, radius_max=0.25)
+    g = pu.render_gpu(engine.OIT_LINKEDLIST, W, H, v, i, tpo, sd, oit_layers=L, nodes_per_pixel=1)
+    full = pu.render_oracle(engine.OIT_LINKEDLIST, W, H, v, i, tpo, sd, oit_layers=L, nodes_per_pixel=64)
+    P = W * H
+    assert g['fragments'] > P  # the pool (P nodes) overflowed
+    assert g['counter'][0] == g['fragments']
+    gl = pu.walk_lists(g['abuf'], g['aux'][:P])
+    ol = pu.walk_lists(full['abuf'], full['aux'][:P])
+    stored = 0
+    for a, b in zip(gl, ol):
+        # lists are in reverse arrival order: the stored ones are the oldest
+        assert a == b[len(b) - len(a):]
+        stored += len(a)
+    assert stored == P - 1  # nodes 1..P-1 are all used
+    import oracle as orc
+    fr = orc.Frame(orc.LINKEDLIST, W, H, oit_layers=L, nodes_per_pixel=1)
+    fr.set_ll_store_limit(np.array([len(a) for a in gl], np.uint32))
+    fr.draw_transparent(sd, v, i, 0, i.shape[0])
+    ref8, _ = fr.composite()
+    d = np.abs(g['image'].astype(np.int32) - ref8.astype(np.int32))
+    assert d.max() <= 1
+
+
+@pytest.mark.parametrize('prec', [0, 1])
+def test_weighted_accumulators(engine, prec):
+    """WBOIT accumulation vs FP64: FP32 within 1e-5 relative, FP16 (RGBA16F
+    emulation, rounding after every blend) within 2e-2 relative."""
+    W, H = 128, 96
+    v, i, tpo, sd = pu.scene(64, W, H, seed=4)
+    g = pu.render_gpu(engine.OIT_WEIGHTED, W, H, v, i, tpo, sd, weighted_precision=prec)
+    o = pu.render_oracle(engine.OIT_WEIGHTED, W, H, v, i, tpo, sd)
+    acc_g, acc_o = g['accum'], o['accum']
+    mask = np.abs(acc_o) > 1e-3
+    rel = np.abs(acc_g - acc_o)[mask] / np.abs(acc_o)[mask]
+    tol = 1e-5 if prec == 1 else 2e-2
+    assert rel.max() < tol, rel.max()
+    rrel = np.abs(g['reveal'] - o['reveal']) / np.maximum(o['reveal'], 1e-3)
+    assert rrel.max() < tol * 10
+    if prec == 1:
+        pu.compare_images(g, o)
+
+
+def test_deterministic(engine):
+    W, H = 160, 120
+    v, i, tpo, sd = pu.scene(64, W, H, seed=2)
+    for alg in ALGS:
+        a = pu.render_gpu(alg, W, H, v, i, tpo, sd, oit_layers=8)
+        b = pu.render_gpu(alg, W, H, v, i, tpo, sd, oit_layers=8)
+        np.testing.assert_array_equal(a['image'], b['image'])
+        if alg != engine.OIT_LINKEDLIST:
+            np.testing.assert_array_equal(a['abuf'], b['abuf'])
+
+
+def test_linked_list_640x480(engine):
+    """The reference's CPU-runnable workload: Linked List, 640x480, OIT_LAYERS=8,
+    8 nodes per pixel, 256 spheres (radii 0.05-0.15), fully transparent."""
+    W, H = 640, 480
+    v, i, tpo, sd = pu.scene(256, W, H, seed=1, radius_min=0.05, radius_max=0.15)
+    g = pu.render_gpu(engine.OIT_LINKEDLIST, W, H, v, i, tpo, sd, oit_layers=8, nodes_per_pixel=8)
+    o = pu.render_oracle(engine.OIT_LINKEDLIST, W, H, v, i, tpo, sd, oit_layers=8, nodes_per_pixel=8)
+    check(engine, engine.OIT_LINKEDLIST, g, o, W, H, 8)
+
+
+@pytest.mark.parametrize('alg', [3, 4])
+def test_kbuffer_1080p(engine, alg):
+    """Loop64 and Spinlock at 1920x1080, OIT_LAYERS=16, 1024 spheres (radii
+    0.03-0.1), 60% transparent over an opaque depth pre-pass, tail blend on."""
+    W, H, L = 1920, 1080, 16
+    v, i, tpo, sd = pu.scene(1024, W, H, seed=2, radius_min=0.03, radius_max=0.1)
+    g = pu.render_gpu(alg, W, H, v, i, tpo, sd, 60, oit_layers=L)
+    o = pu.render_oracle(alg, W, H, v, i, tpo, sd, 60, oit_layers=L)
+    np.testing.assert_array_equal(g['depth'][:W * H], o['depth'][:W * H])
+    check(engine, alg, g, o, W, H, L)

@@ -1,0 +1,717 @@
+// C++ host engine behind the C ABI (include/oit_gb300.h).
+//
+// oit_context plays the role of the reference's Sample (oit.h:165-426): it
+// owns the per-frame buffers sized by the algorithm (createFrameImages,
+// oit.cpp:45-220), records the transparent pass on a CUDA stream
+// (clearTransparent* / drawTransparent*, oitRender.cpp:156-425) and resolves
+// to the back buffer (copyOffscreenToBackBuffer, main.cpp:645-774). Every
+// entry point returns a status and never aborts.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/oit_gb300.h"
+#include "oit_internal.h"
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    bytes = n;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+bool debug_enabled() {
+  static int v = -1;
+  if (v < 0) v = std::getenv("OIT_DEBUG") ? 1 : 0;
+  return v == 1;
+}
+
+int cuda_status(cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return OIT_OK;
+  if (debug_enabled()) std::fprintf(stderr, "oit: CUDA error in %s: %s\n", where, cudaGetErrorString(e));
+  if (e == cudaErrorMemoryAllocation) return OIT_ERR_OUT_OF_MEMORY;
+  return OIT_ERR_CUDA;
+}
+
+#define OIT_TRY_CUDA(expr, where)                   \
+  do {                                              \
+    cudaError_t _e = (expr);                        \
+    if (_e != cudaSuccess) return cuda_status(_e, where); \
+  } while (0)
+
+}  // namespace
+
+struct oit_context {
+  oit_state st{};
+  int msaa = 1, sample_shading = 0, supersample = 1;
+  int W = 0, H = 0, RW = 0, RH = 0;
+  uint32_t P = 0;
+  int S = 1, coverage = 0, L = 1;
+  int tiles_x = 0, tiles_y = 0, num_tiles = 0, key_bits = 1;
+  uint32_t capacity = 0;
+  oit::Mat4 pv{}, view{};
+  bool has_scene = false;
+  float4 background = make_float4(0.2f, 0.2f, 0.2f, 0.2f);
+
+  DevBuf depth, opaque_color, color, abuf, aux, auxdepth, counter, accum, reveal, out, out_linear, err, frag;
+  DevBuf bbox, setup, pair_count, pair_offset, scan_tmp, total;
+  DevBuf keys, tris, keys_alt, tris_alt, hist, tile_begin, tile_end;
+  DevBuf mesh_v, mesh_i;
+  size_t tri_cap = 0, pair_cap = 0;
+  bool opaque_valid = false;
+  bool color_valid = false;
+  cudaStream_t last_stream = nullptr;
+  uint64_t launches = 0;
+
+  // Section timing (oit_profile_*): event pairs recorded around each pass.
+  struct Pending {
+    int section;
+    cudaEvent_t a, b;
+  };
+  bool prof_on = false;
+  std::vector<Pending> prof_pending;
+  std::vector<cudaEvent_t> prof_free;
+  double prof_ms[OIT_PROF_NUM_SECTIONS] = {};
+  uint64_t prof_n[OIT_PROF_NUM_SECTIONS] = {};
+
+  cudaEvent_t prof_event() {
+    if (!prof_free.empty()) {
+      cudaEvent_t e = prof_free.back();
+      prof_free.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+  // Returns the start event (or null when profiling is off).
+  cudaEvent_t prof_begin(cudaStream_t s) {
+    if (!prof_on) return nullptr;
+    cudaEvent_t a = prof_event();
+    cudaEventRecord(a, s);
+    return a;
+  }
+  void prof_end(int section, cudaEvent_t a, cudaStream_t s) {
+    if (!a) return;
+    cudaEvent_t b = prof_event();
+    cudaEventRecord(b, s);
+    prof_pending.push_back({section, a, b});
+  }
+  int prof_collect() {
+    for (const Pending& p : prof_pending) {
+      OIT_TRY_CUDA(cudaEventSynchronize(p.b), "profile sync");
+      float ms = 0.f;
+      OIT_TRY_CUDA(cudaEventElapsedTime(&ms, p.a, p.b), "profile elapsed");
+      prof_ms[p.section] += ms;
+      prof_n[p.section] += 1;
+      prof_free.push_back(p.a);
+      prof_free.push_back(p.b);
+    }
+    prof_pending.clear();
+    return OIT_OK;
+  }
+
+  ~oit_context() {
+    for (const Pending& p : prof_pending) {
+      cudaEventDestroy(p.a);
+      cudaEventDestroy(p.b);
+    }
+    for (cudaEvent_t e : prof_free) cudaEventDestroy(e);
+    DevBuf* all[] = {&depth, &opaque_color, &color, &abuf, &aux, &auxdepth, &counter, &accum, &reveal, &out,
+                     &out_linear, &err, &frag, &bbox, &setup, &pair_count, &pair_offset, &scan_tmp, &total,
+                     &keys, &tris, &keys_alt, &tris_alt, &hist, &tile_begin, &tile_end, &mesh_v, &mesh_i};
+    for (DevBuf* b : all) b->release();
+  }
+
+  oit::Alg alg() const { return static_cast<oit::Alg>(st.algorithm); }
+
+  // ---- Sample::createFrameImages (oit.cpp:45-220) ----
+  int create() {
+    OIT_TRY_CUDA(depth.ensure(4), "alloc");
+    size_t elems = (size_t)P;  // A-buffer elements (no sample shading)
+    size_t abuf_bytes = 0;
+    switch (alg()) {
+      case oit::Alg::Simple:
+      case oit::Alg::Spinlock:
+      case oit::Alg::Interlock:
+        abuf_bytes = elems * L * (coverage ? 16 : 8);
+        break;
+      case oit::Alg::LinkedList:
+        abuf_bytes = (size_t)capacity * 16;
+        break;
+      case oit::Alg::Loop:
+      case oit::Alg::Loop64:
+        abuf_bytes = elems * L * 8;
+        break;
+      default:
+        break;
+    }
+    OIT_TRY_CUDA(abuf.ensure(abuf_bytes), "alloc abuffer");
+    OIT_TRY_CUDA(aux.ensure(elems * 4), "alloc aux");
+    OIT_TRY_CUDA(auxdepth.ensure(elems * 4), "alloc auxdepth");
+    OIT_TRY_CUDA(counter.ensure(4), "alloc counter");
+    OIT_TRY_CUDA(color.ensure((size_t)P * 16), "alloc color");
+    if (alg() == oit::Alg::Weighted) {
+      const bool f32 = st.weighted_precision == OIT_WEIGHTED_FP32;
+      OIT_TRY_CUDA(accum.ensure((size_t)S * P * (f32 ? 16 : 8)), "alloc accum");
+      OIT_TRY_CUDA(reveal.ensure((size_t)S * P * (f32 ? 4 : 2)), "alloc reveal");
+    }
+    OIT_TRY_CUDA(out.ensure((size_t)W * H * 4), "alloc out");
+    OIT_TRY_CUDA(err.ensure(4), "alloc err");
+    OIT_TRY_CUDA(frag.ensure(8), "alloc frag");
+    OIT_TRY_CUDA(tile_begin.ensure((size_t)num_tiles * 4), "alloc bins");
+    OIT_TRY_CUDA(tile_end.ensure((size_t)num_tiles * 4), "alloc bins");
+    OIT_TRY_CUDA(total.ensure(4), "alloc total");
+    OIT_TRY_CUDA(cudaMemset(err.p, 0, 4), "memset");
+    OIT_TRY_CUDA(cudaMemset(frag.p, 0, 8), "memset");
+    OIT_TRY_CUDA(cudaMemset(counter.p, 0, 4), "memset");
+    return OIT_OK;
+  }
+
+  int ensure_opaque_buffers() {
+    OIT_TRY_CUDA(depth.ensure((size_t)S * P * 4), "alloc depth");
+    OIT_TRY_CUDA(opaque_color.ensure((size_t)S * P * 16), "alloc opaque colour");
+    return OIT_OK;
+  }
+
+  int ensure_triangles(size_t n) {
+    if (n <= tri_cap) return OIT_OK;
+    const size_t cap = std::max<size_t>(n, 1024);
+    OIT_TRY_CUDA(bbox.ensure(cap * 8), "alloc bbox");
+    OIT_TRY_CUDA(setup.ensure(cap * 128), "alloc setup");
+    OIT_TRY_CUDA(pair_count.ensure(cap * 4), "alloc pair_count");
+    OIT_TRY_CUDA(pair_offset.ensure((cap + 1) * 4), "alloc pair_offset");
+    tri_cap = cap;
+    return OIT_OK;
+  }
+
+  int ensure_pairs(size_t n) {
+    const size_t hist_words = oit::radix_hist_words(n);
+    const size_t scan_words = std::max(oit::scan_scratch_words(tri_cap), oit::scan_scratch_words(hist_words));
+    OIT_TRY_CUDA(scan_tmp.ensure(scan_words * 4), "alloc scan");
+    if (n > pair_cap) {
+      const float scale = st.bin_capacity_scale > 0.0f ? st.bin_capacity_scale : 1.25f;
+      const size_t cap = std::max<size_t>((size_t)((double)n * std::max(1.0f, scale)), 4096);
+      OIT_TRY_CUDA(keys.ensure(cap * 4), "alloc keys");
+      OIT_TRY_CUDA(tris.ensure(cap * 4), "alloc tris");
+      OIT_TRY_CUDA(keys_alt.ensure(cap * 4), "alloc keys");
+      OIT_TRY_CUDA(tris_alt.ensure(cap * 4), "alloc tris");
+      pair_cap = cap;
+    }
+    OIT_TRY_CUDA(hist.ensure(std::max<size_t>(oit::radix_hist_words(pair_cap), 256) * 4), "alloc hist");
+    return OIT_OK;
+  }
+
+  oit::SetupParams setup_params(const oit_mesh* mesh, uint32_t first, uint32_t count, int cull_back) {
+    oit::SetupParams sp{};
+    sp.vertices = mesh->vertices_device;
+    sp.indices = mesh->indices_device;
+    sp.first_triangle = first;
+    sp.num_triangles = count;
+    sp.proj_view = pv;
+    sp.view = view;
+    sp.RW = RW;
+    sp.RH = RH;
+    sp.alpha_min = st.alpha_min;
+    sp.alpha_width = st.alpha_width;
+    sp.cull_back = cull_back;
+    sp.samples = S;
+    sp.tiles_x = tiles_x;
+    sp.bbox = bbox.as<uint2>();
+    sp.setup = setup.p;
+    sp.pair_count = pair_count.as<uint32_t>();
+    return sp;
+  }
+
+  oit::Bins bins() {
+    oit::Bins b{};
+    b.tile_begin = tile_begin.as<uint32_t>();
+    b.tile_end = tile_end.as<uint32_t>();
+    b.tris = tris.as<uint32_t>();
+    b.keys = keys.as<uint32_t>();
+    b.tris_alt = tris_alt.as<uint32_t>();
+    b.keys_alt = keys_alt.as<uint32_t>();
+    b.pair_offset = pair_offset.as<uint32_t>();
+    b.scan_tmp = scan_tmp.as<uint32_t>();
+    b.hist = hist.as<uint32_t>();
+    b.total = total.as<uint32_t>();
+    b.capacity = pair_cap;
+    return b;
+  }
+
+  // Setup + binning of one draw; afterwards tile_begin/tile_end/tris describe it.
+  int bin(const oit_mesh* mesh, uint32_t first, uint32_t count, int cull_back, cudaStream_t s) {
+    int r = ensure_triangles(count);
+    if (r != OIT_OK) return r;
+    r = ensure_pairs(0);
+    if (r != OIT_OK) return r;
+    oit::SetupParams sp = setup_params(mesh, first, count, cull_back);
+    oit::Bins b = bins();
+    uint32_t total_pairs = 0;
+    OIT_TRY_CUDA(oit::bin_count(sp, b, num_tiles, &total_pairs, s, &launches), "bin_count");
+    r = ensure_pairs(total_pairs);
+    if (r != OIT_OK) return r;
+    b = bins();
+    OIT_TRY_CUDA(oit::bin_sort(sp, b, total_pairs, key_bits, err.as<uint32_t>(), s, &launches), "bin_sort");
+    // bin_sort may have swapped the ping-pong buffers
+    if (b.keys != keys.as<uint32_t>()) {
+      std::swap(keys, keys_alt);
+      std::swap(tris, tris_alt);
+    }
+    return OIT_OK;
+  }
+
+  oit::RasterParams raster_params() {
+    oit::RasterParams p{};
+    p.RW = RW;
+    p.RH = RH;
+    p.tiles_x = tiles_x;
+    p.tiles_y = tiles_y;
+    p.P = P;
+    p.S = S;
+    p.L = L;
+    p.tail = st.tail_blend ? 1 : 0;
+    p.coverage = coverage;
+    p.tile_begin = tile_begin.as<uint32_t>();
+    p.tile_end = tile_end.as<uint32_t>();
+    p.tile_tris = tris.as<uint32_t>();
+    p.bbox = bbox.as<uint2>();
+    p.setup = setup.p;
+    p.depth = depth.as<uint32_t>();
+    p.opaque_color = opaque_color.as<float4>();
+    p.has_opaque = opaque_valid ? 1 : 0;
+    p.background = background;
+    p.color = color.as<float4>();
+    p.abuf = abuf.as<uint32_t>();
+    p.aux = aux.as<uint32_t>();
+    p.auxdepth = auxdepth.as<uint32_t>();
+    p.counter = counter.as<uint32_t>();
+    p.capacity = capacity;
+    p.record_fp32 = st.record_format == OIT_RECORD_RGBA32F;
+    p.accum = accum.p;
+    p.reveal = reveal.p;
+    p.weighted_fp32 = st.weighted_precision == OIT_WEIGHTED_FP32;
+    p.error = err.as<uint32_t>();
+    p.frag_count = frag.as<unsigned long long>();
+    return p;
+  }
+
+  int raster(oit::Alg a, oit::RasterParams& p, cudaStream_t s) {
+    cudaError_t e;
+    switch (a) {
+      case oit::Alg::Simple:
+      case oit::Alg::LinkedList:
+      case oit::Alg::Opaque: e = oit::launch_raster_a(a, p, s); break;
+      case oit::Alg::Loop:
+      case oit::Alg::Loop64: e = oit::launch_raster_b(a, p, s); break;
+      default: e = oit::launch_raster_c(a, p, s); break;
+    }
+    ++launches;
+    return cuda_status(e, "raster");
+  }
+
+  // ---- the transparent pass ----
+  int begin_frame(cudaStream_t s) {
+    last_stream = s;
+    opaque_valid = false;
+    color_valid = false;
+    return OIT_OK;
+  }
+
+  // clearTransparent* (oitRender.cpp:156-356). Only the linked-list counter
+  // needs clearing: the COLOR pass writes every pixel's aux words, k-buffer
+  // layers and WBOIT accumulators itself.
+  int clear_transparent(cudaStream_t s) {
+    last_stream = s;
+    OIT_TRY_CUDA(cudaMemsetAsync(frag.p, 0, 8, s), "clear");
+    if (alg() == oit::Alg::LinkedList) OIT_TRY_CUDA(cudaMemsetAsync(counter.p, 0, 4, s), "clear");
+    return OIT_OK;
+  }
+
+  int draw_opaque(const oit_mesh* mesh, uint32_t first, uint32_t count, cudaStream_t s) {
+    last_stream = s;
+    int r = ensure_opaque_buffers();
+    if (r != OIT_OK) return r;
+    if (!opaque_valid) {
+      OIT_TRY_CUDA(oit::launch_fill_u32(depth.as<uint32_t>(), 0x3F800000u, (size_t)S * P, s), "fill");
+      OIT_TRY_CUDA(oit::launch_fill_f4(opaque_color.as<float4>(), background, (size_t)S * P, s), "fill");
+      launches += 2;
+      opaque_valid = true;
+    }
+    if (!count) return OIT_OK;
+    cudaEvent_t t0 = prof_begin(s);
+    r = bin(mesh, first, count, 1, s);
+    if (r != OIT_OK) return r;
+    prof_end(OIT_PROF_OPAQUE_BIN, t0, s);
+    oit::RasterParams p = raster_params();
+    cudaEvent_t t1 = prof_begin(s);
+    r = raster(oit::Alg::Opaque, p, s);
+    prof_end(OIT_PROF_OPAQUE_RASTER, t1, s);
+    return r;
+  }
+
+  int draw_transparent_color(const oit_mesh* mesh, uint32_t first, uint32_t count, cudaStream_t s) {
+    last_stream = s;
+    cudaEvent_t t0 = prof_begin(s);
+    int r = bin(mesh, first, count, 0, s);
+    if (r != OIT_OK) return r;
+    prof_end(OIT_PROF_TRANSPARENT_BIN, t0, s);
+    oit::RasterParams p = raster_params();
+    cudaEvent_t t1 = prof_begin(s);
+    r = raster(alg(), p, s);
+    prof_end(OIT_PROF_TRANSPARENT_RASTER, t1, s);
+    if (r != OIT_OK) return r;
+    color_valid = true;
+    return OIT_OK;
+  }
+
+  int composite(uint8_t* out_dev, cudaStream_t s) {
+    last_stream = s;
+    if (!color_valid) return OIT_ERR_STATE;
+    oit::CompositeParams c{};
+    c.W = W;
+    c.H = H;
+    c.RW = RW;
+    c.RH = RH;
+    c.ss = supersample;
+    c.P = P;
+    c.S = S;
+    c.L = L;
+    c.tail = st.tail_blend ? 1 : 0;
+    c.coverage = coverage;
+    c.record_fp32 = st.record_format == OIT_RECORD_RGBA32F;
+    c.weighted_fp32 = st.weighted_precision == OIT_WEIGHTED_FP32;
+    c.abuf = abuf.as<uint32_t>();
+    c.aux = aux.as<uint32_t>();
+    c.color = color.as<float4>();
+    c.opaque_color = opaque_color.as<float4>();
+    c.has_opaque = opaque_valid ? 1 : 0;
+    c.background = background;
+    c.accum = accum.p;
+    c.reveal = reveal.p;
+    c.out_rgba8 = out_dev ? out_dev : out.as<uint8_t>();
+    c.out_linear = nullptr;
+    if (st.flags & OIT_FLAG_LINEAR_OUTPUT) {
+      OIT_TRY_CUDA(out_linear.ensure((size_t)W * H * 16), "alloc linear");
+      c.out_linear = out_linear.as<float4>();
+    }
+    ++launches;
+    cudaEvent_t t0 = prof_begin(s);
+    const int r = cuda_status(oit::launch_composite(alg(), c, s), "composite");
+    prof_end(OIT_PROF_COMPOSITE, t0, s);
+    return r;
+  }
+
+  int render_frame(const oit_mesh* mesh, uint32_t tpo, int32_t percent, uint8_t* out_dev, cudaStream_t s) {
+    if (!mesh || !tpo || percent < 0) return OIT_ERR_INVALID_ARGUMENT;
+    // Sample::onRender, oitRender.cpp:43-153
+    const uint32_t num_objects = mesh->num_triangles / tpo;
+    uint32_t num_transparent = (uint32_t)(((uint64_t)num_objects * (uint32_t)percent) / 100u);
+    if (num_transparent > num_objects) num_transparent = num_objects;
+    const uint32_t num_opaque = num_objects - num_transparent;
+    int r = begin_frame(s);
+    if (r == OIT_OK) r = clear_transparent(s);
+    if (r == OIT_OK && num_opaque > 0) r = draw_opaque(mesh, num_transparent * tpo, num_opaque * tpo, s);
+    if (r == OIT_OK) r = draw_transparent_color(mesh, 0, num_transparent * tpo, s);
+    if (r == OIT_OK) r = composite(out_dev, s);
+    return r;
+  }
+};
+
+namespace {
+
+bool pow2_layers(uint32_t l) { return l == 1 || l == 2 || l == 4 || l == 8 || l == 16 || l == 32; }
+
+// State::recomputeAntialiasingSettings (oit.h:84-115)
+bool aa_settings(uint32_t aa, int* msaa, int* sample_shading, int* supersample) {
+  *sample_shading = 0;
+  *supersample = 1;
+  switch (aa) {
+    case OIT_AA_NONE: *msaa = 1; return true;
+    case OIT_AA_MSAA_4X: *msaa = 4; return true;
+    case OIT_AA_SSAA_4X: *msaa = 4; *sample_shading = 1; return true;
+    case OIT_AA_SUPER_4X: *msaa = 1; *supersample = 2; return true;
+    case OIT_AA_MSAA_8X: *msaa = 8; return true;
+    case OIT_AA_SSAA_8X: *msaa = 8; *sample_shading = 1; return true;
+    default: return false;
+  }
+}
+
+int validate(const oit_state* s, int* msaa, int* ss, int* sup) {
+  if (!s) return OIT_ERR_INVALID_ARGUMENT;
+  if (s->algorithm >= OIT_NUM_ALGORITHMS) return OIT_ERR_INVALID_ARGUMENT;
+  if (!pow2_layers(s->oit_layers)) return OIT_ERR_INVALID_ARGUMENT;
+  if (!aa_settings(s->aa_type, msaa, ss, sup)) return OIT_ERR_INVALID_ARGUMENT;
+  if (s->width == 0 || s->height == 0) return OIT_ERR_INVALID_ARGUMENT;
+  if ((uint64_t)s->width * *sup > 16384 || (uint64_t)s->height * *sup > 16384) return OIT_ERR_INVALID_ARGUMENT;
+  if (s->algorithm == OIT_LINKEDLIST && s->linked_list_allocated_per_element < 1) return OIT_ERR_INVALID_ARGUMENT;
+  if (s->record_format > OIT_RECORD_RGBA32F || s->weighted_precision > OIT_WEIGHTED_FP32)
+    return OIT_ERR_INVALID_ARGUMENT;
+  if (!std::isfinite(s->alpha_min) || !std::isfinite(s->alpha_width)) return OIT_ERR_INVALID_ARGUMENT;
+  if (*ss) return OIT_ERR_UNSUPPORTED;                       // per-sample A-buffers
+  if (s->record_format != OIT_RECORD_RGBA8) return OIT_ERR_UNSUPPORTED;
+  return OIT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oit_abuffer_bytes(const oit_state* s, uint64_t* abuffer_bytes, uint64_t* aux_bytes) {
+  int msaa, ss, sup;
+  if (!s) return OIT_ERR_INVALID_ARGUMENT;
+  if (s->algorithm >= OIT_NUM_ALGORITHMS || !pow2_layers(s->oit_layers) || !aa_settings(s->aa_type, &msaa, &ss, &sup))
+    return OIT_ERR_INVALID_ARGUMENT;
+  // oit.cpp:100-163 and 165-201
+  const uint64_t bw = (uint64_t)s->width * sup, bh = (uint64_t)s->height * sup;
+  const bool coverage = msaa > 1 && !ss;
+  uint64_t per_sample = 0, stride = 0, aux = 0;
+  switch (s->algorithm) {
+    case OIT_SIMPLE: per_sample = s->oit_layers; stride = coverage ? 16 : 8; aux = 1; break;
+    case OIT_SPINLOCK: per_sample = s->oit_layers; stride = coverage ? 16 : 8; aux = 3; break;
+    case OIT_INTERLOCK: per_sample = s->oit_layers; stride = coverage ? 16 : 8; aux = 2; break;
+    case OIT_LINKEDLIST: per_sample = (uint64_t)std::max(0, s->linked_list_allocated_per_element); stride = 16; aux = 1; break;
+    case OIT_LOOP: per_sample = 2ull * s->oit_layers; stride = 4; aux = 1; break;
+    case OIT_LOOP64: per_sample = s->oit_layers; stride = 8; aux = 1; break;
+    default: break;
+  }
+  if (ss) per_sample *= (uint64_t)msaa;
+  const uint64_t layers = ss ? (uint64_t)msaa : 1;
+  if (abuffer_bytes) *abuffer_bytes = bw * bh * per_sample * stride;
+  if (aux_bytes) *aux_bytes = bw * bh * 4 * aux * layers + (s->algorithm == OIT_LINKEDLIST ? 4 : 0);
+  return OIT_OK;
+}
+
+int oit_create(const oit_state* state, oit_context** out_ctx) {
+  if (!out_ctx) return OIT_ERR_INVALID_ARGUMENT;
+  *out_ctx = nullptr;
+  int msaa = 1, ss = 0, sup = 1;
+  int r = validate(state, &msaa, &ss, &sup);
+  if (r != OIT_OK) return r;
+  oit_context* c = new (std::nothrow) oit_context();
+  if (!c) return OIT_ERR_OUT_OF_MEMORY;
+  c->st = *state;
+  c->msaa = msaa;
+  c->sample_shading = ss;
+  c->supersample = sup;
+  c->W = (int)state->width;
+  c->H = (int)state->height;
+  c->RW = c->W * sup;
+  c->RH = c->H * sup;
+  c->P = (uint32_t)c->RW * (uint32_t)c->RH;
+  c->S = msaa;
+  c->coverage = (msaa > 1 && !ss) ? 1 : 0;
+  c->L = (int)state->oit_layers;
+  c->tiles_x = (c->RW + oit::kTile - 1) / oit::kTile;
+  c->tiles_y = (c->RH + oit::kTile - 1) / oit::kTile;
+  c->num_tiles = c->tiles_x * c->tiles_y;
+  c->key_bits = 1;
+  while ((1 << c->key_bits) < c->num_tiles) ++c->key_bits;
+  if (state->algorithm == OIT_LINKEDLIST) {
+    const uint64_t cap = (uint64_t)state->linked_list_allocated_per_element * c->P;  // oit.cpp:125
+    if (cap >= 0xFFFFFFFFull) {
+      delete c;
+      return OIT_ERR_INVALID_ARGUMENT;
+    }
+    c->capacity = (uint32_t)cap;
+  }
+  r = c->create();
+  if (r != OIT_OK) {
+    delete c;
+    return r;
+  }
+  *out_ctx = c;
+  return OIT_OK;
+}
+
+int oit_destroy(oit_context* ctx) {
+  if (!ctx) return OIT_ERR_INVALID_ARGUMENT;
+  cudaDeviceSynchronize();
+  delete ctx;
+  return OIT_OK;
+}
+
+int oit_update_scene(oit_context* ctx, const oit_scene_data* scene) {
+  if (!ctx || !scene) return OIT_ERR_INVALID_ARGUMENT;
+  std::memcpy(ctx->pv.m, scene->proj_view_matrix, sizeof(ctx->pv.m));
+  std::memcpy(ctx->view.m, scene->view_matrix, sizeof(ctx->view.m));
+  ctx->has_scene = true;
+  return OIT_OK;
+}
+
+int oit_begin_frame(oit_context* ctx, void* stream) {
+  if (!ctx) return OIT_ERR_INVALID_ARGUMENT;
+  return ctx->begin_frame(static_cast<cudaStream_t>(stream));
+}
+
+int oit_clear_transparent(oit_context* ctx, void* stream) {
+  if (!ctx) return OIT_ERR_INVALID_ARGUMENT;
+  return ctx->clear_transparent(static_cast<cudaStream_t>(stream));
+}
+
+static bool mesh_ok(const oit_mesh* m, uint32_t first, uint32_t count) {
+  if (!m) return false;
+  if (count == 0) return true;
+  if (!m->vertices_device || !m->indices_device) return false;
+  return (uint64_t)first + count <= m->num_triangles;
+}
+
+int oit_draw_opaque(oit_context* ctx, const oit_mesh* mesh, uint32_t first, uint32_t count, void* stream) {
+  if (!ctx || !mesh_ok(mesh, first, count)) return OIT_ERR_INVALID_ARGUMENT;
+  if (!ctx->has_scene) return OIT_ERR_STATE;
+  return ctx->draw_opaque(mesh, first, count, static_cast<cudaStream_t>(stream));
+}
+
+int oit_draw_transparent_color(oit_context* ctx, const oit_mesh* mesh, uint32_t first, uint32_t count, void* stream) {
+  if (!ctx || !mesh_ok(mesh, first, count)) return OIT_ERR_INVALID_ARGUMENT;
+  if (!ctx->has_scene) return OIT_ERR_STATE;
+  return ctx->draw_transparent_color(mesh, first, count, static_cast<cudaStream_t>(stream));
+}
+
+int oit_composite(oit_context* ctx, uint8_t* out, void* stream) {
+  if (!ctx) return OIT_ERR_INVALID_ARGUMENT;
+  return ctx->composite(out, static_cast<cudaStream_t>(stream));
+}
+
+int oit_draw_transparent(oit_context* ctx, const oit_mesh* mesh, uint32_t num_triangles, uint8_t* out, void* stream) {
+  int r = oit_draw_transparent_color(ctx, mesh, 0, num_triangles, stream);
+  if (r != OIT_OK) return r;
+  return oit_composite(ctx, out, stream);
+}
+
+int oit_render_frame(oit_context* ctx, const oit_mesh* mesh, uint32_t tpo, int32_t percent, uint8_t* out,
+                     void* stream) {
+  if (!ctx || !mesh) return OIT_ERR_INVALID_ARGUMENT;
+  if (!ctx->has_scene) return OIT_ERR_STATE;
+  if (!mesh_ok(mesh, 0, mesh->num_triangles)) return OIT_ERR_INVALID_ARGUMENT;
+  return ctx->render_frame(mesh, tpo, percent, out, static_cast<cudaStream_t>(stream));
+}
+
+int oit_render_frame_host(oit_context* ctx, const float* vertices, uint32_t num_vertices, const uint32_t* indices,
+                          uint32_t num_triangles, uint32_t tpo, int32_t percent, uint8_t* out_host, void* stream) {
+  if (!ctx || !vertices || !indices || !out_host || !num_vertices) return OIT_ERR_INVALID_ARGUMENT;
+  if (!ctx->has_scene) return OIT_ERR_STATE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t vb = (size_t)num_vertices * 40, ib = (size_t)num_triangles * 12;
+  OIT_TRY_CUDA(ctx->mesh_v.ensure(vb), "alloc mesh");
+  OIT_TRY_CUDA(ctx->mesh_i.ensure(ib), "alloc mesh");
+  OIT_TRY_CUDA(cudaMemcpyAsync(ctx->mesh_v.p, vertices, vb, cudaMemcpyHostToDevice, s), "h2d");
+  OIT_TRY_CUDA(cudaMemcpyAsync(ctx->mesh_i.p, indices, ib, cudaMemcpyHostToDevice, s), "h2d");
+  oit_mesh m{ctx->mesh_v.as<float>(), ctx->mesh_i.as<uint32_t>(), num_vertices, num_triangles};
+  int r = ctx->render_frame(&m, tpo, percent, nullptr, s);
+  if (r != OIT_OK) return r;
+  OIT_TRY_CUDA(cudaMemcpyAsync(out_host, ctx->out.p, (size_t)ctx->W * ctx->H * 4, cudaMemcpyDeviceToHost, s), "d2h");
+  OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
+  return OIT_OK;
+}
+
+int oit_get_error(oit_context* ctx, uint32_t* bits) {
+  if (!ctx || !bits) return OIT_ERR_INVALID_ARGUMENT;
+  OIT_TRY_CUDA(cudaStreamSynchronize(ctx->last_stream), "sync");
+  OIT_TRY_CUDA(cudaMemcpy(bits, ctx->err.p, 4, cudaMemcpyDeviceToHost), "d2h");
+  OIT_TRY_CUDA(cudaMemset(ctx->err.p, 0, 4), "memset");
+  return OIT_OK;
+}
+
+int oit_get_buffer(oit_context* ctx, int which, void** ptr, size_t* bytes) {
+  if (!ctx || !ptr) return OIT_ERR_INVALID_ARGUMENT;
+  DevBuf* b = nullptr;
+  size_t n = 0;
+  switch (which) {
+    case OIT_BUF_ABUFFER: b = &ctx->abuf; n = b->bytes; break;
+    case OIT_BUF_AUX: b = &ctx->aux; n = (size_t)ctx->P * 4; break;
+    case OIT_BUF_AUXDEPTH: b = &ctx->auxdepth; n = (size_t)ctx->P * 4; break;
+    case OIT_BUF_COUNTER: b = &ctx->counter; n = 4; break;
+    case OIT_BUF_DEPTH: b = &ctx->depth; n = ctx->opaque_valid ? (size_t)ctx->S * ctx->P * 4 : 0; break;
+    case OIT_BUF_OPAQUE_COLOR: b = &ctx->opaque_color; n = ctx->opaque_valid ? (size_t)ctx->S * ctx->P * 16 : 0; break;
+    case OIT_BUF_COLOR: b = &ctx->color; n = (size_t)ctx->P * 16; break;
+    case OIT_BUF_ACCUM: b = &ctx->accum; n = b->bytes; break;
+    case OIT_BUF_REVEAL: b = &ctx->reveal; n = b->bytes; break;
+    case OIT_BUF_OUTPUT: b = &ctx->out; n = (size_t)ctx->W * ctx->H * 4; break;
+    case OIT_BUF_OUTPUT_LINEAR: b = &ctx->out_linear; n = b->p ? (size_t)ctx->W * ctx->H * 16 : 0; break;
+    default: return OIT_ERR_INVALID_ARGUMENT;
+  }
+  *ptr = b->p;
+  if (bytes) *bytes = n;
+  return OIT_OK;
+}
+
+int oit_get_fragment_count(oit_context* ctx, uint64_t* fragments) {
+  if (!ctx || !fragments) return OIT_ERR_INVALID_ARGUMENT;
+  OIT_TRY_CUDA(cudaStreamSynchronize(ctx->last_stream), "sync");
+  unsigned long long v = 0;
+  OIT_TRY_CUDA(cudaMemcpy(&v, ctx->frag.p, 8, cudaMemcpyDeviceToHost), "d2h");
+  *fragments = v;
+  return OIT_OK;
+}
+
+int oit_get_launch_count(oit_context* ctx, uint64_t* launches) {
+  if (!ctx || !launches) return OIT_ERR_INVALID_ARGUMENT;
+  *launches = ctx->launches;
+  return OIT_OK;
+}
+
+int oit_profile_enable(oit_context* ctx, int enable) {
+  if (!ctx) return OIT_ERR_INVALID_ARGUMENT;
+  int r = ctx->prof_collect();
+  if (r != OIT_OK) return r;
+  ctx->prof_on = enable != 0;
+  for (int i = 0; i < OIT_PROF_NUM_SECTIONS; ++i) {
+    ctx->prof_ms[i] = 0.0;
+    ctx->prof_n[i] = 0;
+  }
+  return OIT_OK;
+}
+
+int oit_profile_read(oit_context* ctx, double* total_ms, uint64_t* count) {
+  if (!ctx || !total_ms || !count) return OIT_ERR_INVALID_ARGUMENT;
+  int r = ctx->prof_collect();
+  if (r != OIT_OK) return r;
+  for (int i = 0; i < OIT_PROF_NUM_SECTIONS; ++i) {
+    total_ms[i] = ctx->prof_ms[i];
+    count[i] = ctx->prof_n[i];
+  }
+  return OIT_OK;
+}
+
+const char* oit_status_string(int status) {
+  switch (status) {
+    case OIT_OK: return "ok";
+    case OIT_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case OIT_ERR_UNSUPPORTED: return "unsupported configuration";
+    case OIT_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case OIT_ERR_CUDA: return "CUDA error";
+    case OIT_ERR_DEVICE: return "device error flag raised";
+    case OIT_ERR_STATE: return "call out of order";
+    default: return "unknown status";
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,601 @@
+// Tile rasteriser + per-algorithm A-buffer construction.
+//
+// One CTA per 16x16 tile, one warp per 8x4 micro-tile, one lane per pixel.
+// Each warp walks its tile's triangle list (primitive order, from the bins) in
+// chunks of 32: a ballot keeps the triangles whose bbox touches the micro-tile,
+// then every kept triangle is rasterised against the warp's 32 pixels (and
+// their MSAA samples). A covered pixel's lane runs the algorithm's fragment
+// body (the COLOR/DEPTH shader of the reference) on that pixel's state, so
+// every pixel sees its fragments in primitive order -- the order the
+// reference's hardware blender guarantees for tail blending and the order
+// ordered interlock guarantees for its critical section. Per-pixel k-buffers
+// live in shared memory or registers; the A-buffer, aux images and the
+// tail-blended colour target are written to HBM once, at the end.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "oit_device.cuh"
+
+namespace oitd {
+
+using oit::RasterParams;
+
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr unsigned long long kEmpty64 = 0xFFFFFFFFFFFFFFFFull;
+
+// A transparent fragment as the fragment shaders see it.
+struct Frag {
+  uint32_t packed;  // packUnorm4x8(unPremultLinearToSRGB(shading))
+  uint32_t depth;   // floatBitsToUint(gl_FragCoord.z)
+  uint32_t cover;   // samples covered after early depth (gl_SampleMaskIn with post_depth_coverage)
+  float r, g, b, a; // shading(): linear, unpremultiplied
+  float view_z;     // Interpolants::depth
+};
+
+template <int S>
+struct PixelTargets {
+  uint32_t depth[S];  // opaque depth per sample
+  float4 col[S];      // colour target per sample (premultiplied linear)
+
+  __device__ __forceinline__ void tail(const float4& src, uint32_t cover) {
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+      if (cover & (1u << s)) rop_over(col[s], src);
+  }
+};
+
+__device__ __forceinline__ float4 premult(float r, float g, float b, float a) {
+  return make_float4(r * a, g * a, b * a, a);
+}
+
+// ---------------------------------------------------------------------------
+// Policies. Each provides: kPasses, kShade (needs colour), kViewZ,
+// smem_bytes_per_warp(L, coverage), init, fragment(pass, has, f, ...), flush.
+// ---------------------------------------------------------------------------
+
+// oitSimple.frag.glsl:50-91
+template <int S>
+struct SimplePolicy {
+  static constexpr int kPasses = 1;
+  static constexpr bool kViewZ = false;
+  static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
+  uint32_t count;
+  __device__ void init(const RasterParams&, void*, int, uint32_t) { count = 0; }
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, bool has, const Frag& f, uint32_t pixel,
+                                           PixelTargets<S>& tg) {
+    if (!has) return;
+    const uint32_t old = count++;
+    if (old < (uint32_t)p.L) {
+      const size_t r = (size_t)old * p.P + pixel;
+      if (p.coverage) {
+        reinterpret_cast<uint4*>(p.abuf)[r] = make_uint4(f.packed, f.depth, f.cover, 0u);
+      } else {
+        reinterpret_cast<uint2*>(p.abuf)[r] = make_uint2(f.packed, f.depth);
+      }
+    } else if (p.tail) {
+      tg.tail(premult(f.r, f.g, f.b, f.a), f.cover);
+    }
+  }
+  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
+    if (valid) p.aux[pixel] = count;
+  }
+};
+
+// oitLinkedList.frag.glsl:51-85. The node counter is a global atomic,
+// aggregated per warp: one atomicAdd per (triangle, micro-tile) hands out
+// consecutive node indices to the covered lanes in lane order.
+template <int S>
+struct LinkedListPolicy {
+  static constexpr int kPasses = 1;
+  static constexpr bool kViewZ = false;
+  static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
+  uint32_t head;
+  __device__ void init(const RasterParams&, void*, int, uint32_t) { head = 0; }
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, bool has, const Frag& f, uint32_t,
+                                           PixelTargets<S>& tg) {
+    const uint32_t m = __ballot_sync(kFull, has);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(p.counter, (uint32_t)__popc(m));
+    base = __shfl_sync(kFull, base, leader);
+    if (!has) return;
+    const uint32_t newOffset = base + (uint32_t)__popc(m & ((1u << lane) - 1u)) + 1u;
+    if (newOffset >= p.capacity) {
+      if (p.tail) tg.tail(premult(f.r, f.g, f.b, f.a), f.cover);
+      return;
+    }
+    reinterpret_cast<uint4*>(p.abuf)[newOffset] = make_uint4(f.packed, f.depth, p.coverage ? f.cover : 0u, head);
+    head = newOffset;
+  }
+  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
+    if (valid) p.aux[pixel] = head;
+  }
+};
+
+// oitLoop64.frag.glsl:65-141. The per-pixel k-buffer of 64-bit keys
+// (depth << 32 | rgba8) lives in shared memory, [layer][lane] per warp; the
+// atomicMin insertion loop runs on it in primitive order.
+template <int S>
+struct Loop64Policy {
+  static constexpr int kPasses = 1;
+  static constexpr bool kViewZ = false;
+  static __host__ __device__ size_t smem_bytes_per_warp(int L, int) { return (size_t)L * 32 * 8; }
+  unsigned long long* kb;
+  int lane;
+  __device__ void init(const RasterParams& p, void* smem, int, uint32_t) {
+    lane = threadIdx.x & 31;
+    kb = reinterpret_cast<unsigned long long*>(smem);
+    for (int i = 0; i < p.L; ++i) kb[i * 32 + lane] = kEmpty64;
+  }
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, bool has, const Frag& f, uint32_t,
+                                           PixelTargets<S>& tg) {
+    if (!has) return;
+    const int L = p.L;
+    unsigned long long zcur = ((unsigned long long)f.depth << 32) | f.packed;
+    bool evict = true;
+    if (!(zcur > kb[(L - 1) * 32 + lane])) {
+      int i = (zcur > kb[(L / 2) * 32 + lane]) ? (L / 2) : 0;
+      for (; i < L; ++i) {
+        const unsigned long long ztest = kb[i * 32 + lane];
+        if (zcur < ztest) kb[i * 32 + lane] = zcur;
+        if (ztest == kEmpty64) {
+          evict = false;
+          break;
+        }
+        zcur = ztest > zcur ? ztest : zcur;
+      }
+    }
+    if (evict && p.tail) tg.tail(decode_premult((uint32_t)zcur), f.cover);
+  }
+  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
+    if (!valid) return;
+    unsigned long long* ab = reinterpret_cast<unsigned long long*>(p.abuf);
+    for (int i = 0; i < p.L; ++i) ab[(size_t)i * p.P + pixel] = kb[i * 32 + lane];
+  }
+};
+
+// oitLoop.frag.glsl:57-100 (DEPTH pass 0) and 120-173 (COLOR pass 1). Both
+// passes walk the same triangle list; the sorted depths stay in shared memory
+// between them.
+template <int S>
+struct LoopPolicy {
+  static constexpr int kPasses = 2;
+  static constexpr bool kViewZ = false;
+  static __host__ __device__ size_t smem_bytes_per_warp(int L, int) { return (size_t)L * 32 * 8; }
+  uint32_t* dep;
+  uint32_t* col;
+  int lane;
+  __device__ void init(const RasterParams& p, void* smem, int, uint32_t) {
+    lane = threadIdx.x & 31;
+    dep = reinterpret_cast<uint32_t*>(smem);
+    col = dep + p.L * 32;
+    for (int i = 0; i < p.L; ++i) {
+      dep[i * 32 + lane] = 0xFFFFFFFFu;
+      col[i * 32 + lane] = 0u;
+    }
+  }
+  __device__ __forceinline__ void fragment(const RasterParams& p, int pass, bool has, const Frag& f, uint32_t,
+                                           PixelTargets<S>& tg) {
+    if (!has) return;
+    const int L = p.L;
+    uint32_t zcur = f.depth;
+    if (pass == 0) {
+      if (zcur > dep[(L - 1) * 32 + lane]) return;
+      int i = (zcur > dep[(L / 2) * 32 + lane]) ? (L / 2) : 0;
+      for (; i < L; ++i) {
+        const uint32_t ztest = dep[i * 32 + lane];
+        if (zcur < ztest) dep[i * 32 + lane] = zcur;
+        if (ztest == 0xFFFFFFFFu || ztest == zcur) break;
+        zcur = ztest > zcur ? ztest : zcur;
+      }
+    } else {
+      if (dep[(L - 1) * 32 + lane] < zcur) {
+        if (p.tail) tg.tail(premult(f.r, f.g, f.b, f.a), f.cover);
+        return;
+      }
+      int start = 0, end = L - 1;
+      while (start < end) {
+        const int mid = (start + end) / 2;
+        if (dep[mid * 32 + lane] < zcur) start = mid + 1; else end = mid;
+      }
+      col[start * 32 + lane] = f.packed;
+    }
+  }
+  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
+    if (!valid) return;
+    for (int i = 0; i < p.L; ++i) {
+      p.abuf[(size_t)i * p.P + pixel] = dep[i * 32 + lane];
+      p.abuf[(size_t)(p.L + i) * p.P + pixel] = col[i * 32 + lane];
+    }
+  }
+};
+
+// oitSpinlock.frag.glsl:49-129 / oitInterlock.frag.glsl:90-152. The pixel's
+// owner lane is its critical section: no lock is needed because no other
+// thread ever touches the pixel, and fragments arrive in primitive order.
+template <int S>
+struct LockPolicy {
+  static constexpr int kPasses = 1;
+  static constexpr bool kViewZ = false;
+  static __host__ __device__ size_t smem_bytes_per_warp(int L, int coverage) {
+    return (size_t)L * 32 * (coverage ? 16 : 8);
+  }
+  uint32_t count, auxdepth;
+  uint32_t* rec;  // [layer][lane] x words
+  int lane, words;
+  __device__ void init(const RasterParams& p, void* smem, int, uint32_t) {
+    lane = threadIdx.x & 31;
+    words = p.coverage ? 4 : 2;
+    rec = reinterpret_cast<uint32_t*>(smem);
+    count = 0;
+    auxdepth = 0xFFFFFFFFu;
+  }
+  __device__ __forceinline__ uint32_t* slot(int i) const { return rec + ((size_t)i * 32 + lane) * words; }
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, bool has, const Frag& f, uint32_t,
+                                           PixelTargets<S>& tg) {
+    if (!has) return;
+    const int L = p.L;
+    float4 out = premult(f.r, f.g, f.b, f.a);
+    if (f.depth <= auxdepth) {
+      const uint32_t old = count++;
+      if (old < (uint32_t)L) {
+        uint32_t* r = slot((int)old);
+        r[0] = f.packed;
+        r[1] = f.depth;
+        if (words == 4) {
+          r[2] = f.cover;
+          r[3] = 0u;
+        }
+        out = make_float4(0.f, 0.f, 0.f, 0.f);
+      } else {
+        int furthest = 0;
+        uint32_t maxDepth = 0;
+        for (int i = 0; i < L; ++i) {
+          const uint32_t d = slot(i)[1];
+          if (d > maxDepth) {
+            maxDepth = d;
+            furthest = i;
+          }
+        }
+        if (maxDepth > f.depth) {
+          uint32_t* r = slot(furthest);
+          out = decode_premult(r[0]);
+          r[0] = f.packed;
+          r[1] = f.depth;
+          if (words == 4) {
+            r[2] = f.cover;
+            r[3] = 0u;
+          }
+          auxdepth = maxDepth;
+        }
+      }
+    }
+    if (p.tail) tg.tail(out, f.cover);
+  }
+  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
+    if (!valid) return;
+    p.aux[pixel] = count;
+    p.auxdepth[pixel] = auxdepth;
+    const int n = count < (uint32_t)p.L ? (int)count : p.L;
+    for (int i = 0; i < n; ++i) {
+      const uint32_t* r = slot(i);
+      const size_t o = (size_t)i * p.P + pixel;
+      if (words == 4) {
+        reinterpret_cast<uint4*>(p.abuf)[o] = make_uint4(r[0], r[1], r[2], r[3]);
+      } else {
+        reinterpret_cast<uint2*>(p.abuf)[o] = make_uint2(r[0], r[1]);
+      }
+    }
+  }
+};
+
+// oitWeighted.frag.glsl:53-79 with the blend state of main.cpp:559-577.
+// FP16 mode rounds the accumulators to half after every blend, as an
+// RGBA16F/R16F render target does.
+template <int S>
+struct WeightedPolicy {
+  static constexpr int kPasses = 1;
+  static constexpr bool kViewZ = true;
+  static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
+  float4 acc[S];
+  float rev[S];
+  __device__ void init(const RasterParams&, void*, int, uint32_t) {
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      acc[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+      rev[s] = 1.0f;
+    }
+  }
+  static __device__ __forceinline__ float h(float x) { return __half2float(__float2half_rn(x)); }
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, bool has, const Frag& f, uint32_t,
+                                           PixelTargets<S>&) {
+    if (!has) return;
+    const float4 c = premult(f.r, f.g, f.b, f.a);
+    const float depthZ = -f.view_z * 10.0f;
+    const float x = depthZ / 200.0f;
+    const float x2 = x * x;
+    float distWeight = 0.03f / (1e-5f + x2 * x2);
+    distWeight = fminf(fmaxf(distWeight, 1e-2f), 3e3f);
+    float aw = fminf(1.0f, fmaxf(fmaxf(c.x, c.y), fmaxf(c.z, c.w)) * 40.0f + 0.01f);
+    aw *= aw;
+    const float w = aw * distWeight;
+    const float4 src = make_float4(c.x * w, c.y * w, c.z * w, c.w * w);
+    const bool fp16 = !p.weighted_fp32;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      if (!(f.cover & (1u << s))) continue;
+      if (fp16) {
+        acc[s].x = h(acc[s].x + h(src.x));
+        acc[s].y = h(acc[s].y + h(src.y));
+        acc[s].z = h(acc[s].z + h(src.z));
+        acc[s].w = h(acc[s].w + h(src.w));
+        rev[s] = h(rev[s] * (1.0f - h(c.w)));
+      } else {
+        acc[s].x += src.x;
+        acc[s].y += src.y;
+        acc[s].z += src.z;
+        acc[s].w += src.w;
+        rev[s] *= (1.0f - c.w);
+      }
+    }
+  }
+  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
+    if (!valid) return;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const size_t o = (size_t)s * p.P + pixel;
+      if (p.weighted_fp32) {
+        reinterpret_cast<float4*>(p.accum)[o] = acc[s];
+        reinterpret_cast<float*>(p.reveal)[o] = rev[s];
+      } else {
+        __half2 lo = __floats2half2_rn(acc[s].x, acc[s].y);
+        __half2 hi = __floats2half2_rn(acc[s].z, acc[s].w);
+        uint2 v;
+        v.x = *reinterpret_cast<uint32_t*>(&lo);
+        v.y = *reinterpret_cast<uint32_t*>(&hi);
+        reinterpret_cast<uint2*>(p.accum)[o] = v;
+        reinterpret_cast<__half*>(p.reveal)[o] = __float2half_rn(rev[s]);
+      }
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// The kernel.
+// ---------------------------------------------------------------------------
+template <template <int> class Policy, int S>
+__global__ void __launch_bounds__(256) k_raster_transparent(RasterParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using Pol = Policy<S>;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int tile = blockIdx.x;
+  const int tx = tile % p.tiles_x, ty = tile / p.tiles_x;
+  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
+  const int rx1 = rx0 + 7, ry1 = ry0 + 3;
+  const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
+  const bool valid = px < p.RW && py < p.RH;
+  const uint32_t pixel = valid ? (uint32_t)py * (uint32_t)p.RW + (uint32_t)px : 0u;
+
+  PixelTargets<S> tg;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    if (p.has_opaque && valid) {
+      tg.depth[s] = p.depth[(size_t)s * p.P + pixel];
+      tg.col[s] = p.opaque_color[(size_t)s * p.P + pixel];
+    } else {
+      tg.depth[s] = 0x3F800000u;  // 1.0f
+      tg.col[s] = p.background;
+    }
+  }
+  Pol pol;
+  void* wsmem = smem_raw + (size_t)warp * Pol::smem_bytes_per_warp(p.L, p.coverage);
+  pol.init(p, wsmem, lane, pixel);
+
+  const uint32_t beg = p.tile_begin[tile], end = p.tile_end[tile];
+  const TriSetup* __restrict__ setup = reinterpret_cast<const TriSetup*>(p.setup);
+  uint32_t nfrag = 0;
+
+  for (int pass = 0; pass < Pol::kPasses; ++pass) {
+    for (uint32_t base = beg; base < end; base += 32) {
+      const uint32_t i = base + lane;
+      uint32_t t = 0;
+      uint2 bb = make_uint2(0u, 0u);
+      bool hit = false;
+      if (i < end) {
+        t = __ldg(&p.tile_tris[i]);
+        bb = __ldg(&p.bbox[t]);
+        const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = bb.y >> 16;
+        hit = !(bx1 < rx0 || bx0 > rx1 || by1 < ry0 || by0 > ry1);
+      }
+      uint32_t m = __ballot_sync(kFull, hit);
+      while (m) {
+        const int j = __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t tj = __shfl_sync(kFull, t, j);
+        const uint32_t bbx = __shfl_sync(kFull, bb.x, j), bby = __shfl_sync(kFull, bb.y, j);
+        const bool inb = valid && px >= (int)(bbx & 0xFFFF) && px <= (int)(bby & 0xFFFF) &&
+                         py >= (int)(bbx >> 16) && py <= (int)(bby >> 16);
+        const TriSetup* T = setup + tj;
+        const int4 a = T->xy01, b = T->xy2f;
+        const float4 zc = T->zc;
+        uint32_t cover = 0;
+        Edges ec = {0, 0, 0};
+        float zcen = 0.f;
+        if (inb) {
+          const int bxp = px * 256, byp = py * 256;
+#pragma unroll
+          for (int s = 0; s < S; ++s) {
+            const int2 sp = sample_pos<S>(s);
+            const Edges e = edges_at(a, b, bxp + sp.x, byp + sp.y);
+            if (inside(e, b.z)) {
+              const float z = depth_at(zc, e);
+              if (__float_as_uint(z) < tg.depth[s]) cover |= 1u << s;
+              if (S == 1) {
+                ec = e;
+                zcen = z;
+              }
+            }
+          }
+          if (S > 1 && cover) {
+            ec = edges_at(a, b, bxp + 128, byp + 128);
+            zcen = depth_at(zc, ec);
+          }
+        }
+        const bool has = cover != 0;
+        if (!__any_sync(kFull, has)) continue;
+        Frag f;
+        f.cover = cover;
+        f.depth = __float_as_uint(zcen);
+        if (has && (Pol::kPasses == 1 || pass == Pol::kPasses - 1)) {
+          const Shade sh = shade<Pol::kViewZ>(T, ec, zc.w);
+          f.r = sh.r;
+          f.g = sh.g;
+          f.b = sh.b;
+          f.a = T->q.w;
+          f.view_z = sh.view_z;
+          f.packed = pack_rgba8(sh, (uint32_t)b.w);
+          if (pass == Pol::kPasses - 1) ++nfrag;
+        }
+        pol.fragment(p, pass, has, f, pixel, tg);
+      }
+    }
+  }
+
+  pol.flush(p, valid, pixel);
+  if (valid && p.color) {
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      c.x += tg.col[s].x;
+      c.y += tg.col[s].y;
+      c.z += tg.col[s].z;
+      c.w += tg.col[s].w;
+    }
+    const float k = 1.0f / (float)S;
+    p.color[pixel] = make_float4(c.x * k, c.y * k, c.z * k, c.w * k);
+  }
+  // fragment statistics: one atomic per warp
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nfrag += __shfl_xor_sync(kFull, nfrag, o);
+  if (lane == 0 && nfrag && p.frag_count) atomicAdd(p.frag_count, (unsigned long long)nfrag);
+}
+
+// Opaque pass: opaque.frag.glsl:30-35, depth LESS with write (main.cpp:542-547).
+template <int S>
+__global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int tile = blockIdx.x;
+  const int tx = tile % p.tiles_x, ty = tile / p.tiles_x;
+  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
+  const int rx1 = rx0 + 7, ry1 = ry0 + 3;
+  const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
+  const bool valid = px < p.RW && py < p.RH;
+  const uint32_t pixel = valid ? (uint32_t)py * (uint32_t)p.RW + (uint32_t)px : 0u;
+  uint32_t dep[S];
+  float4 col[S];
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    dep[s] = valid ? p.depth[(size_t)s * p.P + pixel] : 0x3F800000u;
+    col[s] = valid ? p.opaque_color[(size_t)s * p.P + pixel] : p.background;
+  }
+  const uint32_t beg = p.tile_begin[tile], end = p.tile_end[tile];
+  const TriSetup* __restrict__ setup = reinterpret_cast<const TriSetup*>(p.setup);
+  for (uint32_t base = beg; base < end; base += 32) {
+    const uint32_t i = base + lane;
+    uint32_t t = 0;
+    uint2 bb = make_uint2(0u, 0u);
+    bool hit = false;
+    if (i < end) {
+      t = __ldg(&p.tile_tris[i]);
+      bb = __ldg(&p.bbox[t]);
+      const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = bb.y >> 16;
+      hit = !(bx1 < rx0 || bx0 > rx1 || by1 < ry0 || by0 > ry1);
+    }
+    uint32_t m = __ballot_sync(kFull, hit);
+    while (m) {
+      const int j = __ffs(m) - 1;
+      m &= m - 1;
+      const uint32_t tj = __shfl_sync(kFull, t, j);
+      const uint32_t bbx = __shfl_sync(kFull, bb.x, j), bby = __shfl_sync(kFull, bb.y, j);
+      const bool inb = valid && px >= (int)(bbx & 0xFFFF) && px <= (int)(bby & 0xFFFF) &&
+                       py >= (int)(bbx >> 16) && py <= (int)(bby >> 16);
+      if (!inb) continue;  // no warp-collective operation follows in this iteration
+      const TriSetup* T = setup + tj;
+      const int4 a = T->xy01, b = T->xy2f;
+      const float4 zc = T->zc;
+      const int bxp = px * 256, byp = py * 256;
+      uint32_t pass = 0;
+      uint32_t zs[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int2 sp = sample_pos<S>(s);
+        const Edges e = edges_at(a, b, bxp + sp.x, byp + sp.y);
+        zs[s] = 0u;
+        if (inside(e, b.z)) {
+          const uint32_t z = __float_as_uint(depth_at(zc, e));
+          zs[s] = z;
+          if (z < dep[s]) pass |= 1u << s;
+        }
+      }
+      if (!pass) continue;
+      const Edges ec = edges_at(a, b, bxp + 128, byp + 128);
+      const Shade sh = shade<false>(T, ec, zc.w);
+      const float4 c = make_float4(sh.r, sh.g, sh.b, 1.0f);
+#pragma unroll
+      for (int s = 0; s < S; ++s)
+        if (pass & (1u << s)) {
+          dep[s] = zs[s];
+          col[s] = c;
+        }
+    }
+  }
+  if (valid) {
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      p.depth[(size_t)s * p.P + pixel] = dep[s];
+      p.opaque_color[(size_t)s * p.P + pixel] = col[s];
+    }
+  }
+}
+
+}  // namespace oitd
+
+namespace oitd {
+
+template <template <int> class Pol, int S>
+cudaError_t launch_transparent_s(const RasterParams& p, cudaStream_t s) {
+  const size_t smem = (size_t)oit::kWarpsPerTile * Pol<S>::smem_bytes_per_warp(p.L, p.coverage);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_raster_transparent<Pol, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  k_raster_transparent<Pol, S><<<(unsigned)(p.tiles_x * p.tiles_y), 256, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+template <template <int> class Pol>
+cudaError_t launch_transparent(const RasterParams& p, cudaStream_t s) {
+  switch (p.S) {
+    case 1: return launch_transparent_s<Pol, 1>(p, s);
+    case 4: return launch_transparent_s<Pol, 4>(p, s);
+    case 8: return launch_transparent_s<Pol, 8>(p, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+inline cudaError_t launch_opaque(const RasterParams& p, cudaStream_t s) {
+  const unsigned grid = (unsigned)(p.tiles_x * p.tiles_y);
+  switch (p.S) {
+    case 1: k_raster_opaque<1><<<grid, 256, 0, s>>>(p); break;
+    case 4: k_raster_opaque<4><<<grid, 256, 0, s>>>(p); break;
+    case 8: k_raster_opaque<8><<<grid, 256, 0, s>>>(p); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace oitd

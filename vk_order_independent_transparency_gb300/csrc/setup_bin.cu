@@ -1,0 +1,457 @@
+// Triangle setup and order-preserving tile binning.
+//
+// The reference hands its triangles to the fixed-function pipeline
+// (vkCmdDrawIndexed in oitRender.cpp:185, 226, 275, 287, 321, 367, 413), which
+// runs object.vert.glsl and rasterises them while keeping primitive order for
+// blending. Here the same work is split into:
+//   k_setup       one thread per triangle: transform, cull, snap to 1/256 px,
+//                 bbox, interpolation constants (the raster specification);
+//   scan + emit   one (tile, triangle) pair per 16x16 tile the bbox touches,
+//                 written in triangle order;
+//   radix sort    stable LSD sort of the pairs by tile id, so every tile's list
+//                 keeps primitive order;
+//   k_ranges      begin/end of each tile's list.
+#include <algorithm>
+#include <cstdio>
+
+#include "oit_device.cuh"
+#include "oit_internal.h"
+
+namespace oit {
+using namespace oitd;
+
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;  // 4096 elements per block
+constexpr int kRadixThreads = 256;
+constexpr int kRadixRounds = 16;
+constexpr int kRadixTile = kRadixThreads * kRadixRounds;  // 4096 pairs per block
+constexpr int kRadixBits = 8;
+constexpr int kRadixBins = 1 << kRadixBits;
+
+// ---------------------------------------------------------------------------
+// Setup (object.vert.glsl:32-39 + viewport transform + triangle setup)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.num_triangles) return;
+  const uint32_t tg = p.first_triangle + t;
+  const float* __restrict__ vtx = p.vertices;
+  const uint32_t i0 = __ldg(&p.indices[3 * (size_t)tg + 0]);
+  const uint32_t i1 = __ldg(&p.indices[3 * (size_t)tg + 1]);
+  const uint32_t i2 = __ldg(&p.indices[3 * (size_t)tg + 2]);
+  const uint32_t vid[3] = {i0, i1, i2};
+  float cx[3], cy[3], cz[3], cw[3], vz[3], nx[3], ny[3], nz[3];
+  const float* m = p.proj_view.m;
+  const float* v = p.view.m;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float* pv = vtx + 10 * (size_t)vid[k];
+    const float x = __ldg(pv + 0), y = __ldg(pv + 1), z = __ldg(pv + 2);
+    cx[k] = __fmaf_rn(m[0], x, __fmaf_rn(m[4], y, __fmaf_rn(m[8], z, m[12])));
+    cy[k] = __fmaf_rn(m[1], x, __fmaf_rn(m[5], y, __fmaf_rn(m[9], z, m[13])));
+    cz[k] = __fmaf_rn(m[2], x, __fmaf_rn(m[6], y, __fmaf_rn(m[10], z, m[14])));
+    cw[k] = __fmaf_rn(m[3], x, __fmaf_rn(m[7], y, __fmaf_rn(m[11], z, m[15])));
+    vz[k] = __fmaf_rn(v[2], x, __fmaf_rn(v[6], y, __fmaf_rn(v[10], z, v[14])));
+    nx[k] = __ldg(pv + 3);
+    ny[k] = __ldg(pv + 4);
+    nz[k] = __ldg(pv + 5);
+  }
+  uint32_t pairs = 0;
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (!(cw[k] > 0.0f) || !(cz[k] >= 0.0f) || !(cz[k] <= cw[k])) ok = false;
+  int X[3], Y[3];
+  float zz[3], q[3];
+  if (ok) {
+    const float halfW = 0.5f * (float)p.RW, halfH = 0.5f * (float)p.RH;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      q[k] = __fdiv_rn(1.0f, cw[k]);
+      const float ndx = __fmul_rn(cx[k], q[k]), ndy = __fmul_rn(cy[k], q[k]);
+      zz[k] = __fmul_rn(cz[k], q[k]);
+      const float sx = __fmaf_rn(ndx, halfW, halfW), sy = __fmaf_rn(ndy, halfH, halfH);
+      if (!(fabsf(sx) < 16384.0f) || !(fabsf(sy) < 16384.0f)) ok = false;
+      X[k] = __float2int_rn(__fmul_rn(sx, 256.0f));
+      Y[k] = __float2int_rn(__fmul_rn(sy, 256.0f));
+    }
+  }
+  long long area = 0;
+  if (ok) {
+    area = (long long)(X[1] - X[0]) * (long long)(Y[2] - Y[0]) - (long long)(Y[1] - Y[0]) * (long long)(X[2] - X[0]);
+    if (area == 0) ok = false;
+    // area > 0: clockwise on the y-down framebuffer = back face for
+    // VK_FRONT_FACE_COUNTER_CLOCKWISE (main.cpp:520-525).
+    if (area > 0 && p.cull_back) ok = false;
+  }
+  int o1 = 1, o2 = 2;
+  if (ok && area < 0) {
+    area = -area;
+    o1 = 2;
+    o2 = 1;
+  }
+  int bx0 = 0, by0 = 0, bx1 = -1, by1 = -1;
+  int PX[3], PY[3];
+  if (ok) {
+    PX[0] = X[0]; PY[0] = Y[0];
+    PX[1] = X[o1]; PY[1] = Y[o1];
+    PX[2] = X[o2]; PY[2] = Y[o2];
+    const int minX = min(PX[0], min(PX[1], PX[2])), maxX = max(PX[0], max(PX[1], PX[2]));
+    const int minY = min(PY[0], min(PY[1], PY[2])), maxY = max(PY[0], max(PY[1], PY[2]));
+    bx0 = max(minX >> 8, 0);
+    by0 = max(minY >> 8, 0);
+    bx1 = min(maxX >> 8, p.RW - 1);
+    by1 = min(maxY >> 8, p.RH - 1);
+    if (bx0 > bx1 || by0 > by1) ok = false;
+  }
+  int tl = 0;
+  if (ok) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const int a = (i + 1) % 3, b = (i + 2) % 3;
+      const int dx = PX[b] - PX[a], dy = PY[b] - PY[a];
+      if (dy < 0 || (dy == 0 && dx > 0)) tl |= 1 << i;
+    }
+  }
+  // Small triangles: test every sample of the (at most 2x2 pixel) bbox now,
+  // so triangles that cover no sample never reach the bins.
+  if (ok && (bx1 - bx0) <= 1 && (by1 - by0) <= 1) {
+    const int4 a = make_int4(PX[0], PY[0], PX[1], PY[1]);
+    const int4 b = make_int4(PX[2], PY[2], tl, 0);
+    bool any = false;
+    for (int py = by0; py <= by1; ++py)
+      for (int px = bx0; px <= bx1; ++px)
+        for (int s = 0; s < S; ++s) {
+          int2 sp = S == 8 ? sample_pos<8>(s) : (S == 4 ? sample_pos<4>(s) : sample_pos<1>(s));
+          if (inside(edges_at(a, b, px * 256 + sp.x, py * 256 + sp.y), tl)) any = true;
+        }
+    if (!any) ok = false;
+  }
+  if (ok) {
+    const int order[3] = {0, o1, o2};
+    TriSetup T;
+    T.xy01 = make_int4(PX[0], PY[0], PX[1], PY[1]);
+    const float* c0 = vtx + 10 * (size_t)i0;
+    float alpha = __fmaf_rn(__ldg(c0 + 9), p.alpha_width, p.alpha_min);
+    alpha = (alpha > 0.0f) ? alpha : 0.0f;
+    alpha = (alpha < 1.0f) ? alpha : 1.0f;
+    const int acode = __float2int_rn(__fmul_rn(alpha, 255.0f));
+    T.xy2f = make_int4(PX[2], PY[2], tl, acode);
+    const float z0 = zz[0], z1 = zz[order[1]], z2 = zz[order[2]];
+    T.zc = make_float4(z0, __fsub_rn(z1, z0), __fsub_rn(z2, z0), __fdiv_rn(1.0f, __ll2float_rn(area)));
+    const float q0 = q[0], q1 = q[order[1]], q2 = q[order[2]];
+    T.q = make_float4(q0, q1, q2, alpha);
+    T.n0 = make_float4(__fmul_rn(nx[0], q0), __fmul_rn(ny[0], q0), __fmul_rn(nz[0], q0), __fmul_rn(vz[0], q0));
+    const int j1 = order[1], j2 = order[2];
+    T.n1 = make_float4(__fmul_rn(nx[j1], q1), __fmul_rn(ny[j1], q1), __fmul_rn(nz[j1], q1), __fmul_rn(vz[j1], q1));
+    T.n2 = make_float4(__fmul_rn(nx[j2], q2), __fmul_rn(ny[j2], q2), __fmul_rn(nz[j2], q2), __fmul_rn(vz[j2], q2));
+    T.col = make_float4(__ldg(c0 + 6), __ldg(c0 + 7), __ldg(c0 + 8), 0.0f);
+    reinterpret_cast<TriSetup*>(p.setup)[t] = T;
+    p.bbox[t] = make_uint2((uint32_t)bx0 | ((uint32_t)by0 << 16), (uint32_t)bx1 | ((uint32_t)by1 << 16));
+    const int tx0 = bx0 / kTile, tx1 = bx1 / kTile, ty0 = by0 / kTile, ty1 = by1 / kTile;
+    pairs = (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
+  }
+  p.pair_count[t] = pairs;
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan (u32), 4096 elements per block, recursive over block sums.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total, uint32_t* smem) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    uint32_t w = lane < nw ? smem[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    smem[32 + lane] = w;  // inclusive warp prefix
+  }
+  __syncthreads();
+  const uint32_t warp_prefix = warp ? smem[32 + warp - 1] : 0u;
+  *total = smem[32 + (blockDim.x >> 5) - 1];
+  __syncthreads();
+  return warp_prefix + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_sums(const uint32_t* __restrict__ in, size_t n,
+                                                            uint32_t* __restrict__ sums) {
+  __shared__ uint32_t smem[64];
+  const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i)
+    if (base + i < n) s += in[base + i];
+  uint32_t total;
+  block_exclusive_scan(s, &total, smem);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                             size_t n, const uint32_t* __restrict__ offsets,
+                                                             uint32_t* __restrict__ grand_total) {
+  __shared__ uint32_t smem[64];
+  const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = (base + i < n) ? in[base + i] : 0u;
+    s += v[i];
+  }
+  uint32_t total;
+  uint32_t pre = block_exclusive_scan(s, &total, smem) + (offsets ? offsets[blockIdx.x] : 0u);
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i < n) out[base + i] = pre;
+    pre += v[i];
+  }
+  if (grand_total && blockIdx.x == gridDim.x - 1 && threadIdx.x == kScanThreads - 1) *grand_total = pre;
+}
+
+size_t blocks_for(size_t n) { return (n + kScanTile - 1) / kScanTile; }
+
+// Exclusive scan of n u32 values; grand_total (device, may be null) receives the sum.
+cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, size_t n, uint32_t* tmp, uint32_t* grand_total,
+                           cudaStream_t s, uint64_t* launches) {
+  if (n == 0) {
+    if (grand_total) return cudaMemsetAsync(grand_total, 0, 4, s);
+    return cudaSuccess;
+  }
+  const size_t nb = blocks_for(n);
+  if (nb == 1) {
+    k_scan_apply<<<1, kScanThreads, 0, s>>>(in, out, n, nullptr, grand_total);
+    ++*launches;
+    return cudaGetLastError();
+  }
+  uint32_t* sums = tmp;
+  uint32_t* rest = tmp + nb;
+  k_scan_sums<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, sums);
+  ++*launches;
+  cudaError_t e = scan_exclusive(sums, sums, nb, rest, nullptr, s, launches);
+  if (e != cudaSuccess) return e;
+  k_scan_apply<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, sums, grand_total);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Pair emission: pair j of triangle t lands at pair_offset[t] + j.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_emit(const uint32_t* __restrict__ pair_count,
+                                              const uint32_t* __restrict__ pair_offset, const uint2* __restrict__ bbox,
+                                              uint32_t n, int tiles_x, uint32_t tile_base,
+                                              uint32_t* __restrict__ keys, uint32_t* __restrict__ tris,
+                                              size_t capacity, uint32_t* err) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const uint32_t c = pair_count[t];
+  if (!c) return;
+  const uint32_t off = pair_offset[t];
+  const uint2 bb = bbox[t];
+  const int tx0 = (bb.x & 0xFFFF) / kTile, ty0 = (bb.x >> 16) / kTile;
+  const int tx1 = (bb.y & 0xFFFF) / kTile, ty1 = (bb.y >> 16) / kTile;
+  uint32_t j = 0;
+  for (int ty = ty0; ty <= ty1; ++ty)
+    for (int tx = tx0; tx <= tx1; ++tx, ++j) {
+      const size_t pos = (size_t)off + j;
+      if (pos >= capacity) {
+        atomicOr(err, 1u);
+        return;
+      }
+      keys[pos] = tile_base + (uint32_t)(ty * tiles_x + tx);
+      tris[pos] = t;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort of (key, value) pairs, 8-bit digits.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t* __restrict__ keys, size_t n, int shift,
+                                                              uint32_t* __restrict__ hist, uint32_t nblk) {
+  __shared__ uint32_t h[kRadixBins];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const size_t base = (size_t)blockIdx.x * kRadixTile;
+#pragma unroll 4
+  for (int r = 0; r < kRadixRounds; ++r) {
+    const size_t i = base + (size_t)r * kRadixThreads + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & (kRadixBins - 1)], 1u);
+  }
+  __syncthreads();
+  hist[(size_t)threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t* __restrict__ keys_in,
+                                                                 const uint32_t* __restrict__ vals_in,
+                                                                 uint32_t* __restrict__ keys_out,
+                                                                 uint32_t* __restrict__ vals_out, size_t n, int shift,
+                                                                 const uint32_t* __restrict__ offsets, uint32_t nblk) {
+  constexpr int kWarps = kRadixThreads / 32;
+  __shared__ uint32_t base[kRadixBins];
+  __shared__ uint32_t running[kRadixBins];
+  __shared__ uint32_t wh[kWarps][kRadixBins];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  base[threadIdx.x] = offsets[(size_t)threadIdx.x * nblk + blockIdx.x];
+  running[threadIdx.x] = 0;
+  const size_t blk = (size_t)blockIdx.x * kRadixTile;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  for (int r = 0; r < kRadixRounds; ++r) {
+#pragma unroll
+    for (int k = 0; k < kRadixBins / 32; ++k) wh[warp][lane + 32 * k] = 0;
+    __syncthreads();
+    const size_t i = blk + (size_t)r * kRadixThreads + threadIdx.x;
+    const bool valid = i < n;
+    uint32_t key = 0, val = 0, d = kRadixBins;
+    if (valid) {
+      key = keys_in[i];
+      val = vals_in[i];
+      d = (key >> shift) & (kRadixBins - 1);
+    }
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t rank = __popc(peers & lt_mask);
+    if (valid && rank == 0) wh[warp][d] = __popc(peers);
+    __syncthreads();
+    {
+      const int dd = threadIdx.x;
+      uint32_t acc = running[dd];
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w) {
+        const uint32_t c = wh[w][dd];
+        wh[w][dd] = acc;
+        acc += c;
+      }
+      running[dd] = acc;
+    }
+    __syncthreads();
+    if (valid) {
+      const uint32_t pos = base[d] + wh[warp][d] + rank;
+      keys_out[pos] = key;
+      vals_out[pos] = val;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) k_ranges(const uint32_t* __restrict__ keys, size_t n,
+                                                uint32_t* __restrict__ begin, uint32_t* __restrict__ end) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = keys[i];
+  if (i == 0 || keys[i - 1] != k) begin[k] = (uint32_t)i;
+  if (i == n - 1 || keys[i + 1] != k) end[k] = (uint32_t)(i + 1);
+}
+
+__global__ void k_fill_u32(uint32_t* dst, uint32_t v, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) dst[i] = v;
+}
+
+__global__ void k_fill_f4(float4* dst, float4 v, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) dst[i] = v;
+}
+
+}  // namespace
+
+size_t scan_scratch_words(size_t n) {
+  size_t words = 0;
+  while (n > 1) {
+    n = blocks_for(n);
+    words += n;
+  }
+  return words + 1;
+}
+
+cudaError_t launch_fill_u32(uint32_t* dst, uint32_t value, size_t count, cudaStream_t s) {
+  if (!count) return cudaSuccess;
+  const unsigned blocks = (unsigned)std::min<size_t>((count + 255) / 256, 152 * 16);
+  k_fill_u32<<<blocks, 256, 0, s>>>(dst, value, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_f4(float4* dst, float4 value, size_t count, cudaStream_t s) {
+  if (!count) return cudaSuccess;
+  const unsigned blocks = (unsigned)std::min<size_t>((count + 255) / 256, 152 * 16);
+  k_fill_f4<<<blocks, 256, 0, s>>>(dst, value, count);
+  return cudaGetLastError();
+}
+
+// Binning, step 1: setup + pair counts + scan. Synchronises once and returns
+// the number of (tile, triangle) pairs in *total_pairs.
+cudaError_t bin_count(const SetupParams& sp, Bins& b, int num_tiles, uint32_t* total_pairs, cudaStream_t s,
+                      uint64_t* launches) {
+  cudaError_t e;
+  const uint32_t n = sp.num_triangles;
+  *total_pairs = 0;
+  if ((e = launch_fill_u32(b.tile_begin, 0u, (size_t)num_tiles, s)) != cudaSuccess) return e;
+  if ((e = launch_fill_u32(b.tile_end, 0u, (size_t)num_tiles, s)) != cudaSuccess) return e;
+  *launches += 2;
+  if (n == 0) return cudaSuccess;
+  k_setup<<<(n + 255) / 256, 256, 0, s>>>(sp, sp.samples > 1 ? sp.samples : 1);
+  ++*launches;
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = scan_exclusive(sp.pair_count, b.pair_offset, n, b.scan_tmp, b.total, s, launches)) != cudaSuccess) return e;
+  uint32_t total = 0;
+  if ((e = cudaMemcpyAsync(&total, b.total, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  *total_pairs = total;
+  return cudaSuccess;
+}
+
+// Binning, step 2: emit pairs in triangle order, stable radix sort by tile,
+// tile ranges. Requires total <= b.capacity and hist/scan scratch sized for it.
+cudaError_t bin_sort(const SetupParams& sp, Bins& b, uint32_t total, int key_bits, uint32_t* error, cudaStream_t s,
+                     uint64_t* launches) {
+  cudaError_t e;
+  const uint32_t n = sp.num_triangles;
+  if (n == 0 || total == 0) return cudaSuccess;
+  k_emit<<<(n + 255) / 256, 256, 0, s>>>(sp.pair_count, b.pair_offset, sp.bbox, n, sp.tiles_x, 0u, b.keys, b.tris,
+                                         b.capacity, error);
+  ++*launches;
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  const uint32_t nblk = (uint32_t)((total + kRadixTile - 1) / kRadixTile);
+  uint32_t *kin = b.keys, *vin = b.tris, *kout = b.keys_alt, *vout = b.tris_alt;
+  for (int shift = 0; shift < key_bits; shift += kRadixBits) {
+    k_radix_hist<<<nblk, kRadixThreads, 0, s>>>(kin, total, shift, b.hist, nblk);
+    ++*launches;
+    if ((e = scan_exclusive(b.hist, b.hist, (size_t)nblk * kRadixBins, b.scan_tmp, nullptr, s, launches)) != cudaSuccess)
+      return e;
+    k_radix_scatter<<<nblk, kRadixThreads, 0, s>>>(kin, vin, kout, vout, total, shift, b.hist, nblk);
+    ++*launches;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+  }
+  if (kin != b.keys) {
+    std::swap(b.keys, b.keys_alt);
+    std::swap(b.tris, b.tris_alt);
+  }
+  k_ranges<<<(total + 255) / 256, 256, 0, s>>>(b.keys, total, b.tile_begin, b.tile_end);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+size_t radix_hist_words(size_t pairs) { return ((pairs + kRadixTile - 1) / kRadixTile) * kRadixBins; }
+
+void srgb_host_tables(float* thr256, float* dec256) {
+  static const float thr[256] = OIT_SRGB_THR_INIT;
+  static const float dec[256] = OIT_SRGB_DEC_INIT;
+  for (int i = 0; i < 256; ++i) {
+    thr256[i] = thr[i];
+    dec256[i] = dec[i];
+  }
+}
+
+}  // namespace oit
