@@ -66,7 +66,7 @@ def test_scene_is_deterministic_and_closed(lib):
     p = v[:, :3].astype(np.float64)
     a, b, c = p[i[:, 0]], p[i[:, 1]], p[i[:, 2]]
     n = np.cross(b - a, c - a)
-    centre = np.repeat(v[::561, :3], 960, axis=0)
+    centre = np.repeat(v[:, :3].reshape(4, 561, 3).mean(axis=1), 960, axis=0)
     out = ((a + b + c) / 3 - centre)
     scale = np.linalg.norm(n, axis=1) * np.linalg.norm(out, axis=1)
     cosang = np.einsum('ij,ij->i', n, out) / np.maximum(scale, 1e-30)

@@ -119,12 +119,13 @@ template <int L>
 __device__ __forceinline__ float4 composite_list(const CompositeParams& p, uint32_t pixel) {
   const uint4* __restrict__ pool = reinterpret_cast<const uint4*>(p.abuf);
   uint32_t off = p.aux[pixel];
+  if (off >= p.capacity) off = 0;
   int n = 0;
   Arr<L> a;
 #pragma unroll
   for (int i = 0; i < L; ++i) {
     a.c[i] = 0; a.d[i] = 0; a.m[i] = 0;
-    if (off != 0) {
+    if (off != 0 && off < p.capacity) {
       const uint4 nd = pool[off];
       a.c[i] = nd.x; a.d[i] = nd.y; a.m[i] = nd.z;
       off = nd.w;
@@ -133,7 +134,10 @@ __device__ __forceinline__ float4 composite_list(const CompositeParams& p, uint3
   }
   bubble_sort<L>(a, n);
   float4 tail = make_float4(0.f, 0.f, 0.f, 0.f);
-  while (off != 0) {
+  // Lists built by the COLOR pass strictly decrease in node index; the bound
+  // only guards against a list that was never built this frame.
+  uint32_t guard = p.capacity;
+  while (off != 0 && off < p.capacity && guard-- != 0) {
     const uint4 nd = pool[off];
     if (p.tail) {
       const uint32_t ev = insertion_sort_tail<L>(a, nd.x, nd.y, nd.z);

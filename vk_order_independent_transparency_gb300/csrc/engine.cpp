@@ -408,6 +408,7 @@ struct oit_context {
     c.coverage = coverage;
     c.record_fp32 = st.record_format == OIT_RECORD_RGBA32F;
     c.weighted_fp32 = st.weighted_precision == OIT_WEIGHTED_FP32;
+    c.capacity = capacity;
     c.abuf = abuf.as<uint32_t>();
     c.aux = aux.as<uint32_t>();
     c.color = color.as<float4>();

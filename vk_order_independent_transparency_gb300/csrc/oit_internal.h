@@ -108,6 +108,7 @@ struct CompositeParams {
   int coverage;
   int record_fp32;
   int weighted_fp32;
+  uint32_t capacity;             // linked-list pool size in nodes (walks are bounded by it)
   const uint32_t* abuf;
   const uint32_t* aux;
   const float4* color;           // [P] (A-buffer algorithms) colour after tail blend
