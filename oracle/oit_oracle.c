@@ -118,6 +118,7 @@ struct or_frame {
   double* reveal;    /* S*P WBOIT revealage */
   const uint32_t* ll_limit;
   uint32_t* ll_stored;
+  uint32_t ll_alloc;
   uint64_t fragments;
 };
 
@@ -187,6 +188,7 @@ void or_clear_transparent(or_frame* f) {
   memset(f->aux, 0, f->E * 4);
   for (size_t i = 0; i < f->E; ++i) f->auxdepth[i] = EMPTY32;
   memset(f->ll_stored, 0, f->E * 4);
+  f->ll_alloc = 0;
   f->counter = 0;
   if (f->p.algorithm == OR_LOOP) {
     for (int s = 0; s < f->ss_layers; ++s)
@@ -462,7 +464,13 @@ static void frag_linkedlist(or_frame* f, size_t pixel, int s, uint32_t cover, co
   size_t e = (size_t)s * f->P + pixel;
   uint32_t newOffset = f->counter++ + 1u;
   int overflow = newOffset >= f->capacity;
-  if (f->ll_limit && f->ll_stored[e] >= f->ll_limit[e]) overflow = 1;
+  if (f->ll_limit) {
+    /* replay: the caller decides how many nodes each element got; nodes are
+     * numbered in this oracle's own order */
+    overflow = f->ll_stored[e] >= f->ll_limit[e];
+    if (!overflow) newOffset = ++f->ll_alloc;
+    if (newOffset >= f->capacity) overflow = 1;
+  }
   if (overflow) {
     if (f->p.tail_blend) tail_out(f, pixel, s, cover, premult_float(fr->rgba));
     return;
@@ -596,7 +604,7 @@ static void frag_weighted(or_frame* f, size_t pixel, uint32_t cover, const frag_
 }
 
 static void dispatch_fragment(or_frame* f, size_t pixel, int s, uint32_t cover, const frag_t* fr, int loop_pass) {
-  f->fragments++;
+  if (loop_pass == 1) f->fragments++; /* Loop32 sees each fragment twice; count it once */
   switch (f->p.algorithm) {
     case OR_SIMPLE: frag_simple(f, pixel, s, cover, fr); break;
     case OR_LINKEDLIST: frag_linkedlist(f, pixel, s, cover, fr); break;
@@ -629,12 +637,7 @@ void or_inject_fragments(or_frame* f, int n, const int32_t* xy, const int32_t* s
       int s = sample ? sample[i] : 0;
       size_t pixel = (size_t)xy[2 * (size_t)i + 1] * f->RW + (size_t)xy[2 * (size_t)i];
       uint32_t cover = f->p.sample_shading ? (1u << s) : (f->coverage ? m : 1u);
-      if (pass == passes - 1 || f->p.algorithm != OR_LOOP) {
-        dispatch_fragment(f, pixel, f->p.sample_shading ? s : 0, cover, &fr, loop_pass);
-      } else {
-        dispatch_fragment(f, pixel, f->p.sample_shading ? s : 0, cover, &fr, loop_pass);
-        f->fragments--;
-      }
+      dispatch_fragment(f, pixel, f->p.sample_shading ? s : 0, cover, &fr, loop_pass);
     }
   }
 }
