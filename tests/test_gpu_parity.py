@@ -154,3 +154,38 @@ def test_kbuffer_1080p(engine, alg):
     o = pu.render_oracle(alg, W, H, v, i, tpo, sd, 60, oit_layers=L)
     np.testing.assert_array_equal(g['depth'][:W * H], o['depth'][:W * H])
     check(engine, alg, g, o, W, H, L)
+
+
+def big_triangle_mesh(seed=5, n=24):
+    """Hand-built triangles of every size, some far larger than 64 px and some
+    crossing the viewport border (the int64 edge-function path)."""
+    rng = np.random.default_rng(seed)
+    verts, idx = [], []
+    for k in range(n):
+        c = rng.uniform(-1.2, 1.2, 3) * [1, 1, 0.6]
+        size = [0.05, 0.3, 1.5, 3.0][k % 4]
+        col = list(rng.uniform(0, 1, 4))
+        for _ in range(3):
+            p = c + rng.uniform(-size, size, 3) * [1, 1, 0.2]
+            nrm = rng.normal(size=3)
+            nrm /= np.linalg.norm(nrm)
+            verts.append(list(p) + list(nrm) + col)
+        idx.append([3 * k, 3 * k + 1, 3 * k + 2])
+    return np.array(verts, np.float32), np.array(idx, np.uint32)
+
+
+@pytest.mark.parametrize('aa', [0, 4])
+@pytest.mark.parametrize('alg', ALGS)
+def test_large_triangles(engine, alg, aa):
+    W, H, L = 200, 150, 4
+    v, i = big_triangle_mesh()
+    sd = engine.make_camera(W, H)
+    kw = dict(oit_layers=L, nodes_per_pixel=8, aa_type=aa, weighted_precision=engine.OIT_WEIGHTED_FP32)
+    g = pu.render_gpu(alg, W, H, v, i, 1, sd, 100, **kw)
+    o = pu.render_oracle(alg, W, H, v, i, 1, sd, 100, **kw)
+    check(engine, alg, g, o, W, H, L, aa)
+    # opaque half: the first 12 triangles transparent, the rest opaque
+    g = pu.render_gpu(alg, W, H, v, i, 1, sd, 50, **kw)
+    o = pu.render_oracle(alg, W, H, v, i, 1, sd, 50, **kw)
+    np.testing.assert_array_equal(g['depth'], o['depth'])
+    check(engine, alg, g, o, W, H, L, aa)

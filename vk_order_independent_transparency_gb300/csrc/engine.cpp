@@ -81,7 +81,7 @@ struct oit_context {
   float4 background = make_float4(0.2f, 0.2f, 0.2f, 0.2f);
 
   DevBuf depth, opaque_color, color, abuf, aux, auxdepth, counter, accum, reveal, out, out_linear, err, frag;
-  DevBuf bbox, setup, pair_count, pair_offset, scan_tmp, total;
+  DevBuf bbox, setup, persp, pair_count, pair_offset, scan_tmp, total;
   DevBuf keys, tris, keys_alt, tris_alt, hist, tile_begin, tile_end;
   DevBuf mesh_v, mesh_i;
   size_t tri_cap = 0, pair_cap = 0;
@@ -145,7 +145,7 @@ struct oit_context {
     }
     for (cudaEvent_t e : prof_free) cudaEventDestroy(e);
     DevBuf* all[] = {&depth, &opaque_color, &color, &abuf, &aux, &auxdepth, &counter, &accum, &reveal, &out,
-                     &out_linear, &err, &frag, &bbox, &setup, &pair_count, &pair_offset, &scan_tmp, &total,
+                     &out_linear, &err, &frag, &bbox, &setup, &persp, &pair_count, &pair_offset, &scan_tmp, &total,
                      &keys, &tris, &keys_alt, &tris_alt, &hist, &tile_begin, &tile_end, &mesh_v, &mesh_i};
     for (DevBuf* b : all) b->release();
   }
@@ -205,7 +205,8 @@ struct oit_context {
     if (n <= tri_cap) return OIT_OK;
     const size_t cap = std::max<size_t>(n, 1024);
     OIT_TRY_CUDA(bbox.ensure(cap * 8), "alloc bbox");
-    OIT_TRY_CUDA(setup.ensure(cap * 128), "alloc setup");
+    OIT_TRY_CUDA(setup.ensure(cap * 96), "alloc setup");
+    if (alg() == oit::Alg::Weighted) OIT_TRY_CUDA(persp.ensure(cap * 32), "alloc persp");
     OIT_TRY_CUDA(pair_count.ensure(cap * 4), "alloc pair_count");
     OIT_TRY_CUDA(pair_offset.ensure((cap + 1) * 4), "alloc pair_offset");
     tri_cap = cap;
@@ -246,6 +247,7 @@ struct oit_context {
     sp.tiles_x = tiles_x;
     sp.bbox = bbox.as<uint2>();
     sp.setup = setup.p;
+    sp.persp = (alg() == oit::Alg::Weighted && !cull_back) ? persp.p : nullptr;
     sp.pair_count = pair_count.as<uint32_t>();
     return sp;
   }
@@ -304,6 +306,7 @@ struct oit_context {
     p.tile_tris = tris.as<uint32_t>();
     p.bbox = bbox.as<uint2>();
     p.setup = setup.p;
+    p.persp = persp.p;
     p.depth = depth.as<uint32_t>();
     p.opaque_color = opaque_color.as<float4>();
     p.has_opaque = opaque_valid ? 1 : 0;

@@ -34,43 +34,62 @@ __device__ __forceinline__ int2 sample_pos(int s) {
   return make_int2(x[s], y[s]);
 }
 
-// 128-byte triangle setup record, written by the setup kernel and read with
-// broadcast loads by the tile rasteriser.
+// 96-byte triangle setup record, written by the setup kernel and staged into
+// shared memory (cp.async) by the tile rasteriser.
 struct __align__(16) TriSetup {
   int4 xy01;   // X0, Y0, X1, Y1 (1/256 px)
-  int4 xy2f;   // X2, Y2, top-left bits (bit i = edge i), alpha code
+  int4 xy2f;   // X2, Y2, flags (bits 0-2 top-left per edge, bit 3 small, bits 8-15 alpha code), alpha (float bits)
   float4 zc;   // z0, z1 - z0, z2 - z0, 1 / area
-  float4 q;    // 1/w0, 1/w1, 1/w2, alpha
-  float4 n0;   // normal0 / w0 (xyz), view z0 / w0
-  float4 n1;
-  float4 n2;
-  float4 col;  // rgb (linear), unused
+  float4 n0;   // normal0 / w0 (xyz), red
+  float4 n1;   // normal1 / w1 (xyz), green
+  float4 n2;   // normal2 / w2 (xyz), blue
 };
+// Perspective terms used only for the view-space depth of WBOIT.
+struct __align__(16) TriPersp {
+  float4 q;    // 1/w0, 1/w1, 1/w2, 0
+  float4 vzq;  // view z0 / w0, view z1 / w1, view z2 / w2, 0
+};
+constexpr int kFlagSmall = 8;     // bbox extent < 64 px: edge functions fit in int32
+constexpr int kSmallExtent = 1 << 14;
 
 // Edge values at a sample (px, py) in 1/256 pixel units. Edge i is opposite
-// vertex i and runs from vertex (i+1)%3 to (i+2)%3.
-struct Edges {
-  long long e0, e1, e2;
+// vertex i and runs from vertex (i+1)%3 to (i+2)%3. For triangles whose bbox
+// spans less than 2^14 units every product stays below 2^28, so the int32
+// path computes exactly the same values as the int64 one.
+template <typename E>
+struct EdgesT {
+  E e0, e1, e2;
 };
+using Edges = EdgesT<long long>;
 
-__device__ __forceinline__ Edges edges_at(const int4& a, const int4& b, int px, int py) {
-  Edges r;
+template <typename E>
+__device__ __forceinline__ EdgesT<E> edges_at(const int4& a, const int4& b, int px, int py) {
+  EdgesT<E> r;
   const int X0 = a.x, Y0 = a.y, X1 = a.z, Y1 = a.w, X2 = b.x, Y2 = b.y;
-  r.e0 = (long long)(X2 - X1) * (long long)(py - Y1) - (long long)(Y2 - Y1) * (long long)(px - X1);
-  r.e1 = (long long)(X0 - X2) * (long long)(py - Y2) - (long long)(Y0 - Y2) * (long long)(px - X2);
-  r.e2 = (long long)(X1 - X0) * (long long)(py - Y0) - (long long)(Y1 - Y0) * (long long)(px - X0);
+  r.e0 = (E)(X2 - X1) * (E)(py - Y1) - (E)(Y2 - Y1) * (E)(px - X1);
+  r.e1 = (E)(X0 - X2) * (E)(py - Y2) - (E)(Y0 - Y2) * (E)(px - X2);
+  r.e2 = (E)(X1 - X0) * (E)(py - Y0) - (E)(Y1 - Y0) * (E)(px - X0);
   return r;
 }
 
-__device__ __forceinline__ bool inside(const Edges& e, int tl) {
+__device__ __forceinline__ Edges edges_at(const int4& a, const int4& b, int px, int py) {
+  return edges_at<long long>(a, b, px, py);
+}
+
+template <typename E>
+__device__ __forceinline__ bool inside(const EdgesT<E>& e, int tl) {
   return (e.e0 > 0 || (e.e0 == 0 && (tl & 1))) && (e.e1 > 0 || (e.e1 == 0 && (tl & 2))) &&
          (e.e2 > 0 || (e.e2 == 0 && (tl & 4)));
 }
 
+__device__ __forceinline__ float to_float(long long v) { return __ll2float_rn(v); }
+__device__ __forceinline__ float to_float(int v) { return __int2float_rn(v); }
+
 // Window depth at the edge values (screen-linear interpolation), clamped to [0,1].
-__device__ __forceinline__ float depth_at(const float4& zc, const Edges& e) {
-  const float b1 = __fmul_rn(__ll2float_rn(e.e1), zc.w);
-  const float b2 = __fmul_rn(__ll2float_rn(e.e2), zc.w);
+template <typename E>
+__device__ __forceinline__ float depth_at(const float4& zc, const EdgesT<E>& e) {
+  const float b1 = __fmul_rn(to_float(e.e1), zc.w);
+  const float b2 = __fmul_rn(to_float(e.e2), zc.w);
   float z = __fmaf_rn(b2, zc.z, __fmaf_rn(b1, zc.y, zc.x));
   z = (z > 0.0f) ? z : 0.0f;
   z = (z < 1.0f) ? z : 1.0f;
@@ -100,17 +119,18 @@ __device__ __forceinline__ float srgb_decode(uint32_t code) { return __ldg(&g_sr
 
 // Perspective-correct Gooch shading (shaders/shaderCommon.glsl:36-56) at the
 // edge values e; returns linear unpremultiplied rgb, and the interpolated view
-// space z when want_view_z is set.
+// space z when P is given.
 struct Shade {
   float r, g, b, view_z;
 };
 
-template <bool want_view_z>
-__device__ __forceinline__ Shade shade(const TriSetup* __restrict__ T, const Edges& e, float inv_area) {
-  const float b0 = __fmul_rn(__ll2float_rn(e.e0), inv_area);
-  const float b1 = __fmul_rn(__ll2float_rn(e.e1), inv_area);
-  const float b2 = __fmul_rn(__ll2float_rn(e.e2), inv_area);
-  const float4 n0 = T->n0, n1 = T->n1, n2 = T->n2;
+template <typename E>
+__device__ __forceinline__ Shade shade(const TriSetup& T, const EdgesT<E>& e, const TriPersp* P) {
+  const float inv_area = T.zc.w;
+  const float b0 = __fmul_rn(to_float(e.e0), inv_area);
+  const float b1 = __fmul_rn(to_float(e.e1), inv_area);
+  const float b2 = __fmul_rn(to_float(e.e2), inv_area);
+  const float4 n0 = T.n0, n1 = T.n1, n2 = T.n2;
   const float nx = __fmaf_rn(b2, n2.x, __fmaf_rn(b1, n1.x, __fmul_rn(b0, n0.x)));
   const float ny = __fmaf_rn(b2, n2.y, __fmaf_rn(b1, n1.y, __fmul_rn(b0, n0.y)));
   const float nz = __fmaf_rn(b2, n2.z, __fmaf_rn(b1, n1.z, __fmul_rn(b0, n0.z)));
@@ -118,15 +138,14 @@ __device__ __forceinline__ Shade shade(const TriSetup* __restrict__ T, const Edg
   const float d = __fmaf_rn(nz, light_z(), __fmaf_rn(ny, light_y(), __fmul_rn(nx, light_x())));
   const float c = (len2 > 0.0f) ? __fdiv_rn(d, __fsqrt_rn(len2)) : 0.0f;
   const float warmth = __fmaf_rn(c, 0.5f, 0.5f);
-  const float4 col = T->col;
   Shade s;
-  s.r = __fmul_rn(col.x, warmth);
-  s.g = __fmul_rn(col.y, __fmaf_rn(0.75f, warmth, 0.25f));
-  s.b = __fmul_rn(col.z, __fmaf_rn(0.25f, warmth, 0.75f));
+  s.r = __fmul_rn(n0.w, warmth);
+  s.g = __fmul_rn(n1.w, __fmaf_rn(0.75f, warmth, 0.25f));
+  s.b = __fmul_rn(n2.w, __fmaf_rn(0.25f, warmth, 0.75f));
   s.view_z = 0.0f;
-  if (want_view_z) {
-    const float4 q = T->q;
-    const float num = __fmaf_rn(b2, n2.w, __fmaf_rn(b1, n1.w, __fmul_rn(b0, n0.w)));
+  if (P) {
+    const float4 q = P->q, vz = P->vzq;
+    const float num = __fmaf_rn(b2, vz.z, __fmaf_rn(b1, vz.y, __fmul_rn(b0, vz.x)));
     const float den = __fmaf_rn(b2, q.z, __fmaf_rn(b1, q.y, __fmul_rn(b0, q.x)));
     s.view_z = __fdiv_rn(num, den);
   }

@@ -31,7 +31,8 @@ struct SetupParams {
   int tiles_x;
   // outputs
   uint2* bbox;            // [num_triangles] pixel bbox (x0 | y0 << 16, x1 | y1 << 16)
-  void* setup;            // [num_triangles] TriSetup records
+  void* setup;            // [num_triangles] TriSetup records (96 B)
+  void* persp;            // [num_triangles] TriPersp records (32 B, WBOIT only) or null
   uint32_t* pair_count;   // [num_triangles] tiles overlapped (0 = culled)
 };
 
@@ -77,6 +78,7 @@ struct RasterParams {
   const uint32_t* tile_tris;
   const uint2* bbox;
   const void* setup;
+  const void* persp;
   // frame targets
   uint32_t* depth;               // [S][P] opaque depth (read by transparent passes)
   float4* opaque_color;          // [S][P]

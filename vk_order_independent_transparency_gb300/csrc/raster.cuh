@@ -364,72 +364,143 @@ struct WeightedPolicy {
 };
 
 // ---------------------------------------------------------------------------
-// The kernel.
+// Triangle-list walk shared by the transparent and opaque kernels.
+// ---------------------------------------------------------------------------
+struct WarpTile {
+  int lane, px, py, rx0, ry0, rx1, ry1;
+  bool valid;
+  uint32_t pixel;
+};
+
+__device__ __forceinline__ WarpTile warp_tile(const RasterParams& p) {
+  WarpTile w;
+  const int warp = threadIdx.x >> 5;
+  w.lane = threadIdx.x & 31;
+  const int tile = blockIdx.x;
+  const int tx = tile % p.tiles_x, ty = tile / p.tiles_x;
+  w.rx0 = tx * 16 + (warp & 1) * 8;
+  w.ry0 = ty * 16 + (warp >> 1) * 4;
+  w.rx1 = w.rx0 + 7;
+  w.ry1 = w.ry0 + 3;
+  w.px = w.rx0 + (w.lane & 7);
+  w.py = w.ry0 + (w.lane >> 3);
+  w.valid = w.px < p.RW && w.py < p.RH;
+  w.pixel = w.valid ? (uint32_t)w.py * (uint32_t)p.RW + (uint32_t)w.px : 0u;
+  return w;
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+__device__ __forceinline__ bool bbox_hits(uint2 bb, const WarpTile& w) {
+  const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = bb.y >> 16;
+  return !(bx1 < w.rx0 || bx0 > w.rx1 || by1 < w.ry0 || by0 > w.ry1);
+}
+
+// Walks [beg, end) of the tile list in primitive order, 32 entries at a time:
+// the lanes test their triangle's bbox against the warp's micro-tile, the hits
+// copy their setup records into the warp's shared-memory stage in parallel
+// (cp.async), then vis(T, t, inb) runs for each hit in list order. `vis` is
+// warp-uniform: every lane calls it, with inb telling whether the lane's pixel
+// is inside the triangle's pixel bbox.
+template <class Vis>
+__device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile& w, TriSetup* stage, uint32_t beg,
+                                          uint32_t end, Vis&& vis) {
+  const TriSetup* __restrict__ setup = reinterpret_cast<const TriSetup*>(p.setup);
+  const uint32_t lt = (1u << w.lane) - 1u;
+  uint32_t t_next = 0;
+  uint2 bb_next = make_uint2(0xFFFFFFFFu, 0u);  // empty bbox
+  if (beg + w.lane < end) {
+    t_next = __ldg(&p.tile_tris[beg + w.lane]);
+    bb_next = __ldg(&p.bbox[t_next]);
+  }
+  for (uint32_t base = beg; base < end; base += 32) {
+    const uint32_t t = t_next;
+    const uint2 bb = bb_next;
+    const bool hit = (base + w.lane < end) && bbox_hits(bb, w);
+    const uint32_t nb = base + 32;
+    const bool more = nb + w.lane < end;
+    if (more) t_next = __ldg(&p.tile_tris[nb + w.lane]);
+    const uint32_t m = __ballot_sync(kFull, hit);
+    if (hit) {
+      const int slot = __popc(m & lt);
+      const int4* src = reinterpret_cast<const int4*>(setup + t);
+      int4* dst = reinterpret_cast<int4*>(stage + slot);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) cp_async16(dst + k, src + k);
+    }
+    bb_next = more ? __ldg(&p.bbox[t_next]) : make_uint2(0xFFFFFFFFu, 0u);
+    cp_async_wait_all();
+    __syncwarp();
+    uint32_t mm = m;
+    for (int k = 0; mm; ++k) {
+      const int j = __ffs(mm) - 1;
+      mm &= mm - 1;
+      const uint32_t tj = __shfl_sync(kFull, t, j);
+      const uint32_t bbx = __shfl_sync(kFull, bb.x, j), bby = __shfl_sync(kFull, bb.y, j);
+      const bool inb = w.valid && w.px >= (int)(bbx & 0xFFFF) && w.px <= (int)(bby & 0xFFFF) &&
+                       w.py >= (int)(bbx >> 16) && w.py <= (int)(bby >> 16);
+      vis(stage[k], tj, inb);
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Transparent COLOR (+DEPTH) pass.
 // ---------------------------------------------------------------------------
 template <template <int> class Policy, int S>
 __global__ void __launch_bounds__(256) k_raster_transparent(RasterParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using Pol = Policy<S>;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int tile = blockIdx.x;
-  const int tx = tile % p.tiles_x, ty = tile / p.tiles_x;
-  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
-  const int rx1 = rx0 + 7, ry1 = ry0 + 3;
-  const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
-  const bool valid = px < p.RW && py < p.RH;
-  const uint32_t pixel = valid ? (uint32_t)py * (uint32_t)p.RW + (uint32_t)px : 0u;
+  const int warp = threadIdx.x >> 5;
+  const WarpTile w = warp_tile(p);
+  TriSetup* stage = reinterpret_cast<TriSetup*>(smem_raw) + warp * 32;
+  unsigned char* pol_smem = smem_raw + (size_t)oit::kWarpsPerTile * 32 * sizeof(TriSetup);
 
   PixelTargets<S> tg;
 #pragma unroll
   for (int s = 0; s < S; ++s) {
-    if (p.has_opaque && valid) {
-      tg.depth[s] = p.depth[(size_t)s * p.P + pixel];
-      tg.col[s] = p.opaque_color[(size_t)s * p.P + pixel];
+    if (p.has_opaque && w.valid) {
+      tg.depth[s] = p.depth[(size_t)s * p.P + w.pixel];
+      tg.col[s] = p.opaque_color[(size_t)s * p.P + w.pixel];
     } else {
       tg.depth[s] = 0x3F800000u;  // 1.0f
       tg.col[s] = p.background;
     }
   }
   Pol pol;
-  void* wsmem = smem_raw + (size_t)warp * Pol::smem_bytes_per_warp(p.L, p.coverage);
-  pol.init(p, wsmem, lane, pixel);
+  pol.init(p, pol_smem + (size_t)warp * Pol::smem_bytes_per_warp(p.L, p.coverage), w.lane, w.pixel);
 
+  const int tile = blockIdx.x;
   const uint32_t beg = p.tile_begin[tile], end = p.tile_end[tile];
-  const TriSetup* __restrict__ setup = reinterpret_cast<const TriSetup*>(p.setup);
+  const TriPersp* __restrict__ persp = reinterpret_cast<const TriPersp*>(p.persp);
   uint32_t nfrag = 0;
 
   for (int pass = 0; pass < Pol::kPasses; ++pass) {
-    for (uint32_t base = beg; base < end; base += 32) {
-      const uint32_t i = base + lane;
-      uint32_t t = 0;
-      uint2 bb = make_uint2(0u, 0u);
-      bool hit = false;
-      if (i < end) {
-        t = __ldg(&p.tile_tris[i]);
-        bb = __ldg(&p.bbox[t]);
-        const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = bb.y >> 16;
-        hit = !(bx1 < rx0 || bx0 > rx1 || by1 < ry0 || by0 > ry1);
-      }
-      uint32_t m = __ballot_sync(kFull, hit);
-      while (m) {
-        const int j = __ffs(m) - 1;
-        m &= m - 1;
-        const uint32_t tj = __shfl_sync(kFull, t, j);
-        const uint32_t bbx = __shfl_sync(kFull, bb.x, j), bby = __shfl_sync(kFull, bb.y, j);
-        const bool inb = valid && px >= (int)(bbx & 0xFFFF) && px <= (int)(bby & 0xFFFF) &&
-                         py >= (int)(bbx >> 16) && py <= (int)(bby >> 16);
-        const TriSetup* T = setup + tj;
-        const int4 a = T->xy01, b = T->xy2f;
-        const float4 zc = T->zc;
-        uint32_t cover = 0;
-        Edges ec = {0, 0, 0};
-        float zcen = 0.f;
+    const bool shading = Pol::kPasses == 1 || pass == Pol::kPasses - 1;
+    walk_tile(p, w, stage, beg, end, [&](const TriSetup& T, uint32_t tj, bool inb) {
+      const int4 a = T.xy01, b = T.xy2f;
+      const float4 zc = T.zc;
+      uint32_t cover = 0;
+      float zcen = 0.f;
+      Frag f;
+      auto body = [&](auto etag) {
+        using E = decltype(etag);
+        EdgesT<E> ec = {0, 0, 0};
         if (inb) {
-          const int bxp = px * 256, byp = py * 256;
+          const int bxp = w.px * 256, byp = w.py * 256;
 #pragma unroll
           for (int s = 0; s < S; ++s) {
             const int2 sp = sample_pos<S>(s);
-            const Edges e = edges_at(a, b, bxp + sp.x, byp + sp.y);
+            const EdgesT<E> e = edges_at<E>(a, b, bxp + sp.x, byp + sp.y);
             if (inside(e, b.z)) {
               const float z = depth_at(zc, e);
               if (__float_as_uint(z) < tg.depth[s]) cover |= 1u << s;
@@ -440,32 +511,32 @@ __global__ void __launch_bounds__(256) k_raster_transparent(RasterParams p) {
             }
           }
           if (S > 1 && cover) {
-            ec = edges_at(a, b, bxp + 128, byp + 128);
+            ec = edges_at<E>(a, b, bxp + 128, byp + 128);
             zcen = depth_at(zc, ec);
           }
         }
-        const bool has = cover != 0;
-        if (!__any_sync(kFull, has)) continue;
-        Frag f;
-        f.cover = cover;
-        f.depth = __float_as_uint(zcen);
-        if (has && (Pol::kPasses == 1 || pass == Pol::kPasses - 1)) {
-          const Shade sh = shade<Pol::kViewZ>(T, ec, zc.w);
+        if (cover && shading) {
+          const Shade sh = shade(T, ec, Pol::kViewZ ? persp + tj : nullptr);
           f.r = sh.r;
           f.g = sh.g;
           f.b = sh.b;
-          f.a = T->q.w;
           f.view_z = sh.view_z;
-          f.packed = pack_rgba8(sh, (uint32_t)b.w);
-          if (pass == Pol::kPasses - 1) ++nfrag;
+          f.packed = pack_rgba8(sh, (uint32_t)(b.z >> 8) & 255u);
         }
-        pol.fragment(p, pass, has, f, pixel, tg);
-      }
-    }
+      };
+      if (b.z & kFlagSmall) body(int(0)); else body((long long)0);
+      const bool has = cover != 0;
+      if (!__any_sync(kFull, has)) return;
+      f.cover = cover;
+      f.depth = __float_as_uint(zcen);
+      f.a = __int_as_float(b.w);
+      if (has && shading) ++nfrag;
+      pol.fragment(p, pass, has, f, w.pixel, tg);
+    });
   }
 
-  pol.flush(p, valid, pixel);
-  if (valid && p.color) {
+  pol.flush(p, w.valid, w.pixel);
+  if (w.valid && p.color) {
     float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int s = 0; s < S; ++s) {
@@ -475,64 +546,44 @@ __global__ void __launch_bounds__(256) k_raster_transparent(RasterParams p) {
       c.w += tg.col[s].w;
     }
     const float k = 1.0f / (float)S;
-    p.color[pixel] = make_float4(c.x * k, c.y * k, c.z * k, c.w * k);
+    p.color[w.pixel] = make_float4(c.x * k, c.y * k, c.z * k, c.w * k);
   }
   // fragment statistics: one atomic per warp
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) nfrag += __shfl_xor_sync(kFull, nfrag, o);
-  if (lane == 0 && nfrag && p.frag_count) atomicAdd(p.frag_count, (unsigned long long)nfrag);
+  if (w.lane == 0 && nfrag && p.frag_count) atomicAdd(p.frag_count, (unsigned long long)nfrag);
 }
 
+// ---------------------------------------------------------------------------
 // Opaque pass: opaque.frag.glsl:30-35, depth LESS with write (main.cpp:542-547).
+// ---------------------------------------------------------------------------
 template <int S>
 __global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int tile = blockIdx.x;
-  const int tx = tile % p.tiles_x, ty = tile / p.tiles_x;
-  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
-  const int rx1 = rx0 + 7, ry1 = ry0 + 3;
-  const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
-  const bool valid = px < p.RW && py < p.RH;
-  const uint32_t pixel = valid ? (uint32_t)py * (uint32_t)p.RW + (uint32_t)px : 0u;
+  __shared__ TriSetup stage_all[oit::kWarpsPerTile * 32];
+  const int warp = threadIdx.x >> 5;
+  const WarpTile w = warp_tile(p);
+  TriSetup* stage = stage_all + warp * 32;
   uint32_t dep[S];
   float4 col[S];
 #pragma unroll
   for (int s = 0; s < S; ++s) {
-    dep[s] = valid ? p.depth[(size_t)s * p.P + pixel] : 0x3F800000u;
-    col[s] = valid ? p.opaque_color[(size_t)s * p.P + pixel] : p.background;
+    dep[s] = w.valid ? p.depth[(size_t)s * p.P + w.pixel] : 0x3F800000u;
+    col[s] = w.valid ? p.opaque_color[(size_t)s * p.P + w.pixel] : p.background;
   }
-  const uint32_t beg = p.tile_begin[tile], end = p.tile_end[tile];
-  const TriSetup* __restrict__ setup = reinterpret_cast<const TriSetup*>(p.setup);
-  for (uint32_t base = beg; base < end; base += 32) {
-    const uint32_t i = base + lane;
-    uint32_t t = 0;
-    uint2 bb = make_uint2(0u, 0u);
-    bool hit = false;
-    if (i < end) {
-      t = __ldg(&p.tile_tris[i]);
-      bb = __ldg(&p.bbox[t]);
-      const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = bb.y >> 16;
-      hit = !(bx1 < rx0 || bx0 > rx1 || by1 < ry0 || by0 > ry1);
-    }
-    uint32_t m = __ballot_sync(kFull, hit);
-    while (m) {
-      const int j = __ffs(m) - 1;
-      m &= m - 1;
-      const uint32_t tj = __shfl_sync(kFull, t, j);
-      const uint32_t bbx = __shfl_sync(kFull, bb.x, j), bby = __shfl_sync(kFull, bb.y, j);
-      const bool inb = valid && px >= (int)(bbx & 0xFFFF) && px <= (int)(bby & 0xFFFF) &&
-                       py >= (int)(bbx >> 16) && py <= (int)(bby >> 16);
-      if (!inb) continue;  // no warp-collective operation follows in this iteration
-      const TriSetup* T = setup + tj;
-      const int4 a = T->xy01, b = T->xy2f;
-      const float4 zc = T->zc;
-      const int bxp = px * 256, byp = py * 256;
+  const int tile = blockIdx.x;
+  walk_tile(p, w, stage, p.tile_begin[tile], p.tile_end[tile], [&](const TriSetup& T, uint32_t, bool inb) {
+    if (!inb) return;  // no warp-collective operation follows
+    const int4 a = T.xy01, b = T.xy2f;
+    const float4 zc = T.zc;
+    auto body = [&](auto etag) {
+      using E = decltype(etag);
+      const int bxp = w.px * 256, byp = w.py * 256;
       uint32_t pass = 0;
       uint32_t zs[S];
 #pragma unroll
       for (int s = 0; s < S; ++s) {
         const int2 sp = sample_pos<S>(s);
-        const Edges e = edges_at(a, b, bxp + sp.x, byp + sp.y);
+        const EdgesT<E> e = edges_at<E>(a, b, bxp + sp.x, byp + sp.y);
         zs[s] = 0u;
         if (inside(e, b.z)) {
           const uint32_t z = __float_as_uint(depth_at(zc, e));
@@ -540,9 +591,9 @@ __global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
           if (z < dep[s]) pass |= 1u << s;
         }
       }
-      if (!pass) continue;
-      const Edges ec = edges_at(a, b, bxp + 128, byp + 128);
-      const Shade sh = shade<false>(T, ec, zc.w);
+      if (!pass) return;
+      const EdgesT<E> ec = edges_at<E>(a, b, bxp + 128, byp + 128);
+      const Shade sh = shade(T, ec, nullptr);
       const float4 c = make_float4(sh.r, sh.g, sh.b, 1.0f);
 #pragma unroll
       for (int s = 0; s < S; ++s)
@@ -550,13 +601,14 @@ __global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
           dep[s] = zs[s];
           col[s] = c;
         }
-    }
-  }
-  if (valid) {
+    };
+    if (b.z & kFlagSmall) body(int(0)); else body((long long)0);
+  });
+  if (w.valid) {
 #pragma unroll
     for (int s = 0; s < S; ++s) {
-      p.depth[(size_t)s * p.P + pixel] = dep[s];
-      p.opaque_color[(size_t)s * p.P + pixel] = col[s];
+      p.depth[(size_t)s * p.P + w.pixel] = dep[s];
+      p.opaque_color[(size_t)s * p.P + w.pixel] = col[s];
     }
   }
 }
@@ -567,7 +619,7 @@ namespace oitd {
 
 template <template <int> class Pol, int S>
 cudaError_t launch_transparent_s(const RasterParams& p, cudaStream_t s) {
-  const size_t smem = (size_t)oit::kWarpsPerTile * Pol<S>::smem_bytes_per_warp(p.L, p.coverage);
+  const size_t smem = (size_t)oit::kWarpsPerTile * (32 * sizeof(TriSetup) + Pol<S>::smem_bytes_per_warp(p.L, p.coverage));
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_raster_transparent<Pol, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);

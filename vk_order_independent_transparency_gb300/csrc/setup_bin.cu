@@ -139,17 +139,24 @@ __global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
     alpha = (alpha > 0.0f) ? alpha : 0.0f;
     alpha = (alpha < 1.0f) ? alpha : 1.0f;
     const int acode = __float2int_rn(__fmul_rn(alpha, 255.0f));
-    T.xy2f = make_int4(PX[2], PY[2], tl, acode);
+    const int minX = min(PX[0], min(PX[1], PX[2])), maxX = max(PX[0], max(PX[1], PX[2]));
+    const int minY = min(PY[0], min(PY[1], PY[2])), maxY = max(PY[0], max(PY[1], PY[2]));
+    const int small = (maxX - minX < kSmallExtent && maxY - minY < kSmallExtent) ? kFlagSmall : 0;
+    T.xy2f = make_int4(PX[2], PY[2], tl | small | (acode << 8), __float_as_int(alpha));
     const float z0 = zz[0], z1 = zz[order[1]], z2 = zz[order[2]];
     T.zc = make_float4(z0, __fsub_rn(z1, z0), __fsub_rn(z2, z0), __fdiv_rn(1.0f, __ll2float_rn(area)));
     const float q0 = q[0], q1 = q[order[1]], q2 = q[order[2]];
-    T.q = make_float4(q0, q1, q2, alpha);
-    T.n0 = make_float4(__fmul_rn(nx[0], q0), __fmul_rn(ny[0], q0), __fmul_rn(nz[0], q0), __fmul_rn(vz[0], q0));
     const int j1 = order[1], j2 = order[2];
-    T.n1 = make_float4(__fmul_rn(nx[j1], q1), __fmul_rn(ny[j1], q1), __fmul_rn(nz[j1], q1), __fmul_rn(vz[j1], q1));
-    T.n2 = make_float4(__fmul_rn(nx[j2], q2), __fmul_rn(ny[j2], q2), __fmul_rn(nz[j2], q2), __fmul_rn(vz[j2], q2));
-    T.col = make_float4(__ldg(c0 + 6), __ldg(c0 + 7), __ldg(c0 + 8), 0.0f);
+    T.n0 = make_float4(__fmul_rn(nx[0], q0), __fmul_rn(ny[0], q0), __fmul_rn(nz[0], q0), __ldg(c0 + 6));
+    T.n1 = make_float4(__fmul_rn(nx[j1], q1), __fmul_rn(ny[j1], q1), __fmul_rn(nz[j1], q1), __ldg(c0 + 7));
+    T.n2 = make_float4(__fmul_rn(nx[j2], q2), __fmul_rn(ny[j2], q2), __fmul_rn(nz[j2], q2), __ldg(c0 + 8));
     reinterpret_cast<TriSetup*>(p.setup)[t] = T;
+    if (p.persp) {
+      TriPersp Q;
+      Q.q = make_float4(q0, q1, q2, 0.0f);
+      Q.vzq = make_float4(__fmul_rn(vz[0], q0), __fmul_rn(vz[j1], q1), __fmul_rn(vz[j2], q2), 0.0f);
+      reinterpret_cast<TriPersp*>(p.persp)[t] = Q;
+    }
     p.bbox[t] = make_uint2((uint32_t)bx0 | ((uint32_t)by0 << 16), (uint32_t)bx1 | ((uint32_t)by1 << 16));
     const int tx0 = bx0 / kTile, tx1 = bx1 / kTile, ty0 = by0 / kTile, ty1 = by1 / kTile;
     pairs = (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
