@@ -51,20 +51,22 @@ __device__ __forceinline__ float4 premult(float r, float g, float b, float a) {
 
 // ---------------------------------------------------------------------------
 // Policies. Each provides: kPasses, kShade (needs colour), kViewZ,
-// smem_bytes_per_warp(L, coverage), init, fragment(pass, has, f, ...), flush.
+// smem_bytes_per_warp(L, coverage), init, fragment(pass, f, node, pixel, targets), flush.
+// fragment() runs on the pixel's owner lane only, once per fragment, in
+// primitive order.
 // ---------------------------------------------------------------------------
 
 // oitSimple.frag.glsl:50-91
 template <int S>
 struct SimplePolicy {
+  static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
   static constexpr bool kViewZ = false;
   static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
   uint32_t count;
   __device__ void init(const RasterParams&, void*, int, uint32_t) { count = 0; }
-  __device__ __forceinline__ void fragment(const RasterParams& p, int, bool has, const Frag& f, uint32_t pixel,
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, uint32_t pixel,
                                            PixelTargets<S>& tg) {
-    if (!has) return;
     const uint32_t old = count++;
     if (old < (uint32_t)p.L) {
       const size_t r = (size_t)old * p.P + pixel;
@@ -83,32 +85,26 @@ struct SimplePolicy {
 };
 
 // oitLinkedList.frag.glsl:51-85. The node counter is a global atomic,
-// aggregated per warp: one atomicAdd per (triangle, micro-tile) hands out
-// consecutive node indices to the covered lanes in lane order.
+// aggregated per warp: one atomicAdd per batch of queued fragments hands out
+// consecutive node indices in queue (primitive, then pixel) order.
 template <int S>
 struct LinkedListPolicy {
   static constexpr int kPasses = 1;
   static constexpr bool kViewZ = false;
+  static constexpr bool kNodes = true;
   static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
   uint32_t head;
   __device__ void init(const RasterParams&, void*, int, uint32_t) { head = 0; }
-  __device__ __forceinline__ void fragment(const RasterParams& p, int, bool has, const Frag& f, uint32_t,
+  // node: the index the batched counter allocation gave this fragment
+  // (imageAtomicAdd(imgCounter) + 1, oitLinkedList.frag.glsl:55).
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t node, uint32_t,
                                            PixelTargets<S>& tg) {
-    const uint32_t m = __ballot_sync(kFull, has);
-    if (!m) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(p.counter, (uint32_t)__popc(m));
-    base = __shfl_sync(kFull, base, leader);
-    if (!has) return;
-    const uint32_t newOffset = base + (uint32_t)__popc(m & ((1u << lane) - 1u)) + 1u;
-    if (newOffset >= p.capacity) {
+    if (node >= p.capacity) {
       if (p.tail) tg.tail(premult(f.r, f.g, f.b, f.a), f.cover);
       return;
     }
-    reinterpret_cast<uint4*>(p.abuf)[newOffset] = make_uint4(f.packed, f.depth, p.coverage ? f.cover : 0u, head);
-    head = newOffset;
+    reinterpret_cast<uint4*>(p.abuf)[node] = make_uint4(f.packed, f.depth, p.coverage ? f.cover : 0u, head);
+    head = node;
   }
   __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
     if (valid) p.aux[pixel] = head;
@@ -120,6 +116,7 @@ struct LinkedListPolicy {
 // atomicMin insertion loop runs on it in primitive order.
 template <int S>
 struct Loop64Policy {
+  static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
   static constexpr bool kViewZ = false;
   static __host__ __device__ size_t smem_bytes_per_warp(int L, int) { return (size_t)L * 32 * 8; }
@@ -130,9 +127,8 @@ struct Loop64Policy {
     kb = reinterpret_cast<unsigned long long*>(smem);
     for (int i = 0; i < p.L; ++i) kb[i * 32 + lane] = kEmpty64;
   }
-  __device__ __forceinline__ void fragment(const RasterParams& p, int, bool has, const Frag& f, uint32_t,
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, uint32_t,
                                            PixelTargets<S>& tg) {
-    if (!has) return;
     const int L = p.L;
     unsigned long long zcur = ((unsigned long long)f.depth << 32) | f.packed;
     bool evict = true;
@@ -162,6 +158,7 @@ struct Loop64Policy {
 // between them.
 template <int S>
 struct LoopPolicy {
+  static constexpr bool kNodes = false;
   static constexpr int kPasses = 2;
   static constexpr bool kViewZ = false;
   static __host__ __device__ size_t smem_bytes_per_warp(int L, int) { return (size_t)L * 32 * 8; }
@@ -177,9 +174,8 @@ struct LoopPolicy {
       col[i * 32 + lane] = 0u;
     }
   }
-  __device__ __forceinline__ void fragment(const RasterParams& p, int pass, bool has, const Frag& f, uint32_t,
+  __device__ __forceinline__ void fragment(const RasterParams& p, int pass, const Frag& f, uint32_t, uint32_t,
                                            PixelTargets<S>& tg) {
-    if (!has) return;
     const int L = p.L;
     uint32_t zcur = f.depth;
     if (pass == 0) {
@@ -218,6 +214,7 @@ struct LoopPolicy {
 // thread ever touches the pixel, and fragments arrive in primitive order.
 template <int S>
 struct LockPolicy {
+  static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
   static constexpr bool kViewZ = false;
   static __host__ __device__ size_t smem_bytes_per_warp(int L, int coverage) {
@@ -234,9 +231,8 @@ struct LockPolicy {
     auxdepth = 0xFFFFFFFFu;
   }
   __device__ __forceinline__ uint32_t* slot(int i) const { return rec + ((size_t)i * 32 + lane) * words; }
-  __device__ __forceinline__ void fragment(const RasterParams& p, int, bool has, const Frag& f, uint32_t,
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, uint32_t,
                                            PixelTargets<S>& tg) {
-    if (!has) return;
     const int L = p.L;
     float4 out = premult(f.r, f.g, f.b, f.a);
     if (f.depth <= auxdepth) {
@@ -297,6 +293,7 @@ struct LockPolicy {
 // RGBA16F/R16F render target does.
 template <int S>
 struct WeightedPolicy {
+  static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
   static constexpr bool kViewZ = true;
   static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
@@ -310,9 +307,8 @@ struct WeightedPolicy {
     }
   }
   static __device__ __forceinline__ float h(float x) { return __half2float(__float2half_rn(x)); }
-  __device__ __forceinline__ void fragment(const RasterParams& p, int, bool has, const Frag& f, uint32_t,
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, uint32_t,
                                            PixelTargets<S>&) {
-    if (!has) return;
     const float4 c = premult(f.r, f.g, f.b, f.a);
     const float depthZ = -f.view_z * 10.0f;
     const float x = depthZ / 200.0f;
@@ -407,12 +403,14 @@ __device__ __forceinline__ bool bbox_hits(uint2 bb, const WarpTile& w) {
 // Walks [beg, end) of the tile list in primitive order, 32 entries at a time:
 // the lanes test their triangle's bbox against the warp's micro-tile, the hits
 // copy their setup records into the warp's shared-memory stage in parallel
-// (cp.async), then vis(T, t, inb) runs for each hit in list order. `vis` is
-// warp-uniform: every lane calls it, with inb telling whether the lane's pixel
-// is inside the triangle's pixel bbox.
-template <class Vis>
-__device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile& w, TriSetup* stage, uint32_t beg,
-                                          uint32_t end, Vis&& vis) {
+// (cp.async), then vis(slot, t, inb) runs for each hit in list order, and
+// chunk_end() once the chunk's hits are done (before the stage is refilled).
+// Both are warp-uniform: every lane calls them; inb tells whether the lane's
+// pixel is inside the triangle's pixel bbox.
+template <class Vis, class ChunkEnd>
+__device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile& w, TriSetup* stage,
+                                          uint32_t* stage_t, uint32_t beg, uint32_t end, Vis&& vis,
+                                          ChunkEnd&& chunk_end) {
   const TriSetup* __restrict__ setup = reinterpret_cast<const TriSetup*>(p.setup);
   const uint32_t lt = (1u << w.lane) - 1u;
   uint32_t t_next = 0;
@@ -435,6 +433,7 @@ __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile&
       int4* dst = reinterpret_cast<int4*>(stage + slot);
 #pragma unroll
       for (int k = 0; k < 6; ++k) cp_async16(dst + k, src + k);
+      if (stage_t) stage_t[slot] = t;
     }
     bb_next = more ? __ldg(&p.bbox[t_next]) : make_uint2(0xFFFFFFFFu, 0u);
     cp_async_wait_all();
@@ -447,23 +446,41 @@ __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile&
       const uint32_t bbx = __shfl_sync(kFull, bb.x, j), bby = __shfl_sync(kFull, bb.y, j);
       const bool inb = w.valid && w.px >= (int)(bbx & 0xFFFF) && w.px <= (int)(bby & 0xFFFF) &&
                        w.py >= (int)(bbx >> 16) && w.py <= (int)(bby >> 16);
-      vis(stage[k], tj, inb);
+      vis(k, tj, inb);
     }
+    chunk_end();
     __syncwarp();
   }
 }
+
+// Per-warp fragment queue: coverage appends (stage slot, lane, coverage,
+// depth) in primitive-then-lane order; shading then runs one queued fragment
+// per lane; finally each lane feeds its own pixel's fragments, in queue order,
+// to the algorithm.
+constexpr int kQueue = 64;
+struct FragQueue {
+  uint32_t depth[kQueue];
+  uint32_t packed[kQueue];
+  float r[kQueue], g[kQueue], b[kQueue], vz[kQueue];
+  unsigned char tri[kQueue], lane[kQueue], cover[kQueue], pad[kQueue];
+};
+constexpr size_t kWarpStageBytes = 32 * sizeof(TriSetup) + 32 * sizeof(uint32_t) + sizeof(FragQueue);
 
 // ---------------------------------------------------------------------------
 // Transparent COLOR (+DEPTH) pass.
 // ---------------------------------------------------------------------------
 template <template <int> class Policy, int S>
-__global__ void __launch_bounds__(256) k_raster_transparent(RasterParams p) {
+__global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using Pol = Policy<S>;
   const int warp = threadIdx.x >> 5;
   const WarpTile w = warp_tile(p);
-  TriSetup* stage = reinterpret_cast<TriSetup*>(smem_raw) + warp * 32;
-  unsigned char* pol_smem = smem_raw + (size_t)oit::kWarpsPerTile * 32 * sizeof(TriSetup);
+  unsigned char* wbase = smem_raw + (size_t)warp * kWarpStageBytes;
+  TriSetup* stage = reinterpret_cast<TriSetup*>(wbase);
+  uint32_t* stage_t = reinterpret_cast<uint32_t*>(wbase + 32 * sizeof(TriSetup));
+  FragQueue* q = reinterpret_cast<FragQueue*>(wbase + 32 * sizeof(TriSetup) + 32 * sizeof(uint32_t));
+  unsigned char* pol_smem = smem_raw + (size_t)oit::kWarpsPerTile * kWarpStageBytes +
+                            (size_t)warp * Pol::smem_bytes_per_warp(p.L, p.coverage);
 
   PixelTargets<S> tg;
 #pragma unroll
@@ -477,62 +494,110 @@ __global__ void __launch_bounds__(256) k_raster_transparent(RasterParams p) {
     }
   }
   Pol pol;
-  pol.init(p, pol_smem + (size_t)warp * Pol::smem_bytes_per_warp(p.L, p.coverage), w.lane, w.pixel);
+  pol.init(p, pol_smem, w.lane, w.pixel);
 
   const int tile = blockIdx.x;
   const uint32_t beg = p.tile_begin[tile], end = p.tile_end[tile];
   const TriPersp* __restrict__ persp = reinterpret_cast<const TriPersp*>(p.persp);
-  uint32_t nfrag = 0;
+  const uint32_t lt = (1u << w.lane) - 1u;
+  uint32_t nfrag = 0;  // warp-uniform
+  unsigned long long mine = 0;
+  int qn = 0;          // warp-uniform
 
   for (int pass = 0; pass < Pol::kPasses; ++pass) {
     const bool shading = Pol::kPasses == 1 || pass == Pol::kPasses - 1;
-    walk_tile(p, w, stage, beg, end, [&](const TriSetup& T, uint32_t tj, bool inb) {
-      const int4 a = T.xy01, b = T.xy2f;
-      const float4 zc = T.zc;
-      uint32_t cover = 0;
-      float zcen = 0.f;
-      Frag f;
-      auto body = [&](auto etag) {
-        using E = decltype(etag);
-        EdgesT<E> ec = {0, 0, 0};
-        if (inb) {
-          const int bxp = w.px * 256, byp = w.py * 256;
+
+    auto flush = [&]() {
+      if (qn == 0) return;
+      __syncwarp();
+      if (shading) {
+        for (int j = w.lane; j < qn; j += 32) {
+          const TriSetup& T = stage[q->tri[j]];
+          const int l = q->lane[j];
+          const int sx = (w.rx0 + (l & 7)) * 256 + 128, sy = (w.ry0 + (l >> 3)) * 256 + 128;
+          const TriPersp* P = Pol::kViewZ ? persp + stage_t[q->tri[j]] : nullptr;
+          const int4 a = T.xy01, b = T.xy2f;
+          Shade sh;
+          if (b.z & kFlagSmall) sh = shade(T, edges_at<int>(a, b, sx, sy), P);
+          else sh = shade(T, edges_at<long long>(a, b, sx, sy), P);
+          q->packed[j] = pack_rgba8(sh, (uint32_t)(b.z >> 8) & 255u);
+          q->r[j] = sh.r;
+          q->g[j] = sh.g;
+          q->b[j] = sh.b;
+          q->vz[j] = sh.view_z;
+        }
+        __syncwarp();
+      }
+      uint32_t node0 = 0;
+      if (Pol::kNodes && shading) {
+        if (w.lane == 0) node0 = atomicAdd(p.counter, (uint32_t)qn);
+        node0 = __shfl_sync(kFull, node0, 0);
+      }
+      unsigned long long mm = mine;
+      while (mm) {
+        const int j = __ffsll((long long)mm) - 1;
+        mm &= mm - 1;
+        Frag f;
+        f.depth = q->depth[j];
+        f.cover = q->cover[j];
+        if (shading) {
+          f.packed = q->packed[j];
+          f.r = q->r[j];
+          f.g = q->g[j];
+          f.b = q->b[j];
+          f.a = __int_as_float(stage[q->tri[j]].xy2f.w);
+          f.view_z = q->vz[j];
+        }
+        pol.fragment(p, pass, f, node0 + (uint32_t)j + 1u, w.pixel, tg);
+      }
+      if (shading) nfrag += (uint32_t)qn;
+      mine = 0;
+      qn = 0;
+      __syncwarp();
+    };
+
+    walk_tile(
+        p, w, stage, Pol::kViewZ ? stage_t : nullptr, beg, end,
+        [&](int k, uint32_t, bool inb) {
+          const TriSetup& T = stage[k];
+          const int4 a = T.xy01, b = T.xy2f;
+          const float4 zc = T.zc;
+          uint32_t cover = 0;
+          float zcen = 0.f;
+          auto body = [&](auto etag) {
+            using E = decltype(etag);
+            const int bxp = w.px * 256, byp = w.py * 256;
 #pragma unroll
-          for (int s = 0; s < S; ++s) {
-            const int2 sp = sample_pos<S>(s);
-            const EdgesT<E> e = edges_at<E>(a, b, bxp + sp.x, byp + sp.y);
-            if (inside(e, b.z)) {
-              const float z = depth_at(zc, e);
-              if (__float_as_uint(z) < tg.depth[s]) cover |= 1u << s;
-              if (S == 1) {
-                ec = e;
-                zcen = z;
+            for (int s = 0; s < S; ++s) {
+              const int2 sp = sample_pos<S>(s);
+              const EdgesT<E> e = edges_at<E>(a, b, bxp + sp.x, byp + sp.y);
+              if (inside(e, b.z)) {
+                const float z = depth_at(zc, e);
+                if (__float_as_uint(z) < tg.depth[s]) cover |= 1u << s;
+                if (S == 1) zcen = z;
               }
             }
+            if (S > 1 && cover) zcen = depth_at(zc, edges_at<E>(a, b, bxp + 128, byp + 128));
+          };
+          if (inb) {
+            if (b.z & kFlagSmall) body(int(0)); else body((long long)0);
           }
-          if (S > 1 && cover) {
-            ec = edges_at<E>(a, b, bxp + 128, byp + 128);
-            zcen = depth_at(zc, ec);
+          const bool has = cover != 0;
+          const uint32_t m = __ballot_sync(kFull, has);
+          if (!m) return;
+          const int cnt = __popc(m);
+          if (qn + cnt > kQueue) flush();
+          if (has) {
+            const int j = qn + __popc(m & lt);
+            q->tri[j] = (unsigned char)k;
+            q->lane[j] = (unsigned char)w.lane;
+            q->cover[j] = (unsigned char)cover;
+            q->depth[j] = __float_as_uint(zcen);
+            mine |= 1ull << j;
           }
-        }
-        if (cover && shading) {
-          const Shade sh = shade(T, ec, Pol::kViewZ ? persp + tj : nullptr);
-          f.r = sh.r;
-          f.g = sh.g;
-          f.b = sh.b;
-          f.view_z = sh.view_z;
-          f.packed = pack_rgba8(sh, (uint32_t)(b.z >> 8) & 255u);
-        }
-      };
-      if (b.z & kFlagSmall) body(int(0)); else body((long long)0);
-      const bool has = cover != 0;
-      if (!__any_sync(kFull, has)) return;
-      f.cover = cover;
-      f.depth = __float_as_uint(zcen);
-      f.a = __int_as_float(b.w);
-      if (has && shading) ++nfrag;
-      pol.fragment(p, pass, has, f, w.pixel, tg);
-    });
+          qn += cnt;
+        },
+        flush);
   }
 
   pol.flush(p, w.valid, w.pixel);
@@ -548,9 +613,6 @@ __global__ void __launch_bounds__(256) k_raster_transparent(RasterParams p) {
     const float k = 1.0f / (float)S;
     p.color[w.pixel] = make_float4(c.x * k, c.y * k, c.z * k, c.w * k);
   }
-  // fragment statistics: one atomic per warp
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) nfrag += __shfl_xor_sync(kFull, nfrag, o);
   if (w.lane == 0 && nfrag && p.frag_count) atomicAdd(p.frag_count, (unsigned long long)nfrag);
 }
 
@@ -571,8 +633,9 @@ __global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
     col[s] = w.valid ? p.opaque_color[(size_t)s * p.P + w.pixel] : p.background;
   }
   const int tile = blockIdx.x;
-  walk_tile(p, w, stage, p.tile_begin[tile], p.tile_end[tile], [&](const TriSetup& T, uint32_t, bool inb) {
+  walk_tile(p, w, stage, nullptr, p.tile_begin[tile], p.tile_end[tile], [&](int k, uint32_t, bool inb) {
     if (!inb) return;  // no warp-collective operation follows
+    const TriSetup& T = stage[k];
     const int4 a = T.xy01, b = T.xy2f;
     const float4 zc = T.zc;
     auto body = [&](auto etag) {
@@ -603,7 +666,7 @@ __global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
         }
     };
     if (b.z & kFlagSmall) body(int(0)); else body((long long)0);
-  });
+  }, [] {});
   if (w.valid) {
 #pragma unroll
     for (int s = 0; s < S; ++s) {
@@ -619,7 +682,7 @@ namespace oitd {
 
 template <template <int> class Pol, int S>
 cudaError_t launch_transparent_s(const RasterParams& p, cudaStream_t s) {
-  const size_t smem = (size_t)oit::kWarpsPerTile * (32 * sizeof(TriSetup) + Pol<S>::smem_bytes_per_warp(p.L, p.coverage));
+  const size_t smem = (size_t)oit::kWarpsPerTile * (kWarpStageBytes + Pol<S>::smem_bytes_per_warp(p.L, p.coverage));
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_raster_transparent<Pol, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
