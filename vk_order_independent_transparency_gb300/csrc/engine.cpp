@@ -144,6 +144,10 @@ struct oit_context {
       cudaEventDestroy(p.b);
     }
     for (cudaEvent_t e : prof_free) cudaEventDestroy(e);
+    for (PairStat& p : pair_stats) {
+      if (p.ev) cudaEventDestroy(p.ev);
+      if (p.host_total) cudaFreeHost(p.host_total);
+    }
     DevBuf* all[] = {&depth, &opaque_color, &color, &abuf, &aux, &auxdepth, &counter, &accum, &reveal, &out,
                      &out_linear, &err, &frag, &bbox, &setup, &persp, &pair_count, &pair_offset, &scan_tmp, &total,
                      &keys, &tris, &keys_alt, &tris_alt, &hist, &tile_begin, &tile_end, &mesh_v, &mesh_i};
@@ -214,10 +218,7 @@ struct oit_context {
   }
 
   int ensure_pairs(size_t n) {
-    const size_t hist_words = oit::radix_hist_words(n);
-    const size_t scan_words = std::max(oit::scan_scratch_words(tri_cap), oit::scan_scratch_words(hist_words));
-    OIT_TRY_CUDA(scan_tmp.ensure(scan_words * 4), "alloc scan");
-    if (n > pair_cap) {
+    if (n > pair_cap || pair_cap == 0) {
       const float scale = st.bin_capacity_scale > 0.0f ? st.bin_capacity_scale : 1.25f;
       const size_t cap = std::max<size_t>((size_t)((double)n * std::max(1.0f, scale)), 4096);
       OIT_TRY_CUDA(keys.ensure(cap * 4), "alloc keys");
@@ -226,7 +227,10 @@ struct oit_context {
       OIT_TRY_CUDA(tris_alt.ensure(cap * 4), "alloc tris");
       pair_cap = cap;
     }
-    OIT_TRY_CUDA(hist.ensure(std::max<size_t>(oit::radix_hist_words(pair_cap), 256) * 4), "alloc hist");
+    const size_t hist_words = std::max<size_t>(oit::radix_hist_words(pair_cap), 256);
+    OIT_TRY_CUDA(hist.ensure(hist_words * 4), "alloc hist");
+    const size_t scan_words = std::max(oit::scan_scratch_words(tri_cap), oit::scan_scratch_words(hist_words));
+    OIT_TRY_CUDA(scan_tmp.ensure(scan_words * 4), "alloc scan");
     return OIT_OK;
   }
 
@@ -268,24 +272,66 @@ struct oit_context {
     return b;
   }
 
+  // Pair-count history per draw signature: the first draw of a signature reads
+  // its pair count back synchronously to size the bins; later draws run without
+  // a host round trip, sized from earlier frames (their counts are copied back
+  // asynchronously into pinned memory and picked up when ready).
+  struct PairStat {
+    uint64_t key = 0;
+    uint32_t known = 0;
+    uint32_t* host_total = nullptr;  // pinned
+    cudaEvent_t ev = nullptr;
+    bool pending = false;
+  };
+  std::vector<PairStat> pair_stats;
+
+  PairStat* pair_stat(uint64_t key) {
+    for (PairStat& p : pair_stats)
+      if (p.key == key) return &p;
+    return nullptr;
+  }
+
   // Setup + binning of one draw; afterwards tile_begin/tile_end/tris describe it.
   int bin(const oit_mesh* mesh, uint32_t first, uint32_t count, int cull_back, cudaStream_t s) {
     int r = ensure_triangles(count);
     if (r != OIT_OK) return r;
-    r = ensure_pairs(0);
+    const uint64_t key = ((uint64_t)first << 33) ^ ((uint64_t)count << 1) ^ (uint64_t)(cull_back & 1) ^
+                         ((uint64_t)(uintptr_t)mesh->indices_device << 7);
+    PairStat* ps = pair_stat(key);
+    if (ps && ps->pending && cudaEventQuery(ps->ev) == cudaSuccess) {
+      ps->known = std::max(ps->known, *ps->host_total);
+      ps->pending = false;
+    }
+    r = ensure_pairs(ps ? ps->known : 0);
     if (r != OIT_OK) return r;
     oit::SetupParams sp = setup_params(mesh, first, count, cull_back);
     oit::Bins b = bins();
-    uint32_t total_pairs = 0;
-    OIT_TRY_CUDA(oit::bin_count(sp, b, num_tiles, &total_pairs, s, &launches), "bin_count");
-    r = ensure_pairs(total_pairs);
-    if (r != OIT_OK) return r;
-    b = bins();
-    OIT_TRY_CUDA(oit::bin_sort(sp, b, total_pairs, key_bits, err.as<uint32_t>(), s, &launches), "bin_sort");
+    OIT_TRY_CUDA(oit::bin_setup_scan(sp, b, s, &launches), "bin_setup_scan");
+    if (!ps) {
+      // first draw of this signature: size the bins exactly
+      PairStat st;
+      st.key = key;
+      OIT_TRY_CUDA(cudaMallocHost(&st.host_total, 4), "alloc pinned");
+      OIT_TRY_CUDA(cudaEventCreateWithFlags(&st.ev, cudaEventDisableTiming), "event");
+      OIT_TRY_CUDA(cudaMemcpyAsync(st.host_total, total.p, 4, cudaMemcpyDeviceToHost, s), "d2h");
+      OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
+      st.known = *st.host_total;
+      pair_stats.push_back(st);
+      ps = &pair_stats.back();
+      r = ensure_pairs(ps->known);
+      if (r != OIT_OK) return r;
+      b = bins();
+    }
+    OIT_TRY_CUDA(oit::bin_sort(sp, b, key_bits, num_tiles, err.as<uint32_t>(), s, &launches), "bin_sort");
     // bin_sort may have swapped the ping-pong buffers
     if (b.keys != keys.as<uint32_t>()) {
       std::swap(keys, keys_alt);
       std::swap(tris, tris_alt);
+    }
+    if (!ps->pending) {
+      OIT_TRY_CUDA(cudaMemcpyAsync(ps->host_total, total.p, 4, cudaMemcpyDeviceToHost, s), "d2h");
+      OIT_TRY_CUDA(cudaEventRecord(ps->ev, s), "event");
+      ps->pending = true;
     }
     return OIT_OK;
   }

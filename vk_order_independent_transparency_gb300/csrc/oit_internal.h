@@ -124,9 +124,8 @@ struct CompositeParams {
 };
 
 // ---- launch wrappers (defined in the .cu files) -------------------------
-cudaError_t bin_count(const SetupParams& sp, Bins& b, int num_tiles, uint32_t* total_pairs, cudaStream_t s,
-                      uint64_t* launches);
-cudaError_t bin_sort(const SetupParams& sp, Bins& b, uint32_t total, int key_bits, uint32_t* error, cudaStream_t s,
+cudaError_t bin_setup_scan(const SetupParams& sp, Bins& b, cudaStream_t s, uint64_t* launches);
+cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles, uint32_t* error, cudaStream_t s,
                      uint64_t* launches);
 size_t radix_hist_words(size_t pairs);
 cudaError_t launch_raster_a(Alg alg, const RasterParams& p, cudaStream_t s);  // Simple, LinkedList, Opaque

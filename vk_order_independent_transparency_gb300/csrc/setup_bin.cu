@@ -10,7 +10,7 @@
 //                 written in triangle order;
 //   radix sort    stable LSD sort of the pairs by tile id, so every tile's list
 //                 keeps primitive order;
-//   k_ranges      begin/end of each tile's list.
+//   k_tile_ranges begin/end of each tile's list.
 #include <algorithm>
 #include <cstdio>
 
@@ -262,8 +262,9 @@ __global__ void __launch_bounds__(256) k_emit(const uint32_t* __restrict__ pair_
                                               const uint32_t* __restrict__ pair_offset, const uint2* __restrict__ bbox,
                                               uint32_t n, int tiles_x, uint32_t tile_base,
                                               uint32_t* __restrict__ keys, uint32_t* __restrict__ tris,
-                                              size_t capacity, uint32_t* err) {
+                                              size_t capacity, const uint32_t* __restrict__ total, uint32_t* err) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0 && *total > capacity) atomicOr(err, 1u);  // OIT_DEVERR_BIN_OVERFLOW
   if (t >= n) return;
   const uint32_t c = pair_count[t];
   if (!c) return;
@@ -275,10 +276,7 @@ __global__ void __launch_bounds__(256) k_emit(const uint32_t* __restrict__ pair_
   for (int ty = ty0; ty <= ty1; ++ty)
     for (int tx = tx0; tx <= tx1; ++tx, ++j) {
       const size_t pos = (size_t)off + j;
-      if (pos >= capacity) {
-        atomicOr(err, 1u);
-        return;
-      }
+      if (pos >= capacity) return;
       keys[pos] = tile_base + (uint32_t)(ty * tiles_x + tx);
       tris[pos] = t;
     }
@@ -287,16 +285,30 @@ __global__ void __launch_bounds__(256) k_emit(const uint32_t* __restrict__ pair_
 // ---------------------------------------------------------------------------
 // Stable LSD radix sort of (key, value) pairs, 8-bit digits.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t* __restrict__ keys, size_t n, int shift,
-                                                              uint32_t* __restrict__ hist, uint32_t nblk) {
+__device__ __forceinline__ size_t pair_count_of(const uint32_t* total, size_t capacity) {
+  const size_t t = *total;
+  return t < capacity ? t : capacity;
+}
+
+// Per-block digit histogram; one shared-memory atomic per distinct digit per
+// warp (tile ids of neighbouring pairs are mostly equal).
+__global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t* __restrict__ keys,
+                                                              const uint32_t* __restrict__ total, size_t capacity,
+                                                              int shift, uint32_t* __restrict__ hist, uint32_t nblk) {
   __shared__ uint32_t h[kRadixBins];
   h[threadIdx.x] = 0;
   __syncthreads();
+  const size_t n = pair_count_of(total, capacity);
   const size_t base = (size_t)blockIdx.x * kRadixTile;
+  const uint32_t lane = threadIdx.x & 31;
+  if (base < n) {
 #pragma unroll 4
-  for (int r = 0; r < kRadixRounds; ++r) {
-    const size_t i = base + (size_t)r * kRadixThreads + threadIdx.x;
-    if (i < n) atomicAdd(&h[(keys[i] >> shift) & (kRadixBins - 1)], 1u);
+    for (int r = 0; r < kRadixRounds; ++r) {
+      const size_t i = base + (size_t)r * kRadixThreads + threadIdx.x;
+      const uint32_t d = (i < n) ? ((keys[i] >> shift) & (kRadixBins - 1)) : kRadixBins;
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      if (d < kRadixBins && (__ffs(peers) - 1) == (int)lane) atomicAdd(&h[d], (uint32_t)__popc(peers));
+    }
   }
   __syncthreads();
   hist[(size_t)threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];
@@ -305,8 +317,10 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t* __
 __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t* __restrict__ keys_in,
                                                                  const uint32_t* __restrict__ vals_in,
                                                                  uint32_t* __restrict__ keys_out,
-                                                                 uint32_t* __restrict__ vals_out, size_t n, int shift,
-                                                                 const uint32_t* __restrict__ offsets, uint32_t nblk) {
+                                                                 uint32_t* __restrict__ vals_out,
+                                                                 const uint32_t* __restrict__ total, size_t capacity,
+                                                                 int shift, const uint32_t* __restrict__ offsets,
+                                                                 uint32_t nblk) {
   constexpr int kWarps = kRadixThreads / 32;
   __shared__ uint32_t base[kRadixBins];
   __shared__ uint32_t running[kRadixBins];
@@ -315,6 +329,8 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t*
   base[threadIdx.x] = offsets[(size_t)threadIdx.x * nblk + blockIdx.x];
   running[threadIdx.x] = 0;
   const size_t blk = (size_t)blockIdx.x * kRadixTile;
+  const size_t n = pair_count_of(total, capacity);
+  if (blk >= n) return;
   const uint32_t lt_mask = (1u << lane) - 1u;
   for (int r = 0; r < kRadixRounds; ++r) {
 #pragma unroll
@@ -353,13 +369,27 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t*
   }
 }
 
-__global__ void __launch_bounds__(256) k_ranges(const uint32_t* __restrict__ keys, size_t n,
-                                                uint32_t* __restrict__ begin, uint32_t* __restrict__ end) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t k = keys[i];
-  if (i == 0 || keys[i - 1] != k) begin[k] = (uint32_t)i;
-  if (i == n - 1 || keys[i + 1] != k) end[k] = (uint32_t)(i + 1);
+// [begin, end) of every tile's pair range in the sorted keys (binary search).
+__global__ void __launch_bounds__(256) k_tile_ranges(const uint32_t* __restrict__ keys,
+                                                     const uint32_t* __restrict__ total, size_t capacity,
+                                                     int num_tiles, uint32_t* __restrict__ begin,
+                                                     uint32_t* __restrict__ end) {
+  const int tile = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tile >= num_tiles) return;
+  const uint32_t n = (uint32_t)pair_count_of(total, capacity);
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (keys[mid] < (uint32_t)tile) lo = mid + 1; else hi = mid;
+  }
+  const uint32_t b = lo;
+  hi = n;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (keys[mid] <= (uint32_t)tile) lo = mid + 1; else hi = mid;
+  }
+  begin[tile] = b;
+  end[tile] = lo;
 }
 
 __global__ void k_fill_u32(uint32_t* dst, uint32_t v, size_t n) {
@@ -395,47 +425,40 @@ cudaError_t launch_fill_f4(float4* dst, float4 value, size_t count, cudaStream_t
   return cudaGetLastError();
 }
 
-// Binning, step 1: setup + pair counts + scan. Synchronises once and returns
-// the number of (tile, triangle) pairs in *total_pairs.
-cudaError_t bin_count(const SetupParams& sp, Bins& b, int num_tiles, uint32_t* total_pairs, cudaStream_t s,
-                      uint64_t* launches) {
+// Binning, step 1: setup + pair counts + exclusive scan; the number of
+// (tile, triangle) pairs lands in b.total (device).
+cudaError_t bin_setup_scan(const SetupParams& sp, Bins& b, cudaStream_t s, uint64_t* launches) {
   cudaError_t e;
   const uint32_t n = sp.num_triangles;
-  *total_pairs = 0;
-  if ((e = launch_fill_u32(b.tile_begin, 0u, (size_t)num_tiles, s)) != cudaSuccess) return e;
-  if ((e = launch_fill_u32(b.tile_end, 0u, (size_t)num_tiles, s)) != cudaSuccess) return e;
-  *launches += 2;
-  if (n == 0) return cudaSuccess;
+  if (n == 0) return cudaMemsetAsync(b.total, 0, 4, s);
   k_setup<<<(n + 255) / 256, 256, 0, s>>>(sp, sp.samples > 1 ? sp.samples : 1);
   ++*launches;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if ((e = scan_exclusive(sp.pair_count, b.pair_offset, n, b.scan_tmp, b.total, s, launches)) != cudaSuccess) return e;
-  uint32_t total = 0;
-  if ((e = cudaMemcpyAsync(&total, b.total, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-  *total_pairs = total;
-  return cudaSuccess;
+  return scan_exclusive(sp.pair_count, b.pair_offset, n, b.scan_tmp, b.total, s, launches);
 }
 
-// Binning, step 2: emit pairs in triangle order, stable radix sort by tile,
-// tile ranges. Requires total <= b.capacity and hist/scan scratch sized for it.
-cudaError_t bin_sort(const SetupParams& sp, Bins& b, uint32_t total, int key_bits, uint32_t* error, cudaStream_t s,
+// Binning, step 2: emit pairs in triangle order, stable radix sort by tile id,
+// tile ranges. Every kernel reads the pair count from b.total and is bounded
+// by b.capacity, so no host round trip is needed; pairs beyond the capacity
+// are dropped and raise OIT_DEVERR_BIN_OVERFLOW.
+cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles, uint32_t* error, cudaStream_t s,
                      uint64_t* launches) {
   cudaError_t e;
   const uint32_t n = sp.num_triangles;
-  if (n == 0 || total == 0) return cudaSuccess;
-  k_emit<<<(n + 255) / 256, 256, 0, s>>>(sp.pair_count, b.pair_offset, sp.bbox, n, sp.tiles_x, 0u, b.keys, b.tris,
-                                         b.capacity, error);
-  ++*launches;
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  const uint32_t nblk = (uint32_t)((total + kRadixTile - 1) / kRadixTile);
+  if (n > 0) {
+    k_emit<<<(n + 255) / 256, 256, 0, s>>>(sp.pair_count, b.pair_offset, sp.bbox, n, sp.tiles_x, 0u, b.keys,
+                                           b.tris, b.capacity, b.total, error);
+    ++*launches;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  const uint32_t nblk = (uint32_t)((b.capacity + kRadixTile - 1) / kRadixTile);
   uint32_t *kin = b.keys, *vin = b.tris, *kout = b.keys_alt, *vout = b.tris_alt;
   for (int shift = 0; shift < key_bits; shift += kRadixBits) {
-    k_radix_hist<<<nblk, kRadixThreads, 0, s>>>(kin, total, shift, b.hist, nblk);
+    k_radix_hist<<<nblk, kRadixThreads, 0, s>>>(kin, b.total, b.capacity, shift, b.hist, nblk);
     ++*launches;
     if ((e = scan_exclusive(b.hist, b.hist, (size_t)nblk * kRadixBins, b.scan_tmp, nullptr, s, launches)) != cudaSuccess)
       return e;
-    k_radix_scatter<<<nblk, kRadixThreads, 0, s>>>(kin, vin, kout, vout, total, shift, b.hist, nblk);
+    k_radix_scatter<<<nblk, kRadixThreads, 0, s>>>(kin, vin, kout, vout, b.total, b.capacity, shift, b.hist, nblk);
     ++*launches;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     std::swap(kin, kout);
@@ -445,7 +468,8 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, uint32_t total, int key_bit
     std::swap(b.keys, b.keys_alt);
     std::swap(b.tris, b.tris_alt);
   }
-  k_ranges<<<(total + 255) / 256, 256, 0, s>>>(b.keys, total, b.tile_begin, b.tile_end);
+  k_tile_ranges<<<(num_tiles + 255) / 256, 256, 0, s>>>(b.keys, b.total, b.capacity, num_tiles, b.tile_begin,
+                                                         b.tile_end);
   ++*launches;
   return cudaGetLastError();
 }
