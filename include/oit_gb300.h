@@ -57,6 +57,7 @@ extern "C" {
 
 /* oit_state.flags */
 #define OIT_FLAG_LINEAR_OUTPUT 0x1u  /* composite also writes OIT_BUF_OUTPUT_LINEAR */
+#define OIT_FLAG_CUDA_GRAPH 0x2u     /* oit_render_frame replays a captured CUDA graph of the whole frame */
 
 /* Status codes. */
 #define OIT_OK 0

@@ -189,3 +189,42 @@ def test_large_triangles(engine, alg, aa):
     o = pu.render_oracle(alg, W, H, v, i, 1, sd, 50, **kw)
     np.testing.assert_array_equal(g['depth'], o['depth'])
     check(engine, alg, g, o, W, H, L, aa)
+
+
+@pytest.mark.parametrize('alg', [1, 3, 4])
+def test_separate_draw_calls_match_frame(engine, alg):
+    """The reference-style call sequence (begin, clearTransparent, opaque draw,
+    drawTransparent COLOR, COMPOSITE) gives the same image as render_frame,
+    which bins opaque and transparent triangles in one pass."""
+    W, H = 160, 120
+    v, i, tpo, sd = pu.scene(40, W, H, seed=8)
+    frame = pu.render_gpu(alg, W, H, v, i, tpo, sd, 60, oit_layers=8)
+    st = engine.make_state(alg, W, H, oit_layers=8)
+    r = engine.Renderer(st)
+    mesh = engine.DeviceMesh(v, i)
+    r.update_scene(sd)
+    nt = (40 * 60 // 100) * tpo
+    r.begin_frame()
+    r.clear_transparent()
+    r.draw_opaque(mesh, nt, i.shape[0] - nt)
+    r.draw_transparent_color(mesh, 0, nt)
+    r.composite()
+    np.testing.assert_array_equal(r.output(), frame['image'])
+    assert r.fragment_count() == frame['fragments']
+
+
+@pytest.mark.parametrize('alg', [0, 1, 2, 3, 6])
+def test_cuda_graph_replay(engine, alg):
+    """OIT_FLAG_CUDA_GRAPH: the replayed frame equals the plain frame."""
+    W, H = 192, 144
+    v, i, tpo, sd = pu.scene(48, W, H, seed=12)
+    plain = pu.render_gpu(alg, W, H, v, i, tpo, sd, 70, oit_layers=8)
+    st = engine.make_state(alg, W, H, oit_layers=8, flags=engine.OIT_FLAG_CUDA_GRAPH)
+    r = engine.Renderer(st)
+    mesh = engine.DeviceMesh(v, i)
+    r.update_scene(sd)
+    for k in range(3):
+        r.render_frame(mesh, tpo, 70)
+        np.testing.assert_array_equal(r.output(), plain['image'])
+        assert r.fragment_count() == plain['fragments']
+    assert r.get_error() == 0

@@ -25,6 +25,7 @@ OIT_AA_NONE, OIT_AA_MSAA_4X, OIT_AA_SSAA_4X, OIT_AA_SUPER_4X, OIT_AA_MSAA_8X, OI
 OIT_RECORD_RGBA8, OIT_RECORD_RGBA32F = 0, 1
 OIT_WEIGHTED_FP16, OIT_WEIGHTED_FP32 = 0, 1
 OIT_FLAG_LINEAR_OUTPUT = 0x1
+OIT_FLAG_CUDA_GRAPH = 0x2
 
 OIT_OK = 0
 OIT_ERR_INVALID_ARGUMENT = -1

@@ -144,6 +144,7 @@ struct oit_context {
       cudaEventDestroy(p.b);
     }
     for (cudaEvent_t e : prof_free) cudaEventDestroy(e);
+    drop_graph();
     for (PairStat& p : pair_stats) {
       if (p.ev) cudaEventDestroy(p.ev);
       if (p.host_total) cudaFreeHost(p.host_total);
@@ -190,8 +191,8 @@ struct oit_context {
     OIT_TRY_CUDA(out.ensure((size_t)W * H * 4), "alloc out");
     OIT_TRY_CUDA(err.ensure(4), "alloc err");
     OIT_TRY_CUDA(frag.ensure(8), "alloc frag");
-    OIT_TRY_CUDA(tile_begin.ensure((size_t)num_tiles * 4), "alloc bins");
-    OIT_TRY_CUDA(tile_end.ensure((size_t)num_tiles * 4), "alloc bins");
+    OIT_TRY_CUDA(tile_begin.ensure((size_t)2 * num_tiles * 4), "alloc bins");
+    OIT_TRY_CUDA(tile_end.ensure((size_t)2 * num_tiles * 4), "alloc bins");
     OIT_TRY_CUDA(total.ensure(4), "alloc total");
     OIT_TRY_CUDA(cudaMemset(err.p, 0, 4), "memset");
     OIT_TRY_CUDA(cudaMemset(frag.p, 0, 8), "memset");
@@ -234,7 +235,7 @@ struct oit_context {
     return OIT_OK;
   }
 
-  oit::SetupParams setup_params(const oit_mesh* mesh, uint32_t first, uint32_t count, int cull_back) {
+  oit::SetupParams setup_params(const oit_mesh* mesh, uint32_t first, uint32_t count, uint32_t opaque_from) {
     oit::SetupParams sp{};
     sp.vertices = mesh->vertices_device;
     sp.indices = mesh->indices_device;
@@ -246,12 +247,13 @@ struct oit_context {
     sp.RH = RH;
     sp.alpha_min = st.alpha_min;
     sp.alpha_width = st.alpha_width;
-    sp.cull_back = cull_back;
+    sp.opaque_from = opaque_from;
     sp.samples = S;
     sp.tiles_x = tiles_x;
+    sp.num_tiles = num_tiles;
     sp.bbox = bbox.as<uint2>();
     sp.setup = setup.p;
-    sp.persp = (alg() == oit::Alg::Weighted && !cull_back) ? persp.p : nullptr;
+    sp.persp = (alg() == oit::Alg::Weighted && opaque_from > 0) ? persp.p : nullptr;
     sp.pair_count = pair_count.as<uint32_t>();
     return sp;
   }
@@ -292,22 +294,25 @@ struct oit_context {
   }
 
   // Setup + binning of one draw; afterwards tile_begin/tile_end/tris describe it.
-  int bin(const oit_mesh* mesh, uint32_t first, uint32_t count, int cull_back, cudaStream_t s) {
+  // Triangles [first, first + opaque_from) are transparent, the rest of the
+  // range opaque; one setup, scan and sort bins both kinds.
+  int bin(const oit_mesh* mesh, uint32_t first, uint32_t count, uint32_t opaque_from, cudaStream_t s) {
     int r = ensure_triangles(count);
     if (r != OIT_OK) return r;
-    const uint64_t key = ((uint64_t)first << 33) ^ ((uint64_t)count << 1) ^ (uint64_t)(cull_back & 1) ^
+    const uint64_t key = ((uint64_t)first << 32) ^ ((uint64_t)count << 1) ^ ((uint64_t)opaque_from * 0x9E3779B1ull) ^
                          ((uint64_t)(uintptr_t)mesh->indices_device << 7);
     PairStat* ps = pair_stat(key);
-    if (ps && ps->pending && cudaEventQuery(ps->ev) == cudaSuccess) {
+    if (ps && ps->pending && !capturing && cudaEventQuery(ps->ev) == cudaSuccess) {
       ps->known = std::max(ps->known, *ps->host_total);
       ps->pending = false;
     }
     r = ensure_pairs(ps ? ps->known : 0);
     if (r != OIT_OK) return r;
-    oit::SetupParams sp = setup_params(mesh, first, count, cull_back);
+    oit::SetupParams sp = setup_params(mesh, first, count, opaque_from);
     oit::Bins b = bins();
     OIT_TRY_CUDA(oit::bin_setup_scan(sp, b, s, &launches), "bin_setup_scan");
     if (!ps) {
+      if (capturing) return OIT_ERR_STATE;  // a captured frame never sizes bins
       // first draw of this signature: size the bins exactly
       PairStat st;
       st.key = key;
@@ -328,15 +333,18 @@ struct oit_context {
       std::swap(keys, keys_alt);
       std::swap(tris, tris_alt);
     }
-    if (!ps->pending) {
+    if (!ps->pending || capturing) {
       OIT_TRY_CUDA(cudaMemcpyAsync(ps->host_total, total.p, 4, cudaMemcpyDeviceToHost, s), "d2h");
-      OIT_TRY_CUDA(cudaEventRecord(ps->ev, s), "event");
-      ps->pending = true;
+      if (!capturing) {
+        OIT_TRY_CUDA(cudaEventRecord(ps->ev, s), "event");
+        ps->pending = true;
+      }
     }
+    if (capturing) graph_stats.push_back(ps->key);
     return OIT_OK;
   }
 
-  oit::RasterParams raster_params() {
+  oit::RasterParams raster_params(int tile_offset) {
     oit::RasterParams p{};
     p.RW = RW;
     p.RH = RH;
@@ -349,6 +357,7 @@ struct oit_context {
     p.coverage = coverage;
     p.tile_begin = tile_begin.as<uint32_t>();
     p.tile_end = tile_end.as<uint32_t>();
+    p.tile_offset = tile_offset;
     p.tile_tris = tris.as<uint32_t>();
     p.bbox = bbox.as<uint2>();
     p.setup = setup.p;
@@ -406,6 +415,17 @@ struct oit_context {
 
   int draw_opaque(const oit_mesh* mesh, uint32_t first, uint32_t count, cudaStream_t s) {
     last_stream = s;
+    int r = clear_opaque_targets(s);
+    if (r != OIT_OK) return r;
+    if (!count) return OIT_OK;
+    cudaEvent_t t0 = prof_begin(s);
+    r = bin(mesh, first, count, 0u, s);
+    if (r != OIT_OK) return r;
+    prof_end(OIT_PROF_OPAQUE_BIN, t0, s);
+    return raster_opaque(s);
+  }
+
+  int clear_opaque_targets(cudaStream_t s) {
     int r = ensure_opaque_buffers();
     if (r != OIT_OK) return r;
     if (!opaque_valid) {
@@ -414,31 +434,33 @@ struct oit_context {
       launches += 2;
       opaque_valid = true;
     }
-    if (!count) return OIT_OK;
-    cudaEvent_t t0 = prof_begin(s);
-    r = bin(mesh, first, count, 1, s);
-    if (r != OIT_OK) return r;
-    prof_end(OIT_PROF_OPAQUE_BIN, t0, s);
-    oit::RasterParams p = raster_params();
+    return OIT_OK;
+  }
+
+  int raster_opaque(cudaStream_t s) {
+    oit::RasterParams p = raster_params(0);
     cudaEvent_t t1 = prof_begin(s);
-    r = raster(oit::Alg::Opaque, p, s);
+    const int r = raster(oit::Alg::Opaque, p, s);
     prof_end(OIT_PROF_OPAQUE_RASTER, t1, s);
+    return r;
+  }
+
+  int raster_transparent(cudaStream_t s) {
+    oit::RasterParams p = raster_params(num_tiles);
+    cudaEvent_t t1 = prof_begin(s);
+    const int r = raster(alg(), p, s);
+    prof_end(OIT_PROF_TRANSPARENT_RASTER, t1, s);
+    if (r == OIT_OK) color_valid = true;
     return r;
   }
 
   int draw_transparent_color(const oit_mesh* mesh, uint32_t first, uint32_t count, cudaStream_t s) {
     last_stream = s;
     cudaEvent_t t0 = prof_begin(s);
-    int r = bin(mesh, first, count, 0, s);
+    int r = bin(mesh, first, count, count, s);
     if (r != OIT_OK) return r;
     prof_end(OIT_PROF_TRANSPARENT_BIN, t0, s);
-    oit::RasterParams p = raster_params();
-    cudaEvent_t t1 = prof_begin(s);
-    r = raster(alg(), p, s);
-    prof_end(OIT_PROF_TRANSPARENT_RASTER, t1, s);
-    if (r != OIT_OK) return r;
-    color_valid = true;
-    return OIT_OK;
+    return raster_transparent(s);
   }
 
   int composite(uint8_t* out_dev, cudaStream_t s) {
@@ -479,19 +501,101 @@ struct oit_context {
     return r;
   }
 
-  int render_frame(const oit_mesh* mesh, uint32_t tpo, int32_t percent, uint8_t* out_dev, cudaStream_t s) {
-    if (!mesh || !tpo || percent < 0) return OIT_ERR_INVALID_ARGUMENT;
-    // Sample::onRender, oitRender.cpp:43-153
+  // Sample::onRender, oitRender.cpp:43-153. The transparent objects are the
+  // first percent_transparent% of the mesh and the opaque ones the rest, so one
+  // binning pass serves both the opaque and the transparent raster.
+  int render_frame_body(const oit_mesh* mesh, uint32_t tpo, int32_t percent, uint8_t* out_dev, cudaStream_t s) {
     const uint32_t num_objects = mesh->num_triangles / tpo;
     uint32_t num_transparent = (uint32_t)(((uint64_t)num_objects * (uint32_t)percent) / 100u);
     if (num_transparent > num_objects) num_transparent = num_objects;
     const uint32_t num_opaque = num_objects - num_transparent;
+    const uint32_t nt = num_transparent * tpo, total_tris = num_objects * tpo;
     int r = begin_frame(s);
     if (r == OIT_OK) r = clear_transparent(s);
-    if (r == OIT_OK && num_opaque > 0) r = draw_opaque(mesh, num_transparent * tpo, num_opaque * tpo, s);
-    if (r == OIT_OK) r = draw_transparent_color(mesh, 0, num_transparent * tpo, s);
+    if (r == OIT_OK && num_opaque > 0) r = clear_opaque_targets(s);
+    if (r != OIT_OK) return r;
+    cudaEvent_t t0 = prof_begin(s);
+    r = bin(mesh, 0, total_tris, nt, s);
+    if (r != OIT_OK) return r;
+    prof_end(OIT_PROF_TRANSPARENT_BIN, t0, s);
+    if (num_opaque > 0) r = raster_opaque(s);
+    if (r == OIT_OK) r = raster_transparent(s);
     if (r == OIT_OK) r = composite(out_dev, s);
     return r;
+  }
+
+  // ---- CUDA graph of a whole frame (OIT_FLAG_CUDA_GRAPH) ----
+  bool capturing = false;
+  cudaGraphExec_t graph_exec = nullptr;
+  uint64_t graph_sig = 0;
+  uint64_t graph_launches = 0;
+  bool graph_opaque_valid = false;
+  std::vector<uint64_t> graph_stats;
+
+  void drop_graph() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
+    graph_sig = 0;
+  }
+
+  int render_frame(const oit_mesh* mesh, uint32_t tpo, int32_t percent, uint8_t* out_dev, cudaStream_t s) {
+    if (!mesh || !tpo || percent < 0) return OIT_ERR_INVALID_ARGUMENT;
+    last_stream = s;
+    if (!(st.flags & OIT_FLAG_CUDA_GRAPH) || prof_on) return render_frame_body(mesh, tpo, percent, out_dev, s);
+    uint64_t sig = 1469598103934665603ull;
+    const uint64_t parts[] = {(uint64_t)(uintptr_t)mesh->vertices_device, (uint64_t)(uintptr_t)mesh->indices_device,
+                              mesh->num_triangles, tpo, (uint64_t)percent, (uint64_t)(uintptr_t)out_dev,
+                              (uint64_t)(uintptr_t)s};
+    for (uint64_t v : parts) sig = (sig ^ v) * 1099511628211ull;
+    // bins that outgrew their capacity since the capture invalidate the graph
+    for (uint64_t k : graph_stats) {
+      PairStat* ps = pair_stat(k);
+      if (ps && ps->pending && cudaEventQuery(ps->ev) == cudaSuccess) {
+        ps->known = std::max(ps->known, *ps->host_total);
+        ps->pending = false;
+      }
+      if (ps && ps->known > pair_cap) drop_graph();
+    }
+    if (!graph_exec || graph_sig != sig) {
+      drop_graph();
+      // one plain frame sizes every buffer, then the same frame is captured
+      int r = render_frame_body(mesh, tpo, percent, out_dev, s);
+      if (r != OIT_OK) return r;
+      OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
+      graph_stats.clear();
+      const uint64_t l0 = launches;
+      OIT_TRY_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), "capture");
+      capturing = true;
+      r = render_frame_body(mesh, tpo, percent, out_dev, s);
+      capturing = false;
+      cudaGraph_t g = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(s, &g);
+      if (r != OIT_OK) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+      }
+      OIT_TRY_CUDA(ce, "end capture");
+      const cudaError_t ie = cudaGraphInstantiate(&graph_exec, g, 0);
+      cudaGraphDestroy(g);
+      OIT_TRY_CUDA(ie, "instantiate");
+      graph_sig = sig;
+      graph_opaque_valid = opaque_valid;
+      graph_launches = launches - l0;
+      launches = l0;
+      return OIT_OK;  // the plain frame above produced this call's image
+    }
+    OIT_TRY_CUDA(cudaGraphLaunch(graph_exec, s), "graph launch");
+    launches += graph_launches;
+    for (uint64_t k : graph_stats) {
+      PairStat* ps = pair_stat(k);
+      if (ps && !ps->pending) {
+        OIT_TRY_CUDA(cudaEventRecord(ps->ev, s), "event");
+        ps->pending = true;
+      }
+    }
+    opaque_valid = graph_opaque_valid;  // as left by the captured frame
+    color_valid = true;
+    return OIT_OK;
   }
 };
 
@@ -583,7 +687,7 @@ int oit_create(const oit_state* state, oit_context** out_ctx) {
   c->tiles_y = (c->RH + oit::kTile - 1) / oit::kTile;
   c->num_tiles = c->tiles_x * c->tiles_y;
   c->key_bits = 1;
-  while ((1 << c->key_bits) < c->num_tiles) ++c->key_bits;
+  while ((1 << c->key_bits) < 2 * c->num_tiles) ++c->key_bits;  // opaque and transparent lists
   if (state->algorithm == OIT_LINKEDLIST) {
     const uint64_t cap = (uint64_t)state->linked_list_allocated_per_element * c->P;  // oit.cpp:125
     if (cap >= 0xFFFFFFFFull) {

@@ -26,9 +26,10 @@ struct SetupParams {
   Mat4 view;
   int RW, RH;
   float alpha_min, alpha_width;
-  int cull_back;
+  uint32_t opaque_from;     // triangles t >= opaque_from (relative) are opaque: back faces culled, kind 0
   int samples;             // MSAA samples per pixel (1, 4, 8)
   int tiles_x;
+  int num_tiles;           // key = tile + (transparent ? num_tiles : 0)
   // outputs
   uint2* bbox;            // [num_triangles] pixel bbox (x0 | y0 << 16, x1 | y1 << 16)
   void* setup;            // [num_triangles] TriSetup records (96 B)
@@ -73,8 +74,9 @@ struct RasterParams {
   int L;                         // OIT_LAYERS
   int tail;                      // OIT_TAILBLEND
   int coverage;                  // OIT_COVERAGE_SHADING
-  const uint32_t* tile_begin;
+  const uint32_t* tile_begin;    // indexed by tile + tile_offset
   const uint32_t* tile_end;
+  int tile_offset;               // 0: opaque lists, num_tiles: transparent lists
   const uint32_t* tile_tris;
   const uint2* bbox;
   const void* setup;

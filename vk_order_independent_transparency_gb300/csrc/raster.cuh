@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
   Pol pol;
   pol.init(p, pol_smem, w.lane, w.pixel);
 
-  const int tile = blockIdx.x;
+  const int tile = blockIdx.x + p.tile_offset;
   const uint32_t beg = p.tile_begin[tile], end = p.tile_end[tile];
   const TriPersp* __restrict__ persp = reinterpret_cast<const TriPersp*>(p.persp);
   const uint32_t lt = (1u << w.lane) - 1u;
@@ -632,7 +632,7 @@ __global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
     dep[s] = w.valid ? p.depth[(size_t)s * p.P + w.pixel] : 0x3F800000u;
     col[s] = w.valid ? p.opaque_color[(size_t)s * p.P + w.pixel] : p.background;
   }
-  const int tile = blockIdx.x;
+  const int tile = blockIdx.x + p.tile_offset;
   walk_tile(p, w, stage, nullptr, p.tile_begin[tile], p.tile_end[tile], [&](int k, uint32_t, bool inb) {
     if (!inb) return;  // no warp-collective operation follows
     const TriSetup& T = stage[k];

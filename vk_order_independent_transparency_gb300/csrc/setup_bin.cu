@@ -84,8 +84,9 @@ __global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
     area = (long long)(X[1] - X[0]) * (long long)(Y[2] - Y[0]) - (long long)(Y[1] - Y[0]) * (long long)(X[2] - X[0]);
     if (area == 0) ok = false;
     // area > 0: clockwise on the y-down framebuffer = back face for
-    // VK_FRONT_FACE_COUNTER_CLOCKWISE (main.cpp:520-525).
-    if (area > 0 && p.cull_back) ok = false;
+    // VK_FRONT_FACE_COUNTER_CLOCKWISE (main.cpp:520-525); only opaque
+    // triangles cull back faces (transparent ones are double-sided, oit.cpp:703).
+    if (area > 0 && t >= p.opaque_from) ok = false;
   }
   int o1 = 1, o2 = 2;
   if (ok && area < 0) {
@@ -260,7 +261,7 @@ cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, size_t n, uint32_t
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_emit(const uint32_t* __restrict__ pair_count,
                                               const uint32_t* __restrict__ pair_offset, const uint2* __restrict__ bbox,
-                                              uint32_t n, int tiles_x, uint32_t tile_base,
+                                              uint32_t n, int tiles_x, uint32_t opaque_from, uint32_t num_tiles,
                                               uint32_t* __restrict__ keys, uint32_t* __restrict__ tris,
                                               size_t capacity, const uint32_t* __restrict__ total, uint32_t* err) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -272,6 +273,7 @@ __global__ void __launch_bounds__(256) k_emit(const uint32_t* __restrict__ pair_
   const uint2 bb = bbox[t];
   const int tx0 = (bb.x & 0xFFFF) / kTile, ty0 = (bb.x >> 16) / kTile;
   const int tx1 = (bb.y & 0xFFFF) / kTile, ty1 = (bb.y >> 16) / kTile;
+  const uint32_t tile_base = t < opaque_from ? num_tiles : 0u;
   uint32_t j = 0;
   for (int ty = ty0; ty <= ty1; ++ty)
     for (int tx = tx0; tx <= tx1; ++tx, ++j) {
@@ -446,8 +448,8 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles
   cudaError_t e;
   const uint32_t n = sp.num_triangles;
   if (n > 0) {
-    k_emit<<<(n + 255) / 256, 256, 0, s>>>(sp.pair_count, b.pair_offset, sp.bbox, n, sp.tiles_x, 0u, b.keys,
-                                           b.tris, b.capacity, b.total, error);
+    k_emit<<<(n + 255) / 256, 256, 0, s>>>(sp.pair_count, b.pair_offset, sp.bbox, n, sp.tiles_x, sp.opaque_from,
+                                           (uint32_t)sp.num_tiles, b.keys, b.tris, b.capacity, b.total, error);
     ++*launches;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
@@ -468,8 +470,9 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles
     std::swap(b.keys, b.keys_alt);
     std::swap(b.tris, b.tris_alt);
   }
-  k_tile_ranges<<<(num_tiles + 255) / 256, 256, 0, s>>>(b.keys, b.total, b.capacity, num_tiles, b.tile_begin,
-                                                         b.tile_end);
+  // ranges of both kinds: [0, num_tiles) opaque, [num_tiles, 2 num_tiles) transparent
+  k_tile_ranges<<<(2 * num_tiles + 255) / 256, 256, 0, s>>>(b.keys, b.total, b.capacity, 2 * num_tiles,
+                                                             b.tile_begin, b.tile_end);
   ++*launches;
   return cudaGetLastError();
 }
