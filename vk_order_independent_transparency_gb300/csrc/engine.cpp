@@ -145,6 +145,9 @@ struct oit_context {
     }
     for (cudaEvent_t e : prof_free) cudaEventDestroy(e);
     drop_graph();
+    if (graph_stream) cudaStreamDestroy(graph_stream);
+    if (graph_in) cudaEventDestroy(graph_in);
+    if (graph_out) cudaEventDestroy(graph_out);
     for (PairStat& p : pair_stats) {
       if (p.ev) cudaEventDestroy(p.ev);
       if (p.host_total) cudaFreeHost(p.host_total);
@@ -532,10 +535,24 @@ struct oit_context {
   bool graph_opaque_valid = false;
   std::vector<uint64_t> graph_stats;
 
+  // Graphs are captured and replayed on a stream the context owns (the legacy
+  // default stream cannot be captured); events order it after and before the
+  // caller's stream.
+  cudaStream_t graph_stream = nullptr;
+  cudaEvent_t graph_in = nullptr, graph_out = nullptr;
+
   void drop_graph() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     graph_exec = nullptr;
     graph_sig = 0;
+  }
+
+  int ensure_graph_stream() {
+    if (graph_stream) return OIT_OK;
+    OIT_TRY_CUDA(cudaStreamCreateWithFlags(&graph_stream, cudaStreamNonBlocking), "stream");
+    OIT_TRY_CUDA(cudaEventCreateWithFlags(&graph_in, cudaEventDisableTiming), "event");
+    OIT_TRY_CUDA(cudaEventCreateWithFlags(&graph_out, cudaEventDisableTiming), "event");
+    return OIT_OK;
   }
 
   int render_frame(const oit_mesh* mesh, uint32_t tpo, int32_t percent, uint8_t* out_dev, cudaStream_t s) {
@@ -556,6 +573,8 @@ struct oit_context {
       }
       if (ps && ps->known > pair_cap) drop_graph();
     }
+    int gr = ensure_graph_stream();
+    if (gr != OIT_OK) return gr;
     if (!graph_exec || graph_sig != sig) {
       drop_graph();
       // one plain frame sizes every buffer, then the same frame is captured
@@ -564,12 +583,13 @@ struct oit_context {
       OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
       graph_stats.clear();
       const uint64_t l0 = launches;
-      OIT_TRY_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), "capture");
+      OIT_TRY_CUDA(cudaStreamBeginCapture(graph_stream, cudaStreamCaptureModeRelaxed), "capture");
       capturing = true;
-      r = render_frame_body(mesh, tpo, percent, out_dev, s);
+      r = render_frame_body(mesh, tpo, percent, out_dev, graph_stream);
       capturing = false;
+      last_stream = s;
       cudaGraph_t g = nullptr;
-      const cudaError_t ce = cudaStreamEndCapture(s, &g);
+      const cudaError_t ce = cudaStreamEndCapture(graph_stream, &g);
       if (r != OIT_OK) {
         if (g) cudaGraphDestroy(g);
         return r;
@@ -584,12 +604,16 @@ struct oit_context {
       launches = l0;
       return OIT_OK;  // the plain frame above produced this call's image
     }
-    OIT_TRY_CUDA(cudaGraphLaunch(graph_exec, s), "graph launch");
+    OIT_TRY_CUDA(cudaEventRecord(graph_in, s), "event");
+    OIT_TRY_CUDA(cudaStreamWaitEvent(graph_stream, graph_in, 0), "wait");
+    OIT_TRY_CUDA(cudaGraphLaunch(graph_exec, graph_stream), "graph launch");
+    OIT_TRY_CUDA(cudaEventRecord(graph_out, graph_stream), "event");
+    OIT_TRY_CUDA(cudaStreamWaitEvent(s, graph_out, 0), "wait");
     launches += graph_launches;
     for (uint64_t k : graph_stats) {
       PairStat* ps = pair_stat(k);
       if (ps && !ps->pending) {
-        OIT_TRY_CUDA(cudaEventRecord(ps->ev, s), "event");
+        OIT_TRY_CUDA(cudaEventRecord(ps->ev, graph_stream), "event");
         ps->pending = true;
       }
     }

@@ -684,9 +684,17 @@ template <template <int> class Pol, int S>
 cudaError_t launch_transparent_s(const RasterParams& p, cudaStream_t s) {
   const size_t smem = (size_t)oit::kWarpsPerTile * (kWarpStageBytes + Pol<S>::smem_bytes_per_warp(p.L, p.coverage));
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_raster_transparent<Pol, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
+    // raise the kernel's dynamic shared memory cap once per device (never
+    // while a CUDA graph is being captured after the first frame)
+    static int cap_set[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || cap_set[dev] < (int)smem) {
+      cudaError_t e = cudaFuncSetAttribute(k_raster_transparent<Pol, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+      if (e != cudaSuccess) return e;
+      if (dev >= 0 && dev < 64) cap_set[dev] = (int)smem;
+    }
   }
   k_raster_transparent<Pol, S><<<(unsigned)(p.tiles_x * p.tiles_y), 256, smem, s>>>(p);
   return cudaGetLastError();
