@@ -67,6 +67,7 @@ extern "C" {
 #define OIT_ERR_CUDA (-4)
 #define OIT_ERR_DEVICE (-5)      /* a kernel raised a device error bit, see oit_get_error */
 #define OIT_ERR_STATE (-6)       /* call made out of order (e.g. composite before draw) */
+#define OIT_ERR_TOO_LARGE (-7)   /* the frame does not fit oit_render_frame_noalloc's scratch arena */
 
 /* Device error bits reported by oit_get_error. */
 #define OIT_DEVERR_BIN_OVERFLOW 0x1u  /* triangle/tile pairs exceeded the bin capacity */
@@ -183,6 +184,27 @@ int oit_render_frame_host(oit_context* ctx, const float* vertices_host, uint32_t
                           const uint32_t* indices_host, uint32_t num_triangles,
                           uint32_t triangles_per_object, int32_t percent_transparent,
                           uint8_t* out_rgba8_host, void* stream);
+
+/* One whole frame, like oit_render_frame, that allocates no device memory.
+ * No counterpart in the reference: it exists for callers that cannot let a
+ * library call cudaMalloc -- applications that own every device allocation
+ * and give plugins a fixed budget, per-frame paths where cudaMalloc/cudaFree
+ * may synchronise the device and stall other streams, and processes near a
+ * device-memory limit where a mid-frame allocation can fail.
+ * All per-frame scratch (setup records, tile bins, sort scratch, A-buffer,
+ * colour and depth targets) lives in one 64 MiB device array that every
+ * device loading the library holds until the process exits; frames that do
+ * not fit return OIT_ERR_TOO_LARGE. The caller passes the state, scene, mesh
+ * (device) and width*height*4 bytes of device output. 1x and MSAA modes with
+ * RGBA8 records only (supersampling and sample shading return
+ * OIT_ERR_UNSUPPORTED). The call is synchronous on `stream`. The first call
+ * on a device looks up the array's device address (once per device, with
+ * that device current); make it before any stream capture. Every call reuses
+ * the same array, so calls that overlap on the GPU (other host threads,
+ * other streams) race and must be serialised by the caller. */
+int oit_render_frame_noalloc(const oit_state* state, const oit_scene_data* scene, const oit_mesh* mesh,
+                             uint32_t triangles_per_object, int32_t percent_transparent,
+                             uint8_t* out_rgba8_device, void* stream);
 
 /* ---- inspection -------------------------------------------------------- */
 

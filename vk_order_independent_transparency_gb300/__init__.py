@@ -34,6 +34,7 @@ OIT_ERR_OUT_OF_MEMORY = -3
 OIT_ERR_CUDA = -4
 OIT_ERR_DEVICE = -5
 OIT_ERR_STATE = -6
+OIT_ERR_TOO_LARGE = -7
 
 OIT_BUF_ABUFFER, OIT_BUF_AUX, OIT_BUF_AUXDEPTH, OIT_BUF_COUNTER, OIT_BUF_DEPTH, OIT_BUF_OPAQUE_COLOR, \
     OIT_BUF_COLOR, OIT_BUF_ACCUM, OIT_BUF_REVEAL, OIT_BUF_OUTPUT, OIT_BUF_OUTPUT_LINEAR = range(11)
@@ -45,7 +46,7 @@ EXPORTS = [
     'oit_render_frame', 'oit_render_frame_host', 'oit_get_error', 'oit_get_buffer',
     'oit_get_fragment_count', 'oit_get_launch_count', 'oit_status_string', 'oit_abuffer_bytes',
     'oit_scene_size', 'oit_scene_generate', 'oit_camera', 'oit_srgb_tables', 'oit_version',
-    'oit_profile_enable', 'oit_profile_read',
+    'oit_profile_enable', 'oit_profile_read', 'oit_render_frame_noalloc',
 ]
 PROF_SECTIONS = ['opaque_bin', 'opaque_raster', 'transparent_bin', 'transparent_raster', 'composite']
 
@@ -125,6 +126,8 @@ def library():
         'oit_srgb_tables': (I, [P, P]),
         'oit_version': (I, []),
         'oit_profile_enable': (I, [P, I]),
+        'oit_render_frame_noalloc': (I, [ctypes.POINTER(OitState), ctypes.POINTER(OitSceneData),
+                                         ctypes.POINTER(OitMesh), U, ctypes.c_int32, P, P]),
         'oit_profile_read': (I, [P, ctypes.POINTER(ctypes.c_double * 5), ctypes.POINTER(ctypes.c_uint64 * 5)]),
     }
     for name, (res, args) in sig.items():

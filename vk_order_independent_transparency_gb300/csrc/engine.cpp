@@ -888,6 +888,7 @@ const char* oit_status_string(int status) {
     case OIT_ERR_CUDA: return "CUDA error";
     case OIT_ERR_DEVICE: return "device error flag raised";
     case OIT_ERR_STATE: return "call out of order";
+    case OIT_ERR_TOO_LARGE: return "frame exceeds the no-allocation scratch arena";
     default: return "unknown status";
   }
 }
