@@ -650,7 +650,9 @@ static void raster_transparent(or_frame* f, const tri_setup* T, int loop_pass) {
     for (int px = T->bx0; px <= T->bx1; ++px) {
       size_t pixel = (size_t)py * f->RW + px;
       int32_t bx = px * 256, by = py * 256;
-      if (f->p.sample_shading) {
+      /* WBOIT never uses per-sample A-buffers: its COLOR shader does not read
+       * gl_SampleID (oitColorDepthDefines.glsl:49), so it shades per pixel */
+      if (f->p.sample_shading && f->p.algorithm != OR_WEIGHTED) {
         for (int s = 0; s < S; ++s) {
           int64_t e[3];
           edges_at(T, bx + st[s][0], by + st[s][1], e);

@@ -85,32 +85,35 @@ def walk_lists(pool_words, heads):
     return out
 
 
-def compare_abuffer(algorithm, g, o, L, P, coverage):
-    """Bit-exact comparison of the algorithm's A-buffer state."""
+def compare_abuffer(algorithm, g, o, L, P, coverage, ssn=1):
+    """Bit-exact comparison of the algorithm's A-buffer state. With sample
+    shading (ssn > 1) every sample has its own A-buffer block."""
     if algorithm in (oit.OIT_SIMPLE, oit.OIT_SPINLOCK, oit.OIT_INTERLOCK):
-        np.testing.assert_array_equal(g['aux'][:P], o['aux'][:P])
+        np.testing.assert_array_equal(g['aux'][:ssn * P], o['aux'][:ssn * P])
         words = 4 if coverage else 2
-        ga = g['abuf'][:L * P * words].reshape(L, P, words)
-        oa = o['abuf'][:L * P * words].reshape(L, P, words)
-        n = np.minimum(o['aux'][:P], L)
-        for layer in range(L):
-            sel = n > layer
-            np.testing.assert_array_equal(ga[layer][sel], oa[layer][sel], err_msg='layer %d' % layer)
+        ga = g['abuf'][:ssn * L * P * words].reshape(ssn, L, P, words)
+        oa = o['abuf'][:ssn * L * P * words].reshape(ssn, L, P, words)
+        n = np.minimum(o['aux'][:ssn * P].reshape(ssn, P), L)
+        for s in range(ssn):
+            for layer in range(L):
+                sel = n[s] > layer
+                np.testing.assert_array_equal(ga[s, layer][sel], oa[s, layer][sel], err_msg='sample %d layer %d' % (s, layer))
         if algorithm != oit.OIT_SIMPLE:
-            np.testing.assert_array_equal(g['auxdepth'][:P], o['auxdepth'][:P])
+            np.testing.assert_array_equal(g['auxdepth'][:ssn * P], o['auxdepth'][:ssn * P])
     elif algorithm == oit.OIT_LINKEDLIST:
         assert g['counter'][0] == o['counter'][0]
-        assert walk_lists(g['abuf'], g['aux'][:P]) == walk_lists(o['abuf'], o['aux'][:P])
+        assert walk_lists(g['abuf'], g['aux'][:ssn * P]) == walk_lists(o['abuf'], o['aux'][:ssn * P])
     elif algorithm == oit.OIT_LOOP:
-        ga = g['abuf'][:2 * L * P].reshape(2 * L, P)
-        oa = o['abuf'][:2 * L * P].reshape(2 * L, P)
-        np.testing.assert_array_equal(ga[:L], oa[:L])
-        count = (oa[:L] != 0xFFFFFFFF).sum(axis=0)
-        for layer in range(L):
-            sel = count > layer
-            np.testing.assert_array_equal(ga[L + layer][sel], oa[L + layer][sel])
+        ga = g['abuf'][:ssn * 2 * L * P].reshape(ssn, 2 * L, P)
+        oa = o['abuf'][:ssn * 2 * L * P].reshape(ssn, 2 * L, P)
+        np.testing.assert_array_equal(ga[:, :L], oa[:, :L])
+        for s in range(ssn):
+            count = (oa[s, :L] != 0xFFFFFFFF).sum(axis=0)
+            for layer in range(L):
+                sel = count > layer
+                np.testing.assert_array_equal(ga[s, L + layer][sel], oa[s, L + layer][sel])
     elif algorithm == oit.OIT_LOOP64:
-        np.testing.assert_array_equal(g['abuf'][:2 * L * P], o['abuf'][:2 * L * P])
+        np.testing.assert_array_equal(g['abuf'][:ssn * 2 * L * P], o['abuf'][:ssn * 2 * L * P])
 
 
 def compare_images(g, o, max_lsb=1):

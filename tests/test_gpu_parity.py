@@ -14,7 +14,7 @@ import parity_util as pu
 pytestmark = pytest.mark.gpu
 
 ALGS = [0, 1, 2, 3, 4, 5, 6]
-AA = {'1x': 0, 'msaa4': 1, 'msaa8': 4}
+AA = {'1x': 0, 'msaa4': 1, 'msaa8': 4, 'ssaa4': 2, 'ssaa8': 5}
 
 
 def run_pair(engine, alg, W, H, n_obj, percent=100, seed=3, rmin=0.05, rmax=0.2, **kw):
@@ -25,15 +25,19 @@ def run_pair(engine, alg, W, H, n_obj, percent=100, seed=3, rmin=0.05, rmax=0.2,
 
 
 def check(engine, alg, g, o, W, H, L, aa=0, ss=1):
-    msaa = {0: 1, 1: 4, 4: 8, 3: 1}[aa]
-    coverage = msaa > 1
+    msaa, sample_shading, _ = engine.aa_settings(aa)
+    coverage = msaa > 1 and not sample_shading
+    ssn = msaa if sample_shading else 1
     P = W * H * ss * ss
     assert g['error'] == 0
     assert g['fragments'] == o['fragments']
     if alg != engine.OIT_WEIGHTED:
-        pu.compare_abuffer(alg, g, o, L, P, coverage)
-        ref_col = o['color_samples'].mean(axis=0)
-        np.testing.assert_allclose(g['color'][:P], ref_col, atol=2e-5, rtol=0)
+        pu.compare_abuffer(alg, g, o, L, P, coverage, ssn)
+        if ssn > 1:
+            ref_col = o['color_samples'].reshape(-1, 4)
+        else:
+            ref_col = o['color_samples'].mean(axis=0)
+        np.testing.assert_allclose(g['color'][:ssn * P], ref_col, atol=2e-5, rtol=0)
     pu.compare_images(g, o)
 
 
@@ -54,6 +58,13 @@ def test_layers(engine, alg, L):
     W, H = 96, 80
     g, o = run_pair(engine, alg, W, H, 48, seed=11, rmin=0.1, rmax=0.3, oit_layers=L, nodes_per_pixel=40)
     check(engine, alg, g, o, W, H, L)
+
+
+@pytest.mark.parametrize('alg', [0, 1, 2, 3, 4])
+def test_layers_sample_shading(engine, alg):
+    W, H, L = 64, 48, 16
+    g, o = run_pair(engine, alg, W, H, 32, seed=13, rmin=0.1, rmax=0.3, oit_layers=L, nodes_per_pixel=12, aa_type=5)
+    check(engine, alg, g, o, W, H, L, aa=5)
 
 
 @pytest.mark.parametrize('alg', ALGS)
@@ -174,7 +185,7 @@ def big_triangle_mesh(seed=5, n=24):
     return np.array(verts, np.float32), np.array(idx, np.uint32)
 
 
-@pytest.mark.parametrize('aa', [0, 4])
+@pytest.mark.parametrize('aa', [0, 4, 2])
 @pytest.mark.parametrize('alg', ALGS)
 def test_large_triangles(engine, alg, aa):
     W, H, L = 200, 150, 4

@@ -93,14 +93,14 @@ __device__ __forceinline__ float4 blend_array(const Arr<L>& a, int n, int covera
 // Interlock composites, oitSpinlock.frag.glsl:153-207 and
 // oitInterlock.frag.glsl:384-438, are identical).
 template <int L>
-__device__ __forceinline__ float4 composite_records(const CompositeParams& p, uint32_t pixel) {
-  int n = (int)min(p.aux[pixel], (uint32_t)L);
+__device__ __forceinline__ float4 composite_records(const CompositeParams& p, uint32_t eaux, size_t abase) {
+  int n = (int)min(p.aux[eaux], (uint32_t)L);
   Arr<L> a;
 #pragma unroll
   for (int i = 0; i < L; ++i) {
     a.c[i] = 0; a.d[i] = 0; a.m[i] = 0;
     if (i < n) {
-      const size_t o = (size_t)i * p.P + pixel;
+      const size_t o = abase + (size_t)i * p.P;
       if (p.coverage) {
         const uint4 r = reinterpret_cast<const uint4*>(p.abuf)[o];
         a.c[i] = r.x; a.d[i] = r.y; a.m[i] = r.z;
@@ -116,9 +116,9 @@ __device__ __forceinline__ float4 composite_records(const CompositeParams& p, ui
 
 // Linked list: oitLinkedList.frag.glsl:106-172.
 template <int L>
-__device__ __forceinline__ float4 composite_list(const CompositeParams& p, uint32_t pixel) {
+__device__ __forceinline__ float4 composite_list(const CompositeParams& p, uint32_t eaux) {
   const uint4* __restrict__ pool = reinterpret_cast<const uint4*>(p.abuf);
-  uint32_t off = p.aux[pixel];
+  uint32_t off = p.aux[eaux];
   if (off >= p.capacity) off = 0;
   int n = 0;
   Arr<L> a;
@@ -153,22 +153,22 @@ __device__ __forceinline__ float4 composite_list(const CompositeParams& p, uint3
 }
 
 // Loop32: oitLoop.frag.glsl:191-222.
-__device__ __forceinline__ float4 composite_loop(const CompositeParams& p, uint32_t pixel) {
+__device__ __forceinline__ float4 composite_loop(const CompositeParams& p, size_t abase) {
   int n = 0;
   for (int i = 0; i < p.L; ++i) {
-    if (p.abuf[(size_t)i * p.P + pixel] != kEmpty) n++; else break;
+    if (p.abuf[abase + (size_t)i * p.P] != kEmpty) n++; else break;
   }
   float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int i = 0; i < n; ++i) blend_under(sum, decode_premult(p.abuf[(size_t)(p.L + i) * p.P + pixel]));
+  for (int i = 0; i < n; ++i) blend_under(sum, decode_premult(p.abuf[abase + (size_t)(p.L + i) * p.P]));
   return sum;
 }
 
 // Loop64: oitLoop64.frag.glsl:162-183.
-__device__ __forceinline__ float4 composite_loop64(const CompositeParams& p, uint32_t pixel) {
+__device__ __forceinline__ float4 composite_loop64(const CompositeParams& p, size_t abase) {
   const uint2* __restrict__ ab = reinterpret_cast<const uint2*>(p.abuf);
   float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int i = 0; i < p.L; ++i) {
-    const uint2 k = ab[(size_t)i * p.P + pixel];
+    const uint2 k = ab[abase + (size_t)i * p.P];
     if (k.y == kEmpty) break;
     blend_under(sum, decode_premult(k.x));
   }
@@ -194,18 +194,25 @@ __global__ void __launch_bounds__(256) k_composite(CompositeParams p) {
   for (int dy = 0; dy < p.ss; ++dy)
     for (int dx = 0; dx < p.ss; ++dx) {
       const uint32_t pixel = (uint32_t)(y * p.ss + dy) * (uint32_t)p.RW + (uint32_t)(x * p.ss + dx);
-      float4 sum;
-      if (K == kRecords) sum = composite_records<L>(p, pixel);
-      else if (K == kList) sum = composite_list<L>(p, pixel);
-      else if (K == kLoop) sum = composite_loop(p, pixel);
-      else sum = composite_loop64(p, pixel);
-      // composite output over the colour target (which already holds the
-      // tail-blended, sample-averaged opaque + background colour)
-      float4 c = p.color[pixel];
-      rop_over(c, sum);
-      acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
+      // one composite per pixel, or per sample with sample shading (each
+      // sample has its own A-buffer at viewSize * layers * sampleID)
+      for (int s = 0; s < p.ssn; ++s) {
+        const uint32_t eaux = (uint32_t)s * p.P + pixel;
+        const size_t abase = (size_t)s * (K == kLoop ? 2 : 1) * p.L * p.P + pixel;
+        float4 sum;
+        if (K == kRecords) sum = composite_records<L>(p, eaux, abase);
+        else if (K == kList) sum = composite_list<L>(p, eaux);
+        else if (K == kLoop) sum = composite_loop(p, abase);
+        else sum = composite_loop64(p, abase);
+        // composite output over the colour target (which already holds the
+        // tail-blended opaque + background colour, sample-averaged unless
+        // sample shading keeps one per sample)
+        float4 c = p.color[eaux];
+        rop_over(c, sum);
+        acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
+      }
     }
-  const float k = 1.0f / (float)(p.ss * p.ss);
+  const float k = 1.0f / (float)(p.ss * p.ss * p.ssn);
   write_out(p, (uint32_t)y * (uint32_t)p.W + (uint32_t)x, make_float4(acc.x * k, acc.y * k, acc.z * k, acc.w * k));
 }
 

@@ -74,6 +74,7 @@ struct oit_context {
   int W = 0, H = 0, RW = 0, RH = 0;
   uint32_t P = 0;
   int S = 1, coverage = 0, L = 1;
+  int ssn = 1;  // samples with their own A-buffer (sample shading); WBOIT never uses them
   int tiles_x = 0, tiles_y = 0, num_tiles = 0, key_bits = 1;
   uint32_t capacity = 0;
   oit::Mat4 pv{}, view{};
@@ -163,7 +164,7 @@ struct oit_context {
   // ---- Sample::createFrameImages (oit.cpp:45-220) ----
   int create() {
     OIT_TRY_CUDA(depth.ensure(4), "alloc");
-    size_t elems = (size_t)P;  // A-buffer elements (no sample shading)
+    size_t elems = (size_t)P * ssn;  // A-buffer elements (pixels, or samples with sample shading)
     size_t abuf_bytes = 0;
     switch (alg()) {
       case oit::Alg::Simple:
@@ -185,7 +186,7 @@ struct oit_context {
     OIT_TRY_CUDA(aux.ensure(elems * 4), "alloc aux");
     OIT_TRY_CUDA(auxdepth.ensure(elems * 4), "alloc auxdepth");
     OIT_TRY_CUDA(counter.ensure(4), "alloc counter");
-    OIT_TRY_CUDA(color.ensure((size_t)P * 16), "alloc color");
+    OIT_TRY_CUDA(color.ensure((size_t)P * ssn * 16), "alloc color");
     if (alg() == oit::Alg::Weighted) {
       const bool f32 = st.weighted_precision == OIT_WEIGHTED_FP32;
       OIT_TRY_CUDA(accum.ensure((size_t)S * P * (f32 ? 16 : 8)), "alloc accum");
@@ -354,7 +355,8 @@ struct oit_context {
     p.tiles_x = tiles_x;
     p.tiles_y = tiles_y;
     p.P = P;
-    p.S = S;
+    p.S = ssn > 1 ? 1 : S;
+    p.ssn = ssn;
     p.L = L;
     p.tail = st.tail_blend ? 1 : 0;
     p.coverage = coverage;
@@ -477,6 +479,7 @@ struct oit_context {
     c.ss = supersample;
     c.P = P;
     c.S = S;
+    c.ssn = ssn;
     c.L = L;
     c.tail = st.tail_blend ? 1 : 0;
     c.coverage = coverage;
@@ -653,7 +656,6 @@ int validate(const oit_state* s, int* msaa, int* ss, int* sup) {
   if (s->record_format > OIT_RECORD_RGBA32F || s->weighted_precision > OIT_WEIGHTED_FP32)
     return OIT_ERR_INVALID_ARGUMENT;
   if (!std::isfinite(s->alpha_min) || !std::isfinite(s->alpha_width)) return OIT_ERR_INVALID_ARGUMENT;
-  if (*ss) return OIT_ERR_UNSUPPORTED;                       // per-sample A-buffers
   if (s->record_format != OIT_RECORD_RGBA8) return OIT_ERR_UNSUPPORTED;
   return OIT_OK;
 }
@@ -706,6 +708,7 @@ int oit_create(const oit_state* state, oit_context** out_ctx) {
   c->P = (uint32_t)c->RW * (uint32_t)c->RH;
   c->S = msaa;
   c->coverage = (msaa > 1 && !ss) ? 1 : 0;
+  c->ssn = (ss && state->algorithm != OIT_WEIGHTED) ? msaa : 1;
   c->L = (int)state->oit_layers;
   c->tiles_x = (c->RW + oit::kTile - 1) / oit::kTile;
   c->tiles_y = (c->RH + oit::kTile - 1) / oit::kTile;
@@ -713,7 +716,8 @@ int oit_create(const oit_state* state, oit_context** out_ctx) {
   c->key_bits = 1;
   while ((1 << c->key_bits) < 2 * c->num_tiles) ++c->key_bits;  // opaque and transparent lists
   if (state->algorithm == OIT_LINKEDLIST) {
-    const uint64_t cap = (uint64_t)state->linked_list_allocated_per_element * c->P;  // oit.cpp:125
+    // oit.cpp:125 and 148-152: nodes per pixel, per sample with sample shading
+    const uint64_t cap = (uint64_t)state->linked_list_allocated_per_element * c->P * c->ssn;
     if (cap >= 0xFFFFFFFFull) {
       delete c;
       return OIT_ERR_INVALID_ARGUMENT;
@@ -824,12 +828,12 @@ int oit_get_buffer(oit_context* ctx, int which, void** ptr, size_t* bytes) {
   size_t n = 0;
   switch (which) {
     case OIT_BUF_ABUFFER: b = &ctx->abuf; n = b->bytes; break;
-    case OIT_BUF_AUX: b = &ctx->aux; n = (size_t)ctx->P * 4; break;
-    case OIT_BUF_AUXDEPTH: b = &ctx->auxdepth; n = (size_t)ctx->P * 4; break;
+    case OIT_BUF_AUX: b = &ctx->aux; n = (size_t)ctx->P * ctx->ssn * 4; break;
+    case OIT_BUF_AUXDEPTH: b = &ctx->auxdepth; n = (size_t)ctx->P * ctx->ssn * 4; break;
     case OIT_BUF_COUNTER: b = &ctx->counter; n = 4; break;
     case OIT_BUF_DEPTH: b = &ctx->depth; n = ctx->opaque_valid ? (size_t)ctx->S * ctx->P * 4 : 0; break;
     case OIT_BUF_OPAQUE_COLOR: b = &ctx->opaque_color; n = ctx->opaque_valid ? (size_t)ctx->S * ctx->P * 16 : 0; break;
-    case OIT_BUF_COLOR: b = &ctx->color; n = (size_t)ctx->P * 16; break;
+    case OIT_BUF_COLOR: b = &ctx->color; n = (size_t)ctx->P * ctx->ssn * 16; break;
     case OIT_BUF_ACCUM: b = &ctx->accum; n = b->bytes; break;
     case OIT_BUF_REVEAL: b = &ctx->reveal; n = b->bytes; break;
     case OIT_BUF_OUTPUT: b = &ctx->out; n = (size_t)ctx->W * ctx->H * 4; break;

@@ -206,6 +206,7 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   p.tiles_y = tiles_y;
   p.P = (uint32_t)P;
   p.S = S;
+  p.ssn = 1;
   p.L = L;
   p.tail = st->tail_blend ? 1 : 0;
   p.coverage = coverage;
@@ -249,6 +250,7 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   c.ss = 1;
   c.P = (uint32_t)P;
   c.S = S;
+  c.ssn = 1;
   c.L = L;
   c.tail = p.tail;
   c.coverage = coverage;

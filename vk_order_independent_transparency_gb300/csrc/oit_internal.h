@@ -71,6 +71,7 @@ struct RasterParams {
   int tiles_x, tiles_y;
   uint32_t P;                    // render pixels
   int S;                         // samples per pixel
+  int ssn;                       // samples with their own A-buffer (sample shading), else 1
   int L;                         // OIT_LAYERS
   int tail;                      // OIT_TAILBLEND
   int coverage;                  // OIT_COVERAGE_SHADING
@@ -86,7 +87,7 @@ struct RasterParams {
   float4* opaque_color;          // [S][P]
   int has_opaque;                // 0: depth 1.0 and background colour everywhere
   float4 background;
-  float4* color;                 // [P] colour target after tail blend (sample average)
+  float4* color;                 // [ssn][P] colour target after tail blend (sample average unless sample shading)
   // algorithm state
   uint32_t* abuf;
   uint32_t* aux;
@@ -107,6 +108,7 @@ struct CompositeParams {
   int ss;                        // supersample factor
   uint32_t P;
   int S;
+  int ssn;                       // samples with their own A-buffer (sample shading), else 1
   int L;
   int tail;
   int coverage;
@@ -115,7 +117,7 @@ struct CompositeParams {
   uint32_t capacity;             // linked-list pool size in nodes (walks are bounded by it)
   const uint32_t* abuf;
   const uint32_t* aux;
-  const float4* color;           // [P] (A-buffer algorithms) colour after tail blend
+  const float4* color;           // [ssn][P] (A-buffer algorithms) colour after tail blend
   const float4* opaque_color;    // [S][P] (WBOIT) or null
   int has_opaque;
   float4 background;

@@ -51,7 +51,9 @@ __device__ __forceinline__ float4 premult(float r, float g, float b, float a) {
 
 // ---------------------------------------------------------------------------
 // Policies. Each provides: kPasses, kShade (needs colour), kViewZ,
-// smem_bytes_per_warp(L, coverage), init, fragment(pass, f, node, pixel, targets), flush.
+// smem_bytes_per_warp(L, coverage), init(p, smem, lane, sample, pixel),
+// fragment(pass, f, node, targets), flush(p, valid). `sample` is the lane's
+// sample with sample shading (each sample has its own A-buffer) and 0 otherwise.
 // fragment() runs on the pixel's owner lane only, once per fragment, in
 // primitive order.
 // ---------------------------------------------------------------------------
@@ -64,12 +66,17 @@ struct SimplePolicy {
   static constexpr bool kViewZ = false;
   static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
   uint32_t count;
-  __device__ void init(const RasterParams&, void*, int, uint32_t) { count = 0; }
-  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, uint32_t pixel,
-                                           PixelTargets<S>& tg) {
+  uint32_t eaux;
+  size_t abase;  // listPos = viewSize * OIT_LAYERS * sampleID + pixel (oitSimple.frag.glsl:60)
+  __device__ void init(const RasterParams& p, void*, int, int sample, uint32_t pixel) {
+    count = 0;
+    eaux = (uint32_t)sample * p.P + pixel;
+    abase = (size_t)sample * p.L * p.P + pixel;
+  }
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, PixelTargets<S>& tg) {
     const uint32_t old = count++;
     if (old < (uint32_t)p.L) {
-      const size_t r = (size_t)old * p.P + pixel;
+      const size_t r = abase + (size_t)old * p.P;
       if (p.coverage) {
         reinterpret_cast<uint4*>(p.abuf)[r] = make_uint4(f.packed, f.depth, f.cover, 0u);
       } else {
@@ -79,8 +86,8 @@ struct SimplePolicy {
       tg.tail(premult(f.r, f.g, f.b, f.a), f.cover);
     }
   }
-  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
-    if (valid) p.aux[pixel] = count;
+  __device__ void flush(const RasterParams& p, bool valid) {
+    if (valid) p.aux[eaux] = count;
   }
 };
 
@@ -94,10 +101,14 @@ struct LinkedListPolicy {
   static constexpr bool kNodes = true;
   static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
   uint32_t head;
-  __device__ void init(const RasterParams&, void*, int, uint32_t) { head = 0; }
+  uint32_t eaux;
+  __device__ void init(const RasterParams& p, void*, int, int sample, uint32_t pixel) {
+    head = 0;
+    eaux = (uint32_t)sample * p.P + pixel;
+  }
   // node: the index the batched counter allocation gave this fragment
   // (imageAtomicAdd(imgCounter) + 1, oitLinkedList.frag.glsl:55).
-  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t node, uint32_t,
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t node,
                                            PixelTargets<S>& tg) {
     if (node >= p.capacity) {
       if (p.tail) tg.tail(premult(f.r, f.g, f.b, f.a), f.cover);
@@ -106,8 +117,8 @@ struct LinkedListPolicy {
     reinterpret_cast<uint4*>(p.abuf)[node] = make_uint4(f.packed, f.depth, p.coverage ? f.cover : 0u, head);
     head = node;
   }
-  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
-    if (valid) p.aux[pixel] = head;
+  __device__ void flush(const RasterParams& p, bool valid) {
+    if (valid) p.aux[eaux] = head;
   }
 };
 
@@ -122,13 +133,14 @@ struct Loop64Policy {
   static __host__ __device__ size_t smem_bytes_per_warp(int L, int) { return (size_t)L * 32 * 8; }
   unsigned long long* kb;
   int lane;
-  __device__ void init(const RasterParams& p, void* smem, int, uint32_t) {
+  size_t abase;
+  __device__ void init(const RasterParams& p, void* smem, int, int sample, uint32_t pixel) {
     lane = threadIdx.x & 31;
+    abase = (size_t)sample * p.L * p.P + pixel;
     kb = reinterpret_cast<unsigned long long*>(smem);
     for (int i = 0; i < p.L; ++i) kb[i * 32 + lane] = kEmpty64;
   }
-  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, uint32_t,
-                                           PixelTargets<S>& tg) {
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, PixelTargets<S>& tg) {
     const int L = p.L;
     unsigned long long zcur = ((unsigned long long)f.depth << 32) | f.packed;
     bool evict = true;
@@ -146,10 +158,10 @@ struct Loop64Policy {
     }
     if (evict && p.tail) tg.tail(decode_premult((uint32_t)zcur), f.cover);
   }
-  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
+  __device__ void flush(const RasterParams& p, bool valid) {
     if (!valid) return;
     unsigned long long* ab = reinterpret_cast<unsigned long long*>(p.abuf);
-    for (int i = 0; i < p.L; ++i) ab[(size_t)i * p.P + pixel] = kb[i * 32 + lane];
+    for (int i = 0; i < p.L; ++i) ab[abase + (size_t)i * p.P] = kb[i * 32 + lane];
   }
 };
 
@@ -165,8 +177,10 @@ struct LoopPolicy {
   uint32_t* dep;
   uint32_t* col;
   int lane;
-  __device__ void init(const RasterParams& p, void* smem, int, uint32_t) {
+  size_t abase;  // viewSize * OIT_LAYERS * 2 * sampleID + pixel (oitLoop.frag.glsl:231)
+  __device__ void init(const RasterParams& p, void* smem, int, int sample, uint32_t pixel) {
     lane = threadIdx.x & 31;
+    abase = (size_t)sample * 2 * p.L * p.P + pixel;
     dep = reinterpret_cast<uint32_t*>(smem);
     col = dep + p.L * 32;
     for (int i = 0; i < p.L; ++i) {
@@ -174,7 +188,7 @@ struct LoopPolicy {
       col[i * 32 + lane] = 0u;
     }
   }
-  __device__ __forceinline__ void fragment(const RasterParams& p, int pass, const Frag& f, uint32_t, uint32_t,
+  __device__ __forceinline__ void fragment(const RasterParams& p, int pass, const Frag& f, uint32_t,
                                            PixelTargets<S>& tg) {
     const int L = p.L;
     uint32_t zcur = f.depth;
@@ -200,11 +214,11 @@ struct LoopPolicy {
       col[start * 32 + lane] = f.packed;
     }
   }
-  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
+  __device__ void flush(const RasterParams& p, bool valid) {
     if (!valid) return;
     for (int i = 0; i < p.L; ++i) {
-      p.abuf[(size_t)i * p.P + pixel] = dep[i * 32 + lane];
-      p.abuf[(size_t)(p.L + i) * p.P + pixel] = col[i * 32 + lane];
+      p.abuf[abase + (size_t)i * p.P] = dep[i * 32 + lane];
+      p.abuf[abase + (size_t)(p.L + i) * p.P] = col[i * 32 + lane];
     }
   }
 };
@@ -223,16 +237,19 @@ struct LockPolicy {
   uint32_t count, auxdepth;
   uint32_t* rec;  // [layer][lane] x words
   int lane, words;
-  __device__ void init(const RasterParams& p, void* smem, int, uint32_t) {
+  uint32_t eaux;
+  size_t abase;
+  __device__ void init(const RasterParams& p, void* smem, int, int sample, uint32_t pixel) {
     lane = threadIdx.x & 31;
+    eaux = (uint32_t)sample * p.P + pixel;
+    abase = (size_t)sample * p.L * p.P + pixel;
     words = p.coverage ? 4 : 2;
     rec = reinterpret_cast<uint32_t*>(smem);
     count = 0;
     auxdepth = 0xFFFFFFFFu;
   }
   __device__ __forceinline__ uint32_t* slot(int i) const { return rec + ((size_t)i * 32 + lane) * words; }
-  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, uint32_t,
-                                           PixelTargets<S>& tg) {
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, PixelTargets<S>& tg) {
     const int L = p.L;
     float4 out = premult(f.r, f.g, f.b, f.a);
     if (f.depth <= auxdepth) {
@@ -271,14 +288,14 @@ struct LockPolicy {
     }
     if (p.tail) tg.tail(out, f.cover);
   }
-  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
+  __device__ void flush(const RasterParams& p, bool valid) {
     if (!valid) return;
-    p.aux[pixel] = count;
-    p.auxdepth[pixel] = auxdepth;
+    p.aux[eaux] = count;
+    p.auxdepth[eaux] = auxdepth;
     const int n = count < (uint32_t)p.L ? (int)count : p.L;
     for (int i = 0; i < n; ++i) {
       const uint32_t* r = slot(i);
-      const size_t o = (size_t)i * p.P + pixel;
+      const size_t o = abase + (size_t)i * p.P;
       if (words == 4) {
         reinterpret_cast<uint4*>(p.abuf)[o] = make_uint4(r[0], r[1], r[2], r[3]);
       } else {
@@ -299,7 +316,9 @@ struct WeightedPolicy {
   static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
   float4 acc[S];
   float rev[S];
-  __device__ void init(const RasterParams&, void*, int, uint32_t) {
+  uint32_t px_;
+  __device__ void init(const RasterParams&, void*, int, int, uint32_t pixel) {
+    px_ = pixel;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       acc[s] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -307,8 +326,7 @@ struct WeightedPolicy {
     }
   }
   static __device__ __forceinline__ float h(float x) { return __half2float(__float2half_rn(x)); }
-  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, uint32_t,
-                                           PixelTargets<S>&) {
+  __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, PixelTargets<S>&) {
     const float4 c = premult(f.r, f.g, f.b, f.a);
     const float depthZ = -f.view_z * 10.0f;
     const float x = depthZ / 200.0f;
@@ -338,11 +356,11 @@ struct WeightedPolicy {
       }
     }
   }
-  __device__ void flush(const RasterParams& p, bool valid, uint32_t pixel) {
+  __device__ void flush(const RasterParams& p, bool valid) {
     if (!valid) return;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
-      const size_t o = (size_t)s * p.P + pixel;
+      const size_t o = (size_t)s * p.P + px_;
       if (p.weighted_fp32) {
         reinterpret_cast<float4*>(p.accum)[o] = acc[s];
         reinterpret_cast<float*>(p.reveal)[o] = rev[s];
@@ -362,24 +380,45 @@ struct WeightedPolicy {
 // ---------------------------------------------------------------------------
 // Triangle-list walk shared by the transparent and opaque kernels.
 // ---------------------------------------------------------------------------
+// A warp's piece of a 16x16 tile. Without sample shading (SSN = 1) a warp
+// owns an 8x4 micro-tile, one lane per pixel, and a CTA of 8 warps covers the
+// tile. With sample shading every sample has its own A-buffer, so a lane owns
+// one sample: a warp covers 4x2 pixels x 4 samples or 2x2 pixels x 8 samples
+// and SSN CTAs cover the tile.
 struct WarpTile {
   int lane, px, py, rx0, ry0, rx1, ry1;
+  int sample;  // the lane's sample with sample shading, else 0
   bool valid;
   uint32_t pixel;
 };
 
+template <int SSN>
+struct LaneMap {
+  static constexpr int kPix = 32 / SSN;                  // pixels per warp
+  static constexpr int kW = SSN == 1 ? 8 : (SSN == 4 ? 4 : 2);
+  static constexpr int kH = kPix / kW;
+  __device__ static int pix(int lane) { return lane % kPix; }
+  __device__ static int sample(int lane) { return lane / kPix; }
+};
+
+template <int SSN>
 __device__ __forceinline__ WarpTile warp_tile(const RasterParams& p) {
+  using M = LaneMap<SSN>;
   WarpTile w;
   const int warp = threadIdx.x >> 5;
   w.lane = threadIdx.x & 31;
-  const int tile = blockIdx.x;
+  const int gw = blockIdx.x * oit::kWarpsPerTile + warp;   // warp within the pass
+  const int tile = gw / (oit::kWarpsPerTile * SSN);
+  const int mt = gw % (oit::kWarpsPerTile * SSN);           // micro-tile within the tile
   const int tx = tile % p.tiles_x, ty = tile / p.tiles_x;
-  w.rx0 = tx * 16 + (warp & 1) * 8;
-  w.ry0 = ty * 16 + (warp >> 1) * 4;
-  w.rx1 = w.rx0 + 7;
-  w.ry1 = w.ry0 + 3;
-  w.px = w.rx0 + (w.lane & 7);
-  w.py = w.ry0 + (w.lane >> 3);
+  w.rx0 = tx * 16 + (mt % (16 / M::kW)) * M::kW;
+  w.ry0 = ty * 16 + (mt / (16 / M::kW)) * M::kH;
+  w.rx1 = w.rx0 + M::kW - 1;
+  w.ry1 = w.ry0 + M::kH - 1;
+  const int pix = M::pix(w.lane);
+  w.sample = M::sample(w.lane);
+  w.px = w.rx0 + pix % M::kW;
+  w.py = w.ry0 + pix / M::kW;
   w.valid = w.px < p.RW && w.py < p.RH;
   w.pixel = w.valid ? (uint32_t)w.py * (uint32_t)p.RW + (uint32_t)w.px : 0u;
   return w;
@@ -469,12 +508,16 @@ constexpr size_t kWarpStageBytes = 32 * sizeof(TriSetup) + 32 * sizeof(uint32_t)
 // ---------------------------------------------------------------------------
 // Transparent COLOR (+DEPTH) pass.
 // ---------------------------------------------------------------------------
-template <template <int> class Policy, int S>
+// S: samples each lane evaluates (MSAA coverage); SSN: samples mapped to
+// lanes (sample shading, S = 1 then).
+template <template <int> class Policy, int S, int SSN>
 __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using Pol = Policy<S>;
+  using M = LaneMap<SSN>;
   const int warp = threadIdx.x >> 5;
-  const WarpTile w = warp_tile(p);
+  const WarpTile w = warp_tile<SSN>(p);
+  const uint32_t elem = (uint32_t)w.sample * p.P + w.pixel;  // this lane's sample of the pixel
   unsigned char* wbase = smem_raw + (size_t)warp * kWarpStageBytes;
   TriSetup* stage = reinterpret_cast<TriSetup*>(wbase);
   uint32_t* stage_t = reinterpret_cast<uint32_t*>(wbase + 32 * sizeof(TriSetup));
@@ -485,18 +528,19 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
   PixelTargets<S> tg;
 #pragma unroll
   for (int s = 0; s < S; ++s) {
+    const size_t o = (size_t)(SSN > 1 ? w.sample : s) * p.P + w.pixel;
     if (p.has_opaque && w.valid) {
-      tg.depth[s] = p.depth[(size_t)s * p.P + w.pixel];
-      tg.col[s] = p.opaque_color[(size_t)s * p.P + w.pixel];
+      tg.depth[s] = p.depth[o];
+      tg.col[s] = p.opaque_color[o];
     } else {
       tg.depth[s] = 0x3F800000u;  // 1.0f
       tg.col[s] = p.background;
     }
   }
   Pol pol;
-  pol.init(p, pol_smem, w.lane, w.pixel);
+  pol.init(p, pol_smem, w.lane, w.sample, w.pixel);
 
-  const int tile = blockIdx.x + p.tile_offset;
+  const int tile = blockIdx.x / SSN + p.tile_offset;
   const uint32_t beg = p.tile_begin[tile], end = p.tile_end[tile];
   const TriPersp* __restrict__ persp = reinterpret_cast<const TriPersp*>(p.persp);
   const uint32_t lt = (1u << w.lane) - 1u;
@@ -514,7 +558,10 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
         for (int j = w.lane; j < qn; j += 32) {
           const TriSetup& T = stage[q->tri[j]];
           const int l = q->lane[j];
-          const int sx = (w.rx0 + (l & 7)) * 256 + 128, sy = (w.ry0 + (l >> 3)) * 256 + 128;
+          // shading point: the pixel centre, or the lane's sample with sample shading
+          const int pl = M::pix(l);
+          const int2 sp = SSN > 1 ? sample_pos<SSN>(M::sample(l)) : make_int2(128, 128);
+          const int sx = (w.rx0 + pl % M::kW) * 256 + sp.x, sy = (w.ry0 + pl / M::kW) * 256 + sp.y;
           const TriPersp* P = Pol::kViewZ ? persp + stage_t[q->tri[j]] : nullptr;
           const int4 a = T.xy01, b = T.xy2f;
           Shade sh;
@@ -548,7 +595,7 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
           f.a = __int_as_float(stage[q->tri[j]].xy2f.w);
           f.view_z = q->vz[j];
         }
-        pol.fragment(p, pass, f, node0 + (uint32_t)j + 1u, w.pixel, tg);
+        pol.fragment(p, pass, f, node0 + (uint32_t)j + 1u, tg);
       }
       if (shading) nfrag += (uint32_t)qn;
       mine = 0;
@@ -569,7 +616,7 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
             const int bxp = w.px * 256, byp = w.py * 256;
 #pragma unroll
             for (int s = 0; s < S; ++s) {
-              const int2 sp = sample_pos<S>(s);
+              const int2 sp = SSN > 1 ? sample_pos<SSN>(w.sample) : sample_pos<S>(s);
               const EdgesT<E> e = edges_at<E>(a, b, bxp + sp.x, byp + sp.y);
               if (inside(e, b.z)) {
                 const float z = depth_at(zc, e);
@@ -600,7 +647,7 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
         flush);
   }
 
-  pol.flush(p, w.valid, w.pixel);
+  pol.flush(p, w.valid);
   if (w.valid && p.color) {
     float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
@@ -611,7 +658,7 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
       c.w += tg.col[s].w;
     }
     const float k = 1.0f / (float)S;
-    p.color[w.pixel] = make_float4(c.x * k, c.y * k, c.z * k, c.w * k);
+    p.color[elem] = make_float4(c.x * k, c.y * k, c.z * k, c.w * k);
   }
   if (w.lane == 0 && nfrag && p.frag_count) atomicAdd(p.frag_count, (unsigned long long)nfrag);
 }
@@ -623,7 +670,7 @@ template <int S>
 __global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
   __shared__ TriSetup stage_all[oit::kWarpsPerTile * 32];
   const int warp = threadIdx.x >> 5;
-  const WarpTile w = warp_tile(p);
+  const WarpTile w = warp_tile<1>(p);
   TriSetup* stage = stage_all + warp * 32;
   uint32_t dep[S];
   float4 col[S];
@@ -680,7 +727,7 @@ __global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
 
 namespace oitd {
 
-template <template <int> class Pol, int S>
+template <template <int> class Pol, int S, int SSN>
 cudaError_t launch_transparent_s(const RasterParams& p, cudaStream_t s) {
   const size_t smem = (size_t)oit::kWarpsPerTile * (kWarpStageBytes + Pol<S>::smem_bytes_per_warp(p.L, p.coverage));
   if (smem > 48 * 1024) {
@@ -690,22 +737,29 @@ cudaError_t launch_transparent_s(const RasterParams& p, cudaStream_t s) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || cap_set[dev] < (int)smem) {
-      cudaError_t e = cudaFuncSetAttribute(k_raster_transparent<Pol, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem);
+      cudaError_t e = cudaFuncSetAttribute(k_raster_transparent<Pol, S, SSN>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
       if (dev >= 0 && dev < 64) cap_set[dev] = (int)smem;
     }
   }
-  k_raster_transparent<Pol, S><<<(unsigned)(p.tiles_x * p.tiles_y), 256, smem, s>>>(p);
+  k_raster_transparent<Pol, S, SSN><<<(unsigned)(p.tiles_x * p.tiles_y * SSN), 256, smem, s>>>(p);
   return cudaGetLastError();
 }
 
 template <template <int> class Pol>
 cudaError_t launch_transparent(const RasterParams& p, cudaStream_t s) {
+  if (p.ssn > 1) {
+    switch (p.ssn) {
+      case 4: return launch_transparent_s<Pol, 1, 4>(p, s);
+      case 8: return launch_transparent_s<Pol, 1, 8>(p, s);
+      default: return cudaErrorInvalidValue;
+    }
+  }
   switch (p.S) {
-    case 1: return launch_transparent_s<Pol, 1>(p, s);
-    case 4: return launch_transparent_s<Pol, 4>(p, s);
-    case 8: return launch_transparent_s<Pol, 8>(p, s);
+    case 1: return launch_transparent_s<Pol, 1, 1>(p, s);
+    case 4: return launch_transparent_s<Pol, 4, 1>(p, s);
+    case 8: return launch_transparent_s<Pol, 8, 1>(p, s);
     default: return cudaErrorInvalidValue;
   }
 }
