@@ -444,6 +444,8 @@ struct oit_context {
 
   int raster_opaque(cudaStream_t s) {
     oit::RasterParams p = raster_params(0);
+    p.S = S;    // the opaque pass always tests every sample of a pixel
+    p.ssn = 1;
     cudaEvent_t t1 = prof_begin(s);
     const int r = raster(oit::Alg::Opaque, p, s);
     prof_end(OIT_PROF_OPAQUE_RASTER, t1, s);
