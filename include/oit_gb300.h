@@ -206,6 +206,34 @@ int oit_render_frame_noalloc(const oit_state* state, const oit_scene_data* scene
                              uint32_t triangles_per_object, int32_t percent_transparent,
                              uint8_t* out_rgba8_device, void* stream);
 
+/* ---- batched views ----------------------------------------------------- */
+
+/* One view of a batch: a context (own resolution, algorithm, OIT_LAYERS, record
+ * format), its mesh and the frame parameters of oit_render_frame. */
+typedef struct oit_view_frame {
+  oit_context* ctx;
+  const oit_mesh* mesh;
+  uint32_t triangles_per_object;
+  int32_t percent_transparent;
+  uint8_t* out_rgba8_device;  /* NULL = the view context's OIT_BUF_OUTPUT */
+} oit_view_frame;
+
+typedef struct oit_batch oit_batch;
+
+/* A batch renders many views' frames as one CUDA graph in which the views run
+ * concurrently on `parallel_streams` forked streams (0 = 8). The scene
+ * constants of each view come from its context (oit_update_scene). */
+int oit_batch_create(uint32_t parallel_streams, oit_batch** out_batch);
+int oit_batch_destroy(oit_batch* batch);
+
+/* Renders every view (Sample::onRender per view). The first call with a given
+ * set of views renders them one by one (sizing their buffers) and captures the
+ * graph; later calls replay it. Ordered after prior work on `stream`. */
+int oit_batch_render(oit_batch* batch, const oit_view_frame* views, uint32_t num_views, void* stream);
+
+/* Kernel launches per replay of the batch's graph. */
+int oit_batch_launch_count(oit_batch* batch, uint64_t* launches);
+
 /* ---- inspection -------------------------------------------------------- */
 
 /* Synchronises the context's last stream and returns the device error bits

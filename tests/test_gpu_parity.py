@@ -239,3 +239,26 @@ def test_cuda_graph_replay(engine, alg):
         np.testing.assert_array_equal(r.output(), plain['image'])
         assert r.fragment_count() == plain['fragments']
     assert r.get_error() == 0
+
+
+def test_batched_views_match_single_frames(engine):
+    """oit_batch_render (one CUDA graph, views on forked streams) gives every
+    view the image its own oit_render_frame gives."""
+    specs = [(1, 96, 80, 4, 12), (3, 160, 120, 16, 40), (1, 64, 64, 8, 8), (3, 128, 128, 32, 30),
+             (0, 80, 60, 8, 20), (6, 96, 96, 8, 24)]
+    views, refs, keep = [], [], []
+    for k, (alg, W, H, L, n) in enumerate(specs):
+        v, i, tpo, sd = pu.scene(n, W, H, seed=30 + k)
+        refs.append(pu.render_gpu(alg, W, H, v, i, tpo, sd, 80, oit_layers=L)['image'])
+        r = engine.Renderer(engine.make_state(alg, W, H, oit_layers=L))
+        r.update_scene(sd)
+        mesh = engine.DeviceMesh(v, i)
+        views.append((r, mesh, tpo, 80))
+    batch = engine.Batch(parallel_streams=4)
+    batch.set_views(views)
+    for _ in range(3):
+        batch.render()
+        for (r, _, _, _), ref in zip(views, refs):
+            np.testing.assert_array_equal(r.output(), ref)
+            assert r.get_error() == 0
+    assert batch.launch_count() >= len(specs) * 10

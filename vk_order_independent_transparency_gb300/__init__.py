@@ -47,6 +47,7 @@ EXPORTS = [
     'oit_get_fragment_count', 'oit_get_launch_count', 'oit_status_string', 'oit_abuffer_bytes',
     'oit_scene_size', 'oit_scene_generate', 'oit_camera', 'oit_srgb_tables', 'oit_version',
     'oit_profile_enable', 'oit_profile_read', 'oit_render_frame_noalloc',
+    'oit_batch_create', 'oit_batch_destroy', 'oit_batch_render', 'oit_batch_launch_count',
 ]
 PROF_SECTIONS = ['opaque_bin', 'opaque_raster', 'transparent_bin', 'transparent_raster', 'composite']
 
@@ -76,6 +77,11 @@ class OitSceneDesc(ctypes.Structure):
     _fields_ = [('seed', ctypes.c_uint64), ('num_objects', ctypes.c_uint32), ('stacks', ctypes.c_uint32),
                 ('slices', ctypes.c_uint32), ('half_extent', ctypes.c_float), ('radius_min', ctypes.c_float),
                 ('radius_max', ctypes.c_float)]
+
+
+class OitViewFrame(ctypes.Structure):
+    _fields_ = [('ctx', ctypes.c_void_p), ('mesh', ctypes.POINTER(OitMesh)), ('triangles_per_object', ctypes.c_uint32),
+                ('percent_transparent', ctypes.c_int32), ('out_rgba8_device', ctypes.c_void_p)]
 
 
 class OitError(RuntimeError):
@@ -126,6 +132,10 @@ def library():
         'oit_srgb_tables': (I, [P, P]),
         'oit_version': (I, []),
         'oit_profile_enable': (I, [P, I]),
+        'oit_batch_create': (I, [U, ctypes.POINTER(P)]),
+        'oit_batch_destroy': (I, [P]),
+        'oit_batch_render': (I, [P, ctypes.POINTER(OitViewFrame), U, P]),
+        'oit_batch_launch_count': (I, [P, ctypes.POINTER(ctypes.c_uint64)]),
         'oit_render_frame_noalloc': (I, [ctypes.POINTER(OitState), ctypes.POINTER(OitSceneData),
                                          ctypes.POINTER(OitMesh), U, ctypes.c_int32, P, P]),
         'oit_profile_read': (I, [P, ctypes.POINTER(ctypes.c_double * 5), ctypes.POINTER(ctypes.c_uint64 * 5)]),
@@ -342,6 +352,49 @@ class Renderer:
     def launch_count(self):
         v = ctypes.c_uint64()
         _check(self.lib.oit_get_launch_count(self._ctx, ctypes.byref(v)), 'oit_get_launch_count')
+        return v.value
+
+
+class Batch:
+    """Many views (Renderer, DeviceMesh, triangles per object, percent
+    transparent) rendered as one CUDA graph with the views running concurrently."""
+
+    def __init__(self, parallel_streams=8):
+        self.lib = library()
+        self._b = ctypes.c_void_p()
+        _check(self.lib.oit_batch_create(parallel_streams, ctypes.byref(self._b)), 'oit_batch_create')
+        self._frames = None
+        self._keep = None
+
+    def close(self):
+        if self._b:
+            self.lib.oit_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_views(self, views):
+        """views: list of (Renderer, DeviceMesh, triangles_per_object, percent_transparent)."""
+        arr = (OitViewFrame * len(views))()
+        for k, (r, mesh, tpo, pct) in enumerate(views):
+            arr[k].ctx = r._ctx.value
+            arr[k].mesh = ctypes.pointer(mesh.c)
+            arr[k].triangles_per_object = tpo
+            arr[k].percent_transparent = pct
+            arr[k].out_rgba8_device = None
+        self._frames = arr
+        self._keep = views
+
+    def render(self, stream=None):
+        _check(self.lib.oit_batch_render(self._b, self._frames, len(self._frames), stream), 'oit_batch_render')
+
+    def launch_count(self):
+        v = ctypes.c_uint64()
+        _check(self.lib.oit_batch_launch_count(self._b, ctypes.byref(v)), 'oit_batch_launch_count')
         return v.value
 
 

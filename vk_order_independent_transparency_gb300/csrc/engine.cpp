@@ -560,6 +560,33 @@ struct oit_context {
     return OIT_OK;
   }
 
+  // Pair counts copied back by a graph replay become known once their event
+  // completes; returns false when a bin outgrew its capacity (the graph that
+  // reads these bins must be re-captured).
+  bool graph_bins_fit() {
+    bool fit = true;
+    for (uint64_t k : graph_stats) {
+      PairStat* ps = pair_stat(k);
+      if (ps && ps->pending && cudaEventQuery(ps->ev) == cudaSuccess) {
+        ps->known = std::max(ps->known, *ps->host_total);
+        ps->pending = false;
+      }
+      if (ps && ps->known > pair_cap) fit = false;
+    }
+    return fit;
+  }
+
+  int after_graph_launch(cudaStream_t s) {
+    for (uint64_t k : graph_stats) {
+      PairStat* ps = pair_stat(k);
+      if (ps && !ps->pending) {
+        OIT_TRY_CUDA(cudaEventRecord(ps->ev, s), "event");
+        ps->pending = true;
+      }
+    }
+    return OIT_OK;
+  }
+
   int render_frame(const oit_mesh* mesh, uint32_t tpo, int32_t percent, uint8_t* out_dev, cudaStream_t s) {
     if (!mesh || !tpo || percent < 0) return OIT_ERR_INVALID_ARGUMENT;
     last_stream = s;
@@ -570,14 +597,7 @@ struct oit_context {
                               (uint64_t)(uintptr_t)s};
     for (uint64_t v : parts) sig = (sig ^ v) * 1099511628211ull;
     // bins that outgrew their capacity since the capture invalidate the graph
-    for (uint64_t k : graph_stats) {
-      PairStat* ps = pair_stat(k);
-      if (ps && ps->pending && cudaEventQuery(ps->ev) == cudaSuccess) {
-        ps->known = std::max(ps->known, *ps->host_total);
-        ps->pending = false;
-      }
-      if (ps && ps->known > pair_cap) drop_graph();
-    }
+    if (!graph_bins_fit()) drop_graph();
     int gr = ensure_graph_stream();
     if (gr != OIT_OK) return gr;
     if (!graph_exec || graph_sig != sig) {
@@ -615,16 +635,41 @@ struct oit_context {
     OIT_TRY_CUDA(cudaEventRecord(graph_out, graph_stream), "event");
     OIT_TRY_CUDA(cudaStreamWaitEvent(s, graph_out, 0), "wait");
     launches += graph_launches;
-    for (uint64_t k : graph_stats) {
-      PairStat* ps = pair_stat(k);
-      if (ps && !ps->pending) {
-        OIT_TRY_CUDA(cudaEventRecord(ps->ev, graph_stream), "event");
-        ps->pending = true;
-      }
-    }
+    int ar = after_graph_launch(graph_stream);
+    if (ar != OIT_OK) return ar;
     opaque_valid = graph_opaque_valid;  // as left by the captured frame
     color_valid = true;
     return OIT_OK;
+  }
+};
+
+// A batch of views rendered as one CUDA graph: the views' frames are captured
+// on forked streams so the GPU runs them concurrently (small views alone leave
+// most of the 152 SMs idle) and the whole batch costs one graph launch.
+struct oit_batch {
+  cudaStream_t stream = nullptr;
+  std::vector<cudaStream_t> lanes;
+  cudaEvent_t fork = nullptr, in = nullptr, out = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t sig = 0;
+  uint64_t graph_launches = 0;
+  std::vector<oit_context*> ctxs;
+  std::vector<bool> opaque_valid;
+
+  void drop() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    sig = 0;
+  }
+  ~oit_batch() {
+    drop();
+    for (cudaStream_t l : lanes) cudaStreamDestroy(l);
+    for (cudaEvent_t e : joins) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (in) cudaEventDestroy(in);
+    if (out) cudaEventDestroy(out);
+    if (stream) cudaStreamDestroy(stream);
   }
 };
 
@@ -813,6 +858,132 @@ int oit_render_frame_host(oit_context* ctx, const float* vertices, uint32_t num_
   if (r != OIT_OK) return r;
   OIT_TRY_CUDA(cudaMemcpyAsync(out_host, ctx->out.p, (size_t)ctx->W * ctx->H * 4, cudaMemcpyDeviceToHost, s), "d2h");
   OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
+  return OIT_OK;
+}
+
+int oit_batch_create(uint32_t parallel_streams, oit_batch** out) {
+  if (!out) return OIT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  const uint32_t n = parallel_streams ? std::min<uint32_t>(parallel_streams, 64) : 8;
+  oit_batch* b = new (std::nothrow) oit_batch();
+  if (!b) return OIT_ERR_OUT_OF_MEMORY;
+  auto fail = [&](cudaError_t e) {
+    delete b;
+    return cuda_status(e, "batch create");
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return fail(e);
+  for (uint32_t i = 0; i < n; ++i) {
+    cudaStream_t l = nullptr;
+    cudaEvent_t j = nullptr;
+    if ((e = cudaStreamCreateWithFlags(&l, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+    b->lanes.push_back(l);
+    if ((e = cudaEventCreateWithFlags(&j, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+    b->joins.push_back(j);
+  }
+  for (cudaEvent_t* ev : {&b->fork, &b->in, &b->out})
+    if ((e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+  *out = b;
+  return OIT_OK;
+}
+
+int oit_batch_destroy(oit_batch* b) {
+  if (!b) return OIT_ERR_INVALID_ARGUMENT;
+  cudaDeviceSynchronize();
+  delete b;
+  return OIT_OK;
+}
+
+int oit_batch_launch_count(oit_batch* b, uint64_t* launches) {
+  if (!b || !launches) return OIT_ERR_INVALID_ARGUMENT;
+  *launches = b->graph_launches;
+  return OIT_OK;
+}
+
+int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void* stream) {
+  if (!b || !views || n == 0) return OIT_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  uint64_t sig = 1469598103934665603ull;
+  for (uint32_t i = 0; i < n; ++i) {
+    const oit_view_frame& v = views[i];
+    if (!v.ctx || !v.mesh || !v.triangles_per_object || v.percent_transparent < 0) return OIT_ERR_INVALID_ARGUMENT;
+    if (!v.ctx->has_scene) return OIT_ERR_STATE;
+    if (!mesh_ok(v.mesh, 0, v.mesh->num_triangles)) return OIT_ERR_INVALID_ARGUMENT;
+    for (uint32_t j = 0; j < i; ++j)
+      if (views[j].ctx == v.ctx) return OIT_ERR_INVALID_ARGUMENT;  // one frame per context
+    const uint64_t parts[] = {(uint64_t)(uintptr_t)v.ctx, (uint64_t)(uintptr_t)v.mesh->vertices_device,
+                              (uint64_t)(uintptr_t)v.mesh->indices_device, v.mesh->num_triangles,
+                              v.triangles_per_object, (uint64_t)v.percent_transparent,
+                              (uint64_t)(uintptr_t)v.out_rgba8_device};
+    for (uint64_t x : parts) sig = (sig ^ x) * 1099511628211ull;
+  }
+  sig ^= n;
+  bool fit = true;
+  for (uint32_t i = 0; i < n; ++i) fit = views[i].ctx->graph_bins_fit() && fit;
+  if (!fit || sig != b->sig) b->drop();
+  if (!b->exec) {
+    // plain frames, one view after the other, size every buffer
+    for (uint32_t i = 0; i < n; ++i) {
+      const oit_view_frame& v = views[i];
+      int r = v.ctx->render_frame_body(v.mesh, v.triangles_per_object, v.percent_transparent, v.out_rgba8_device, s);
+      if (r != OIT_OK) return r;
+    }
+    OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
+    OIT_TRY_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed), "capture");
+    int r = OIT_OK;
+    cudaError_t e = cudaEventRecord(b->fork, b->stream);
+    const size_t K = b->lanes.size();
+    for (size_t k = 0; k < K && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b->lanes[k], b->fork, 0);
+    uint64_t nodes = 0;
+    b->ctxs.assign(n, nullptr);
+    b->opaque_valid.assign(n, false);
+    for (uint32_t i = 0; i < n && e == cudaSuccess && r == OIT_OK; ++i) {
+      const oit_view_frame& v = views[i];
+      oit_context* c = v.ctx;
+      const uint64_t l0 = c->launches;
+      c->graph_stats.clear();
+      c->capturing = true;
+      r = c->render_frame_body(v.mesh, v.triangles_per_object, v.percent_transparent, v.out_rgba8_device,
+                               b->lanes[i % K]);
+      c->capturing = false;
+      nodes += c->launches - l0;
+      c->launches = l0;
+      c->last_stream = s;
+      b->ctxs[i] = c;
+      b->opaque_valid[i] = c->opaque_valid;
+    }
+    for (size_t k = 0; k < K && e == cudaSuccess; ++k) {
+      e = cudaEventRecord(b->joins[k], b->lanes[k]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->joins[k], 0);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    if (r != OIT_OK || e != cudaSuccess || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      if (r != OIT_OK) return r;
+      return cuda_status(e != cudaSuccess ? e : ce, "batch capture");
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&b->exec, g, 0);
+    cudaGraphDestroy(g);
+    OIT_TRY_CUDA(ie, "batch instantiate");
+    b->sig = sig;
+    b->graph_launches = nodes;
+    return OIT_OK;  // the plain frames produced this call's images
+  }
+  OIT_TRY_CUDA(cudaEventRecord(b->in, s), "event");
+  OIT_TRY_CUDA(cudaStreamWaitEvent(b->stream, b->in, 0), "wait");
+  OIT_TRY_CUDA(cudaGraphLaunch(b->exec, b->stream), "graph launch");
+  OIT_TRY_CUDA(cudaEventRecord(b->out, b->stream), "event");
+  OIT_TRY_CUDA(cudaStreamWaitEvent(s, b->out, 0), "wait");
+  for (uint32_t i = 0; i < n; ++i) {
+    oit_context* c = b->ctxs[i];
+    int r = c->after_graph_launch(b->stream);
+    if (r != OIT_OK) return r;
+    c->launches += 0;
+    c->opaque_valid = b->opaque_valid[i];
+    c->color_valid = true;
+    c->last_stream = s;
+  }
   return OIT_OK;
 }
 
