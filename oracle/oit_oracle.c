@@ -148,9 +148,10 @@ or_frame* or_frame_create(const or_params* p) {
       f->abuf_words = f->E * (size_t)f->L * (size_t)f->rec_words; break;
     case OR_LINKEDLIST:
       f->capacity = (uint32_t)((size_t)p->nodes_per_pixel * f->E);
-      f->abuf_words = (size_t)f->capacity * 4; break;
+      f->abuf_words = (size_t)f->capacity * (p->record_fp32 ? 8 : 4); break;
     case OR_LOOP: f->abuf_words = f->E * (size_t)f->L * 2; break;
-    case OR_LOOP64: f->abuf_words = f->E * (size_t)f->L * 2; break;
+    /* RGBA32F: a float4 payload block follows the 64-bit keys */
+    case OR_LOOP64: f->abuf_words = f->E * (size_t)f->L * (p->record_fp32 ? 6 : 2); break;
     default: f->abuf_words = 0; break;
   }
   f->abuf = (uint32_t*)xcalloc(f->abuf_words, 4);
@@ -478,6 +479,13 @@ static void frag_linkedlist(or_frame* f, size_t pixel, int s, uint32_t cover, co
   f->ll_stored[e]++;
   uint32_t oldOffset = f->aux[e];
   f->aux[e] = newOffset;
+  if (f->p.record_fp32) {
+    /* RGBA32F node: linear unpremultiplied colour, depth, mask, next, 0 */
+    uint32_t* n = f->abuf + (size_t)newOffset * 8;
+    for (int k = 0; k < 4; ++k) n[k] = float_to_bits(fr->rgba[k]);
+    n[4] = fr->depth; n[5] = f->coverage ? fr->mask : 0u; n[6] = oldOffset; n[7] = 0;
+    return;
+  }
   uint32_t* n = f->abuf + (size_t)newOffset * 4;
   n[0] = fr->packed; n[1] = fr->depth; n[2] = f->coverage ? fr->mask : 0u; n[3] = oldOffset;
 }
@@ -522,7 +530,9 @@ static void frag_loop64(or_frame* f, size_t pixel, int s, uint32_t cover, const 
   const int L = f->L;
   size_t listPos = (size_t)s * L * f->P + pixel;
   uint64_t* ab = (uint64_t*)f->abuf; /* little-endian: low word = colour, high word = depth */
+  float* pay = f->p.record_fp32 ? (float*)(f->abuf + f->E * (size_t)L * 2) : NULL;
   uint64_t zcur = ((uint64_t)fr->depth << 32) | fr->packed;
+  float pcur[4] = {fr->rgba[0], fr->rgba[1], fr->rgba[2], fr->rgba[3]};
   int i = 0, canInsert = 1;
   uint64_t pretest = ab[listPos + (size_t)(L - 1) * f->P];
   if (zcur > pretest) {
@@ -536,13 +546,19 @@ static void frag_loop64(or_frame* f, size_t pixel, int s, uint32_t cover, const 
     for (; i < L; ++i) {
       uint64_t* slot = &ab[listPos + (size_t)i * f->P];
       uint64_t ztest = *slot;
-      if (zcur < ztest) *slot = zcur; /* atomicMin */
+      if (zcur < ztest) { /* atomicMin; a float payload moves with its key */
+        *slot = zcur;
+        if (pay) {
+          float* ps = pay + 4 * (listPos + (size_t)i * f->P);
+          for (int k = 0; k < 4; ++k) { float t = ps[k]; ps[k] = pcur[k]; pcur[k] = t; }
+        }
+      }
       if (ztest == EMPTY64) { evict = 0; break; }
       zcur = ztest > zcur ? ztest : zcur;
     }
   }
   if (evict && f->p.tail_blend)
-    tail_out(f, pixel, s, cover, premult(decode_packed((uint32_t)(zcur & 0xFFFFFFFFu))));
+    tail_out(f, pixel, s, cover, pay ? premult_float(pcur) : premult(decode_packed((uint32_t)(zcur & 0xFFFFFFFFu))));
 }
 
 /* oitSpinlock.frag.glsl:49-129 and oitInterlock.frag.glsl:90-152. Both run
@@ -788,6 +804,17 @@ static rec3 insertion_sort_tail(rec3* a, int L, rec3 item) {
   return newlast;
 }
 
+/* Premultiplied colour of a sorted entry: the packed RGBA8 record, or with
+ * RGBA32F linked-list records the float colour of the node it names. */
+static rgba_d entry_colour(const or_frame* f, uint32_t r) {
+  if (f->p.record_fp32 && f->p.algorithm == OR_LINKEDLIST) {
+    const uint32_t* n = f->abuf + (size_t)r * 8;
+    rgba_d c = {bits_to_float(n[0]), bits_to_float(n[1]), bits_to_float(n[2]), bits_to_float(n[3])};
+    return premult(c);
+  }
+  return premult(decode_packed(r));
+}
+
 static rgba_d blend_array(const or_frame* f, const rec3* arr, int n) {
   rgba_d sum = zero_rgba();
   if (f->coverage) {
@@ -795,12 +822,12 @@ static rgba_d blend_array(const or_frame* f, const rec3* arr, int n) {
     for (int s = 0; s < f->S; ++s) {
       rgba_d sc = zero_rgba();
       for (int i = 0; i < n; ++i)
-        if (arr[i].b & (1u << s)) do_blend_packed(&sc, arr[i].r);
+        if (arr[i].b & (1u << s)) do_blend(&sc, entry_colour(f, arr[i].r));
       sum.r += sc.r; sum.g += sc.g; sum.b += sc.b; sum.a += sc.a;
     }
     sum.r /= f->S; sum.g /= f->S; sum.b /= f->S; sum.a /= f->S;
   } else {
-    for (int i = 0; i < n; ++i) do_blend_packed(&sum, arr[i].r);
+    for (int i = 0; i < n; ++i) do_blend(&sum, entry_colour(f, arr[i].r));
   }
   return sum;
 }
@@ -823,26 +850,41 @@ static rgba_d composite_element(or_frame* f, size_t pixel, int s) {
     }
     case OR_LINKEDLIST: {
       /* oitLinkedList.frag.glsl:106-172 */
+      /* RGBA32F nodes: the arrays carry node indices instead of colours */
+      const int fp32 = f->p.record_fp32;
       int n = 0;
       uint32_t off = f->aux[e];
       while (off != 0 && n < L) {
-        const uint32_t* nd = f->abuf + (size_t)off * 4;
-        arr[n].r = nd[0]; arr[n].g = nd[1]; arr[n].b = nd[2];
+        if (fp32) {
+          const uint32_t* nd = f->abuf + (size_t)off * 8;
+          arr[n].r = off; arr[n].g = nd[4]; arr[n].b = nd[5];
+          off = nd[6];
+        } else {
+          const uint32_t* nd = f->abuf + (size_t)off * 4;
+          arr[n].r = nd[0]; arr[n].g = nd[1]; arr[n].b = nd[2];
+          off = nd[3];
+        }
         n++;
-        off = nd[3];
       }
       bubble_sort(arr, n);
       rgba_d tail = zero_rgba();
       while (off != 0) {
-        const uint32_t* nd = f->abuf + (size_t)off * 4;
-        rec3 item = {nd[0], nd[1], nd[2]};
+        rec3 item;
+        uint32_t next;
+        if (fp32) {
+          const uint32_t* nd = f->abuf + (size_t)off * 8;
+          item.r = off; item.g = nd[4]; item.b = nd[5]; next = nd[6];
+        } else {
+          const uint32_t* nd = f->abuf + (size_t)off * 4;
+          item.r = nd[0]; item.g = nd[1]; item.b = nd[2]; next = nd[3];
+        }
         if (f->p.tail_blend) {
           rec3 t = insertion_sort_tail(arr, L, item);
-          do_blend_packed(&tail, t.r);
+          do_blend(&tail, entry_colour(f, t.r));
         } else {
           insertion_sort(arr, L, item);
         }
-        off = nd[3];
+        off = next;
       }
       rgba_d sum = blend_array(f, arr, n);
       do_blend(&sum, tail);
@@ -862,11 +904,14 @@ static rgba_d composite_element(or_frame* f, size_t pixel, int s) {
     case OR_LOOP64: {
       /* oitLoop64.frag.glsl:162-183 */
       const uint64_t* ab = (const uint64_t*)f->abuf;
+      const float* pay = f->p.record_fp32 ? (const float*)(f->abuf + f->E * (size_t)L * 2) : NULL;
       size_t listPos = (size_t)s * L * f->P + pixel;
       rgba_d sum = zero_rgba();
       for (int i = 0; i < L; ++i) {
         uint64_t k = ab[listPos + (size_t)i * f->P];
-        if ((uint32_t)(k >> 32) != EMPTY32) do_blend_packed(&sum, (uint32_t)k); else break;
+        if ((uint32_t)(k >> 32) == EMPTY32) break;
+        if (pay) do_blend(&sum, premult_float(pay + 4 * (listPos + (size_t)i * f->P)));
+        else do_blend_packed(&sum, (uint32_t)k);
       }
       return sum;
     }

@@ -51,7 +51,7 @@ typedef struct or_params {
   int32_t tail_blend;       /* OIT_TAILBLEND */
   int32_t width, height;    /* output (viewport) size in pixels */
   float alpha_min, alpha_width; /* SceneData::alphaMin/alphaWidth (common.h:89-90) */
-  int32_t record_fp32;      /* 1: keep fragment colours unquantised (plain FP32 records) */
+  int32_t record_fp32;      /* 1: RGBA32F records (linked list, Loop64): colours kept unquantised */
   float background[4];      /* render-pass clear colour, oitRender.cpp:90 */
 } or_params;
 

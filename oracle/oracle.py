@@ -73,7 +73,7 @@ class Frame:
     """One oracle frame: the reference's per-frame images plus the FP64 colour target."""
 
     def __init__(self, algorithm, width, height, oit_layers=8, nodes_per_pixel=8, aa_type=0, tail_blend=True,
-                 alpha_min=0.2, alpha_width=0.6, background=(0.2, 0.2, 0.2, 0.2)):
+                 alpha_min=0.2, alpha_width=0.6, background=(0.2, 0.2, 0.2, 0.2), record_fp32=False):
         msaa, ss, sup = aa_settings(aa_type)
         p = OrParams()
         p.algorithm = algorithm
@@ -87,7 +87,7 @@ class Frame:
         p.height = height
         p.alpha_min = alpha_min
         p.alpha_width = alpha_width
-        p.record_fp32 = 0
+        p.record_fp32 = 1 if record_fp32 else 0
         p.background = (ctypes.c_float * 4)(*background)
         self.p = p
         self.msaa = msaa

@@ -46,10 +46,10 @@ def render_gpu(algorithm, width, height, v, i, tpo, sd, percent=100, **kw):
 
 
 def render_oracle(algorithm, width, height, v, i, tpo, sd, percent=100, oit_layers=8, nodes_per_pixel=8,
-                  aa_type=0, tail_blend=True, alpha_min=0.2, alpha_width=0.6, **_):
+                  aa_type=0, tail_blend=True, alpha_min=0.2, alpha_width=0.6, record_format=0, **_):
     fr = orc.render(algorithm, width, height, sd, v, i, tpo, percent, oit_layers=oit_layers,
                     nodes_per_pixel=nodes_per_pixel, aa_type=aa_type, tail_blend=tail_blend, alpha_min=alpha_min,
-                    alpha_width=alpha_width)
+                    alpha_width=alpha_width, record_fp32=record_format == oit.OIT_RECORD_RGBA32F)
     state = {
         'abuf': fr.buffer(orc.BUF_ABUFFER),
         'aux': fr.buffer(orc.BUF_AUX),
@@ -68,8 +68,10 @@ def render_oracle(algorithm, width, height, v, i, tpo, sd, percent=100, oit_laye
     return state
 
 
-def walk_lists(pool_words, heads):
-    pool = pool_words.reshape(-1, 4)
+def walk_lists(pool_words, heads, fp32=False):
+    """Each list's entries in list order: (colour, depth, mask) per node; with
+    RGBA32F nodes the colour is the four float bit patterns."""
+    pool = pool_words.reshape(-1, 8 if fp32 else 4)
     out = []
     for h in heads:
         seq = []
@@ -77,15 +79,19 @@ def walk_lists(pool_words, heads):
         guard = 0
         while off:
             n = pool[off]
-            seq.append((int(n[0]), int(n[1]), int(n[2])))
-            off = int(n[3])
+            if fp32:
+                seq.append((tuple(int(x) for x in n[:4]), int(n[4]), int(n[5])))
+                off = int(n[6])
+            else:
+                seq.append((int(n[0]), int(n[1]), int(n[2])))
+                off = int(n[3])
             guard += 1
             assert guard <= pool.shape[0], 'cycle in linked list'
         out.append(seq)
     return out
 
 
-def compare_abuffer(algorithm, g, o, L, P, coverage, ssn=1):
+def compare_abuffer(algorithm, g, o, L, P, coverage, ssn=1, fp32=False):
     """Bit-exact comparison of the algorithm's A-buffer state. With sample
     shading (ssn > 1) every sample has its own A-buffer block."""
     if algorithm in (oit.OIT_SIMPLE, oit.OIT_SPINLOCK, oit.OIT_INTERLOCK):
@@ -102,7 +108,7 @@ def compare_abuffer(algorithm, g, o, L, P, coverage, ssn=1):
             np.testing.assert_array_equal(g['auxdepth'][:ssn * P], o['auxdepth'][:ssn * P])
     elif algorithm == oit.OIT_LINKEDLIST:
         assert g['counter'][0] == o['counter'][0]
-        assert walk_lists(g['abuf'], g['aux'][:ssn * P]) == walk_lists(o['abuf'], o['aux'][:ssn * P])
+        assert walk_lists(g['abuf'], g['aux'][:ssn * P], fp32) == walk_lists(o['abuf'], o['aux'][:ssn * P], fp32)
     elif algorithm == oit.OIT_LOOP:
         ga = g['abuf'][:ssn * 2 * L * P].reshape(ssn, 2 * L, P)
         oa = o['abuf'][:ssn * 2 * L * P].reshape(ssn, 2 * L, P)
@@ -114,6 +120,13 @@ def compare_abuffer(algorithm, g, o, L, P, coverage, ssn=1):
                 np.testing.assert_array_equal(ga[s, L + layer][sel], oa[s, L + layer][sel])
     elif algorithm == oit.OIT_LOOP64:
         np.testing.assert_array_equal(g['abuf'][:ssn * 2 * L * P], o['abuf'][:ssn * 2 * L * P])
+        if fp32:
+            keys = o['abuf'][:ssn * 2 * L * P].reshape(-1, 2)
+            used = keys[:, 1] != 0xFFFFFFFF
+            base = ssn * 2 * L * P
+            gp = g['abuf'][base:base + 4 * ssn * L * P].reshape(-1, 4)
+            op = o['abuf'][base:base + 4 * ssn * L * P].reshape(-1, 4)
+            np.testing.assert_array_equal(gp[used], op[used])
 
 
 def compare_images(g, o, max_lsb=1):

@@ -24,7 +24,7 @@ def run_pair(engine, alg, W, H, n_obj, percent=100, seed=3, rmin=0.05, rmax=0.2,
     return g, o
 
 
-def check(engine, alg, g, o, W, H, L, aa=0, ss=1):
+def check(engine, alg, g, o, W, H, L, aa=0, ss=1, fp32=False):
     msaa, sample_shading, _ = engine.aa_settings(aa)
     coverage = msaa > 1 and not sample_shading
     ssn = msaa if sample_shading else 1
@@ -32,7 +32,7 @@ def check(engine, alg, g, o, W, H, L, aa=0, ss=1):
     assert g['error'] == 0
     assert g['fragments'] == o['fragments']
     if alg != engine.OIT_WEIGHTED:
-        pu.compare_abuffer(alg, g, o, L, P, coverage, ssn)
+        pu.compare_abuffer(alg, g, o, L, P, coverage, ssn, fp32)
         if ssn > 1:
             ref_col = o['color_samples'].reshape(-1, 4)
         else:
@@ -262,3 +262,23 @@ def test_batched_views_match_single_frames(engine):
             np.testing.assert_array_equal(r.output(), ref)
             assert r.get_error() == 0
     assert batch.launch_count() >= len(specs) * 10
+
+
+@pytest.mark.parametrize('aa', [0, 1, 5])
+@pytest.mark.parametrize('L', [4, 16])
+@pytest.mark.parametrize('alg', [1, 3])
+def test_rgba32f_records(engine, alg, L, aa):
+    """Plain FP32 records: float colours stored bit-exactly (nodes / payloads),
+    kept sets and order as with RGBA8 keys, image within 1 LSB of the oracle."""
+    W, H = 128, 96
+    kw = dict(oit_layers=L, nodes_per_pixel=10, aa_type=aa, record_format=engine.OIT_RECORD_RGBA32F)
+    g, o = run_pair(engine, alg, W, H, 40, percent=70, seed=17, **kw)
+    check(engine, alg, g, o, W, H, L, aa, fp32=True)
+
+
+def test_rgba32f_unsupported_combinations(engine):
+    import ctypes
+    for alg, L in ((0, 8), (2, 8), (3, 32), (6, 8)):
+        st = engine.make_state(alg, 64, 64, oit_layers=L, record_format=engine.OIT_RECORD_RGBA32F)
+        ctx = ctypes.c_void_p()
+        assert engine.library().oit_create(ctypes.byref(st), ctypes.byref(ctx)) == engine.OIT_ERR_UNSUPPORTED

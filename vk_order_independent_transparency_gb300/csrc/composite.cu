@@ -68,13 +68,27 @@ __device__ __forceinline__ uint32_t insertion_sort_tail(Arr<L>& a, uint32_t ic, 
   return last;
 }
 
-template <int L>
-__device__ __forceinline__ float4 blend_array(const Arr<L>& a, int n, int coverage, int S) {
+// Premultiplied colour of an array entry: the packed RGBA8 record itself, or
+// (RGBA32F linked-list nodes) the float colour of the node the entry names.
+struct PackedColour {
+  __device__ __forceinline__ float4 operator()(uint32_t c) const { return decode_premult(c); }
+};
+struct NodeColour {
+  const uint4* pool;
+  __device__ __forceinline__ float4 operator()(uint32_t node) const {
+    const uint4 v = pool[2 * (size_t)node];
+    const float a = __uint_as_float(v.w);
+    return make_float4(__uint_as_float(v.x) * a, __uint_as_float(v.y) * a, __uint_as_float(v.z) * a, a);
+  }
+};
+
+template <int L, class Col = PackedColour>
+__device__ __forceinline__ float4 blend_array(const Arr<L>& a, int n, int coverage, int S, Col col = Col()) {
   float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
   if (!coverage) {
 #pragma unroll
     for (int i = 0; i < L; ++i)
-      if (i < n) blend_under(sum, decode_premult(a.c[i]));
+      if (i < n) blend_under(sum, col(a.c[i]));
     return sum;
   }
   // oitSimple.frag.glsl:142-159: per MSAA sample, blend the fragments covering it.
@@ -82,7 +96,7 @@ __device__ __forceinline__ float4 blend_array(const Arr<L>& a, int n, int covera
     float4 sc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int i = 0; i < L; ++i)
-      if (i < n && ((a.m[i] >> s) & 1u)) blend_under(sc, decode_premult(a.c[i]));
+      if (i < n && ((a.m[i] >> s) & 1u)) blend_under(sc, col(a.c[i]));
     sum.x += sc.x; sum.y += sc.y; sum.z += sc.z; sum.w += sc.w;
   }
   const float k = 1.0f / (float)S;
@@ -114,8 +128,10 @@ __device__ __forceinline__ float4 composite_records(const CompositeParams& p, ui
   return blend_array<L>(a, n, p.coverage, p.S);
 }
 
-// Linked list: oitLinkedList.frag.glsl:106-172.
-template <int L>
+// Linked list: oitLinkedList.frag.glsl:106-172. With RGBA32F records (F32)
+// nodes are 32 bytes and the sort arrays carry node indices; colours are
+// fetched when blended.
+template <int L, bool F32>
 __device__ __forceinline__ float4 composite_list(const CompositeParams& p, uint32_t eaux) {
   const uint4* __restrict__ pool = reinterpret_cast<const uint4*>(p.abuf);
   uint32_t off = p.aux[eaux];
@@ -126,9 +142,15 @@ __device__ __forceinline__ float4 composite_list(const CompositeParams& p, uint3
   for (int i = 0; i < L; ++i) {
     a.c[i] = 0; a.d[i] = 0; a.m[i] = 0;
     if (off != 0 && off < p.capacity) {
-      const uint4 nd = pool[off];
-      a.c[i] = nd.x; a.d[i] = nd.y; a.m[i] = nd.z;
-      off = nd.w;
+      if (F32) {
+        const uint4 nd = pool[2 * (size_t)off + 1];  // depth, mask, next
+        a.c[i] = off; a.d[i] = nd.x; a.m[i] = nd.y;
+        off = nd.z;
+      } else {
+        const uint4 nd = pool[off];
+        a.c[i] = nd.x; a.d[i] = nd.y; a.m[i] = nd.z;
+        off = nd.w;
+      }
       n = i + 1;
     }
   }
@@ -138,16 +160,19 @@ __device__ __forceinline__ float4 composite_list(const CompositeParams& p, uint3
   // only guards against a list that was never built this frame.
   uint32_t guard = p.capacity;
   while (off != 0 && off < p.capacity && guard-- != 0) {
-    const uint4 nd = pool[off];
-    if (p.tail) {
-      const uint32_t ev = insertion_sort_tail<L>(a, nd.x, nd.y, nd.z);
-      blend_under(tail, decode_premult(ev));
+    uint32_t ic, id, im, next;
+    if (F32) {
+      const uint4 nd = pool[2 * (size_t)off + 1];
+      ic = off; id = nd.x; im = nd.y; next = nd.z;
     } else {
-      insertion_sort_tail<L>(a, nd.x, nd.y, nd.z);
+      const uint4 nd = pool[off];
+      ic = nd.x; id = nd.y; im = nd.z; next = nd.w;
     }
-    off = nd.w;
+    const uint32_t ev = insertion_sort_tail<L>(a, ic, id, im);
+    if (p.tail) blend_under(tail, F32 ? NodeColour{pool}(ev) : decode_premult(ev));
+    off = next;
   }
-  float4 sum = blend_array<L>(a, n, p.coverage, p.S);
+  float4 sum = F32 ? blend_array<L>(a, n, p.coverage, p.S, NodeColour{pool}) : blend_array<L>(a, n, p.coverage, p.S);
   blend_under(sum, tail);
   return sum;
 }
@@ -164,13 +189,21 @@ __device__ __forceinline__ float4 composite_loop(const CompositeParams& p, size_
 }
 
 // Loop64: oitLoop64.frag.glsl:162-183.
+// With RGBA32F records a float4 payload block follows the keys.
 __device__ __forceinline__ float4 composite_loop64(const CompositeParams& p, size_t abase) {
   const uint2* __restrict__ ab = reinterpret_cast<const uint2*>(p.abuf);
+  const float4* __restrict__ pay =
+      p.record_fp32 ? reinterpret_cast<const float4*>(ab + (size_t)p.ssn * p.L * p.P) : nullptr;
   float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int i = 0; i < p.L; ++i) {
     const uint2 k = ab[abase + (size_t)i * p.P];
     if (k.y == kEmpty) break;
-    blend_under(sum, decode_premult(k.x));
+    if (pay) {
+      const float4 c = pay[abase + (size_t)i * p.P];
+      blend_under(sum, make_float4(c.x * c.w, c.y * c.w, c.z * c.w, c.w));
+    } else {
+      blend_under(sum, decode_premult(k.x));
+    }
   }
   return sum;
 }
@@ -183,7 +216,7 @@ __device__ __forceinline__ void write_out(const CompositeParams& p, uint32_t o, 
   if (p.out_linear) p.out_linear[o] = c;
 }
 
-enum Kind { kRecords = 0, kList = 1, kLoop = 2, kLoop64 = 3 };
+enum Kind { kRecords = 0, kList = 1, kLoop = 2, kLoop64 = 3, kListF32 = 4 };
 
 template <int K, int L>
 __global__ void __launch_bounds__(256) k_composite(CompositeParams p) {
@@ -201,7 +234,8 @@ __global__ void __launch_bounds__(256) k_composite(CompositeParams p) {
         const size_t abase = (size_t)s * (K == kLoop ? 2 : 1) * p.L * p.P + pixel;
         float4 sum;
         if (K == kRecords) sum = composite_records<L>(p, eaux, abase);
-        else if (K == kList) sum = composite_list<L>(p, eaux);
+        else if (K == kList) sum = composite_list<L, false>(p, eaux);
+        else if (K == kListF32) sum = composite_list<L, true>(p, eaux);
         else if (K == kLoop) sum = composite_loop(p, abase);
         else sum = composite_loop64(p, abase);
         // composite output over the colour target (which already holds the
@@ -277,7 +311,7 @@ cudaError_t launch_composite(Alg alg, const CompositeParams& p, cudaStream_t s) 
     case Alg::Simple:
     case Alg::Spinlock:
     case Alg::Interlock: return launch_kind<kRecords>(p, s);
-    case Alg::LinkedList: return launch_kind<kList>(p, s);
+    case Alg::LinkedList: return p.record_fp32 ? launch_kind<kListF32>(p, s) : launch_kind<kList>(p, s);
     case Alg::Loop: k_composite<kLoop, 1><<<grid, block, 0, s>>>(p); return cudaGetLastError();
     case Alg::Loop64: k_composite<kLoop64, 1><<<grid, block, 0, s>>>(p); return cudaGetLastError();
     case Alg::Weighted: k_composite_weighted<<<grid, block, 0, s>>>(p); return cudaGetLastError();

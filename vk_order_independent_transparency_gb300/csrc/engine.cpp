@@ -165,6 +165,7 @@ struct oit_context {
   int create() {
     OIT_TRY_CUDA(depth.ensure(4), "alloc");
     size_t elems = (size_t)P * ssn;  // A-buffer elements (pixels, or samples with sample shading)
+    const bool fp32 = st.record_format == OIT_RECORD_RGBA32F;
     size_t abuf_bytes = 0;
     switch (alg()) {
       case oit::Alg::Simple:
@@ -173,11 +174,13 @@ struct oit_context {
         abuf_bytes = elems * L * (coverage ? 16 : 8);
         break;
       case oit::Alg::LinkedList:
-        abuf_bytes = (size_t)capacity * 16;
+        abuf_bytes = (size_t)capacity * (fp32 ? 32 : 16);
         break;
       case oit::Alg::Loop:
-      case oit::Alg::Loop64:
         abuf_bytes = elems * L * 8;
+        break;
+      case oit::Alg::Loop64:
+        abuf_bytes = elems * L * (fp32 ? 24 : 8);  // keys (+ float4 payloads)
         break;
       default:
         break;
@@ -703,7 +706,12 @@ int validate(const oit_state* s, int* msaa, int* ss, int* sup) {
   if (s->record_format > OIT_RECORD_RGBA32F || s->weighted_precision > OIT_WEIGHTED_FP32)
     return OIT_ERR_INVALID_ARGUMENT;
   if (!std::isfinite(s->alpha_min) || !std::isfinite(s->alpha_width)) return OIT_ERR_INVALID_ARGUMENT;
-  if (s->record_format != OIT_RECORD_RGBA8) return OIT_ERR_UNSUPPORTED;
+  if (s->record_format == OIT_RECORD_RGBA32F) {
+    // float records exist for the linked list and Loop64; Loop64's float
+    // payloads need 24 bytes of shared memory per layer and lane (L <= 16)
+    if (s->algorithm != OIT_LINKEDLIST && s->algorithm != OIT_LOOP64) return OIT_ERR_UNSUPPORTED;
+    if (s->algorithm == OIT_LOOP64 && s->oit_layers > 16) return OIT_ERR_UNSUPPORTED;
+  }
   return OIT_OK;
 }
 

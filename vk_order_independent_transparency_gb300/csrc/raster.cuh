@@ -64,7 +64,7 @@ struct SimplePolicy {
   static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
   static constexpr bool kViewZ = false;
-  static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
+  static __host__ __device__ size_t smem_bytes_per_warp(int, int, int = 0) { return 0; }
   uint32_t count;
   uint32_t eaux;
   size_t abase;  // listPos = viewSize * OIT_LAYERS * sampleID + pixel (oitSimple.frag.glsl:60)
@@ -99,7 +99,7 @@ struct LinkedListPolicy {
   static constexpr int kPasses = 1;
   static constexpr bool kViewZ = false;
   static constexpr bool kNodes = true;
-  static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
+  static __host__ __device__ size_t smem_bytes_per_warp(int, int, int = 0) { return 0; }
   uint32_t head;
   uint32_t eaux;
   __device__ void init(const RasterParams& p, void*, int, int sample, uint32_t pixel) {
@@ -114,7 +114,14 @@ struct LinkedListPolicy {
       if (p.tail) tg.tail(premult(f.r, f.g, f.b, f.a), f.cover);
       return;
     }
-    reinterpret_cast<uint4*>(p.abuf)[node] = make_uint4(f.packed, f.depth, p.coverage ? f.cover : 0u, head);
+    if (p.record_fp32) {
+      // RGBA32F node: linear unpremultiplied colour, then depth, mask, next
+      uint4* n = reinterpret_cast<uint4*>(p.abuf) + 2 * (size_t)node;
+      n[0] = make_uint4(__float_as_uint(f.r), __float_as_uint(f.g), __float_as_uint(f.b), __float_as_uint(f.a));
+      n[1] = make_uint4(f.depth, p.coverage ? f.cover : 0u, head, 0u);
+    } else {
+      reinterpret_cast<uint4*>(p.abuf)[node] = make_uint4(f.packed, f.depth, p.coverage ? f.cover : 0u, head);
+    }
     head = node;
   }
   __device__ void flush(const RasterParams& p, bool valid) {
@@ -130,25 +137,38 @@ struct Loop64Policy {
   static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
   static constexpr bool kViewZ = false;
-  static __host__ __device__ size_t smem_bytes_per_warp(int L, int) { return (size_t)L * 32 * 8; }
+  // keys, plus a float4 colour per slot with RGBA32F records
+  static __host__ __device__ size_t smem_bytes_per_warp(int L, int, int fp32 = 0) {
+    return (size_t)L * 32 * (fp32 ? 24 : 8);
+  }
   unsigned long long* kb;
+  float4* pay;  // RGBA32F payload moving with its key, or null
   int lane;
   size_t abase;
   __device__ void init(const RasterParams& p, void* smem, int, int sample, uint32_t pixel) {
     lane = threadIdx.x & 31;
     abase = (size_t)sample * p.L * p.P + pixel;
     kb = reinterpret_cast<unsigned long long*>(smem);
+    pay = p.record_fp32 ? reinterpret_cast<float4*>(kb + p.L * 32) : nullptr;
     for (int i = 0; i < p.L; ++i) kb[i * 32 + lane] = kEmpty64;
   }
   __device__ __forceinline__ void fragment(const RasterParams& p, int, const Frag& f, uint32_t, PixelTargets<S>& tg) {
     const int L = p.L;
     unsigned long long zcur = ((unsigned long long)f.depth << 32) | f.packed;
+    float4 pcur = make_float4(f.r, f.g, f.b, f.a);
     bool evict = true;
     if (!(zcur > kb[(L - 1) * 32 + lane])) {
       int i = (zcur > kb[(L / 2) * 32 + lane]) ? (L / 2) : 0;
       for (; i < L; ++i) {
         const unsigned long long ztest = kb[i * 32 + lane];
-        if (zcur < ztest) kb[i * 32 + lane] = zcur;
+        if (zcur < ztest) {
+          kb[i * 32 + lane] = zcur;
+          if (pay) {
+            const float4 t = pay[i * 32 + lane];
+            pay[i * 32 + lane] = pcur;
+            pcur = t;
+          }
+        }
         if (ztest == kEmpty64) {
           evict = false;
           break;
@@ -156,12 +176,17 @@ struct Loop64Policy {
         zcur = ztest > zcur ? ztest : zcur;
       }
     }
-    if (evict && p.tail) tg.tail(decode_premult((uint32_t)zcur), f.cover);
+    if (evict && p.tail) tg.tail(pay ? premult(pcur.x, pcur.y, pcur.z, pcur.w) : decode_premult((uint32_t)zcur), f.cover);
   }
   __device__ void flush(const RasterParams& p, bool valid) {
     if (!valid) return;
     unsigned long long* ab = reinterpret_cast<unsigned long long*>(p.abuf);
     for (int i = 0; i < p.L; ++i) ab[abase + (size_t)i * p.P] = kb[i * 32 + lane];
+    if (pay) {
+      // payload block after the keys of every sample: [sample][layer][pixel] float4
+      float4* pb = reinterpret_cast<float4*>(ab + (size_t)p.ssn * p.L * p.P);
+      for (int i = 0; i < p.L; ++i) pb[abase + (size_t)i * p.P] = pay[i * 32 + lane];
+    }
   }
 };
 
@@ -173,7 +198,7 @@ struct LoopPolicy {
   static constexpr bool kNodes = false;
   static constexpr int kPasses = 2;
   static constexpr bool kViewZ = false;
-  static __host__ __device__ size_t smem_bytes_per_warp(int L, int) { return (size_t)L * 32 * 8; }
+  static __host__ __device__ size_t smem_bytes_per_warp(int L, int, int = 0) { return (size_t)L * 32 * 8; }
   uint32_t* dep;
   uint32_t* col;
   int lane;
@@ -231,7 +256,7 @@ struct LockPolicy {
   static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
   static constexpr bool kViewZ = false;
-  static __host__ __device__ size_t smem_bytes_per_warp(int L, int coverage) {
+  static __host__ __device__ size_t smem_bytes_per_warp(int L, int coverage, int = 0) {
     return (size_t)L * 32 * (coverage ? 16 : 8);
   }
   uint32_t count, auxdepth;
@@ -313,7 +338,7 @@ struct WeightedPolicy {
   static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
   static constexpr bool kViewZ = true;
-  static __host__ __device__ size_t smem_bytes_per_warp(int, int) { return 0; }
+  static __host__ __device__ size_t smem_bytes_per_warp(int, int, int = 0) { return 0; }
   float4 acc[S];
   float rev[S];
   uint32_t px_;
@@ -523,7 +548,7 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
   uint32_t* stage_t = reinterpret_cast<uint32_t*>(wbase + 32 * sizeof(TriSetup));
   FragQueue* q = reinterpret_cast<FragQueue*>(wbase + 32 * sizeof(TriSetup) + 32 * sizeof(uint32_t));
   unsigned char* pol_smem = smem_raw + (size_t)oit::kWarpsPerTile * kWarpStageBytes +
-                            (size_t)warp * Pol::smem_bytes_per_warp(p.L, p.coverage);
+                            (size_t)warp * Pol::smem_bytes_per_warp(p.L, p.coverage, p.record_fp32);
 
   PixelTargets<S> tg;
 #pragma unroll
@@ -729,7 +754,8 @@ namespace oitd {
 
 template <template <int> class Pol, int S, int SSN>
 cudaError_t launch_transparent_s(const RasterParams& p, cudaStream_t s) {
-  const size_t smem = (size_t)oit::kWarpsPerTile * (kWarpStageBytes + Pol<S>::smem_bytes_per_warp(p.L, p.coverage));
+  const size_t smem =
+      (size_t)oit::kWarpsPerTile * (kWarpStageBytes + Pol<S>::smem_bytes_per_warp(p.L, p.coverage, p.record_fp32));
   if (smem > 48 * 1024) {
     // raise the kernel's dynamic shared memory cap once per device (never
     // while a CUDA graph is being captured after the first frame)
