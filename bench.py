@@ -32,9 +32,29 @@ WORKLOADS = {
     'simple_2560x1440_msaa8_L8_4096spheres': ('simple', 2560, 1440, 8, 8, 4, 4096, 0.02, 0.08, 100, 0.2, 0.6),
     'weighted_3840x2160_16384spheres': ('weighted', 3840, 2160, 8, 8, 0, 16384, 0.01, 0.05, 100, 0.05, 0.9),
 }
-DEFAULT_WORKLOAD = 'loop64_1920x1080_L16_1024spheres_60pct'
 ALGS = ['simple', 'linkedlist', 'loop', 'loop64', 'spinlock', 'interlock', 'weighted']
 SEED = 2
+BATCH_WORKLOAD = 'batch_64views_ll_loop64_mixed_vs_fp32'
+DEFAULT_WORKLOAD = 'loop64_1920x1080_L16_1024spheres_60pct'
+
+
+def batch_views(seed=SEED, n=64):
+    """The batched workload's views: square resolutions log-uniform in
+    [256, 2048], sphere counts log-uniform in [64, 8192], radii 0.01-0.05,
+    Linked List and Loop64 alternating, OIT_LAYERS cycling 4, 8, 16, 32
+    (Loop64 views use 4, 8, 16: its float-record variant keeps 16 at most)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    views = []
+    for k in range(n):
+        side = int(round(256 * 8 ** rng.uniform()))
+        spheres = int(round(64 * 128 ** rng.uniform()))
+        alg = 'linkedlist' if k % 2 == 0 else 'loop64'
+        L = [4, 8, 16, 32][(k // 2) % 4] if alg == 'linkedlist' else [4, 8, 16][(k // 2) % 3]
+        views.append(dict(algorithm=alg, width=side, height=side, oit_layers=L, nodes_per_pixel=8, aa_type=0,
+                          spheres=spheres, radius_min=0.01, radius_max=0.05, percent_transparent=100,
+                          alpha_min=0.2, alpha_width=0.6, seed=seed * 1000 + k))
+    return views
 
 
 def parse():
@@ -42,13 +62,20 @@ def parse():
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=5)
-    ap.add_argument('--workload', default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument('--workload', default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [BATCH_WORKLOAD])
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
     return ap.parse_args()
 
 
 def workload_dict(name):
+    if name == BATCH_WORKLOAD:
+        vs = batch_views()
+        return dict(workload=name, views=len(vs), algorithm='linkedlist+loop64', record_formats='rgba8 batched vs '
+                    'rgba32f one view per call', resolutions='%d..%d square' % (min(v['width'] for v in vs),
+                                                                                 max(v['width'] for v in vs)),
+                    spheres='%d..%d' % (min(v['spheres'] for v in vs), max(v['spheres'] for v in vs)),
+                    radius_min=0.01, radius_max=0.05, oit_layers='4,8,16,32', seed=SEED)
     alg, W, H, L, npp, aa, n, rmin, rmax, pct, amin, awid = WORKLOADS[name]
     return dict(workload=name, algorithm=alg, width=W, height=H, oit_layers=L, nodes_per_pixel=npp, aa_type=aa,
                 spheres=n, radius_min=rmin, radius_max=rmax, percent_transparent=pct, alpha_min=amin,
@@ -309,6 +336,157 @@ def run_gpu(a, wd, rank, world):
     return res
 
 
+def run_batch(a, rank):
+    """Batched mixed-precision views (one CUDA graph, RGBA8 records) against the
+    plain path (one oit_render_frame per view, RGBA32F records)."""
+    import numpy as np
+    import torch
+    import vk_order_independent_transparency_gb300 as oit
+    from vk_order_independent_transparency_gb300 import _build
+    _build.build()
+    torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
+    stream = torch.cuda.current_stream().cuda_stream
+    vs = batch_views(SEED + rank)
+    mixed, plain, meshes, host = [], [], [], []
+    for vd in vs:
+        v, i, tpo = oit.make_scene(vd['spheres'], seed=vd['seed'], radius_min=vd['radius_min'],
+                                   radius_max=vd['radius_max'])
+        sd = oit.make_camera(vd['width'], vd['height'])
+        mesh = oit.DeviceMesh(v, i)
+        meshes.append(mesh)
+        host.append((v, i, tpo))
+        for recs, fmt in ((mixed, oit.OIT_RECORD_RGBA8), (plain, oit.OIT_RECORD_RGBA32F)):
+            r = oit.Renderer(oit.make_state(ALGS.index(vd['algorithm']), vd['width'], vd['height'],
+                                            oit_layers=vd['oit_layers'], nodes_per_pixel=vd['nodes_per_pixel'],
+                                            alpha_min=vd['alpha_min'], alpha_width=vd['alpha_width'],
+                                            record_format=fmt))
+            r.update_scene(sd)
+            recs.append(r)
+    batch = oit.Batch(parallel_streams=8)
+    batch.set_views([(r, m, h[2], 100) for r, m, h in zip(mixed, meshes, host)])
+
+    def step_mixed():
+        batch.render(stream)
+
+    def step_plain():
+        for r, m, h in zip(plain, meshes, host):
+            r.render_frame(m, h[2], 100, None, stream)
+
+    for _ in range(max(3, a.warmup)):
+        step_mixed()
+        step_plain()
+    torch.cuda.synchronize()
+    frags = sum(r.fragment_count() for r in mixed)
+    frags_plain = sum(r.fragment_count() for r in plain)
+    assert frags == frags_plain, (frags, frags_plain)
+    for r in mixed + plain:
+        assert r.get_error() == 0
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(a.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    clocks = Clocks(int(os.environ.get('LOCAL_RANK', '0')))
+    clocks.start()
+    t_mixed = timed(step_mixed)
+    clk = clocks.stop()
+    t_plain = timed(step_plain)
+    launches = batch.launch_count() * a.steps
+
+    # per-pass times: every view rendered alone with section timing
+    sections = {}
+    for r, m, h in zip(mixed, meshes, host):
+        r.profile_enable(True)
+        r.render_frame(m, h[2], 100, None, stream)
+        for k, (ms, n) in r.profile_read().items():
+            if n:
+                sections[k] = sections.get(k, 0.0) + ms / n
+        r.profile_enable(False)
+
+    # end to end: every view's mesh from pinned host memory, the batch, every image back
+    hv = [(torch.from_numpy(np.ascontiguousarray(v)).pin_memory(), torch.from_numpy(
+        np.ascontiguousarray(i).view(np.int32)).pin_memory()) for v, i, _ in host]
+    outs = [torch.empty((vd['height'], vd['width'], 4), dtype=torch.uint8).pin_memory() for vd in vs]
+    h2d = sum(x.nbytes + y.nbytes for x, y in hv)
+    d2h = sum(o.nbytes for o in outs)
+
+    def step_e2e():
+        for (x, y), m in zip(hv, meshes):
+            m.vertices.copy_(x, non_blocking=True)
+            m.indices.copy_(y, non_blocking=True)
+        batch.render(stream)
+        for r, o, vd in zip(mixed, outs, vs):
+            ptr, nb = r.buffer(oit.OIT_BUF_OUTPUT)
+            _copy_d2h(o, ptr, nb, stream)
+        torch.cuda.current_stream().synchronize()
+
+    step_e2e()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        step_e2e()
+    e2e_s = time.perf_counter() - t0
+    return dict(frags=frags, t_mixed=t_mixed, t_plain=t_plain, launches=launches, clocks=clk, sections=sections,
+                e2e_s=e2e_s, h2d=h2d, d2h=d2h, views=vs)
+
+
+def _copy_d2h(host_tensor, dev_ptr, nbytes, stream):
+    import ctypes
+    import vk_order_independent_transparency_gb300 as oit
+    rt = oit._cudart()
+    rt.cudaMemcpyAsync.restype = ctypes.c_int
+    rt.cudaMemcpyAsync(ctypes.c_void_p(host_tensor.data_ptr()), ctypes.c_void_p(dev_ptr), ctypes.c_size_t(nbytes), 2,
+                       ctypes.c_void_p(stream))
+
+
+def main_batch(a, rank, world):
+    import torch
+    res = run_batch(a, rank)
+    t = torch.tensor([res['t_mixed'], res['t_plain'], res['e2e_s']], dtype=torch.float64, device='cuda')
+    fr = torch.tensor([float(res['frags'] * a.steps)], dtype=torch.float64, device='cuda')
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(fr)
+    if rank != 0:
+        return
+    t_mixed, t_plain, e2e_s = [float(x) for x in t.tolist()]
+    total = float(fr.item())
+    value = total / (t_mixed * 1e-3) / 1e6
+    plain = total / (t_plain * 1e-3) / 1e6
+    peak, peak_kind = peaks()
+    sec = res['sections']
+    dom = max(sec, key=sec.get)
+    line = {
+        'metric': 'Mfragments/s', 'value': round(value, 3), 'unit': 'Mfragments/s', 'n_gpus': world,
+        'steps': a.steps, 'warmup': a.warmup, 'ms_per_step': round(t_mixed / a.steps, 4), 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'rgba8 records + f32 blend',
+        'data': 'synthetic: 64 seeded UV-sphere scenes, inputs resident in HBM',
+        'config': dict(workload_dict(BATCH_WORKLOAD), fragments_per_batch=res['frags'],
+                       parallelism='replicas' if world > 1 else 'single',
+                       frame='all 64 views in one CUDA graph, 8 parallel streams',
+                       l2='working set larger than L2, no flush'),
+        'plain_fp32': {'value': round(plain, 3), 'unit': 'Mfragments/s', 'ms_per_step': round(t_plain / a.steps, 4),
+                       'path': 'one oit_render_frame per view, RGBA32F records, no graph'},
+        'speedup_vs_plain_fp32': round(value / plain, 3),
+        'e2e': {'value': round(total / e2e_s / 1e6, 3), 'unit': 'Mfragments/s', 'h2d_bytes_per_step': res['h2d'],
+                'd2h_bytes_per_step': res['d2h'], 'ms_per_step': round(e2e_s / a.steps * 1e3, 4)},
+        'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': None, 'peak': peak, 'unit': 'GB/s', 'frac': None,
+                     'traffic': None, 'peak_source': peak_kind, 'note': 'per-pass times summed over views; see the '
+                     'single-view workloads for per-kernel roofline fractions'},
+        'kernels': {k: {'ms_sum_over_views': round(v, 4)} for k, v in sec.items()},
+        'cpu_baseline': None,
+        'clocks': res['clocks'],
+        'gpu_launches': int(res['launches']),
+    }
+    print(json.dumps(line))
+
+
 def main():
     a = parse()
     wd = workload_dict(a.workload)
@@ -347,6 +525,11 @@ def main():
     import torch
     if world > 1:
         torch.distributed.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
+    if a.workload == BATCH_WORKLOAD:
+        main_batch(a, rank, world)
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
     res = run_gpu(a, wd, rank, world)
     elapsed = torch.tensor([res['elapsed_ms']], dtype=torch.float64, device='cuda')
     frags_all = torch.tensor([float(res['frags'] * a.steps)], dtype=torch.float64, device='cuda')
