@@ -467,14 +467,12 @@ __device__ __forceinline__ bool bbox_hits(uint2 bb, const WarpTile& w) {
 // Walks [beg, end) of the tile list in primitive order, 32 entries at a time:
 // the lanes test their triangle's bbox against the warp's micro-tile, the hits
 // copy their setup records into the warp's shared-memory stage in parallel
-// (cp.async), then vis(slot, t, inb) runs for each hit in list order, and
-// chunk_end() once the chunk's hits are done (before the stage is refilled).
-// Both are warp-uniform: every lane calls them; inb tells whether the lane's
-// pixel is inside the triangle's pixel bbox.
-template <class Vis, class ChunkEnd>
+// (cp.async) with their triangle ids and bboxes, then chunk(nh) processes
+// stage slots 0..nh-1, which are in list order. chunk is warp-uniform.
+template <class Chunk>
 __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile& w, TriSetup* stage,
-                                          uint32_t* stage_t, uint32_t beg, uint32_t end, Vis&& vis,
-                                          ChunkEnd&& chunk_end) {
+                                          uint32_t* stage_t, uint2* stage_bb, uint32_t beg, uint32_t end,
+                                          Chunk&& chunk) {
   const TriSetup* __restrict__ setup = reinterpret_cast<const TriSetup*>(p.setup);
   const uint32_t lt = (1u << w.lane) - 1u;
   uint32_t t_next = 0;
@@ -497,24 +495,20 @@ __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile&
       int4* dst = reinterpret_cast<int4*>(stage + slot);
 #pragma unroll
       for (int k = 0; k < 6; ++k) cp_async16(dst + k, src + k);
-      if (stage_t) stage_t[slot] = t;
+      stage_t[slot] = t;
+      stage_bb[slot] = bb;
     }
     bb_next = more ? __ldg(&p.bbox[t_next]) : make_uint2(0xFFFFFFFFu, 0u);
     cp_async_wait_all();
     __syncwarp();
-    uint32_t mm = m;
-    for (int k = 0; mm; ++k) {
-      const int j = __ffs(mm) - 1;
-      mm &= mm - 1;
-      const uint32_t tj = __shfl_sync(kFull, t, j);
-      const uint32_t bbx = __shfl_sync(kFull, bb.x, j), bby = __shfl_sync(kFull, bb.y, j);
-      const bool inb = w.valid && w.px >= (int)(bbx & 0xFFFF) && w.px <= (int)(bby & 0xFFFF) &&
-                       w.py >= (int)(bbx >> 16) && w.py <= (int)(bby >> 16);
-      vis(k, tj, inb);
-    }
-    chunk_end();
+    if (m) chunk(__popc(m));
     __syncwarp();
   }
+}
+
+__device__ __forceinline__ bool lane_in_bbox(uint2 bb, const WarpTile& w) {
+  return w.valid && w.px >= (int)(bb.x & 0xFFFF) && w.px <= (int)(bb.y & 0xFFFF) && w.py >= (int)(bb.x >> 16) &&
+         w.py <= (int)(bb.y >> 16);
 }
 
 // Per-warp fragment queue: coverage appends (stage slot, lane, coverage,
@@ -528,7 +522,10 @@ struct FragQueue {
   float r[kQueue], g[kQueue], b[kQueue], vz[kQueue];
   unsigned char tri[kQueue], lane[kQueue], cover[kQueue], pad[kQueue];
 };
-constexpr size_t kWarpStageBytes = 32 * sizeof(TriSetup) + 32 * sizeof(uint32_t) + sizeof(FragQueue);
+// per warp: 32 staged records, their triangle ids and bboxes, the queue, and
+// the queue-position masks the tiny-triangle path hands to owner lanes
+constexpr size_t kWarpStageBytes =
+    32 * sizeof(TriSetup) + 32 * sizeof(uint32_t) + 32 * sizeof(uint2) + sizeof(FragQueue) + 32 * sizeof(uint64_t);
 
 // ---------------------------------------------------------------------------
 // Transparent COLOR (+DEPTH) pass.
@@ -546,7 +543,11 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
   unsigned char* wbase = smem_raw + (size_t)warp * kWarpStageBytes;
   TriSetup* stage = reinterpret_cast<TriSetup*>(wbase);
   uint32_t* stage_t = reinterpret_cast<uint32_t*>(wbase + 32 * sizeof(TriSetup));
-  FragQueue* q = reinterpret_cast<FragQueue*>(wbase + 32 * sizeof(TriSetup) + 32 * sizeof(uint32_t));
+  uint2* stage_bb = reinterpret_cast<uint2*>(wbase + 32 * (sizeof(TriSetup) + sizeof(uint32_t)));
+  FragQueue* q = reinterpret_cast<FragQueue*>(wbase + 32 * (sizeof(TriSetup) + sizeof(uint32_t) + sizeof(uint2)));
+  unsigned long long* wmine = reinterpret_cast<unsigned long long*>(
+      wbase + 32 * (sizeof(TriSetup) + sizeof(uint32_t) + sizeof(uint2)) + sizeof(FragQueue));
+  wmine[w.lane] = 0ull;
   unsigned char* pol_smem = smem_raw + (size_t)oit::kWarpsPerTile * kWarpStageBytes +
                             (size_t)warp * Pol::smem_bytes_per_warp(p.L, p.coverage, p.record_fp32);
 
@@ -628,48 +629,127 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
       __syncwarp();
     };
 
-    walk_tile(
-        p, w, stage, Pol::kViewZ ? stage_t : nullptr, beg, end,
-        [&](int k, uint32_t, bool inb) {
-          const TriSetup& T = stage[k];
-          const int4 a = T.xy01, b = T.xy2f;
-          const float4 zc = T.zc;
-          uint32_t cover = 0;
-          float zcen = 0.f;
-          auto body = [&](auto etag) {
-            using E = decltype(etag);
-            const int bxp = w.px * 256, byp = w.py * 256;
+    // Coverage of one staged triangle against the warp's pixels (one lane per
+    // pixel or sample); appends the covered fragments to the queue.
+    auto cover_one = [&](int k) {
+      const TriSetup& T = stage[k];
+      const bool inb = lane_in_bbox(stage_bb[k], w);
+      const int4 a = T.xy01, b = T.xy2f;
+      const float4 zc = T.zc;
+      uint32_t cover = 0;
+      float zcen = 0.f;
+      auto body = [&](auto etag) {
+        using E = decltype(etag);
+        const int bxp = w.px * 256, byp = w.py * 256;
 #pragma unroll
-            for (int s = 0; s < S; ++s) {
-              const int2 sp = SSN > 1 ? sample_pos<SSN>(w.sample) : sample_pos<S>(s);
-              const EdgesT<E> e = edges_at<E>(a, b, bxp + sp.x, byp + sp.y);
-              if (inside(e, b.z)) {
-                const float z = depth_at(zc, e);
-                if (__float_as_uint(z) < tg.depth[s]) cover |= 1u << s;
-                if (S == 1) zcen = z;
-              }
-            }
-            if (S > 1 && cover) zcen = depth_at(zc, edges_at<E>(a, b, bxp + 128, byp + 128));
-          };
-          if (inb) {
-            if (b.z & kFlagSmall) body(int(0)); else body((long long)0);
+        for (int s = 0; s < S; ++s) {
+          const int2 sp = SSN > 1 ? sample_pos<SSN>(w.sample) : sample_pos<S>(s);
+          const EdgesT<E> e = edges_at<E>(a, b, bxp + sp.x, byp + sp.y);
+          if (inside(e, b.z)) {
+            const float z = depth_at(zc, e);
+            if (__float_as_uint(z) < tg.depth[s]) cover |= 1u << s;
+            if (S == 1) zcen = z;
           }
-          const bool has = cover != 0;
-          const uint32_t m = __ballot_sync(kFull, has);
-          if (!m) return;
-          const int cnt = __popc(m);
-          if (qn + cnt > kQueue) flush();
-          if (has) {
-            const int j = qn + __popc(m & lt);
-            q->tri[j] = (unsigned char)k;
-            q->lane[j] = (unsigned char)w.lane;
-            q->cover[j] = (unsigned char)cover;
-            q->depth[j] = __float_as_uint(zcen);
-            mine |= 1ull << j;
+        }
+        if (S > 1 && cover) zcen = depth_at(zc, edges_at<E>(a, b, bxp + 128, byp + 128));
+      };
+      if (inb) {
+        if (b.z & kFlagSmall) body(int(0)); else body((long long)0);
+      }
+      const bool has = cover != 0;
+      const uint32_t m = __ballot_sync(kFull, has);
+      if (!m) return;
+      const int cnt = __popc(m);
+      if (qn + cnt > kQueue) flush();
+      if (has) {
+        const int j = qn + __popc(m & lt);
+        q->tri[j] = (unsigned char)k;
+        q->lane[j] = (unsigned char)w.lane;
+        q->cover[j] = (unsigned char)cover;
+        q->depth[j] = __float_as_uint(zcen);
+        mine |= 1ull << j;
+      }
+      qn += cnt;
+    };
+
+    // Up to 8 consecutive triangles whose bbox spans at most 2x2 pixels: lane
+    // 4g+j tests pixel j of triangle k0+g's bbox (fragment-parallel coverage),
+    // reading the owner lane's opaque depth by shuffle. Entries are appended in
+    // lane order, i.e. triangle then pixel, the order cover_one would give.
+    auto cover_tiny = [&](int k0, int run) {
+      const int g = w.lane >> 2, jj = w.lane & 3;
+      const bool act = g < run;
+      const int k = k0 + (act ? g : 0);
+      const uint2 bb = stage_bb[k];
+      const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = bb.y >> 16;
+      const int px = bx0 + (jj & 1), py = by0 + (jj >> 1);
+      const bool ok = act && px <= bx1 && py <= by1 && px >= w.rx0 && px <= w.rx1 && py >= w.ry0 && py <= w.ry1 &&
+                      px < p.RW && py < p.RH;
+      const int owner = ok ? (py - w.ry0) * M::kW + (px - w.rx0) : 0;
+      uint32_t od[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) od[s] = __shfl_sync(kFull, tg.depth[s], owner);
+      uint32_t cover = 0;
+      float zcen = 0.f;
+      if (ok) {
+        const TriSetup& T = stage[k];
+        const int4 a = T.xy01, b = T.xy2f;
+        const float4 zc = T.zc;
+        const int bxp = px * 256, byp = py * 256;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+          const int2 sp = sample_pos<S>(s);
+          const EdgesT<int> e = edges_at<int>(a, b, bxp + sp.x, byp + sp.y);
+          if (inside(e, b.z)) {
+            const float z = depth_at(zc, e);
+            if (__float_as_uint(z) < od[s]) cover |= 1u << s;
+            if (S == 1) zcen = z;
           }
-          qn += cnt;
-        },
-        flush);
+        }
+        if (S > 1 && cover) zcen = depth_at(zc, edges_at<int>(a, b, bxp + 128, byp + 128));
+      }
+      const bool has = cover != 0;
+      const uint32_t m = __ballot_sync(kFull, has);
+      if (!m) return;
+      const int cnt = __popc(m);
+      if (qn + cnt > kQueue) flush();
+      if (has) {
+        const int j = qn + __popc(m & lt);
+        q->tri[j] = (unsigned char)k;
+        q->lane[j] = (unsigned char)owner;
+        q->cover[j] = (unsigned char)cover;
+        q->depth[j] = __float_as_uint(zcen);
+        atomicOr(&wmine[owner], 1ull << j);
+      }
+      __syncwarp();
+      mine |= wmine[w.lane];
+      wmine[w.lane] = 0ull;
+      __syncwarp();
+      qn += cnt;
+    };
+
+    walk_tile(p, w, stage, stage_t, stage_bb, beg, end, [&](int nh) {
+      // tiny triangles: bbox of at most 2x2 pixels (always on the int32 edge path)
+      uint32_t tmask = 0;
+      if (SSN == 1) {
+        const uint2 bb = stage_bb[w.lane < nh ? w.lane : 0];
+        const bool tiny = w.lane < nh && (bb.y & 0xFFFF) - (bb.x & 0xFFFF) <= 1 && (bb.y >> 16) - (bb.x >> 16) <= 1;
+        tmask = __ballot_sync(kFull, tiny);
+      }
+      for (int k = 0; k < nh;) {
+        const uint32_t rest = tmask >> k;
+        if (rest & 1u) {
+          int run = (~rest) ? __ffs(~rest) - 1 : 32 - k;
+          run = run < 8 ? run : 8;
+          cover_tiny(k, run);
+          k += run;
+        } else {
+          cover_one(k);
+          ++k;
+        }
+      }
+      flush();
+    });
   }
 
   pol.flush(p, w.valid);
@@ -694,9 +774,12 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
 template <int S>
 __global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
   __shared__ TriSetup stage_all[oit::kWarpsPerTile * 32];
+  __shared__ uint32_t stage_t_all[oit::kWarpsPerTile * 32];
+  __shared__ uint2 stage_bb_all[oit::kWarpsPerTile * 32];
   const int warp = threadIdx.x >> 5;
   const WarpTile w = warp_tile<1>(p);
   TriSetup* stage = stage_all + warp * 32;
+  uint2* stage_bb = stage_bb_all + warp * 32;
   uint32_t dep[S];
   float4 col[S];
 #pragma unroll
@@ -705,40 +788,42 @@ __global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
     col[s] = w.valid ? p.opaque_color[(size_t)s * p.P + w.pixel] : p.background;
   }
   const int tile = blockIdx.x + p.tile_offset;
-  walk_tile(p, w, stage, nullptr, p.tile_begin[tile], p.tile_end[tile], [&](int k, uint32_t, bool inb) {
-    if (!inb) return;  // no warp-collective operation follows
-    const TriSetup& T = stage[k];
-    const int4 a = T.xy01, b = T.xy2f;
-    const float4 zc = T.zc;
-    auto body = [&](auto etag) {
-      using E = decltype(etag);
-      const int bxp = w.px * 256, byp = w.py * 256;
-      uint32_t pass = 0;
-      uint32_t zs[S];
+  walk_tile(p, w, stage, stage_t_all + warp * 32, stage_bb, p.tile_begin[tile], p.tile_end[tile], [&](int nh) {
+    for (int k = 0; k < nh; ++k) {
+      if (!lane_in_bbox(stage_bb[k], w)) continue;  // no warp-collective operation follows
+      const TriSetup& T = stage[k];
+      const int4 a = T.xy01, b = T.xy2f;
+      const float4 zc = T.zc;
+      auto body = [&](auto etag) {
+        using E = decltype(etag);
+        const int bxp = w.px * 256, byp = w.py * 256;
+        uint32_t pass = 0;
+        uint32_t zs[S];
 #pragma unroll
-      for (int s = 0; s < S; ++s) {
-        const int2 sp = sample_pos<S>(s);
-        const EdgesT<E> e = edges_at<E>(a, b, bxp + sp.x, byp + sp.y);
-        zs[s] = 0u;
-        if (inside(e, b.z)) {
-          const uint32_t z = __float_as_uint(depth_at(zc, e));
-          zs[s] = z;
-          if (z < dep[s]) pass |= 1u << s;
+        for (int s = 0; s < S; ++s) {
+          const int2 sp = sample_pos<S>(s);
+          const EdgesT<E> e = edges_at<E>(a, b, bxp + sp.x, byp + sp.y);
+          zs[s] = 0u;
+          if (inside(e, b.z)) {
+            const uint32_t z = __float_as_uint(depth_at(zc, e));
+            zs[s] = z;
+            if (z < dep[s]) pass |= 1u << s;
+          }
         }
-      }
-      if (!pass) return;
-      const EdgesT<E> ec = edges_at<E>(a, b, bxp + 128, byp + 128);
-      const Shade sh = shade(T, ec, nullptr);
-      const float4 c = make_float4(sh.r, sh.g, sh.b, 1.0f);
+        if (!pass) return;
+        const EdgesT<E> ec = edges_at<E>(a, b, bxp + 128, byp + 128);
+        const Shade sh = shade(T, ec, nullptr);
+        const float4 c = make_float4(sh.r, sh.g, sh.b, 1.0f);
 #pragma unroll
-      for (int s = 0; s < S; ++s)
-        if (pass & (1u << s)) {
-          dep[s] = zs[s];
-          col[s] = c;
-        }
-    };
-    if (b.z & kFlagSmall) body(int(0)); else body((long long)0);
-  }, [] {});
+        for (int s = 0; s < S; ++s)
+          if (pass & (1u << s)) {
+            dep[s] = zs[s];
+            col[s] = c;
+          }
+      };
+      if (b.z & kFlagSmall) body(int(0)); else body((long long)0);
+    }
+  });
   if (w.valid) {
 #pragma unroll
     for (int s = 0; s < S; ++s) {
