@@ -523,9 +523,14 @@ struct FragQueue {
   unsigned char tri[kQueue], lane[kQueue], cover[kQueue], pad[kQueue];
 };
 // per warp: 32 staged records, their triangle ids and bboxes, the queue, and
-// the queue-position masks the tiny-triangle path hands to owner lanes
+// the per-hit pixel ranges of the coverage enumeration
+struct HitRanges {
+  int prefix[32];    // exclusive prefix of the hits' pixel counts
+  int origin[32];    // x | y << 16 of bbox ∩ micro-tile
+  int width[32];     // width | ceil(256 / width) << 8
+};
 constexpr size_t kWarpStageBytes =
-    32 * sizeof(TriSetup) + 32 * sizeof(uint32_t) + 32 * sizeof(uint2) + sizeof(FragQueue) + 32 * sizeof(uint64_t);
+    32 * sizeof(TriSetup) + 32 * sizeof(uint32_t) + 32 * sizeof(uint2) + sizeof(FragQueue) + sizeof(HitRanges);
 
 // ---------------------------------------------------------------------------
 // Transparent COLOR (+DEPTH) pass.
@@ -545,9 +550,8 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
   uint32_t* stage_t = reinterpret_cast<uint32_t*>(wbase + 32 * sizeof(TriSetup));
   uint2* stage_bb = reinterpret_cast<uint2*>(wbase + 32 * (sizeof(TriSetup) + sizeof(uint32_t)));
   FragQueue* q = reinterpret_cast<FragQueue*>(wbase + 32 * (sizeof(TriSetup) + sizeof(uint32_t) + sizeof(uint2)));
-  unsigned long long* wmine = reinterpret_cast<unsigned long long*>(
-      wbase + 32 * (sizeof(TriSetup) + sizeof(uint32_t) + sizeof(uint2)) + sizeof(FragQueue));
-  wmine[w.lane] = 0ull;
+  HitRanges* hr = reinterpret_cast<HitRanges*>(wbase + 32 * (sizeof(TriSetup) + sizeof(uint32_t) + sizeof(uint2)) +
+                                               sizeof(FragQueue));
   unsigned char* pol_smem = smem_raw + (size_t)oit::kWarpsPerTile * kWarpStageBytes +
                             (size_t)warp * Pol::smem_bytes_per_warp(p.L, p.coverage, p.record_fp32);
 
@@ -571,8 +575,8 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
   const TriPersp* __restrict__ persp = reinterpret_cast<const TriPersp*>(p.persp);
   const uint32_t lt = (1u << w.lane) - 1u;
   uint32_t nfrag = 0;  // warp-uniform
-  unsigned long long mine = 0;
   int qn = 0;          // warp-uniform
+  const uint32_t lane_bytes = (uint32_t)w.lane * 0x01010101u;
 
   for (int pass = 0; pass < Pol::kPasses; ++pass) {
     const bool shading = Pol::kPasses == 1 || pass == Pol::kPasses - 1;
@@ -606,7 +610,15 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
         if (w.lane == 0) node0 = atomicAdd(p.counter, (uint32_t)qn);
         node0 = __shfl_sync(kFull, node0, 0);
       }
-      unsigned long long mm = mine;
+      // this lane's entries: scan the owner byte of every queued fragment
+      unsigned long long mm = 0;
+      const uint32_t* lanes = reinterpret_cast<const uint32_t*>(q->lane);
+      for (int wi = 0; wi * 4 < qn; ++wi) {
+        const uint32_t eq = __vcmpeq4(lanes[wi], lane_bytes);  // 0xff per matching byte
+        const uint32_t bits = ((eq >> 7) & 1u) | ((eq >> 14) & 2u) | ((eq >> 21) & 4u) | ((eq >> 28) & 8u);
+        mm |= (unsigned long long)bits << (4 * wi);
+      }
+      if (qn < 64) mm &= (1ull << qn) - 1ull;
       while (mm) {
         const int j = __ffsll((long long)mm) - 1;
         mm &= mm - 1;
@@ -624,7 +636,6 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
         pol.fragment(p, pass, f, node0 + (uint32_t)j + 1u, tg);
       }
       if (shading) nfrag += (uint32_t)qn;
-      mine = 0;
       qn = 0;
       __syncwarp();
     };
@@ -667,86 +678,106 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
         q->lane[j] = (unsigned char)w.lane;
         q->cover[j] = (unsigned char)cover;
         q->depth[j] = __float_as_uint(zcen);
-        mine |= 1ull << j;
       }
       qn += cnt;
     };
 
-    // Up to 8 consecutive triangles whose bbox spans at most 2x2 pixels: lane
-    // 4g+j tests pixel j of triangle k0+g's bbox (fragment-parallel coverage),
-    // reading the owner lane's opaque depth by shuffle. Entries are appended in
-    // lane order, i.e. triangle then pixel, the order cover_one would give.
-    auto cover_tiny = [&](int k0, int run) {
-      const int g = w.lane >> 2, jj = w.lane & 3;
-      const bool act = g < run;
-      const int k = k0 + (act ? g : 0);
-      const uint2 bb = stage_bb[k];
-      const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = bb.y >> 16;
-      const int px = bx0 + (jj & 1), py = by0 + (jj >> 1);
-      const bool ok = act && px <= bx1 && py <= by1 && px >= w.rx0 && px <= w.rx1 && py >= w.ry0 && py <= w.ry1 &&
-                      px < p.RW && py < p.RH;
-      const int owner = ok ? (py - w.ry0) * M::kW + (px - w.rx0) : 0;
-      uint32_t od[S];
+    // Coverage of a staged chunk by enumeration (no sample shading): the
+    // pixels of every hit's bbox ∩ micro-tile are numbered hit by hit, row by
+    // row, and lane g of each group of 32 tests pair g, reading the owner
+    // lane's opaque depth by shuffle. Fragments enter the queue in lane order,
+    // i.e. primitive order then pixel order, as the owners will consume them.
+    auto cover_pairs = [&](int nh) {
+      int n = 0, ox = 0, oy = 0, wd = 1;
+      if (w.lane < nh) {
+        const uint2 bb = stage_bb[w.lane];
+        ox = max((int)(bb.x & 0xFFFF), w.rx0);
+        oy = max((int)(bb.x >> 16), w.ry0);
+        const int x1 = min(min((int)(bb.y & 0xFFFF), w.rx1), p.RW - 1);
+        const int y1 = min(min((int)(bb.y >> 16), w.ry1), p.RH - 1);
+        wd = x1 - ox + 1;
+        const int ht = y1 - oy + 1;
+        n = (wd > 0 && ht > 0) ? wd * ht : 0;
+      }
+      int incl = n;
 #pragma unroll
-      for (int s = 0; s < S; ++s) od[s] = __shfl_sync(kFull, tg.depth[s], owner);
-      uint32_t cover = 0;
-      float zcen = 0.f;
-      if (ok) {
-        const TriSetup& T = stage[k];
-        const int4 a = T.xy01, b = T.xy2f;
-        const float4 zc = T.zc;
-        const int bxp = px * 256, byp = py * 256;
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-          const int2 sp = sample_pos<S>(s);
-          const EdgesT<int> e = edges_at<int>(a, b, bxp + sp.x, byp + sp.y);
-          if (inside(e, b.z)) {
-            const float z = depth_at(zc, e);
-            if (__float_as_uint(z) < od[s]) cover |= 1u << s;
-            if (S == 1) zcen = z;
-          }
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, incl, o);
+        if (w.lane >= o) incl += y;
+      }
+      const int total = __shfl_sync(kFull, incl, 31);
+      if (w.lane < nh) {
+        hr->prefix[w.lane] = incl - n;
+        hr->origin[w.lane] = ox | (oy << 16);
+        const int wdp = wd > 0 ? wd : 1;
+        hr->width[w.lane] = wdp | (((256 + wdp - 1) / wdp) << 8);
+      }
+      __syncwarp();
+      for (int base = 0; base < total; base += 32) {
+        const int g = base + w.lane;
+        const bool act = g < total;
+        // the hit holding pair g: the last hit whose prefix is <= g
+        int lo = 0, hi = nh - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (hr->prefix[mid] <= g) lo = mid; else hi = mid - 1;
         }
-        if (S > 1 && cover) zcen = depth_at(zc, edges_at<int>(a, b, bxp + 128, byp + 128));
-      }
-      const bool has = cover != 0;
-      const uint32_t m = __ballot_sync(kFull, has);
-      if (!m) return;
-      const int cnt = __popc(m);
-      if (qn + cnt > kQueue) flush();
-      if (has) {
-        const int j = qn + __popc(m & lt);
-        q->tri[j] = (unsigned char)k;
-        q->lane[j] = (unsigned char)owner;
-        q->cover[j] = (unsigned char)cover;
-        q->depth[j] = __float_as_uint(zcen);
-        atomicOr(&wmine[owner], 1ull << j);
+        const int k = lo;
+        const int r = g - hr->prefix[k];
+        const int wpk = hr->width[k];
+        const int wdt = wpk & 0xFF;
+        const int row = (r * (wpk >> 8)) >> 8;  // exact r / wdt for r < 32, wdt <= 8
+        const int org = hr->origin[k];
+        const int px = (org & 0xFFFF) + r - row * wdt, py = (org >> 16) + row;
+        const int owner = act ? (py - w.ry0) * M::kW + (px - w.rx0) : 0;
+        uint32_t od[S];
+#pragma unroll
+        for (int s = 0; s < S; ++s) od[s] = __shfl_sync(kFull, tg.depth[s], owner);
+        uint32_t cover = 0;
+        float zcen = 0.f;
+        if (act) {
+          const TriSetup& T = stage[k];
+          const int4 a = T.xy01, b = T.xy2f;
+          const float4 zc = T.zc;
+          const int bxp = px * 256, byp = py * 256;
+          auto body = [&](auto etag) {
+            using E = decltype(etag);
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+              const int2 sp = sample_pos<S>(s);
+              const EdgesT<E> e = edges_at<E>(a, b, bxp + sp.x, byp + sp.y);
+              if (inside(e, b.z)) {
+                const float z = depth_at(zc, e);
+                if (__float_as_uint(z) < od[s]) cover |= 1u << s;
+                if (S == 1) zcen = z;
+              }
+            }
+            if (S > 1 && cover) zcen = depth_at(zc, edges_at<E>(a, b, bxp + 128, byp + 128));
+          };
+          if (b.z & kFlagSmall) body(int(0)); else body((long long)0);
+        }
+        const bool has = cover != 0;
+        const uint32_t m = __ballot_sync(kFull, has);
+        if (!m) continue;
+        const int cnt = __popc(m);
+        if (qn + cnt > kQueue) flush();
+        if (has) {
+          const int j = qn + __popc(m & lt);
+          q->tri[j] = (unsigned char)k;
+          q->lane[j] = (unsigned char)owner;
+          q->cover[j] = (unsigned char)cover;
+          q->depth[j] = __float_as_uint(zcen);
+        }
+        qn += cnt;
       }
       __syncwarp();
-      mine |= wmine[w.lane];
-      wmine[w.lane] = 0ull;
-      __syncwarp();
-      qn += cnt;
     };
 
     walk_tile(p, w, stage, stage_t, stage_bb, beg, end, [&](int nh) {
-      // tiny triangles: bbox of at most 2x2 pixels (always on the int32 edge path)
-      uint32_t tmask = 0;
       if (SSN == 1) {
-        const uint2 bb = stage_bb[w.lane < nh ? w.lane : 0];
-        const bool tiny = w.lane < nh && (bb.y & 0xFFFF) - (bb.x & 0xFFFF) <= 1 && (bb.y >> 16) - (bb.x >> 16) <= 1;
-        tmask = __ballot_sync(kFull, tiny);
-      }
-      for (int k = 0; k < nh;) {
-        const uint32_t rest = tmask >> k;
-        if (rest & 1u) {
-          int run = (~rest) ? __ffs(~rest) - 1 : 32 - k;
-          run = run < 8 ? run : 8;
-          cover_tiny(k, run);
-          k += run;
-        } else {
-          cover_one(k);
-          ++k;
-        }
+        cover_pairs(nh);
+      } else {
+        for (int k = 0; k < nh; ++k) cover_one(k);  // one lane per sample
       }
       flush();
     });
