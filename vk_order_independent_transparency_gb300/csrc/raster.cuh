@@ -525,9 +525,10 @@ struct FragQueue {
 // per warp: 32 staged records, their triangle ids and bboxes, the queue, and
 // the per-hit pixel ranges of the coverage enumeration
 struct HitRanges {
-  int prefix[32];    // exclusive prefix of the hits' pixel counts
-  int origin[32];    // x | y << 16 of bbox ∩ micro-tile
-  int width[32];     // width | ceil(256 / width) << 8
+  // per hit: prefix (bits 0-10, exclusive prefix of the pixel counts), x and y
+  // of bbox ∩ micro-tile relative to the micro-tile (bits 11-13, 14-15), its
+  // width (bits 16-19) and ceil(256 / width) (bits 20-28)
+  uint32_t packed[32];
 };
 constexpr size_t kWarpStageBytes =
     32 * sizeof(TriSetup) + 32 * sizeof(uint32_t) + 32 * sizeof(uint2) + sizeof(FragQueue) + sizeof(HitRanges);
@@ -707,10 +708,10 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
       }
       const int total = __shfl_sync(kFull, incl, 31);
       if (w.lane < nh) {
-        hr->prefix[w.lane] = incl - n;
-        hr->origin[w.lane] = ox | (oy << 16);
         const int wdp = wd > 0 ? wd : 1;
-        hr->width[w.lane] = wdp | (((256 + wdp - 1) / wdp) << 8);
+        const int rx = n ? ox - w.rx0 : 0, ry = n ? oy - w.ry0 : 0;
+        hr->packed[w.lane] = (uint32_t)(incl - n) | ((uint32_t)rx << 11) | ((uint32_t)ry << 14) |
+                             ((uint32_t)wdp << 16) | ((uint32_t)((256 + wdp - 1) / wdp) << 20);
       }
       __syncwarp();
       for (int base = 0; base < total; base += 32) {
@@ -720,15 +721,14 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
         int lo = 0, hi = nh - 1;
         while (lo < hi) {
           const int mid = (lo + hi + 1) >> 1;
-          if (hr->prefix[mid] <= g) lo = mid; else hi = mid - 1;
+          if ((int)(hr->packed[mid] & 0x7FFu) <= g) lo = mid; else hi = mid - 1;
         }
         const int k = lo;
-        const int r = g - hr->prefix[k];
-        const int wpk = hr->width[k];
-        const int wdt = wpk & 0xFF;
-        const int row = (r * (wpk >> 8)) >> 8;  // exact r / wdt for r < 32, wdt <= 8
-        const int org = hr->origin[k];
-        const int px = (org & 0xFFFF) + r - row * wdt, py = (org >> 16) + row;
+        const uint32_t hk = hr->packed[k];
+        const int r = g - (int)(hk & 0x7FFu);
+        const int wdt = (int)((hk >> 16) & 0xFu);
+        const int row = (r * (int)(hk >> 20)) >> 8;  // exact r / wdt for r < 32, wdt <= 8
+        const int px = w.rx0 + (int)((hk >> 11) & 7u) + r - row * wdt, py = w.ry0 + (int)((hk >> 14) & 3u) + row;
         const int owner = act ? (py - w.ry0) * M::kW + (px - w.rx0) : 0;
         uint32_t od[S];
 #pragma unroll
