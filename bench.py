@@ -445,18 +445,24 @@ def _copy_d2h(host_tensor, dev_ptr, nbytes, stream):
                        ctypes.c_void_p(stream))
 
 
-def main_batch(a, rank, world):
+def reduce_replicas(maxes, sums, world, device='cuda'):
+    """The only exchange between replicas: the max over ranks of each timed
+    duration and the sum over ranks of the work each rank did."""
     import torch
-    res = run_batch(a, rank)
-    t = torch.tensor([res['t_mixed'], res['t_plain'], res['e2e_s']], dtype=torch.float64, device='cuda')
-    fr = torch.tensor([float(res['frags'] * a.steps)], dtype=torch.float64, device='cuda')
+    m = torch.tensor([float(x) for x in maxes], dtype=torch.float64, device=device)
+    s = torch.tensor([float(x) for x in sums], dtype=torch.float64, device=device)
     if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(fr)
+        torch.distributed.all_reduce(m, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(s)
+    return m.tolist(), s.tolist()
+
+
+def main_batch(a, rank, world):
+    res = run_batch(a, rank)
+    (t_mixed, t_plain, e2e_s), (total,) = reduce_replicas([res['t_mixed'], res['t_plain'], res['e2e_s']],
+                                                          [res['frags'] * a.steps], world)
     if rank != 0:
         return
-    t_mixed, t_plain, e2e_s = [float(x) for x in t.tolist()]
-    total = float(fr.item())
     value = total / (t_mixed * 1e-3) / 1e6
     plain = total / (t_plain * 1e-3) / 1e6
     peak, peak_kind = peaks()
@@ -531,19 +537,12 @@ def main():
             torch.distributed.destroy_process_group()
         return
     res = run_gpu(a, wd, rank, world)
-    elapsed = torch.tensor([res['elapsed_ms']], dtype=torch.float64, device='cuda')
-    frags_all = torch.tensor([float(res['frags'] * a.steps)], dtype=torch.float64, device='cuda')
-    e2e = torch.tensor([res['e2e_s']], dtype=torch.float64, device='cuda')
-    if world > 1:
-        torch.distributed.all_reduce(elapsed, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(frags_all)
-        torch.distributed.all_reduce(e2e, op=torch.distributed.ReduceOp.MAX)
+    (t_ms, e2e_s), (frags_all,) = reduce_replicas([res['elapsed_ms'], res['e2e_s']], [res['frags'] * a.steps], world)
     if rank != 0:
         torch.distributed.destroy_process_group()
         return
-    t_ms = float(elapsed.item())
-    value = float(frags_all.item()) / (t_ms * 1e-3) / 1e6
-    e2e_value = float(frags_all.item()) / float(e2e.item()) / 1e6
+    value = frags_all / (t_ms * 1e-3) / 1e6
+    e2e_value = frags_all / e2e_s / 1e6
 
     peak, peak_kind = peaks()
     prof = res['prof']
@@ -584,7 +583,7 @@ def main():
                        frame='one CUDA graph per frame (opaque + transparent binning, rasters, composite)',
                        l2='working set larger than L2 (A-buffer + triangle setup > 129 MB), no flush'),
         'e2e': {'value': round(e2e_value, 3), 'unit': 'Mfragments/s', 'h2d_bytes_per_step': res['h2d'],
-                'd2h_bytes_per_step': res['d2h'], 'ms_per_step': round(float(e2e.item()) / a.steps * 1e3, 4)},
+                'd2h_bytes_per_step': res['d2h'], 'ms_per_step': round(e2e_s / a.steps * 1e3, 4)},
         'roofline': roofline,
         'kernels': kernels,
         'cpu_baseline': cpu,

@@ -129,6 +129,26 @@ def compare_abuffer(algorithm, g, o, L, P, coverage, ssn=1, fp32=False):
             np.testing.assert_array_equal(gp[used], op[used])
 
 
+def check_pair(alg, g, o, W, H, L, aa=0, ss=1, fp32=False):
+    """Every bit-exact and colour comparison of one engine frame against the
+    oracle's: error bits, fragment counts, A-buffer state, the tail-blended
+    colour target (2e-5 absolute) and the RGBA8 image (1 LSB)."""
+    msaa, sample_shading, _ = oit.aa_settings(aa)
+    coverage = msaa > 1 and not sample_shading
+    ssn = msaa if sample_shading else 1
+    P = W * H * ss * ss
+    assert g['error'] == 0
+    assert g['fragments'] == o['fragments']
+    if alg != oit.OIT_WEIGHTED:
+        compare_abuffer(alg, g, o, L, P, coverage, ssn, fp32)
+        if ssn > 1:
+            ref_col = o['color_samples'].reshape(-1, 4)
+        else:
+            ref_col = o['color_samples'].mean(axis=0)
+        np.testing.assert_allclose(g['color'][:ssn * P], ref_col, atol=2e-5, rtol=0)
+    return compare_images(g, o)
+
+
 def compare_images(g, o, max_lsb=1):
     d = np.abs(g['image'].astype(np.int32) - o['image'].astype(np.int32))
     assert d.max() <= max_lsb, 'image differs by %d LSB at %s' % (d.max(), np.argwhere(d == d.max())[:4])

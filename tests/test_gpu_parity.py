@@ -25,20 +25,7 @@ def run_pair(engine, alg, W, H, n_obj, percent=100, seed=3, rmin=0.05, rmax=0.2,
 
 
 def check(engine, alg, g, o, W, H, L, aa=0, ss=1, fp32=False):
-    msaa, sample_shading, _ = engine.aa_settings(aa)
-    coverage = msaa > 1 and not sample_shading
-    ssn = msaa if sample_shading else 1
-    P = W * H * ss * ss
-    assert g['error'] == 0
-    assert g['fragments'] == o['fragments']
-    if alg != engine.OIT_WEIGHTED:
-        pu.compare_abuffer(alg, g, o, L, P, coverage, ssn, fp32)
-        if ssn > 1:
-            ref_col = o['color_samples'].reshape(-1, 4)
-        else:
-            ref_col = o['color_samples'].mean(axis=0)
-        np.testing.assert_allclose(g['color'][:ssn * P], ref_col, atol=2e-5, rtol=0)
-    pu.compare_images(g, o)
+    pu.check_pair(alg, g, o, W, H, L, aa, ss, fp32)
 
 
 @pytest.mark.parametrize('tail', [True, False])
