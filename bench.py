@@ -256,6 +256,39 @@ def count_kept(wd, r):
     return 0
 
 
+class _DeviceArray:
+    """A zero-copy view of an engine buffer for torch (__cuda_array_interface__)."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {'shape': shape, 'typestr': typestr, 'data': (ptr, False), 'version': 3}
+
+
+def resolve_bytes(views, renderers):
+    """Algorithmic bytes of one batched resolve: per pixel the colour target
+    (16 B) in and RGBA8 (4 B) out; linked lists: the head (4 B) and every
+    stored node (16 B); Loop64: every kept key plus the terminating empty key
+    (8 B each); the work list (4 B per micro-tile, written and read) and the
+    micro-tile lengths (read twice). Counted on the device, outside timing."""
+    import torch
+    import vk_order_independent_transparency_gb300 as oit
+    total = 0
+    tiles = 0
+    for vd, r in zip(views, renderers):
+        W, H, L = vd['width'], vd['height'], vd['oit_layers']
+        P = W * H
+        tiles += ((W + 7) // 8) * ((H + 3) // 4)
+        b = P * (16 + 4)
+        if vd['algorithm'] == 'linkedlist':
+            b += P * 4 + 16 * min(r.fragment_count(), vd['nodes_per_pixel'] * P - 1)
+        else:
+            ptr, _ = r.buffer(oit.OIT_BUF_ABUFFER)
+            keys = torch.as_tensor(_DeviceArray(ptr, (L, P), '<i8'), device='cuda')
+            n = (keys != -1).sum(0)
+            b += 8 * int(n.sum().item() + (n < L).sum().item())
+        total += b
+    return total + tiles * (4 + 4 + 2)
+
+
 def run_gpu(a, wd, rank, world):
     import numpy as np
     import torch
@@ -432,8 +465,29 @@ def run_batch(a, rank):
     for _ in range(a.steps):
         step_e2e()
     e2e_s = time.perf_counter() - t0
+
+    # resolve alone: the batched persistent resolve of the mixed views against
+    # one FP32-record composite launch per view, on the frames rendered above
+    batch.render(stream)
+    step_plain()
+
+    def step_resolve_mixed():
+        batch.resolve(stream)
+
+    def step_resolve_plain():
+        for r in plain:
+            r.composite(None, stream)
+
+    for _ in range(max(3, a.warmup)):
+        step_resolve_mixed()
+        step_resolve_plain()
+    t_res_mixed = timed(step_resolve_mixed)
+    t_res_plain = timed(step_resolve_plain)
+    res_cfg = batch.resolve_config()
+    res_bytes = resolve_bytes(vs, mixed)
     return dict(frags=frags, t_mixed=t_mixed, t_plain=t_plain, launches=launches, clocks=clk, sections=sections,
-                e2e_s=e2e_s, h2d=h2d, d2h=d2h, views=vs)
+                e2e_s=e2e_s, h2d=h2d, d2h=d2h, views=vs, t_res_mixed=t_res_mixed, t_res_plain=t_res_plain,
+                res_cfg=res_cfg, res_bytes=res_bytes)
 
 
 def _copy_d2h(host_tensor, dev_ptr, nbytes, stream):
@@ -459,8 +513,9 @@ def reduce_replicas(maxes, sums, world, device='cuda'):
 
 def main_batch(a, rank, world):
     res = run_batch(a, rank)
-    (t_mixed, t_plain, e2e_s), (total,) = reduce_replicas([res['t_mixed'], res['t_plain'], res['e2e_s']],
-                                                          [res['frags'] * a.steps], world)
+    (t_mixed, t_plain, e2e_s, t_res_mixed, t_res_plain), (total,) = reduce_replicas(
+        [res['t_mixed'], res['t_plain'], res['e2e_s'], res['t_res_mixed'], res['t_res_plain']],
+        [res['frags'] * a.steps], world)
     if rank != 0:
         return
     value = total / (t_mixed * 1e-3) / 1e6
@@ -486,11 +541,35 @@ def main_batch(a, rank, world):
                      'traffic': None, 'peak_source': peak_kind, 'note': 'per-pass times summed over views; see the '
                      'single-view workloads for per-kernel roofline fractions'},
         'kernels': {k: {'ms_sum_over_views': round(v, 4)} for k, v in sec.items()},
+        'resolve': resolve_line(res, a, world, total, t_res_mixed, t_res_plain, peak, peak_kind),
         'cpu_baseline': None,
         'clocks': res['clocks'],
         'gpu_launches': int(res['launches']),
     }
     print(json.dumps(line))
+
+
+def resolve_line(res, a, world, total, t_mixed, t_plain, peak, peak_kind):
+    """The batched resolve (one persistent launch over every view, RGBA8
+    records) against the plain path (one composite launch per view, FP32
+    records): fragments of the batch resolved per second, and the batched
+    kernel's achieved HBM bandwidth from its algorithmic bytes."""
+    value = total / (t_mixed * 1e-3) / 1e6
+    plain = total / (t_plain * 1e-3) / 1e6
+    per = t_mixed / a.steps
+    gbs = res['res_bytes'] / (per * 1e-3) / 1e9
+    return {
+        'value': round(value, 3), 'unit': 'Mfragments/s', 'ms_per_step': round(per, 4),
+        'plain_fp32': {'value': round(plain, 3), 'unit': 'Mfragments/s', 'ms_per_step': round(t_plain / a.steps, 4),
+                       'path': 'oit_composite per view, RGBA32F records'},
+        'speedup_vs_plain_fp32': round(value / plain, 3),
+        'roofline': {'bound': 'hbm', 'kernel': 'k_resolve_list + k_resolve_loop64 side by side (+ binning)',
+                     'achieved': round(gbs, 1),
+                     'peak': peak, 'unit': 'GB/s', 'frac': round(gbs / peak, 4),
+                     'traffic': ncu_traffic('resolve', BATCH_WORKLOAD), 'bytes_per_step': int(res['res_bytes']),
+                     'peak_source': peak_kind},
+        'autotuned': res['res_cfg'],
+    }
 
 
 def main():

@@ -86,7 +86,8 @@ typedef struct oit_state {
   float alpha_min, alpha_width;            /* SceneData::alphaMin / alphaWidth */
   uint32_t record_format;                  /* OIT_RECORD_* */
   uint32_t weighted_precision;             /* OIT_WEIGHTED_* */
-  float bin_capacity_scale;                /* tile-bin pairs per triangle reserved (0 = default 4) */
+  float bin_capacity_scale;                /* tile-bin headroom over the (triangle, tile) pair count
+                                              measured on earlier frames (0 = default 1.25) */
   uint32_t flags;                          /* OIT_FLAG_* */
 } oit_state;
 
@@ -185,6 +186,41 @@ int oit_render_frame_host(oit_context* ctx, const float* vertices_host, uint32_t
                           uint32_t triangles_per_object, int32_t percent_transparent,
                           uint8_t* out_rgba8_host, void* stream);
 
+/* ---- instanced meshes -------------------------------------------------- */
+
+/* One template mesh drawn once per instance: what Sample::initScene
+ * (main.cpp:343-387) flattens into one vertex/index buffer, kept as a template
+ * sphere plus a 32-byte record per object (the comment at main.cpp:343-345
+ * names instancing as the alternative). No counterpart in the reference's
+ * API. Template vertex: pos.xyz, normal.xyz (24 bytes). Instance: centre.xyz,
+ * radius, color.rgba (32 bytes; the table must be 16-byte aligned). Frame
+ * triangle t is template triangle t % template_triangles of instance
+ * t / template_triangles; its positions are template_pos * radius + centre,
+ * multiply and add each rounded to FP32, and its colour is the instance's, so
+ * a frame is bit-identical to the frame of the flattened mesh that
+ * oit_scene_generate builds from the same oit_scene_desc. */
+typedef struct oit_instanced_mesh {
+  const float* template_vertices_device;
+  const uint32_t* template_indices_device;
+  const float* instances_device;
+  uint32_t template_vertices;
+  uint32_t template_triangles;
+  uint32_t num_instances;
+} oit_instanced_mesh;
+
+/* oit_render_frame over an instanced mesh: one object per instance, the first
+ * percent_transparent% transparent. */
+int oit_render_frame_instanced(oit_context* ctx, const oit_instanced_mesh* mesh, int32_t percent_transparent,
+                               uint8_t* out_rgba8_device, void* stream);
+
+/* Same frame from host memory (template, instance table in; RGBA8 image out),
+ * synchronous on the stream. */
+int oit_render_frame_instanced_host(oit_context* ctx, const float* template_vertices_host,
+                                    uint32_t template_vertices, const uint32_t* template_indices_host,
+                                    uint32_t template_triangles, const float* instances_host,
+                                    uint32_t num_instances, int32_t percent_transparent,
+                                    uint8_t* out_rgba8_host, void* stream);
+
 /* One whole frame, like oit_render_frame, that allocates no device memory.
  * No counterpart in the reference: it exists for callers that cannot let a
  * library call cudaMalloc -- applications that own every device allocation
@@ -233,6 +269,27 @@ int oit_batch_render(oit_batch* batch, const oit_view_frame* views, uint32_t num
 
 /* Kernel launches per replay of the batch's graph. */
 int oit_batch_launch_count(oit_batch* batch, uint64_t* launches);
+
+/* COMPOSITE of every view's current frame (the composite draws of
+ * drawTransparent*, oitRender.cpp:191-198 and 327-334, once per view in the
+ * reference), for views whose frame has been rendered. Linked-list and Loop64
+ * views at 1x with RGBA8 records and no linear output are resolved together:
+ * one persistent launch for all linked-list views and one for all Loop64
+ * views, running side by side; each walks the views' 8x4 micro-tiles, binned
+ * by the longest per-pixel list of each (the transparent raster records it),
+ * costliest first, or in view order. The other views get their own composite
+ * launch. oit_batch_render resolves the same way. The first call for a set of
+ * views times candidate shapes on these frames (an autotuner; see
+ * oit_batch_resolve_config) and keeps the fastest. */
+int oit_batch_resolve(oit_batch* batch, const oit_view_frame* views, uint32_t num_views, void* stream);
+
+/* The shape the autotuner picked for one part of the batched resolve (part 0:
+ * linked-list views, 1: Loop64 views): threads per block, blocks, binned (1)
+ * or view-order (0) work list, and the register slots holding the first sort
+ * entries of a list (0, 4 or 8; the rest live in local memory). A part without
+ * views reports zeros. OIT_ERR_STATE before the first resolve. */
+int oit_batch_resolve_config(oit_batch* batch, uint32_t part, uint32_t* threads_per_block, uint32_t* blocks,
+                             int32_t* binned, int32_t* register_slots);
 
 /* ---- inspection -------------------------------------------------------- */
 
@@ -296,6 +353,12 @@ int oit_scene_size(const oit_scene_desc* desc, uint32_t* num_vertices, uint32_t*
 
 /* Fills host arrays of num_vertices*10 floats and num_triangles*3 indices. */
 int oit_scene_generate(const oit_scene_desc* desc, float* vertices_host, uint32_t* indices_host);
+
+/* The same scene as a template sphere and an instance table (see
+ * oit_instanced_mesh): (stacks+1)*(slices+1) template vertices of 6 floats,
+ * triangles_per_object*3 template indices, num_objects*8 instance floats. */
+int oit_scene_generate_instanced(const oit_scene_desc* desc, float* template_vertices_host,
+                                 uint32_t* template_indices_host, float* instances_host);
 
 /* Camera at `eye` looking at `target` (up +y), vertical fov in degrees,
  * Vulkan clip space (z in [0,1], y down): the engine's stand-in for

@@ -48,6 +48,8 @@ EXPORTS = [
     'oit_scene_size', 'oit_scene_generate', 'oit_camera', 'oit_srgb_tables', 'oit_version',
     'oit_profile_enable', 'oit_profile_read', 'oit_render_frame_noalloc',
     'oit_batch_create', 'oit_batch_destroy', 'oit_batch_render', 'oit_batch_launch_count',
+    'oit_render_frame_instanced', 'oit_render_frame_instanced_host', 'oit_scene_generate_instanced',
+    'oit_batch_resolve', 'oit_batch_resolve_config',
 ]
 PROF_SECTIONS = ['opaque_bin', 'opaque_raster', 'transparent_bin', 'transparent_raster', 'composite']
 
@@ -71,6 +73,12 @@ class OitSceneData(ctypes.Structure):
 class OitMesh(ctypes.Structure):
     _fields_ = [('vertices_device', ctypes.c_void_p), ('indices_device', ctypes.c_void_p),
                 ('num_vertices', ctypes.c_uint32), ('num_triangles', ctypes.c_uint32)]
+
+
+class OitInstancedMesh(ctypes.Structure):
+    _fields_ = [('template_vertices_device', ctypes.c_void_p), ('template_indices_device', ctypes.c_void_p),
+                ('instances_device', ctypes.c_void_p), ('template_vertices', ctypes.c_uint32),
+                ('template_triangles', ctypes.c_uint32), ('num_instances', ctypes.c_uint32)]
 
 
 class OitSceneDesc(ctypes.Structure):
@@ -139,6 +147,12 @@ def library():
         'oit_render_frame_noalloc': (I, [ctypes.POINTER(OitState), ctypes.POINTER(OitSceneData),
                                          ctypes.POINTER(OitMesh), U, ctypes.c_int32, P, P]),
         'oit_profile_read': (I, [P, ctypes.POINTER(ctypes.c_double * 5), ctypes.POINTER(ctypes.c_uint64 * 5)]),
+        'oit_render_frame_instanced': (I, [P, ctypes.POINTER(OitInstancedMesh), ctypes.c_int32, P, P]),
+        'oit_render_frame_instanced_host': (I, [P, P, U, P, U, P, U, ctypes.c_int32, P, P]),
+        'oit_scene_generate_instanced': (I, [ctypes.POINTER(OitSceneDesc), P, P, P]),
+        'oit_batch_resolve': (I, [P, ctypes.POINTER(OitViewFrame), U, P]),
+        'oit_batch_resolve_config': (I, [P, U, ctypes.POINTER(U), ctypes.POINTER(U), ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.POINTER(ctypes.c_int32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -210,6 +224,23 @@ def make_scene(num_objects, seed=1, radius_min=0.05, radius_max=0.15, half_exten
     return v, i, tpo.value
 
 
+def make_scene_instanced(num_objects, seed=1, radius_min=0.05, radius_max=0.15, half_extent=1.0, stacks=16,
+                         slices=32):
+    """The scene of make_scene as a template sphere and an instance table:
+    (template vertices float32 [vpo,6], template indices uint32 [tpo,3],
+    instances float32 [num_objects,8] = centre.xyz, radius, color.rgba)."""
+    d = OitSceneDesc(seed, num_objects, stacks, slices, half_extent, radius_min, radius_max)
+    tpo = ctypes.c_uint32()
+    lib = library()
+    _check(lib.oit_scene_size(ctypes.byref(d), None, None, ctypes.byref(tpo)), 'oit_scene_size')
+    tv = np.empty(((stacks + 1) * (slices + 1), 6), np.float32)
+    ti = np.empty((tpo.value, 3), np.uint32)
+    inst = np.empty((num_objects, 8), np.float32)
+    _check(lib.oit_scene_generate_instanced(ctypes.byref(d), tv.ctypes.data, ti.ctypes.data, inst.ctypes.data),
+           'oit_scene_generate_instanced')
+    return tv, ti, inst
+
+
 def make_camera(width, height, eye=(0.0, 0.0, 3.0), target=(0.0, 0.0, 0.0), fov_y=45.0, z_near=0.1, z_far=10.0):
     """SceneData matrices (column-major) for a camera looking at `target`."""
     sd = OitSceneData()
@@ -237,6 +268,20 @@ class DeviceMesh:
         self.num_vertices = int(vertices.shape[0])
         self.num_triangles = int(indices.shape[0])
         self.c = OitMesh(self.vertices.data_ptr(), self.indices.data_ptr(), self.num_vertices, self.num_triangles)
+
+
+class DeviceInstancedMesh:
+    """A template mesh and its instance table resident in device memory."""
+
+    def __init__(self, template_vertices, template_indices, instances, device='cuda'):
+        import torch
+        self.template_vertices = torch.as_tensor(np.ascontiguousarray(template_vertices, np.float32)).to(device)
+        self.template_indices = torch.as_tensor(
+            np.ascontiguousarray(template_indices, np.uint32).view(np.int32)).to(device)
+        self.instances = torch.as_tensor(np.ascontiguousarray(instances, np.float32)).to(device)
+        self.c = OitInstancedMesh(self.template_vertices.data_ptr(), self.template_indices.data_ptr(),
+                                  self.instances.data_ptr(), int(template_vertices.shape[0]),
+                                  int(template_indices.shape[0]), int(instances.shape[0]))
 
 
 class Renderer:
@@ -308,7 +353,24 @@ class Renderer:
                                               triangles_per_object, percent_transparent, out.ctypes.data,
                                               stream), 'oit_render_frame_host')
 
+    def render_frame_instanced(self, mesh, percent_transparent=100, out_ptr=None, stream=None):
+        """render_frame over a DeviceInstancedMesh (one object per instance)."""
+        _check(self.lib.oit_render_frame_instanced(self._ctx, ctypes.byref(mesh.c), percent_transparent, out_ptr,
+                                                   stream), 'oit_render_frame_instanced')
+
+    def render_frame_instanced_host(self, template_vertices, template_indices, instances, percent_transparent, out,
+                                    stream=None):
+        """Whole frame from a host template and instance table; `out` is (height, width, 4) uint8."""
+        tv = np.ascontiguousarray(template_vertices, np.float32)
+        ti = np.ascontiguousarray(template_indices, np.uint32)
+        inst = np.ascontiguousarray(instances, np.float32)
+        _check(self.lib.oit_render_frame_instanced_host(self._ctx, tv.ctypes.data, tv.shape[0], ti.ctypes.data,
+                                                        ti.shape[0], inst.ctypes.data, inst.shape[0],
+                                                        percent_transparent, out.ctypes.data, stream),
+               'oit_render_frame_instanced_host')
+
     # ---- inspection ----
+
     def buffer(self, which):
         p = ctypes.c_void_p()
         n = ctypes.c_size_t()
@@ -396,6 +458,24 @@ class Batch:
         v = ctypes.c_uint64()
         _check(self.lib.oit_batch_launch_count(self._b, ctypes.byref(v)), 'oit_batch_launch_count')
         return v.value
+
+    def resolve(self, stream=None):
+        """COMPOSITE of every view's current frame: one persistent launch for the
+        linked-list and Loop64 views, a composite launch per other view."""
+        _check(self.lib.oit_batch_resolve(self._b, self._frames, len(self._frames), stream), 'oit_batch_resolve')
+
+    def resolve_config(self):
+        """{'linkedlist': ..., 'loop64': ...}: per part of the batched resolve,
+        the shape the autotuner picked (threads per block, blocks, binned work
+        list, register slots for the first sort entries)."""
+        out = {}
+        for part, name in ((0, 'linkedlist'), (1, 'loop64')):
+            t, n, b, k = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_int32(), ctypes.c_int32()
+            _check(self.lib.oit_batch_resolve_config(self._b, part, ctypes.byref(t), ctypes.byref(n), ctypes.byref(b),
+                                                     ctypes.byref(k)), 'oit_batch_resolve_config')
+            out[name] = {'threads_per_block': t.value, 'blocks': n.value, 'binned': bool(b.value),
+                         'register_slots': k.value}
+        return out
 
 
 _cudart_lib = None

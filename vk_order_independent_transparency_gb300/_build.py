@@ -15,7 +15,8 @@ CSRC = os.path.join(PKG, 'csrc')
 LIB = os.path.join(PKG, 'liboit_gb300.so')
 BUILD = os.path.join(PKG, '_objs')
 
-CU_SOURCES = ['setup_bin.cu', 'raster_a.cu', 'raster_b.cu', 'raster_c.cu', 'composite.cu', 'noalloc.cu']
+CU_SOURCES = ['setup_bin.cu', 'raster_a.cu', 'raster_b.cu', 'raster_c.cu', 'composite.cu', 'resolve.cu',
+              'noalloc.cu']
 CPP_SOURCES = ['engine.cpp', 'scene.cpp']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 

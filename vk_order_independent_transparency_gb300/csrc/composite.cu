@@ -10,6 +10,7 @@
 // arrays with compile-time OIT_LAYERS, so every index is static.
 #include <cuda_fp16.h>
 
+#include "list_walk.cuh"
 #include "oit_device.cuh"
 #include "oit_internal.h"
 
@@ -177,6 +178,23 @@ __device__ __forceinline__ float4 composite_list(const CompositeParams& p, uint3
   return sum;
 }
 
+// Linked list per pixel: register sort arrays for OIT_LAYERS <= 8; beyond,
+// the local-array walk (list_walk.cuh), whose register use does not grow with
+// OIT_LAYERS (register arrays of 16 or 32 entries cost one or two resident
+// blocks per SM on a latency-bound pointer chase).
+template <int L, bool F32>
+__device__ __forceinline__ float4 list_pixel(const CompositeParams& p, uint32_t eaux) {
+  if (L <= 8) return composite_list<L, F32>(p, eaux);
+  const uint4* __restrict__ pool = reinterpret_cast<const uint4*>(p.abuf);
+  const uint32_t head = p.aux[eaux];
+  if (p.coverage) {
+    WalkArrays<true> a;
+    return walk_list<F32, true>(pool, head, p.capacity, L, p.tail, p.S, a);
+  }
+  WalkArrays<false> a;
+  return walk_list<F32, false>(pool, head, p.capacity, L, p.tail, p.S, a);
+}
+
 // Loop32: oitLoop.frag.glsl:191-222.
 __device__ __forceinline__ float4 composite_loop(const CompositeParams& p, size_t abase) {
   int n = 0;
@@ -209,11 +227,7 @@ __device__ __forceinline__ float4 composite_loop64(const CompositeParams& p, siz
 }
 
 __device__ __forceinline__ void write_out(const CompositeParams& p, uint32_t o, float4 c) {
-  const float a = fminf(fmaxf(c.w, 0.0f), 1.0f);
-  const uint32_t ac = (uint32_t)__float2int_rn(a * 255.0f);
-  const uint32_t v = srgb_encode(c.x) | (srgb_encode(c.y) << 8) | (srgb_encode(c.z) << 16) | (ac << 24);
-  reinterpret_cast<uint32_t*>(p.out_rgba8)[o] = v;
-  if (p.out_linear) p.out_linear[o] = c;
+  write_rgba8(p.out_rgba8, p.out_linear, o, c);
 }
 
 enum Kind { kRecords = 0, kList = 1, kLoop = 2, kLoop64 = 3, kListF32 = 4 };
@@ -234,8 +248,7 @@ __global__ void __launch_bounds__(256) k_composite(CompositeParams p) {
         const size_t abase = (size_t)s * (K == kLoop ? 2 : 1) * p.L * p.P + pixel;
         float4 sum;
         if (K == kRecords) sum = composite_records<L>(p, eaux, abase);
-        else if (K == kList) sum = composite_list<L, false>(p, eaux);
-        else if (K == kListF32) sum = composite_list<L, true>(p, eaux);
+        else if (K == kList || K == kListF32) sum = list_pixel<L, K == kListF32>(p, eaux);
         else if (K == kLoop) sum = composite_loop(p, abase);
         else sum = composite_loop64(p, abase);
         // composite output over the colour target (which already holds the

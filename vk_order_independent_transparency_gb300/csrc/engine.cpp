@@ -85,6 +85,7 @@ struct oit_context {
   DevBuf bbox, setup, persp, pair_count, pair_offset, scan_tmp, total;
   DevBuf keys, tris, keys_alt, tris_alt, hist, tile_begin, tile_end;
   DevBuf mesh_v, mesh_i;
+  DevBuf lens;  // per 8x4 micro-tile fragment counts for the batched resolve
   size_t tri_cap = 0, pair_cap = 0;
   bool opaque_valid = false;
   bool color_valid = false;
@@ -155,11 +156,21 @@ struct oit_context {
     }
     DevBuf* all[] = {&depth, &opaque_color, &color, &abuf, &aux, &auxdepth, &counter, &accum, &reveal, &out,
                      &out_linear, &err, &frag, &bbox, &setup, &persp, &pair_count, &pair_offset, &scan_tmp, &total,
-                     &keys, &tris, &keys_alt, &tris_alt, &hist, &tile_begin, &tile_end, &mesh_v, &mesh_i};
+                     &keys, &tris, &keys_alt, &tris_alt, &hist, &tile_begin, &tile_end, &mesh_v, &mesh_i,
+                     &lens};
     for (DevBuf* b : all) b->release();
   }
 
   oit::Alg alg() const { return static_cast<oit::Alg>(st.algorithm); }
+
+  // Views the batched resolve handles: linked list or Loop64, 1x, RGBA8 records.
+  bool batch_resolvable() const {
+    return (alg() == oit::Alg::LinkedList || alg() == oit::Alg::Loop64) && st.record_format == OIT_RECORD_RGBA8 &&
+           S == 1 && ssn == 1 && supersample == 1 && !(st.flags & OIT_FLAG_LINEAR_OUTPUT);
+  }
+  int lens_stride() const { return (RW + 7) / 8; }
+  int lens_rows() const { return (RH + 3) / 4; }
+  size_t lens_count() const { return (size_t)lens_stride() * (size_t)lens_rows(); }
 
   // ---- Sample::createFrameImages (oit.cpp:45-220) ----
   int create() {
@@ -204,6 +215,10 @@ struct oit_context {
     OIT_TRY_CUDA(cudaMemset(err.p, 0, 4), "memset");
     OIT_TRY_CUDA(cudaMemset(frag.p, 0, 8), "memset");
     OIT_TRY_CUDA(cudaMemset(counter.p, 0, 4), "memset");
+    if (batch_resolvable()) {
+      OIT_TRY_CUDA(lens.ensure(lens_count()), "alloc lens");
+      OIT_TRY_CUDA(cudaMemset(lens.p, 0, lens_count()), "memset");
+    }
     return OIT_OK;
   }
 
@@ -242,10 +257,12 @@ struct oit_context {
     return OIT_OK;
   }
 
-  oit::SetupParams setup_params(const oit_mesh* mesh, uint32_t first, uint32_t count, uint32_t opaque_from) {
+  oit::SetupParams setup_params(const oit::MeshRef& mesh, uint32_t first, uint32_t count, uint32_t opaque_from) {
     oit::SetupParams sp{};
-    sp.vertices = mesh->vertices_device;
-    sp.indices = mesh->indices_device;
+    sp.vertices = mesh.vertices;
+    sp.indices = mesh.indices;
+    sp.instances = mesh.instances;
+    sp.template_triangles = mesh.template_triangles;
     sp.first_triangle = first;
     sp.num_triangles = count;
     sp.proj_view = pv;
@@ -303,11 +320,11 @@ struct oit_context {
   // Setup + binning of one draw; afterwards tile_begin/tile_end/tris describe it.
   // Triangles [first, first + opaque_from) are transparent, the rest of the
   // range opaque; one setup, scan and sort bins both kinds.
-  int bin(const oit_mesh* mesh, uint32_t first, uint32_t count, uint32_t opaque_from, cudaStream_t s) {
+  int bin(const oit::MeshRef& mesh, uint32_t first, uint32_t count, uint32_t opaque_from, cudaStream_t s) {
     int r = ensure_triangles(count);
     if (r != OIT_OK) return r;
     const uint64_t key = ((uint64_t)first << 32) ^ ((uint64_t)count << 1) ^ ((uint64_t)opaque_from * 0x9E3779B1ull) ^
-                         ((uint64_t)(uintptr_t)mesh->indices_device << 7);
+                         ((uint64_t)(uintptr_t)mesh.indices << 7) ^ ((uint64_t)(uintptr_t)mesh.instances << 3);
     PairStat* ps = pair_stat(key);
     if (ps && ps->pending && !capturing && cudaEventQuery(ps->ev) == cudaSuccess) {
       ps->known = std::max(ps->known, *ps->host_total);
@@ -386,7 +403,32 @@ struct oit_context {
     p.weighted_fp32 = st.weighted_precision == OIT_WEIGHTED_FP32;
     p.error = err.as<uint32_t>();
     p.frag_count = frag.as<unsigned long long>();
+    if (tile_offset != 0 && batch_resolvable()) {
+      p.lens = lens.as<uint8_t>();
+      p.lens_stride = lens_stride();
+    }
     return p;
+  }
+
+  // The batched resolve's descriptor of this context's current frame.
+  oit::ResolveView resolve_view(uint8_t* out_dev) const {
+    oit::ResolveView v{};
+    v.abuf = abuf.as<uint32_t>();
+    v.aux = aux.as<uint32_t>();
+    v.color = color.as<float4>();
+    v.out = out_dev ? out_dev : out.as<uint8_t>();
+    v.out_linear = nullptr;
+    v.lens = lens.as<uint8_t>();
+    v.P = P;
+    v.capacity = capacity;
+    v.W = RW;
+    v.H = RH;
+    v.L = L;
+    v.kind = alg() == oit::Alg::LinkedList ? oit::kResolveList : oit::kResolveLoop64;
+    v.tail = st.tail_blend ? 1 : 0;
+    v.mtx = lens_stride();
+    v.mty = lens_rows();
+    return v;
   }
 
   int raster(oit::Alg a, oit::RasterParams& p, cudaStream_t s) {
@@ -421,7 +463,7 @@ struct oit_context {
     return OIT_OK;
   }
 
-  int draw_opaque(const oit_mesh* mesh, uint32_t first, uint32_t count, cudaStream_t s) {
+  int draw_opaque(const oit::MeshRef& mesh, uint32_t first, uint32_t count, cudaStream_t s) {
     last_stream = s;
     int r = clear_opaque_targets(s);
     if (r != OIT_OK) return r;
@@ -464,7 +506,7 @@ struct oit_context {
     return r;
   }
 
-  int draw_transparent_color(const oit_mesh* mesh, uint32_t first, uint32_t count, cudaStream_t s) {
+  int draw_transparent_color(const oit::MeshRef& mesh, uint32_t first, uint32_t count, cudaStream_t s) {
     last_stream = s;
     cudaEvent_t t0 = prof_begin(s);
     int r = bin(mesh, first, count, count, s);
@@ -515,8 +557,9 @@ struct oit_context {
   // Sample::onRender, oitRender.cpp:43-153. The transparent objects are the
   // first percent_transparent% of the mesh and the opaque ones the rest, so one
   // binning pass serves both the opaque and the transparent raster.
-  int render_frame_body(const oit_mesh* mesh, uint32_t tpo, int32_t percent, uint8_t* out_dev, cudaStream_t s) {
-    const uint32_t num_objects = mesh->num_triangles / tpo;
+  int render_frame_body(const oit::MeshRef& mesh, uint32_t tpo, int32_t percent, uint8_t* out_dev, cudaStream_t s,
+                        bool resolve = true) {
+    const uint32_t num_objects = mesh.num_triangles / tpo;
     uint32_t num_transparent = (uint32_t)(((uint64_t)num_objects * (uint32_t)percent) / 100u);
     if (num_transparent > num_objects) num_transparent = num_objects;
     const uint32_t num_opaque = num_objects - num_transparent;
@@ -531,7 +574,7 @@ struct oit_context {
     prof_end(OIT_PROF_TRANSPARENT_BIN, t0, s);
     if (num_opaque > 0) r = raster_opaque(s);
     if (r == OIT_OK) r = raster_transparent(s);
-    if (r == OIT_OK) r = composite(out_dev, s);
+    if (r == OIT_OK && resolve) r = composite(out_dev, s);
     return r;
   }
 
@@ -590,14 +633,14 @@ struct oit_context {
     return OIT_OK;
   }
 
-  int render_frame(const oit_mesh* mesh, uint32_t tpo, int32_t percent, uint8_t* out_dev, cudaStream_t s) {
-    if (!mesh || !tpo || percent < 0) return OIT_ERR_INVALID_ARGUMENT;
+  int render_frame(const oit::MeshRef& mesh, uint32_t tpo, int32_t percent, uint8_t* out_dev, cudaStream_t s) {
+    if (!tpo || percent < 0) return OIT_ERR_INVALID_ARGUMENT;
     last_stream = s;
     if (!(st.flags & OIT_FLAG_CUDA_GRAPH) || prof_on) return render_frame_body(mesh, tpo, percent, out_dev, s);
     uint64_t sig = 1469598103934665603ull;
-    const uint64_t parts[] = {(uint64_t)(uintptr_t)mesh->vertices_device, (uint64_t)(uintptr_t)mesh->indices_device,
-                              mesh->num_triangles, tpo, (uint64_t)percent, (uint64_t)(uintptr_t)out_dev,
-                              (uint64_t)(uintptr_t)s};
+    const uint64_t parts[] = {(uint64_t)(uintptr_t)mesh.vertices, (uint64_t)(uintptr_t)mesh.indices,
+                              (uint64_t)(uintptr_t)mesh.instances, mesh.num_triangles, tpo, (uint64_t)percent,
+                              (uint64_t)(uintptr_t)out_dev, (uint64_t)(uintptr_t)s};
     for (uint64_t v : parts) sig = (sig ^ v) * 1099511628211ull;
     // bins that outgrew their capacity since the capture invalidate the graph
     if (!graph_bins_fit()) drop_graph();
@@ -660,6 +703,22 @@ struct oit_batch {
   std::vector<oit_context*> ctxs;
   std::vector<bool> opaque_valid;
 
+  // Batched resolve of the views that allow it (oit_context::batch_resolvable),
+  // in two parts, linked-list views and Loop64 views, each with its view
+  // descriptors, binned work list and the launch shape picked by timing
+  // candidates on the batch's own frames; the parts run side by side.
+  struct ResolvePart {
+    DevBuf views, base, hist, items;
+    oit::ResolveBatch rb{};
+    int variant = 0, threads = 128, blocks = 0;
+    bool binned = false;
+  };
+  ResolvePart rparts[2];
+  uint64_t rsig = 0;
+  bool r_tuned = false;
+  int num_sms = 0;
+  cudaEvent_t rfork = nullptr, rjoin[2] = {nullptr, nullptr};
+
   void drop() {
     if (exec) cudaGraphExecDestroy(exec);
     exec = nullptr;
@@ -667,6 +726,14 @@ struct oit_batch {
   }
   ~oit_batch() {
     drop();
+    for (ResolvePart& rp : rparts) {
+      rp.views.release();
+      rp.base.release();
+      rp.hist.release();
+      rp.items.release();
+    }
+    for (cudaEvent_t e : {rfork, rjoin[0], rjoin[1]})
+      if (e) cudaEventDestroy(e);
     for (cudaStream_t l : lanes) cudaStreamDestroy(l);
     for (cudaEvent_t e : joins) cudaEventDestroy(e);
     if (fork) cudaEventDestroy(fork);
@@ -713,6 +780,154 @@ int validate(const oit_state* s, int* msaa, int* ss, int* sup) {
     if (s->algorithm == OIT_LOOP64 && s->oit_layers > 16) return OIT_ERR_UNSUPPORTED;
   }
   return OIT_OK;
+}
+
+// Descriptors of the batch's resolvable views, rebuilt when the set of views
+// (contexts and outputs) changes. Synchronous: never called under capture.
+int batch_prepare_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n) {
+  uint64_t sig = 1469598103934665603ull;
+  uint32_t count = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!views[i].ctx->batch_resolvable()) continue;
+    ++count;
+    for (uint64_t x : {(uint64_t)(uintptr_t)views[i].ctx, (uint64_t)(uintptr_t)views[i].out_rgba8_device})
+      sig = (sig ^ x) * 1099511628211ull;
+  }
+  sig ^= count;
+  if (sig == b->rsig) return OIT_OK;
+  b->rsig = 0;
+  b->r_tuned = false;
+  if (b->num_sms == 0) OIT_TRY_CUDA(cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, 0), "attr");
+  for (int part = 0; part < 2; ++part) {
+    const int kind = part == 0 ? oit::kResolveList : oit::kResolveLoop64;
+    std::vector<oit::ResolveView> hv;
+    std::vector<uint32_t> base;
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+      oit_context* c = views[i].ctx;
+      if (!c->batch_resolvable()) continue;
+      oit::ResolveView v = c->resolve_view(views[i].out_rgba8_device);
+      if (v.kind != kind) continue;
+      v.tile_base = (uint32_t)total;
+      total += c->lens_count();
+      hv.push_back(v);
+      base.push_back(v.tile_base);
+    }
+    if (hv.size() > (size_t)oit::kResolveMaxViews || total > 0xFFFFFFFFull) return OIT_ERR_INVALID_ARGUMENT;
+    oit_batch::ResolvePart& rp = b->rparts[part];
+    OIT_TRY_CUDA(rp.views.ensure(hv.size() * sizeof(oit::ResolveView)), "alloc resolve");
+    OIT_TRY_CUDA(rp.base.ensure(base.size() * 4), "alloc resolve");
+    OIT_TRY_CUDA(rp.hist.ensure(2 * oit::kResolveBuckets * 4), "alloc resolve");
+    OIT_TRY_CUDA(rp.items.ensure(total * 4), "alloc resolve");
+    if (!hv.empty()) {
+      OIT_TRY_CUDA(cudaMemcpy(rp.views.p, hv.data(), hv.size() * sizeof(oit::ResolveView), cudaMemcpyHostToDevice),
+                   "h2d");
+      OIT_TRY_CUDA(cudaMemcpy(rp.base.p, base.data(), base.size() * 4, cudaMemcpyHostToDevice), "h2d");
+    }
+    oit::ResolveBatch& rb = rp.rb;
+    rb.views = rp.views.as<oit::ResolveView>();
+    rb.tile_base = rp.base.as<uint32_t>();
+    rb.num_views = (int)hv.size();
+    rb.total_tiles = (uint32_t)total;
+    rb.hist = rp.hist.as<uint32_t>();
+    rb.fill = rb.hist + oit::kResolveBuckets;
+    rb.items = rp.items.as<uint32_t>();
+    rp.variant = part == 0 ? oit::kResolveVariantList0 : oit::kResolveVariantLoop64;
+  }
+  b->rsig = sig;
+  return OIT_OK;
+}
+
+int part_launch(const oit_batch::ResolvePart& rp, cudaStream_t s, int variant, bool binned, int threads, int blocks,
+                uint64_t* launches) {
+  oit::ResolveBatch rb = rp.rb;
+  if (rb.num_views == 0) return OIT_OK;
+  if (!binned) rb.items = nullptr;
+  OIT_TRY_CUDA(oit::resolve_bin(rb, s, launches), "resolve bin");
+  OIT_TRY_CUDA(oit::resolve_run(rb, variant, threads, blocks, s), "resolve");
+  ++*launches;
+  return OIT_OK;
+}
+
+// Both parts with their tuned shapes, side by side on two of the batch's
+// streams, ordered after and before `s`.
+int batch_resolve_launch(oit_batch* b, cudaStream_t s, uint64_t* launches) {
+  const bool two = b->rparts[0].rb.num_views > 0 && b->rparts[1].rb.num_views > 0 && b->lanes.size() >= 2;
+  if (!two) {
+    for (const oit_batch::ResolvePart& rp : b->rparts) {
+      const int r = part_launch(rp, s, rp.variant, rp.binned, rp.threads, rp.blocks, launches);
+      if (r != OIT_OK) return r;
+    }
+    return OIT_OK;
+  }
+  OIT_TRY_CUDA(cudaEventRecord(b->rfork, s), "event");
+  for (int k = 0; k < 2; ++k) {
+    const oit_batch::ResolvePart& rp = b->rparts[k];
+    OIT_TRY_CUDA(cudaStreamWaitEvent(b->lanes[k], b->rfork, 0), "wait");
+    const int r = part_launch(rp, b->lanes[k], rp.variant, rp.binned, rp.threads, rp.blocks, launches);
+    if (r != OIT_OK) return r;
+    OIT_TRY_CUDA(cudaEventRecord(b->rjoin[k], b->lanes[k]), "event");
+    OIT_TRY_CUDA(cudaStreamWaitEvent(s, b->rjoin[k], 0), "wait");
+  }
+  return OIT_OK;
+}
+
+// The autotuner, per part: kernel variant (linked lists: 0, 4 or 8 register
+// slots for the first sort entries), block size and binned versus view-order
+// work lists, each timed with CUDA events on the batch's current frames (the
+// resolve only writes the outputs, so reruns are harmless); the grid holds
+// every block that fits. The fastest shape is kept for the batch's views.
+int batch_autotune(oit_batch* b, cudaStream_t s) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  OIT_TRY_CUDA(cudaEventCreate(&e0), "event");
+  OIT_TRY_CUDA(cudaEventCreate(&e1), "event");
+  int r = OIT_OK;
+  uint64_t scratch = 0;
+  for (int part = 0; part < 2 && r == OIT_OK; ++part) {
+    oit_batch::ResolvePart& rp = b->rparts[part];
+    if (rp.rb.num_views == 0) continue;
+    float best = 1e30f;
+    std::vector<int> variants;
+    if (part == 0) variants = {oit::kResolveVariantList0, oit::kResolveVariantList4, oit::kResolveVariantList8};
+    else variants = {oit::kResolveVariantLoop64};
+    for (int variant : variants) {
+      for (int threads : {64, 128, 256}) {
+        const int bps = oit::resolve_blocks_per_sm(rp.rb, variant, threads);
+        if (bps <= 0) continue;
+        const int blocks = bps * b->num_sms;
+        for (bool binned : {true, false}) {
+          r = part_launch(rp, s, variant, binned, threads, blocks, &scratch);  // warm-up
+          if (r != OIT_OK) break;
+          cudaEventRecord(e0, s);
+          for (int k = 0; k < 3 && r == OIT_OK; ++k) r = part_launch(rp, s, variant, binned, threads, blocks, &scratch);
+          cudaEventRecord(e1, s);
+          if (r != OIT_OK) break;
+          if (cudaEventSynchronize(e1) != cudaSuccess) {
+            r = OIT_ERR_CUDA;
+            break;
+          }
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          if (ms < best) {
+            best = ms;
+            rp.variant = variant;
+            rp.threads = threads;
+            rp.blocks = blocks;
+            rp.binned = binned;
+          }
+        }
+        if (r != OIT_OK) break;
+      }
+      if (r != OIT_OK) break;
+    }
+    if (r == OIT_OK && best >= 1e30f) r = OIT_ERR_UNSUPPORTED;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (r != OIT_OK) return r;
+  b->r_tuned = true;
+  // leave the outputs written by the chosen shapes
+  return batch_resolve_launch(b, s, &scratch);
 }
 
 }  // namespace
@@ -820,16 +1035,34 @@ static bool mesh_ok(const oit_mesh* m, uint32_t first, uint32_t count) {
   return (uint64_t)first + count <= m->num_triangles;
 }
 
+static oit::MeshRef mesh_ref(const oit_mesh* m) {
+  return oit::MeshRef{m->vertices_device, m->indices_device, nullptr, m->num_triangles, 0};
+}
+
+// Template and instance table present, instance table 16-byte aligned (it is
+// read as float4), frame triangle count within 32 bits.
+static bool instanced_ok(const oit_instanced_mesh* m) {
+  if (!m || !m->template_vertices_device || !m->template_indices_device || !m->instances_device) return false;
+  if (!m->template_vertices || !m->template_triangles || !m->num_instances) return false;
+  if ((uintptr_t)m->instances_device % 16 != 0) return false;
+  return (uint64_t)m->template_triangles * m->num_instances <= 0xFFFFFFFFull / 3;
+}
+
+static oit::MeshRef instanced_ref(const oit_instanced_mesh* m) {
+  return oit::MeshRef{m->template_vertices_device, m->template_indices_device, m->instances_device,
+                      m->template_triangles * m->num_instances, m->template_triangles};
+}
+
 int oit_draw_opaque(oit_context* ctx, const oit_mesh* mesh, uint32_t first, uint32_t count, void* stream) {
   if (!ctx || !mesh_ok(mesh, first, count)) return OIT_ERR_INVALID_ARGUMENT;
   if (!ctx->has_scene) return OIT_ERR_STATE;
-  return ctx->draw_opaque(mesh, first, count, static_cast<cudaStream_t>(stream));
+  return ctx->draw_opaque(mesh_ref(mesh), first, count, static_cast<cudaStream_t>(stream));
 }
 
 int oit_draw_transparent_color(oit_context* ctx, const oit_mesh* mesh, uint32_t first, uint32_t count, void* stream) {
   if (!ctx || !mesh_ok(mesh, first, count)) return OIT_ERR_INVALID_ARGUMENT;
   if (!ctx->has_scene) return OIT_ERR_STATE;
-  return ctx->draw_transparent_color(mesh, first, count, static_cast<cudaStream_t>(stream));
+  return ctx->draw_transparent_color(mesh_ref(mesh), first, count, static_cast<cudaStream_t>(stream));
 }
 
 int oit_composite(oit_context* ctx, uint8_t* out, void* stream) {
@@ -848,7 +1081,7 @@ int oit_render_frame(oit_context* ctx, const oit_mesh* mesh, uint32_t tpo, int32
   if (!ctx || !mesh) return OIT_ERR_INVALID_ARGUMENT;
   if (!ctx->has_scene) return OIT_ERR_STATE;
   if (!mesh_ok(mesh, 0, mesh->num_triangles)) return OIT_ERR_INVALID_ARGUMENT;
-  return ctx->render_frame(mesh, tpo, percent, out, static_cast<cudaStream_t>(stream));
+  return ctx->render_frame(mesh_ref(mesh), tpo, percent, out, static_cast<cudaStream_t>(stream));
 }
 
 int oit_render_frame_host(oit_context* ctx, const float* vertices, uint32_t num_vertices, const uint32_t* indices,
@@ -862,7 +1095,42 @@ int oit_render_frame_host(oit_context* ctx, const float* vertices, uint32_t num_
   OIT_TRY_CUDA(cudaMemcpyAsync(ctx->mesh_v.p, vertices, vb, cudaMemcpyHostToDevice, s), "h2d");
   OIT_TRY_CUDA(cudaMemcpyAsync(ctx->mesh_i.p, indices, ib, cudaMemcpyHostToDevice, s), "h2d");
   oit_mesh m{ctx->mesh_v.as<float>(), ctx->mesh_i.as<uint32_t>(), num_vertices, num_triangles};
-  int r = ctx->render_frame(&m, tpo, percent, nullptr, s);
+  int r = ctx->render_frame(mesh_ref(&m), tpo, percent, nullptr, s);
+  if (r != OIT_OK) return r;
+  OIT_TRY_CUDA(cudaMemcpyAsync(out_host, ctx->out.p, (size_t)ctx->W * ctx->H * 4, cudaMemcpyDeviceToHost, s), "d2h");
+  OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
+  return OIT_OK;
+}
+
+int oit_render_frame_instanced(oit_context* ctx, const oit_instanced_mesh* mesh, int32_t percent, uint8_t* out,
+                               void* stream) {
+  if (!ctx || !instanced_ok(mesh)) return OIT_ERR_INVALID_ARGUMENT;
+  if (!ctx->has_scene) return OIT_ERR_STATE;
+  return ctx->render_frame(instanced_ref(mesh), mesh->template_triangles, percent, out, static_cast<cudaStream_t>(stream));
+}
+
+int oit_render_frame_instanced_host(oit_context* ctx, const float* template_vertices, uint32_t num_template_vertices,
+                                    const uint32_t* template_indices, uint32_t num_template_triangles,
+                                    const float* instances, uint32_t num_instances, int32_t percent,
+                                    uint8_t* out_host, void* stream) {
+  if (!ctx || !template_vertices || !template_indices || !instances || !out_host) return OIT_ERR_INVALID_ARGUMENT;
+  if (!ctx->has_scene) return OIT_ERR_STATE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // one device buffer: template vertices, instances (16-byte aligned), indices
+  const size_t vb = (size_t)num_template_vertices * 24, nb = (size_t)num_instances * 32;
+  const size_t ib = (size_t)num_template_triangles * 12;
+  const size_t v_pad = (vb + 255) & ~(size_t)255;
+  OIT_TRY_CUDA(ctx->mesh_v.ensure(v_pad + nb), "alloc mesh");
+  OIT_TRY_CUDA(ctx->mesh_i.ensure(ib), "alloc mesh");
+  oit_instanced_mesh m{ctx->mesh_v.as<float>(), ctx->mesh_i.as<uint32_t>(),
+                       reinterpret_cast<const float*>(static_cast<char*>(ctx->mesh_v.p) + v_pad),
+                       num_template_vertices, num_template_triangles, num_instances};
+  if (!instanced_ok(&m)) return OIT_ERR_INVALID_ARGUMENT;
+  OIT_TRY_CUDA(cudaMemcpyAsync(ctx->mesh_v.p, template_vertices, vb, cudaMemcpyHostToDevice, s), "h2d");
+  OIT_TRY_CUDA(cudaMemcpyAsync(static_cast<char*>(ctx->mesh_v.p) + v_pad, instances, nb, cudaMemcpyHostToDevice, s),
+               "h2d");
+  OIT_TRY_CUDA(cudaMemcpyAsync(ctx->mesh_i.p, template_indices, ib, cudaMemcpyHostToDevice, s), "h2d");
+  int r = ctx->render_frame(instanced_ref(&m), num_template_triangles, percent, nullptr, s);
   if (r != OIT_OK) return r;
   OIT_TRY_CUDA(cudaMemcpyAsync(out_host, ctx->out.p, (size_t)ctx->W * ctx->H * 4, cudaMemcpyDeviceToHost, s), "d2h");
   OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
@@ -889,7 +1157,7 @@ int oit_batch_create(uint32_t parallel_streams, oit_batch** out) {
     if ((e = cudaEventCreateWithFlags(&j, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
     b->joins.push_back(j);
   }
-  for (cudaEvent_t* ev : {&b->fork, &b->in, &b->out})
+  for (cudaEvent_t* ev : {&b->fork, &b->in, &b->out, &b->rfork, &b->rjoin[0], &b->rjoin[1]})
     if ((e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   *out = b;
   return OIT_OK;
@@ -930,12 +1198,19 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
   for (uint32_t i = 0; i < n; ++i) fit = views[i].ctx->graph_bins_fit() && fit;
   if (!fit || sig != b->sig) b->drop();
   if (!b->exec) {
-    // plain frames, one view after the other, size every buffer
+    // plain frames, one view after the other, size every buffer; views the
+    // batched resolve handles are resolved together afterwards
     for (uint32_t i = 0; i < n; ++i) {
       const oit_view_frame& v = views[i];
-      int r = v.ctx->render_frame_body(v.mesh, v.triangles_per_object, v.percent_transparent, v.out_rgba8_device, s);
+      int r = v.ctx->render_frame_body(mesh_ref(v.mesh), v.triangles_per_object, v.percent_transparent,
+                                       v.out_rgba8_device, s, !v.ctx->batch_resolvable());
       if (r != OIT_OK) return r;
     }
+    int pr = batch_prepare_resolve(b, views, n);
+    if (pr != OIT_OK) return pr;
+    uint64_t scratch = 0;
+    pr = b->r_tuned ? batch_resolve_launch(b, s, &scratch) : batch_autotune(b, s);
+    if (pr != OIT_OK) return pr;
     OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
     OIT_TRY_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed), "capture");
     int r = OIT_OK;
@@ -951,8 +1226,8 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
       const uint64_t l0 = c->launches;
       c->graph_stats.clear();
       c->capturing = true;
-      r = c->render_frame_body(v.mesh, v.triangles_per_object, v.percent_transparent, v.out_rgba8_device,
-                               b->lanes[i % K]);
+      r = c->render_frame_body(mesh_ref(v.mesh), v.triangles_per_object, v.percent_transparent, v.out_rgba8_device,
+                               b->lanes[i % K], !c->batch_resolvable());
       c->capturing = false;
       nodes += c->launches - l0;
       c->launches = l0;
@@ -964,6 +1239,7 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
       e = cudaEventRecord(b->joins[k], b->lanes[k]);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->joins[k], 0);
     }
+    if (e == cudaSuccess && r == OIT_OK) r = batch_resolve_launch(b, b->stream, &nodes);
     cudaGraph_t g = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
     if (r != OIT_OK || e != cudaSuccess || ce != cudaSuccess) {
@@ -992,6 +1268,42 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
     c->color_valid = true;
     c->last_stream = s;
   }
+  return OIT_OK;
+}
+
+int oit_batch_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n, void* stream) {
+  if (!b || !views || n == 0) return OIT_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!views[i].ctx) return OIT_ERR_INVALID_ARGUMENT;
+    if (!views[i].ctx->color_valid) return OIT_ERR_STATE;
+    for (uint32_t j = 0; j < i; ++j)
+      if (views[j].ctx == views[i].ctx) return OIT_ERR_INVALID_ARGUMENT;
+  }
+  int r = batch_prepare_resolve(b, views, n);
+  if (r != OIT_OK) return r;
+  for (uint32_t i = 0; i < n; ++i) {
+    oit_context* c = views[i].ctx;
+    if (c->batch_resolvable()) continue;
+    r = c->composite(views[i].out_rgba8_device, s);
+    if (r != OIT_OK) return r;
+  }
+  uint64_t launches = 0;
+  r = b->r_tuned ? batch_resolve_launch(b, s, &launches) : batch_autotune(b, s);
+  for (uint32_t i = 0; i < n; ++i) views[i].ctx->last_stream = s;
+  return r;
+}
+
+int oit_batch_resolve_config(oit_batch* b, uint32_t part, uint32_t* threads_per_block, uint32_t* blocks,
+                             int32_t* binned, int32_t* register_slots) {
+  if (!b || part > 1 || !threads_per_block || !blocks || !binned || !register_slots) return OIT_ERR_INVALID_ARGUMENT;
+  if (!b->r_tuned) return OIT_ERR_STATE;
+  const oit_batch::ResolvePart& rp = b->rparts[part];
+  const bool any = rp.rb.num_views > 0;
+  *threads_per_block = any ? (uint32_t)rp.threads : 0u;
+  *blocks = any ? (uint32_t)rp.blocks : 0u;
+  *binned = any && rp.binned ? 1 : 0;
+  *register_slots = rp.variant == oit::kResolveVariantList4 ? 4 : (rp.variant == oit::kResolveVariantList8 ? 8 : 0);
   return OIT_OK;
 }
 

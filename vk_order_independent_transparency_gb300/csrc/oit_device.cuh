@@ -182,4 +182,14 @@ __device__ __forceinline__ void rop_over(float4& dst, const float4& src) {
 
 __device__ __forceinline__ void set_error(uint32_t* err, uint32_t bits) { atomicOr(err, bits); }
 
+// Resolved premultiplied colour to the RGBA8 sRGB output (alpha stays
+// linear), plus the optional linear copy.
+__device__ __forceinline__ void write_rgba8(uint8_t* out8, float4* out_linear, uint32_t o, float4 c) {
+  const float a = fminf(fmaxf(c.w, 0.0f), 1.0f);
+  const uint32_t ac = (uint32_t)__float2int_rn(a * 255.0f);
+  const uint32_t v = srgb_encode(c.x) | (srgb_encode(c.y) << 8) | (srgb_encode(c.z) << 16) | (ac << 24);
+  reinterpret_cast<uint32_t*>(out8)[o] = v;
+  if (out_linear) out_linear[o] = c;
+}
+
 }  // namespace oitd

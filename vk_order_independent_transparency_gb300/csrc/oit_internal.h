@@ -18,8 +18,10 @@ struct Mat4 {
 
 // Triangle setup: transform, cull, snap, bbox, interpolation constants.
 struct SetupParams {
-  const float* vertices;
-  const uint32_t* indices;
+  const float* vertices;    // 10 floats per vertex; with instances: template vertices, 6 floats (pos, normal)
+  const uint32_t* indices;  // 3 per triangle; with instances: the template's triangles
+  const float* instances;   // null, or 8 floats per instance: centre.xyz, radius, color.rgba
+  uint32_t template_triangles;  // triangles per instance
   uint32_t first_triangle;
   uint32_t num_triangles;
   Mat4 proj_view;
@@ -35,6 +37,16 @@ struct SetupParams {
   void* setup;            // [num_triangles] TriSetup records (96 B)
   void* persp;            // [num_triangles] TriPersp records (32 B, WBOIT only) or null
   uint32_t* pair_count;   // [num_triangles] tiles overlapped (0 = culled)
+};
+
+// The engine's view of a frame's geometry: a flattened triangle mesh
+// (oit_mesh) or one template drawn per instance (oit_instanced_mesh).
+struct MeshRef {
+  const float* vertices;
+  const uint32_t* indices;
+  const float* instances;       // null for a flattened mesh
+  uint32_t num_triangles;       // triangles of the frame
+  uint32_t template_triangles;  // instanced: triangles per instance
 };
 
 // Tile bins of one draw: triangles sorted by tile, primitive order kept.
@@ -100,6 +112,11 @@ struct RasterParams {
   int weighted_fp32;
   uint32_t* error;
   unsigned long long* frag_count;
+  // per 8x4 micro-tile: the most fragments any of its pixels received (capped
+  // at 255), written by the transparent raster for the batched resolve's
+  // work binning; null = not wanted (1x only)
+  uint8_t* lens;
+  int lens_stride;               // micro-tiles per row, (RW + 7) / 8
 };
 
 struct CompositeParams {
@@ -127,6 +144,33 @@ struct CompositeParams {
   float4* out_linear;            // optional [W*H]
 };
 
+// One view of the batched resolve (linked list or Loop64, 1x, RGBA8 records).
+enum ResolveKind : int { kResolveList = 0, kResolveLoop64 = 1 };
+struct ResolveView {
+  const uint32_t* abuf;          // node pool (list) or keys [L][P] (Loop64)
+  const uint32_t* aux;           // list heads [P]
+  const float4* color;           // [P] colour target after tail blend
+  uint8_t* out;                  // [P] RGBA8
+  float4* out_linear;            // optional [P]
+  const uint8_t* lens;           // [mty][mtx] per 8x4 micro-tile fragment counts
+  uint32_t P, capacity;
+  int W, H, L, kind, tail, mtx, mty;
+  uint32_t tile_base;            // first global micro-tile index of this view
+};
+
+constexpr int kResolveBuckets = 8;
+constexpr int kResolveMaxViews = 4096;
+
+struct ResolveBatch {
+  const ResolveView* views;      // [num_views] (device)
+  const uint32_t* tile_base;     // [num_views] (device) copy of views[i].tile_base
+  int num_views;
+  uint32_t total_tiles;          // micro-tiles over all views
+  uint32_t* hist;                // [kResolveBuckets] (device)
+  uint32_t* fill;                // [kResolveBuckets] (device)
+  uint32_t* items;               // [total_tiles] work list, costliest bucket first; null = view order
+};
+
 // ---- launch wrappers (defined in the .cu files) -------------------------
 cudaError_t bin_setup_scan(const SetupParams& sp, Bins& b, cudaStream_t s, uint64_t* launches);
 cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles, uint32_t* error, cudaStream_t s,
@@ -136,6 +180,20 @@ cudaError_t launch_raster_a(Alg alg, const RasterParams& p, cudaStream_t s);  //
 cudaError_t launch_raster_b(Alg alg, const RasterParams& p, cudaStream_t s);  // Loop, Loop64
 cudaError_t launch_raster_c(Alg alg, const RasterParams& p, cudaStream_t s);  // Spinlock, Interlock, Weighted
 cudaError_t launch_composite(Alg alg, const CompositeParams& p, cudaStream_t s);
+// Batched resolve: bin the micro-tiles of every view by cost (costliest
+// first), then one persistent launch resolves them all.
+// Kernel variants: Loop64 views, or linked-list views with 0, 4 or 8 register
+// slots for the first sort entries (the rest in local memory).
+enum ResolveVariant : int {
+  kResolveVariantLoop64 = 0,
+  kResolveVariantList0 = 1,
+  kResolveVariantList4 = 2,
+  kResolveVariantList8 = 3,
+};
+cudaError_t resolve_bin(const ResolveBatch& b, cudaStream_t s, uint64_t* launches);
+cudaError_t resolve_run(const ResolveBatch& b, int variant, int threads, int blocks, cudaStream_t s);
+// Resident blocks per SM of a resolve variant for a block size (0 on error).
+int resolve_blocks_per_sm(const ResolveBatch& b, int variant, int threads);
 cudaError_t launch_fill_u32(uint32_t* dst, uint32_t value, size_t count, cudaStream_t s);
 cudaError_t launch_fill_f4(float4* dst, float4 value, size_t count, cudaStream_t s);
 size_t scan_scratch_words(size_t n);

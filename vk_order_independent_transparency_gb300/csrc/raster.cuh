@@ -576,6 +576,7 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
   const TriPersp* __restrict__ persp = reinterpret_cast<const TriPersp*>(p.persp);
   const uint32_t lt = (1u << w.lane) - 1u;
   uint32_t nfrag = 0;  // warp-uniform
+  uint32_t mine = 0;   // fragments delivered to this lane's pixel
   int qn = 0;          // warp-uniform
   const uint32_t lane_bytes = (uint32_t)w.lane * 0x01010101u;
 
@@ -620,6 +621,7 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
         mm |= (unsigned long long)bits << (4 * wi);
       }
       if (qn < 64) mm &= (1ull << qn) - 1ull;
+      if (shading) mine += (uint32_t)__popcll(mm);
       while (mm) {
         const int j = __ffsll((long long)mm) - 1;
         mm &= mm - 1;
@@ -797,6 +799,12 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
     p.color[elem] = make_float4(c.x * k, c.y * k, c.z * k, c.w * k);
   }
   if (w.lane == 0 && nfrag && p.frag_count) atomicAdd(p.frag_count, (unsigned long long)nfrag);
+  if (SSN == 1 && p.lens) {
+    const uint32_t mx = __reduce_max_sync(kFull, w.valid ? mine : 0u);
+    // micro-tiles of edge tiles may lie wholly outside the image
+    if (w.lane == 0 && w.rx0 < p.RW && w.ry0 < p.RH)
+      p.lens[(size_t)(w.ry0 >> 2) * p.lens_stride + (w.rx0 >> 3)] = (uint8_t)min(mx, 255u);
+  }
 }
 
 // ---------------------------------------------------------------------------

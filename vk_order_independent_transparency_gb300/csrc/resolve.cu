@@ -1,0 +1,253 @@
+// Batched resolve: the COMPOSITE pass of many views (linked list and Loop64,
+// 1x, RGBA8 records) in one persistent launch.
+//
+//   k_rbin_count / k_rbin_scatter  counting sort of every view's 8x4
+//                                  micro-tiles into cost buckets, costliest
+//                                  bucket first. The cost of a micro-tile is
+//                                  the most fragments any of its pixels
+//                                  received (the transparent raster writes
+//                                  it), i.e. the longest list its warp walks.
+//   k_resolve_list<K> /            persistent: every warp resolves micro-tiles
+//   k_resolve_loop64               (one lane per pixel) of one view kind from
+//                                  the work list in a static cyclic order;
+//                                  K = register slots for the first sort
+//                                  entries of a list (0, 4 or 8: the
+//                                  autotuner picks).
+//
+// Per pixel the result equals the per-view composite (composite.cu): the
+// linked list's kept entries are the first OIT_LAYERS nodes in list order,
+// ordered as bubbleSort orders them (oitCompositeDefines.glsl:51-89), the
+// rest go through insertionSortTail (:94-139) and are tail blended in
+// eviction order. Here the kept entries are sorted on insertion in a per-
+// thread local array; bubbleSort's swap-on-equal makes its order of equal
+// depths depend on the passes, so a pixel with equal depths among its first
+// OIT_LAYERS nodes re-reads them and runs bubbleSort itself.
+#include "list_walk.cuh"
+#include "oit_device.cuh"
+#include "oit_internal.h"
+
+namespace oit {
+using namespace oitd;
+
+namespace {
+
+constexpr int kBinThreads = 256;
+constexpr int kBinPerThread = 16;
+constexpr int kBinChunk = kBinThreads * kBinPerThread;
+constexpr uint32_t kEmptyKey = 0xFFFFFFFFu;
+
+// the view holding global micro-tile g: the last view whose base is <= g
+__device__ __forceinline__ int find_view(const uint32_t* tb, int n, uint32_t g) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tb[mid] <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Cost bucket of a micro-tile: 0 for no node reads, else 1 + floor(log2(cost)),
+// at most kResolveBuckets - 1. A list pixel reads one node per fragment; a
+// Loop64 pixel reads its kept keys plus the terminating empty key.
+__device__ __forceinline__ int tile_bucket(const ResolveView* __restrict__ views, const uint32_t* tb, int nv,
+                                           uint32_t g) {
+  const int v = find_view(tb, nv, g);
+  const uint32_t len = __ldg(views[v].lens + (g - tb[v]));
+  const int L = views[v].L;
+  const uint32_t cost = views[v].kind == kResolveList ? len : min(len, (uint32_t)L) + (len < (uint32_t)L ? 1u : 0u);
+  if (cost == 0) return 0;
+  return min(32 - __clz(cost), kResolveBuckets - 1);
+}
+
+__device__ __forceinline__ void load_bases(const ResolveBatch& b, uint32_t* tb) {
+  for (int i = threadIdx.x; i < b.num_views; i += blockDim.x) tb[i] = b.tile_base[i];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kBinThreads) k_rbin_count(ResolveBatch b) {
+  __shared__ uint32_t tb[kResolveMaxViews];
+  __shared__ uint32_t cnt[kResolveBuckets];
+  if (threadIdx.x < kResolveBuckets) cnt[threadIdx.x] = 0;
+  load_bases(b, tb);
+  const uint32_t lane = threadIdx.x & 31;
+  for (int i = 0; i < kBinPerThread; ++i) {
+    const uint32_t g = blockIdx.x * kBinChunk + i * kBinThreads + threadIdx.x;
+    const int bk = g < b.total_tiles ? tile_bucket(b.views, tb, b.num_views, g) : -1;
+    const uint32_t peers = __match_any_sync(0xffffffffu, bk);
+    if (bk >= 0 && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&cnt[bk], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  if (threadIdx.x < kResolveBuckets && cnt[threadIdx.x]) atomicAdd(&b.hist[threadIdx.x], cnt[threadIdx.x]);
+}
+
+__global__ void __launch_bounds__(kBinThreads) k_rbin_scatter(ResolveBatch b) {
+  __shared__ uint32_t tb[kResolveMaxViews];
+  __shared__ uint32_t cnt[kResolveBuckets];
+  __shared__ uint32_t base[kResolveBuckets];
+  if (threadIdx.x < kResolveBuckets) cnt[threadIdx.x] = 0;
+  load_bases(b, tb);
+  const uint32_t lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
+  int bk[kBinPerThread];
+  uint32_t rank[kBinPerThread];
+#pragma unroll
+  for (int i = 0; i < kBinPerThread; ++i) {
+    const uint32_t g = blockIdx.x * kBinChunk + i * kBinThreads + threadIdx.x;
+    bk[i] = g < b.total_tiles ? tile_bucket(b.views, tb, b.num_views, g) : -1;
+    const uint32_t peers = __match_any_sync(0xffffffffu, bk[i]);
+    const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+    uint32_t r = 0;
+    if (bk[i] >= 0 && lane == leader) r = atomicAdd(&cnt[bk[i]], (uint32_t)__popc(peers));
+    r = __shfl_sync(0xffffffffu, r, (int)leader);
+    rank[i] = r + (uint32_t)__popc(peers & lt);
+  }
+  __syncthreads();
+  if (threadIdx.x < kResolveBuckets) {
+    // buckets are laid out costliest first
+    uint32_t start = 0;
+    for (int k = kResolveBuckets - 1; k > (int)threadIdx.x; --k) start += b.hist[k];
+    base[threadIdx.x] = start + (cnt[threadIdx.x] ? atomicAdd(&b.fill[threadIdx.x], cnt[threadIdx.x]) : 0u);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < kBinPerThread; ++i) {
+    const uint32_t g = blockIdx.x * kBinChunk + i * kBinThreads + threadIdx.x;
+    if (bk[i] >= 0) b.items[base[bk[i]] + rank[i]] = g;
+  }
+}
+
+// oitLoop64.frag.glsl:162-183: the keys are sorted; blend until the first
+// empty one. key0 was fetched ahead; `nmax` bounds the keys to read (the
+// micro-tile's longest list plus its terminator), fetched four at a time
+// without waiting on each other (lanes of a row share every layer's sectors).
+__device__ __forceinline__ float4 resolve_loop64(const ResolveView& v, uint32_t pixel, uint2 key0, int nmax) {
+  const uint2* __restrict__ ab = reinterpret_cast<const uint2*>(v.abuf) + pixel;
+  float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (key0.y == kEmptyKey) return sum;
+  blend_under(sum, decode_premult(key0.x));
+  for (int i0 = 1; i0 < nmax; i0 += 4) {
+    uint2 key[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) key[j] = i0 + j < nmax ? __ldg(ab + (size_t)(i0 + j) * v.P) : make_uint2(0u, kEmptyKey);
+    bool done = false;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      done |= key[j].y == kEmptyKey;
+      if (!done) blend_under(sum, decode_premult(key[j].x));
+    }
+    if (done) break;
+  }
+  return sum;
+}
+
+// The pixel of lane `lane` in work item `it`, or false outside the view.
+struct ItemPixel {
+  const ResolveView* v;
+  uint32_t tile, pixel;
+};
+
+__device__ __forceinline__ bool item_pixel(const ResolveBatch& b, const uint32_t* tb, uint32_t it, int lane,
+                                           ItemPixel& o) {
+  const uint32_t g = b.items ? __ldg(b.items + it) : it;
+  const int vi = find_view(tb, b.num_views, g);
+  const ResolveView& v = b.views[vi];
+  o.v = &v;
+  o.tile = g - tb[vi];
+  const int mtx = v.mtx;
+  const int x = (int)(o.tile % (uint32_t)mtx) * 8 + (lane & 7), y = (int)(o.tile / (uint32_t)mtx) * 4 + (lane >> 3);
+  if (x >= v.W || y >= v.H) return false;
+  o.pixel = (uint32_t)y * (uint32_t)v.W + (uint32_t)x;
+  return true;
+}
+
+// Persistent: every warp resolves micro-tiles (one lane per pixel) from the
+// work list in static cyclic order. One kernel per view kind, so each gets the
+// registers (and the occupancy) its own per-pixel work needs; the linked-list
+// kernel comes with K register slots for the first sort entries.
+template <int K>
+__global__ void __launch_bounds__(256) k_resolve_list(ResolveBatch b) {
+  extern __shared__ __align__(16) uint32_t rsm[];
+  load_bases(b, rsm);
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  WalkArrays<false> a;
+  for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < b.total_tiles; it += warps) {
+    ItemPixel ip;
+    if (!item_pixel(b, rsm, it, lane, ip)) continue;
+    const ResolveView& v = *ip.v;
+    float4 c = __ldcs(v.color + ip.pixel);  // read once: streaming
+    const float4 sum = walk_list<false, false, K>(reinterpret_cast<const uint4*>(v.abuf), __ldg(v.aux + ip.pixel),
+                                                   v.capacity, v.L, v.tail, 1, a);
+    rop_over(c, sum);
+    write_rgba8(v.out, v.out_linear, ip.pixel, c);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_resolve_loop64(ResolveBatch b) {
+  extern __shared__ __align__(16) uint32_t rsm[];
+  load_bases(b, rsm);
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < b.total_tiles; it += warps) {
+    ItemPixel ip;
+    if (!item_pixel(b, rsm, it, lane, ip)) continue;
+    const ResolveView& v = *ip.v;
+    float4 c = __ldcs(v.color + ip.pixel);
+    const uint2 key0 = __ldg(reinterpret_cast<const uint2*>(v.abuf) + ip.pixel);
+    const float4 sum = resolve_loop64(v, ip.pixel, key0, min((int)__ldg(v.lens + ip.tile) + 1, v.L));
+    rop_over(c, sum);
+    write_rgba8(v.out, v.out_linear, ip.pixel, c);
+  }
+}
+
+size_t resolve_smem(const ResolveBatch& b) { return (size_t)((b.num_views + 3) & ~3) * 4; }
+
+template <class F>
+cudaError_t with_kernel(int variant, F f) {
+  switch (variant) {
+    case kResolveVariantLoop64: return f(k_resolve_loop64);
+    case kResolveVariantList0: return f(k_resolve_list<0>);
+    case kResolveVariantList4: return f(k_resolve_list<4>);
+    case kResolveVariantList8: return f(k_resolve_list<8>);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+cudaError_t resolve_bin(const ResolveBatch& b, cudaStream_t s, uint64_t* launches) {
+  if (!b.items || b.total_tiles == 0) return cudaSuccess;
+  if (b.num_views > kResolveMaxViews) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(b.hist, 0, kResolveBuckets * sizeof(uint32_t), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.fill, 0, kResolveBuckets * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  const uint32_t nb = (b.total_tiles + kBinChunk - 1) / kBinChunk;
+  k_rbin_count<<<nb, kBinThreads, 0, s>>>(b);
+  k_rbin_scatter<<<nb, kBinThreads, 0, s>>>(b);
+  *launches += 2;
+  return cudaGetLastError();
+}
+
+int resolve_blocks_per_sm(const ResolveBatch& b, int variant, int threads) {
+  const size_t smem = resolve_smem(b);
+  int n = 0;
+  const cudaError_t e = with_kernel(variant, [&](auto kern) {
+    if (smem > 48 * 1024) {
+      const cudaError_t a = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (a != cudaSuccess) return a;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, threads, smem);
+  });
+  return e == cudaSuccess ? n : 0;
+}
+
+cudaError_t resolve_run(const ResolveBatch& b, int variant, int threads, int blocks, cudaStream_t s) {
+  if (b.total_tiles == 0) return cudaSuccess;
+  if (b.num_views > kResolveMaxViews || threads % 32 != 0 || threads < 32 || threads > 256 || blocks < 1)
+    return cudaErrorInvalidValue;
+  return with_kernel(variant, [&](auto kern) {
+    kern<<<blocks, threads, resolve_smem(b), s>>>(b);
+    return cudaGetLastError();
+  });
+}
+
+}  // namespace oit

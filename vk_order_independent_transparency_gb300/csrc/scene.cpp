@@ -32,6 +32,60 @@ bool valid_desc(const oit_scene_desc* d) {
 uint32_t sphere_vertices(const oit_scene_desc* d) { return (d->stacks + 1) * (d->slices + 1); }
 uint32_t sphere_triangles(const oit_scene_desc* d) { return d->slices * (2 * (d->stacks - 2) + 2); }
 
+// UV sphere (the role of nvutils::createSphereUv(1, 2*subdiv, subdiv),
+// main.cpp:346): unit-radius positions (which are also the normals) and
+// triangles wound counter-clockwise seen from outside.
+void sphere_template(const oit_scene_desc* d, float* tp, uint32_t* tt) {
+  const uint32_t stacks = d->stacks, slices = d->slices;
+  for (uint32_t i = 0; i <= stacks; ++i) {
+    const double th = M_PI * (double)i / (double)stacks;
+    for (uint32_t j = 0; j <= slices; ++j) {
+      const double ph = 2.0 * M_PI * (double)j / (double)slices;
+      float* p = tp + 3 * (size_t)(i * (slices + 1) + j);
+      p[0] = (float)(std::sin(th) * std::cos(ph));
+      p[1] = (float)std::cos(th);
+      p[2] = (float)(std::sin(th) * std::sin(ph));
+    }
+  }
+  uint32_t k = 0;
+  auto emit = [&](uint32_t a, uint32_t b, uint32_t c) {
+    // orient outward: (b - a) x (c - a) must point away from the centre
+    const float* A = tp + 3 * (size_t)a;
+    const float* B = tp + 3 * (size_t)b;
+    const float* C = tp + 3 * (size_t)c;
+    const double ux = B[0] - A[0], uy = B[1] - A[1], uz = B[2] - A[2];
+    const double vx = C[0] - A[0], vy = C[1] - A[1], vz = C[2] - A[2];
+    const double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+    const double dd = nx * (A[0] + B[0] + C[0]) + ny * (A[1] + B[1] + C[1]) + nz * (A[2] + B[2] + C[2]);
+    tt[3 * k + 0] = a;
+    tt[3 * k + 1] = dd >= 0 ? b : c;
+    tt[3 * k + 2] = dd >= 0 ? c : b;
+    ++k;
+  };
+  for (uint32_t i = 0; i < stacks; ++i) {
+    for (uint32_t j = 0; j < slices; ++j) {
+      const uint32_t v00 = i * (slices + 1) + j, v01 = v00 + 1;
+      const uint32_t v10 = v00 + (slices + 1), v11 = v10 + 1;
+      if (i != 0) emit(v00, v10, v01);
+      if (i != stacks - 1) emit(v01, v10, v11);
+    }
+  }
+}
+
+// Per object, in stream order: centre, radius, colour (main.cpp:353-369 draws
+// the same quantities). inst = centre.xyz, radius, color.rgba.
+void instance_params(const oit_scene_desc* d, float* inst) {
+  SplitMix64 rng{d->seed};
+  for (uint32_t o = 0; o < d->num_objects; ++o) {
+    float* q = inst + 8 * (size_t)o;
+    q[0] = (rng.uniform() * 2.0f - 1.0f) * d->half_extent;
+    q[1] = (rng.uniform() * 2.0f - 1.0f) * d->half_extent;
+    q[2] = (rng.uniform() * 2.0f - 1.0f) * d->half_extent;
+    q[3] = d->radius_min + rng.uniform() * (d->radius_max - d->radius_min);
+    for (int c = 0; c < 4; ++c) q[4 + c] = rng.uniform();
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -48,73 +102,33 @@ int oit_scene_size(const oit_scene_desc* desc, uint32_t* num_vertices, uint32_t*
   return OIT_OK;
 }
 
-// UV sphere (the role of nvutils::createSphereUv(1, 2*subdiv, subdiv),
-// main.cpp:346), outward counter-clockwise winding, then num_objects scaled
-// and translated copies flattened into one mesh (main.cpp:353-387).
+// num_objects scaled and translated copies of the template flattened into one
+// mesh (main.cpp:353-387): position = template * radius + centre, normal =
+// template, colour = the object's.
 int oit_scene_generate(const oit_scene_desc* desc, float* vertices, uint32_t* indices) {
   if (!valid_desc(desc) || !vertices || !indices) return OIT_ERR_INVALID_ARGUMENT;
   uint32_t nv = 0, nt = 0, tpo = 0;
   int st = oit_scene_size(desc, &nv, &nt, &tpo);
   if (st != OIT_OK) return st;
-  const uint32_t stacks = desc->stacks, slices = desc->slices;
   const uint32_t vpo = sphere_vertices(desc);
-  // template sphere
   float* tp = new float[3 * (size_t)vpo];
-  for (uint32_t i = 0; i <= stacks; ++i) {
-    const double th = M_PI * (double)i / (double)stacks;
-    for (uint32_t j = 0; j <= slices; ++j) {
-      const double ph = 2.0 * M_PI * (double)j / (double)slices;
-      float* p = tp + 3 * (size_t)(i * (slices + 1) + j);
-      p[0] = (float)(std::sin(th) * std::cos(ph));
-      p[1] = (float)std::cos(th);
-      p[2] = (float)(std::sin(th) * std::sin(ph));
-    }
-  }
   uint32_t* tt = new uint32_t[3 * (size_t)tpo];
-  uint32_t k = 0;
-  auto emit = [&](uint32_t a, uint32_t b, uint32_t c) {
-    // orient outward: (b - a) x (c - a) must point away from the centre
-    const float* A = tp + 3 * (size_t)a;
-    const float* B = tp + 3 * (size_t)b;
-    const float* C = tp + 3 * (size_t)c;
-    const double ux = B[0] - A[0], uy = B[1] - A[1], uz = B[2] - A[2];
-    const double vx = C[0] - A[0], vy = C[1] - A[1], vz = C[2] - A[2];
-    const double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
-    const double d = nx * (A[0] + B[0] + C[0]) + ny * (A[1] + B[1] + C[1]) + nz * (A[2] + B[2] + C[2]);
-    tt[3 * k + 0] = a;
-    tt[3 * k + 1] = d >= 0 ? b : c;
-    tt[3 * k + 2] = d >= 0 ? c : b;
-    ++k;
-  };
-  for (uint32_t i = 0; i < stacks; ++i) {
-    for (uint32_t j = 0; j < slices; ++j) {
-      const uint32_t v00 = i * (slices + 1) + j, v01 = v00 + 1;
-      const uint32_t v10 = v00 + (slices + 1), v11 = v10 + 1;
-      if (i != 0) emit(v00, v10, v01);
-      if (i != stacks - 1) emit(v01, v10, v11);
-    }
-  }
-  SplitMix64 rng{desc->seed};
+  float* inst = new float[8 * (size_t)desc->num_objects];
+  sphere_template(desc, tp, tt);
+  instance_params(desc, inst);
   for (uint32_t o = 0; o < desc->num_objects; ++o) {
-    const float cx = (rng.uniform() * 2.0f - 1.0f) * desc->half_extent;
-    const float cy = (rng.uniform() * 2.0f - 1.0f) * desc->half_extent;
-    const float cz = (rng.uniform() * 2.0f - 1.0f) * desc->half_extent;
-    const float r = desc->radius_min + rng.uniform() * (desc->radius_max - desc->radius_min);
-    const float col[4] = {rng.uniform(), rng.uniform(), rng.uniform(), rng.uniform()};
+    const float* q = inst + 8 * (size_t)o;
     float* vo = vertices + 10 * (size_t)o * vpo;
     for (uint32_t v = 0; v < vpo; ++v) {
       const float* p = tp + 3 * (size_t)v;
       float* out = vo + 10 * (size_t)v;
-      out[0] = p[0] * r + cx;
-      out[1] = p[1] * r + cy;
-      out[2] = p[2] * r + cz;
+      out[0] = p[0] * q[3] + q[0];
+      out[1] = p[1] * q[3] + q[1];
+      out[2] = p[2] * q[3] + q[2];
       out[3] = p[0];
       out[4] = p[1];
       out[5] = p[2];
-      out[6] = col[0];
-      out[7] = col[1];
-      out[8] = col[2];
-      out[9] = col[3];
+      for (int c = 0; c < 4; ++c) out[6 + c] = q[4 + c];
     }
     uint32_t* io = indices + 3 * (size_t)o * tpo;
     const uint32_t base = o * vpo;
@@ -122,6 +136,25 @@ int oit_scene_generate(const oit_scene_desc* desc, float* vertices, uint32_t* in
   }
   delete[] tp;
   delete[] tt;
+  delete[] inst;
+  return OIT_OK;
+}
+
+int oit_scene_generate_instanced(const oit_scene_desc* desc, float* template_vertices, uint32_t* template_indices,
+                                 float* instances) {
+  if (!valid_desc(desc) || !template_vertices || !template_indices || !instances) return OIT_ERR_INVALID_ARGUMENT;
+  int st = oit_scene_size(desc, nullptr, nullptr, nullptr);
+  if (st != OIT_OK) return st;
+  const uint32_t vpo = sphere_vertices(desc);
+  float* tp = new float[3 * (size_t)vpo];
+  sphere_template(desc, tp, template_indices);
+  for (uint32_t v = 0; v < vpo; ++v)
+    for (int c = 0; c < 3; ++c) {
+      template_vertices[6 * (size_t)v + c] = tp[3 * (size_t)v + c];
+      template_vertices[6 * (size_t)v + 3 + c] = tp[3 * (size_t)v + c];
+    }
+  instance_params(desc, instances);
+  delete[] tp;
   return OIT_OK;
 }
 

@@ -39,17 +39,35 @@ __global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
   if (t >= p.num_triangles) return;
   const uint32_t tg = p.first_triangle + t;
   const float* __restrict__ vtx = p.vertices;
-  const uint32_t i0 = __ldg(&p.indices[3 * (size_t)tg + 0]);
-  const uint32_t i1 = __ldg(&p.indices[3 * (size_t)tg + 1]);
-  const uint32_t i2 = __ldg(&p.indices[3 * (size_t)tg + 2]);
+  // Flattened mesh: 10 floats per vertex, colour of the first vertex. Instanced:
+  // template vertex (6 floats) scaled by the instance's radius and moved to its
+  // centre, one multiply and one add each rounded (as a flattened copy of the
+  // template is built on the host), colour of the instance.
+  const float* inst = nullptr;
+  uint32_t tri = tg;
+  if (p.instances) {
+    const uint32_t o = tg / p.template_triangles;
+    tri = tg - o * p.template_triangles;
+    inst = p.instances + 8 * (size_t)o;
+  }
+  const uint32_t i0 = __ldg(&p.indices[3 * (size_t)tri + 0]);
+  const uint32_t i1 = __ldg(&p.indices[3 * (size_t)tri + 1]);
+  const uint32_t i2 = __ldg(&p.indices[3 * (size_t)tri + 2]);
   const uint32_t vid[3] = {i0, i1, i2};
   float cx[3], cy[3], cz[3], cw[3], vz[3], nx[3], ny[3], nz[3];
   const float* m = p.proj_view.m;
   const float* v = p.view.m;
+  float4 ic = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+  if (inst) ic = __ldg(reinterpret_cast<const float4*>(inst));
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const float* pv = vtx + 10 * (size_t)vid[k];
-    const float x = __ldg(pv + 0), y = __ldg(pv + 1), z = __ldg(pv + 2);
+    const float* pv = inst ? vtx + 6 * (size_t)vid[k] : vtx + 10 * (size_t)vid[k];
+    float x = __ldg(pv + 0), y = __ldg(pv + 1), z = __ldg(pv + 2);
+    if (inst) {
+      x = __fadd_rn(__fmul_rn(x, ic.w), ic.x);
+      y = __fadd_rn(__fmul_rn(y, ic.w), ic.y);
+      z = __fadd_rn(__fmul_rn(z, ic.w), ic.z);
+    }
     cx[k] = __fmaf_rn(m[0], x, __fmaf_rn(m[4], y, __fmaf_rn(m[8], z, m[12])));
     cy[k] = __fmaf_rn(m[1], x, __fmaf_rn(m[5], y, __fmaf_rn(m[9], z, m[13])));
     cz[k] = __fmaf_rn(m[2], x, __fmaf_rn(m[6], y, __fmaf_rn(m[10], z, m[14])));
@@ -135,8 +153,8 @@ __global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
     const int order[3] = {0, o1, o2};
     TriSetup T;
     T.xy01 = make_int4(PX[0], PY[0], PX[1], PY[1]);
-    const float* c0 = vtx + 10 * (size_t)i0;
-    float alpha = __fmaf_rn(__ldg(c0 + 9), p.alpha_width, p.alpha_min);
+    const float* c0 = inst ? inst + 4 : vtx + 10 * (size_t)i0 + 6;  // color.rgba
+    float alpha = __fmaf_rn(__ldg(c0 + 3), p.alpha_width, p.alpha_min);
     alpha = (alpha > 0.0f) ? alpha : 0.0f;
     alpha = (alpha < 1.0f) ? alpha : 1.0f;
     const int acode = __float2int_rn(__fmul_rn(alpha, 255.0f));
@@ -148,9 +166,9 @@ __global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
     T.zc = make_float4(z0, __fsub_rn(z1, z0), __fsub_rn(z2, z0), __fdiv_rn(1.0f, __ll2float_rn(area)));
     const float q0 = q[0], q1 = q[order[1]], q2 = q[order[2]];
     const int j1 = order[1], j2 = order[2];
-    T.n0 = make_float4(__fmul_rn(nx[0], q0), __fmul_rn(ny[0], q0), __fmul_rn(nz[0], q0), __ldg(c0 + 6));
-    T.n1 = make_float4(__fmul_rn(nx[j1], q1), __fmul_rn(ny[j1], q1), __fmul_rn(nz[j1], q1), __ldg(c0 + 7));
-    T.n2 = make_float4(__fmul_rn(nx[j2], q2), __fmul_rn(ny[j2], q2), __fmul_rn(nz[j2], q2), __ldg(c0 + 8));
+    T.n0 = make_float4(__fmul_rn(nx[0], q0), __fmul_rn(ny[0], q0), __fmul_rn(nz[0], q0), __ldg(c0 + 0));
+    T.n1 = make_float4(__fmul_rn(nx[j1], q1), __fmul_rn(ny[j1], q1), __fmul_rn(nz[j1], q1), __ldg(c0 + 1));
+    T.n2 = make_float4(__fmul_rn(nx[j2], q2), __fmul_rn(ny[j2], q2), __fmul_rn(nz[j2], q2), __ldg(c0 + 2));
     reinterpret_cast<TriSetup*>(p.setup)[t] = T;
     if (p.persp) {
       TriPersp Q;

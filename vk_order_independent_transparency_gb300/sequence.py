@@ -19,7 +19,8 @@ import zlib
 
 import numpy as np
 
-from . import (OIT_INTERLOCK, DeviceMesh, Renderer, aa_settings, make_camera, make_scene, make_state)
+from . import (OIT_INTERLOCK, OIT_LINKEDLIST, DeviceMesh, Renderer, aa_settings, make_camera, make_scene,
+                make_state)
 
 ALGORITHM_NAMES = ['simple', 'linkedlist', 'loop', 'loop64', 'spinlock', 'interlock', 'weighted']
 TAIL_NAMES = ['notail', 'tail']
