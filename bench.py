@@ -263,9 +263,9 @@ class _DeviceArray:
         self.__cuda_array_interface__ = {'shape': shape, 'typestr': typestr, 'data': (ptr, False), 'version': 3}
 
 
-def resolve_bytes(views, renderers):
+def resolve_bytes(views, renderers, color_bytes=8):
     """Algorithmic bytes of one batched resolve: per pixel the colour target
-    (16 B) in and RGBA8 (4 B) out; linked lists: the head (4 B) and every
+    (8 B: FP16) in and RGBA8 (4 B) out; linked lists: the head (4 B) and every
     stored node (16 B); Loop64: every kept key plus the terminating empty key
     (8 B each); the work list (4 B per micro-tile, written and read) and the
     micro-tile lengths (read twice). Counted on the device, outside timing."""
@@ -277,7 +277,7 @@ def resolve_bytes(views, renderers):
         W, H, L = vd['width'], vd['height'], vd['oit_layers']
         P = W * H
         tiles += ((W + 7) // 8) * ((H + 3) // 4)
-        b = P * (16 + 4)
+        b = P * (color_bytes + 4)
         if vd['algorithm'] == 'linkedlist':
             b += P * 4 + 16 * min(r.fragment_count(), vd['nodes_per_pixel'] * P - 1)
         else:
@@ -388,11 +388,12 @@ def run_batch(a, rank):
         mesh = oit.DeviceMesh(v, i)
         meshes.append(mesh)
         host.append((v, i, tpo))
-        for recs, fmt in ((mixed, oit.OIT_RECORD_RGBA8), (plain, oit.OIT_RECORD_RGBA32F)):
+        for recs, fmt, flags in ((mixed, oit.OIT_RECORD_RGBA8, oit.OIT_FLAG_HALF_COLOR),
+                                 (plain, oit.OIT_RECORD_RGBA32F, 0)):
             r = oit.Renderer(oit.make_state(ALGS.index(vd['algorithm']), vd['width'], vd['height'],
                                             oit_layers=vd['oit_layers'], nodes_per_pixel=vd['nodes_per_pixel'],
                                             alpha_min=vd['alpha_min'], alpha_width=vd['alpha_width'],
-                                            record_format=fmt))
+                                            record_format=fmt, flags=flags))
             r.update_scene(sd)
             recs.append(r)
     batch = oit.Batch(parallel_streams=8)
@@ -526,7 +527,7 @@ def main_batch(a, rank, world):
     line = {
         'metric': 'Mfragments/s', 'value': round(value, 3), 'unit': 'Mfragments/s', 'n_gpus': world,
         'steps': a.steps, 'warmup': a.warmup, 'ms_per_step': round(t_mixed / a.steps, 4), 'higher_is_better': True,
-        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'rgba8 records + f32 blend',
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'rgba8 records, f16 colour target, f32 blend',
         'data': 'synthetic: 64 seeded UV-sphere scenes, inputs resident in HBM',
         'config': dict(workload_dict(BATCH_WORKLOAD), fragments_per_batch=res['frags'],
                        parallelism='replicas' if world > 1 else 'single',

@@ -58,6 +58,8 @@ extern "C" {
 /* oit_state.flags */
 #define OIT_FLAG_LINEAR_OUTPUT 0x1u  /* composite also writes OIT_BUF_OUTPUT_LINEAR */
 #define OIT_FLAG_CUDA_GRAPH 0x2u     /* oit_render_frame replays a captured CUDA graph of the whole frame */
+#define OIT_FLAG_HALF_COLOR 0x4u     /* colour target after tail blending stored as FP16 (blended in FP32
+                                        within a tile, rounded once); the reference's is RGBA8 sRGB */
 
 /* Status codes. */
 #define OIT_OK 0
@@ -285,11 +287,11 @@ int oit_batch_resolve(oit_batch* batch, const oit_view_frame* views, uint32_t nu
 
 /* The shape the autotuner picked for one part of the batched resolve (part 0:
  * linked-list views, 1: Loop64 views): threads per block, blocks, binned (1)
- * or view-order (0) work list, and the register slots holding the first sort
- * entries of a list (0, 4 or 8; the rest live in local memory). A part without
- * views reports zeros. OIT_ERR_STATE before the first resolve. */
+ * or view-order (0) work list, and the sort-array entries per thread held in
+ * shared memory (0 or 8; the rest live in local memory). A part without views
+ * reports zeros. OIT_ERR_STATE before the first resolve. */
 int oit_batch_resolve_config(oit_batch* batch, uint32_t part, uint32_t* threads_per_block, uint32_t* blocks,
-                             int32_t* binned, int32_t* register_slots);
+                             int32_t* binned, int32_t* shared_slots);
 
 /* ---- inspection -------------------------------------------------------- */
 

@@ -28,7 +28,9 @@ def render_gpu(algorithm, width, height, v, i, tpo, sd, percent=100, **kw):
         'aux': r.read_buffer(oit.OIT_BUF_AUX),
         'auxdepth': r.read_buffer(oit.OIT_BUF_AUXDEPTH),
         'counter': r.read_buffer(oit.OIT_BUF_COUNTER),
-        'color': r.read_buffer(oit.OIT_BUF_COLOR, np.float32).reshape(-1, 4),
+        'color': (r.read_buffer(oit.OIT_BUF_COLOR, np.float16).astype(np.float32)
+                  if kw.get('flags', 0) & oit.OIT_FLAG_HALF_COLOR else
+                  r.read_buffer(oit.OIT_BUF_COLOR, np.float32)).reshape(-1, 4),
         'depth': r.read_buffer(oit.OIT_BUF_DEPTH),
         'fragments': r.fragment_count(),
         'error': r.get_error(),
@@ -129,7 +131,7 @@ def compare_abuffer(algorithm, g, o, L, P, coverage, ssn=1, fp32=False):
             np.testing.assert_array_equal(gp[used], op[used])
 
 
-def check_pair(alg, g, o, W, H, L, aa=0, ss=1, fp32=False):
+def check_pair(alg, g, o, W, H, L, aa=0, ss=1, fp32=False, color_atol=2e-5, color_rtol=0.0):
     """Every bit-exact and colour comparison of one engine frame against the
     oracle's: error bits, fragment counts, A-buffer state, the tail-blended
     colour target (2e-5 absolute) and the RGBA8 image (1 LSB)."""
@@ -145,7 +147,7 @@ def check_pair(alg, g, o, W, H, L, aa=0, ss=1, fp32=False):
             ref_col = o['color_samples'].reshape(-1, 4)
         else:
             ref_col = o['color_samples'].mean(axis=0)
-        np.testing.assert_allclose(g['color'][:ssn * P], ref_col, atol=2e-5, rtol=0)
+        np.testing.assert_allclose(g['color'][:ssn * P], ref_col, atol=color_atol, rtol=color_rtol)
     return compare_images(g, o)
 
 

@@ -269,3 +269,16 @@ def test_rgba32f_unsupported_combinations(engine):
         st = engine.make_state(alg, 64, 64, oit_layers=L, record_format=engine.OIT_RECORD_RGBA32F)
         ctx = ctypes.c_void_p()
         assert engine.library().oit_create(ctypes.byref(st), ctypes.byref(ctx)) == engine.OIT_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize('aa', [0, 1, 2])
+@pytest.mark.parametrize('alg', [0, 1, 2, 3, 4])
+def test_half_colour_target(engine, alg, aa):
+    """OIT_FLAG_HALF_COLOR: the tail-blended colour target stored as FP16
+    (rounded once per tile). A-buffer bit-exact; colour target within half
+    precision (relative 2^-11, plus 1e-4 absolute for the FP32 blend); image
+    within 1 LSB."""
+    W, H, L = 128, 96, 4
+    kw = dict(oit_layers=L, nodes_per_pixel=6, aa_type=aa, flags=engine.OIT_FLAG_HALF_COLOR)
+    g, o = run_pair(engine, alg, W, H, 40, percent=70, **kw)
+    pu.check_pair(alg, g, o, W, H, L, aa, color_atol=1e-4, color_rtol=2.0 ** -11)

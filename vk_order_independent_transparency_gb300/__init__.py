@@ -26,6 +26,7 @@ OIT_RECORD_RGBA8, OIT_RECORD_RGBA32F = 0, 1
 OIT_WEIGHTED_FP16, OIT_WEIGHTED_FP32 = 0, 1
 OIT_FLAG_LINEAR_OUTPUT = 0x1
 OIT_FLAG_CUDA_GRAPH = 0x2
+OIT_FLAG_HALF_COLOR = 0x4
 
 OIT_OK = 0
 OIT_ERR_INVALID_ARGUMENT = -1
@@ -474,7 +475,7 @@ class Batch:
             _check(self.lib.oit_batch_resolve_config(self._b, part, ctypes.byref(t), ctypes.byref(n), ctypes.byref(b),
                                                      ctypes.byref(k)), 'oit_batch_resolve_config')
             out[name] = {'threads_per_block': t.value, 'blocks': n.value, 'binned': bool(b.value),
-                         'register_slots': k.value}
+                         'shared_slots': k.value}
         return out
 
 

@@ -189,10 +189,10 @@ __device__ __forceinline__ float4 list_pixel(const CompositeParams& p, uint32_t 
   const uint32_t head = p.aux[eaux];
   if (p.coverage) {
     WalkArrays<true> a;
-    return walk_list<F32, true>(pool, head, p.capacity, L, p.tail, p.S, a);
+    return walk_list<F32>(pool, head, p.capacity, L, p.tail, p.S, a);
   }
   WalkArrays<false> a;
-  return walk_list<F32, false>(pool, head, p.capacity, L, p.tail, p.S, a);
+  return walk_list<F32>(pool, head, p.capacity, L, p.tail, p.S, a);
 }
 
 // Loop32: oitLoop.frag.glsl:191-222.
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256) k_composite(CompositeParams p) {
         // composite output over the colour target (which already holds the
         // tail-blended opaque + background colour, sample-averaged unless
         // sample shading keeps one per sample)
-        float4 c = p.color[eaux];
+        float4 c = load_color(p.color, p.color_half != 0, eaux);
         rop_over(c, sum);
         acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
       }

@@ -162,6 +162,8 @@ struct oit_context {
   }
 
   oit::Alg alg() const { return static_cast<oit::Alg>(st.algorithm); }
+  bool color_half() const { return (st.flags & OIT_FLAG_HALF_COLOR) != 0; }
+  size_t color_bytes() const { return color_half() ? 8 : 16; }
 
   // Views the batched resolve handles: linked list or Loop64, 1x, RGBA8 records.
   bool batch_resolvable() const {
@@ -200,7 +202,7 @@ struct oit_context {
     OIT_TRY_CUDA(aux.ensure(elems * 4), "alloc aux");
     OIT_TRY_CUDA(auxdepth.ensure(elems * 4), "alloc auxdepth");
     OIT_TRY_CUDA(counter.ensure(4), "alloc counter");
-    OIT_TRY_CUDA(color.ensure((size_t)P * ssn * 16), "alloc color");
+    OIT_TRY_CUDA(color.ensure((size_t)P * ssn * color_bytes()), "alloc color");
     if (alg() == oit::Alg::Weighted) {
       const bool f32 = st.weighted_precision == OIT_WEIGHTED_FP32;
       OIT_TRY_CUDA(accum.ensure((size_t)S * P * (f32 ? 16 : 8)), "alloc accum");
@@ -392,6 +394,7 @@ struct oit_context {
     p.has_opaque = opaque_valid ? 1 : 0;
     p.background = background;
     p.color = color.as<float4>();
+    p.color_half = color_half() ? 1 : 0;
     p.abuf = abuf.as<uint32_t>();
     p.aux = aux.as<uint32_t>();
     p.auxdepth = auxdepth.as<uint32_t>();
@@ -416,6 +419,7 @@ struct oit_context {
     v.abuf = abuf.as<uint32_t>();
     v.aux = aux.as<uint32_t>();
     v.color = color.as<float4>();
+    v.color_half = color_half() ? 1 : 0;
     v.out = out_dev ? out_dev : out.as<uint8_t>();
     v.out_linear = nullptr;
     v.lens = lens.as<uint8_t>();
@@ -536,6 +540,7 @@ struct oit_context {
     c.abuf = abuf.as<uint32_t>();
     c.aux = aux.as<uint32_t>();
     c.color = color.as<float4>();
+    c.color_half = color_half() ? 1 : 0;
     c.opaque_color = opaque_color.as<float4>();
     c.has_opaque = opaque_valid ? 1 : 0;
     c.background = background;
@@ -832,7 +837,7 @@ int batch_prepare_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n)
     rb.hist = rp.hist.as<uint32_t>();
     rb.fill = rb.hist + oit::kResolveBuckets;
     rb.items = rp.items.as<uint32_t>();
-    rp.variant = part == 0 ? oit::kResolveVariantList0 : oit::kResolveVariantLoop64;
+    rp.variant = part == 0 ? oit::kResolveVariantList : oit::kResolveVariantLoop64;
   }
   b->rsig = sig;
   return OIT_OK;
@@ -872,8 +877,8 @@ int batch_resolve_launch(oit_batch* b, cudaStream_t s, uint64_t* launches) {
   return OIT_OK;
 }
 
-// The autotuner, per part: kernel variant (linked lists: 0, 4 or 8 register
-// slots for the first sort entries), block size and binned versus view-order
+// The autotuner, per part: kernel variant (linked lists: sort arrays in local
+// memory, or the first 8 entries in shared memory), block size and binned versus view-order
 // work lists, each timed with CUDA events on the batch's current frames (the
 // resolve only writes the outputs, so reruns are harmless); the grid holds
 // every block that fits. The fastest shape is kept for the batch's views.
@@ -888,7 +893,7 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
     if (rp.rb.num_views == 0) continue;
     float best = 1e30f;
     std::vector<int> variants;
-    if (part == 0) variants = {oit::kResolveVariantList0, oit::kResolveVariantList4, oit::kResolveVariantList8};
+    if (part == 0) variants = {oit::kResolveVariantList, oit::kResolveVariantListShared};
     else variants = {oit::kResolveVariantLoop64};
     for (int variant : variants) {
       for (int threads : {64, 128, 256}) {
@@ -1295,15 +1300,15 @@ int oit_batch_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n, voi
 }
 
 int oit_batch_resolve_config(oit_batch* b, uint32_t part, uint32_t* threads_per_block, uint32_t* blocks,
-                             int32_t* binned, int32_t* register_slots) {
-  if (!b || part > 1 || !threads_per_block || !blocks || !binned || !register_slots) return OIT_ERR_INVALID_ARGUMENT;
+                             int32_t* binned, int32_t* shared_slots) {
+  if (!b || part > 1 || !threads_per_block || !blocks || !binned || !shared_slots) return OIT_ERR_INVALID_ARGUMENT;
   if (!b->r_tuned) return OIT_ERR_STATE;
   const oit_batch::ResolvePart& rp = b->rparts[part];
   const bool any = rp.rb.num_views > 0;
   *threads_per_block = any ? (uint32_t)rp.threads : 0u;
   *blocks = any ? (uint32_t)rp.blocks : 0u;
   *binned = any && rp.binned ? 1 : 0;
-  *register_slots = rp.variant == oit::kResolveVariantList4 ? 4 : (rp.variant == oit::kResolveVariantList8 ? 8 : 0);
+  *shared_slots = rp.variant == oit::kResolveVariantListShared ? 8 : 0;
   return OIT_OK;
 }
 
@@ -1326,7 +1331,7 @@ int oit_get_buffer(oit_context* ctx, int which, void** ptr, size_t* bytes) {
     case OIT_BUF_COUNTER: b = &ctx->counter; n = 4; break;
     case OIT_BUF_DEPTH: b = &ctx->depth; n = ctx->opaque_valid ? (size_t)ctx->S * ctx->P * 4 : 0; break;
     case OIT_BUF_OPAQUE_COLOR: b = &ctx->opaque_color; n = ctx->opaque_valid ? (size_t)ctx->S * ctx->P * 16 : 0; break;
-    case OIT_BUF_COLOR: b = &ctx->color; n = (size_t)ctx->P * ctx->ssn * 16; break;
+    case OIT_BUF_COLOR: b = &ctx->color; n = (size_t)ctx->P * ctx->ssn * ctx->color_bytes(); break;
     case OIT_BUF_ACCUM: b = &ctx->accum; n = b->bytes; break;
     case OIT_BUF_REVEAL: b = &ctx->reveal; n = b->bytes; break;
     case OIT_BUF_OUTPUT: b = &ctx->out; n = (size_t)ctx->W * ctx->H * 4; break;

@@ -1,16 +1,17 @@
-// Linked-list composite of one pixel (oitLinkedList.frag.glsl:106-172) as a
-// walk that consumes one node per step, with the sort arrays in a per-thread
-// local array (warp-interleaved in local memory: short lists touch a few L1
-// lines per warp, and occupancy is set by registers, not by OIT_LAYERS).
+// Linked-list composite of one pixel (oitLinkedList.frag.glsl:106-172) with
+// the sort arrays outside registers, so register use (and occupancy) does not
+// grow with OIT_LAYERS: a per-thread local array (warp-interleaved in local
+// memory, so short lists touch a few L1 lines per warp), or a shared-memory
+// column for the first entries.
 //
 // Semantics, as the reference's composite: the first OIT_LAYERS nodes in list
 // order are kept and ordered as bubbleSort orders them
 // (oitCompositeDefines.glsl:51-89, swap on >=); every later node goes through
 // insertionSortTail (:94-139) and the entry it evicts, or the node itself, is
-// tail blended in that order. The kept entries are sorted on insertion;
-// bubbleSort's swap-on-equal makes its order of equal depths depend on the
-// passes, so when the first OIT_LAYERS nodes hold equal depths they are read
-// again and bubbleSort runs itself.
+// tail blended in that order. The kept entries are sorted on insertion as the
+// walk goes; bubbleSort's swap-on-equal makes its order of equal depths depend
+// on its passes, so when the first OIT_LAYERS nodes hold equal depths they are
+// read again and bubbleSort runs itself.
 #pragma once
 
 #include "oit_device.cuh"
@@ -50,11 +51,31 @@ __device__ __forceinline__ float4 node_colour(const uint4* __restrict__ pool, ui
   return decode_premult(c);
 }
 
+// Sort arrays in local memory.
 template <bool Mask>
 struct WalkArrays {
+  static constexpr bool kMask = Mask;
   uint32_t c[kWalkMaxLayers];
   uint32_t d[kWalkMaxLayers];
   uint32_t m[Mask ? kWalkMaxLayers : 1];
+  __device__ __forceinline__ uint32_t& C(int i) { return c[i]; }
+  __device__ __forceinline__ uint32_t& D(int i) { return d[i]; }
+  __device__ __forceinline__ uint32_t& M(int i) { return m[Mask ? i : 0]; }
+};
+
+// Sort arrays whose first KS entries live in a shared-memory column of the
+// thread (entry i at [i * T], so a warp's lanes always hit distinct banks),
+// the rest in local memory (no masks).
+template <int KS>
+struct SplitArrays {
+  static constexpr bool kMask = false;
+  uint32_t* sc;
+  uint32_t* sd;
+  int T;
+  uint32_t lc[kWalkMaxLayers - KS], ld[kWalkMaxLayers - KS], lm;
+  __device__ __forceinline__ uint32_t& C(int i) { return i < KS ? sc[i * T] : lc[i - KS]; }
+  __device__ __forceinline__ uint32_t& D(int i) { return i < KS ? sd[i * T] : ld[i - KS]; }
+  __device__ __forceinline__ uint32_t& M(int) { return lm; }
 };
 
 struct ListWalk {
@@ -64,68 +85,68 @@ struct ListWalk {
   float4 tail;
 };
 
-__device__ __forceinline__ void walk_begin(ListWalk& w, uint32_t head, uint32_t cap) {
-  w.head = head < cap ? head : 0u;
-  w.off = w.head;
-  w.guard = cap;
-  w.k = 0;
-  w.tie = false;
-  w.tail = make_float4(0.f, 0.f, 0.f, 0.f);
-}
-
-// bubbleSort exactly over the first k nodes in list order.
-template <bool F32, bool Mask>
-__device__ __noinline__ void walk_bubble(const uint4* __restrict__ pool, uint32_t head, uint32_t cap, int k,
-                                         WalkArrays<Mask>& a) {
+// bubbleSort exactly (swap on >=) over the first k nodes in list order, read
+// again from the pool.
+template <bool F32, class A>
+__device__ __noinline__ void walk_bubble(const uint4* __restrict__ pool, uint32_t head, uint32_t cap, int k, A& a) {
+  constexpr bool Mask = A::kMask;
   uint32_t o = head;
+#pragma unroll 1
   for (int i = 0; i < k; ++i) {
     const WalkNode n = load_node<F32>(pool, o);
-    a.c[i] = n.c;
-    a.d[i] = n.d;
-    if (Mask) a.m[i] = n.m;
+    a.C(i) = n.c;
+    a.D(i) = n.d;
+    if (Mask) a.M(i) = n.m;
     o = n.next < cap ? n.next : 0u;
   }
+#pragma unroll 1
   for (int i = k - 2; i >= 0; --i)
+#pragma unroll 1
     for (int j = 0; j <= i; ++j) {
-      const uint32_t x = a.d[j], y = a.d[j + 1];
+      const uint32_t x = a.D(j), y = a.D(j + 1);
       if (walk_dge(x, y)) {
-        uint32_t t = a.c[j];
-        a.c[j] = a.c[j + 1];
-        a.c[j + 1] = t;
-        a.d[j] = y;
-        a.d[j + 1] = x;
+        uint32_t t = a.C(j);
+        a.C(j) = a.C(j + 1);
+        a.C(j + 1) = t;
+        a.D(j) = y;
+        a.D(j + 1) = x;
         if (Mask) {
-          t = a.m[j];
-          a.m[j] = a.m[j + 1];
-          a.m[j + 1] = t;
+          t = a.M(j);
+          a.M(j) = a.M(j + 1);
+          a.M(j + 1) = t;
         }
       }
     }
 }
 
-// Consumes node n (the one at w.off).
-template <bool F32, bool Mask>
-__device__ __forceinline__ void walk_step(ListWalk& w, WalkArrays<Mask>& a, const WalkNode& n,
-                                          const uint4* __restrict__ pool, uint32_t cap, int L, int tail) {
+// Consumes node n (the one at w.off). The first OIT_LAYERS nodes are sorted on
+// insertion, each placed before equal depths; equal depths are flagged, and on
+// reaching OIT_LAYERS nodes (or the end of a shorter list) a flagged array is
+// rebuilt by bubbleSort itself. Later nodes go through insertionSortTail.
+template <bool F32, class A>
+__device__ __forceinline__ void walk_step(ListWalk& w, A& a, const WalkNode& n, const uint4* __restrict__ pool,
+                                          uint32_t cap, int L, int tail) {
+  constexpr bool Mask = A::kMask;
   const uint32_t next = n.next < cap ? n.next : 0u;
   if (w.k < L) {
     int pos = w.k;
+#pragma unroll 1
     while (pos > 0) {
-      const uint32_t dp = a.d[pos - 1];
+      const uint32_t dp = a.D(pos - 1);
       if (!walk_dge(dp, n.d)) break;
       w.tie |= !walk_dlt(n.d, dp);  // equal depths
-      a.d[pos] = dp;
-      a.c[pos] = a.c[pos - 1];
-      if (Mask) a.m[pos] = a.m[pos - 1];
+      a.D(pos) = dp;
+      a.C(pos) = a.C(pos - 1);
+      if (Mask) a.M(pos) = a.M(pos - 1);
       --pos;
     }
-    a.d[pos] = n.d;
-    a.c[pos] = n.c;
-    if (Mask) a.m[pos] = n.m;
+    a.D(pos) = n.d;
+    a.C(pos) = n.c;
+    if (Mask) a.M(pos) = n.m;
     ++w.k;
     w.off = next;
     if (w.tie && (w.k == L || next == 0)) {
-      walk_bubble<F32, Mask>(pool, w.head, cap, w.k, a);
+      walk_bubble<F32>(pool, w.head, cap, w.k, a);
       w.tie = false;
     }
     return;
@@ -136,132 +157,59 @@ __device__ __forceinline__ void walk_step(ListWalk& w, WalkArrays<Mask>& a, cons
   }
   --w.guard;
   uint32_t ev = n.c;
-  if (walk_dlt(n.d, a.d[L - 1])) {
-    ev = a.c[L - 1];
+  if (walk_dlt(n.d, a.D(L - 1))) {
+    ev = a.C(L - 1);
     int pos = L - 1;
-    while (pos > 0 && walk_dlt(n.d, a.d[pos - 1])) {
-      a.d[pos] = a.d[pos - 1];
-      a.c[pos] = a.c[pos - 1];
-      if (Mask) a.m[pos] = a.m[pos - 1];
+#pragma unroll 1
+    while (pos > 0 && walk_dlt(n.d, a.D(pos - 1))) {
+      a.D(pos) = a.D(pos - 1);
+      a.C(pos) = a.C(pos - 1);
+      if (Mask) a.M(pos) = a.M(pos - 1);
       --pos;
     }
-    a.d[pos] = n.d;
-    a.c[pos] = n.c;
-    if (Mask) a.m[pos] = n.m;
+    a.D(pos) = n.d;
+    a.C(pos) = n.c;
+    if (Mask) a.M(pos) = n.m;
   }
   // the linked list's tail ignores coverage (oitLinkedList.frag.glsl:137-138)
   if (tail) blend_under(w.tail, node_colour<F32>(pool, ev));
   w.off = next;
 }
 
-// Insertion of node n into the first k entries held in registers (static
-// indices: K slots, the loop fully unrolled), placed before equal depths as
-// the local-array insertion places it; flags equal depths.
-template <int K, bool Mask>
-__device__ __forceinline__ void insert_reg(uint32_t (&rc)[K], uint32_t (&rd)[K], uint32_t (&rm)[Mask ? K : 1], int k,
-                                           const WalkNode& n, bool& tie) {
-  bool placed = false;
-#pragma unroll
-  for (int i = K - 1; i >= 0; --i) {
-    if (i <= k && !placed) {
-      if (i >= 1 && walk_dge(rd[i - 1], n.d)) {
-        tie |= !walk_dlt(n.d, rd[i - 1]);
-        rd[i] = rd[i - 1];
-        rc[i] = rc[i - 1];
-        if (Mask) rm[i] = rm[i - 1];
-      } else {
-        rd[i] = n.d;
-        rc[i] = n.c;
-        if (Mask) rm[i] = n.m;
-        placed = true;
-      }
-    }
-  }
-}
-
-template <bool F32, bool Mask, class Get>
-__device__ __forceinline__ float4 blend_kept(const uint4* __restrict__ pool, int k, int S, Get get) {
+// Walks the list from `head` and returns the composited colour: kept entries
+// front to back (with coverage: per MSAA sample, the entries covering it,
+// averaged over the S samples, oitSimple.frag.glsl:142-159), then the tail.
+template <bool F32, class A>
+__device__ __forceinline__ float4 walk_list(const uint4* __restrict__ pool, uint32_t head, uint32_t cap, int L,
+                                            int tail, int S, A& a) {
+  constexpr bool Mask = A::kMask;
+  ListWalk w;
+  w.head = head < cap ? head : 0u;
+  w.off = w.head;
+  w.guard = cap;
+  w.k = 0;
+  w.tie = false;
+  w.tail = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+  while (w.off != 0) walk_step<F32>(w, a, load_node<F32>(pool, w.off), pool, cap, L, tail);
   float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
   if (!Mask) {
-    for (int i = 0; i < k; ++i) blend_under(sum, node_colour<F32>(pool, get(i).x));
-    return sum;
-  }
-  for (int s = 0; s < S; ++s) {
-    float4 sc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int i = 0; i < k; ++i) {
-      const uint2 e = get(i);
-      if ((e.y >> s) & 1u) blend_under(sc, node_colour<F32>(pool, e.x));
-    }
-    sum.x += sc.x;
-    sum.y += sc.y;
-    sum.z += sc.z;
-    sum.w += sc.w;
-  }
-  const float kk = 1.0f / (float)S;
-  return make_float4(sum.x * kk, sum.y * kk, sum.z * kk, sum.w * kk);
-}
-
-// Walks the whole list from `head` and returns the composited colour: kept
-// entries front to back (with coverage: per MSAA sample, the entries covering
-// it, averaged over the S samples, oitSimple.frag.glsl:142-159), then the tail.
-// Lists of at most min(L, K) nodes without equal depths stay in K registers
-// per array; longer ones continue in the local arrays `a` (K = 0: always).
-template <bool F32, bool Mask, int K = 4>
-__device__ __forceinline__ float4 walk_list(const uint4* __restrict__ pool, uint32_t head, uint32_t cap, int L,
-                                            int tail, int S, WalkArrays<Mask>& a) {
-  constexpr int KR = K > 0 ? K : 1;
-  uint32_t rc[KR], rd[KR], rm[Mask ? KR : 1];
-  ListWalk w;
-  walk_begin(w, head, cap);
-  bool local = K == 0;
-  while (w.off != 0) {
-    const WalkNode n = load_node<F32>(pool, w.off);
-    if (!local && w.k < L && w.k < K) {
-      insert_reg<KR, Mask>(rc, rd, rm, w.k, n, w.tie);
-      ++w.k;
-      w.off = n.next < cap ? n.next : 0u;
-      if (w.tie && (w.k == L || w.off == 0)) {
-        walk_bubble<F32, Mask>(pool, w.head, cap, w.k, a);
-        w.tie = false;
-        local = true;
-      }
-      continue;
-    }
-    if (!local) {
-#pragma unroll
-      for (int i = 0; i < KR; ++i)
-        if (i < w.k) {
-          a.c[i] = rc[i];
-          a.d[i] = rd[i];
-          if (Mask) a.m[i] = rm[i];
-        }
-      local = true;
-    }
-    walk_step<F32, Mask>(w, a, n, pool, cap, L, tail);
-  }
-  float4 sum;
-  if (local) {
-    sum = blend_kept<F32, Mask>(pool, w.k, S, [&](int i) { return make_uint2(a.c[i], Mask ? a.m[i] : 0u); });
+#pragma unroll 1
+    for (int i = 0; i < w.k; ++i) blend_under(sum, node_colour<F32>(pool, a.C(i)));
   } else {
-    sum = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (!Mask) {
-#pragma unroll
-      for (int i = 0; i < KR; ++i)
-        if (i < w.k) blend_under(sum, node_colour<F32>(pool, rc[i]));
-    } else {
-      for (int s = 0; s < S; ++s) {
-        float4 sc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-        for (int i = 0; i < KR; ++i)
-          if (i < w.k && ((rm[i] >> s) & 1u)) blend_under(sc, node_colour<F32>(pool, rc[i]));
-        sum.x += sc.x;
-        sum.y += sc.y;
-        sum.z += sc.z;
-        sum.w += sc.w;
-      }
-      const float kk = 1.0f / (float)S;
-      sum = make_float4(sum.x * kk, sum.y * kk, sum.z * kk, sum.w * kk);
+#pragma unroll 1
+    for (int s = 0; s < S; ++s) {
+      float4 sc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+      for (int i = 0; i < w.k; ++i)
+        if ((a.M(i) >> s) & 1u) blend_under(sc, node_colour<F32>(pool, a.C(i)));
+      sum.x += sc.x;
+      sum.y += sc.y;
+      sum.z += sc.z;
+      sum.w += sc.w;
     }
+    const float kk = 1.0f / (float)S;
+    sum = make_float4(sum.x * kk, sum.y * kk, sum.z * kk, sum.w * kk);
   }
   blend_under(sum, w.tail);
   return sum;

@@ -6,6 +6,8 @@
 // on every run and equal to the CPU oracle's.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -181,6 +183,28 @@ __device__ __forceinline__ void rop_over(float4& dst, const float4& src) {
 }
 
 __device__ __forceinline__ void set_error(uint32_t* err, uint32_t bits) { atomicOr(err, bits); }
+
+// Colour target element: float4, or (OIT_FLAG_HALF_COLOR) four halves.
+__device__ __forceinline__ void store_color(float4* base, bool half, size_t i, float4 c) {
+  if (half) {
+    const __half2 lo = __floats2half2_rn(c.x, c.y), hi = __floats2half2_rn(c.z, c.w);
+    reinterpret_cast<uint2*>(base)[i] =
+        make_uint2(*reinterpret_cast<const uint32_t*>(&lo), *reinterpret_cast<const uint32_t*>(&hi));
+  } else {
+    base[i] = c;
+  }
+}
+
+// Read once by the composite: streaming loads.
+__device__ __forceinline__ float4 load_color(const float4* base, bool half, size_t i) {
+  if (half) {
+    const uint2 v = __ldcs(reinterpret_cast<const uint2*>(base) + i);
+    const float2 lo = __half22float2(*reinterpret_cast<const __half2*>(&v.x));
+    const float2 hi = __half22float2(*reinterpret_cast<const __half2*>(&v.y));
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
+  }
+  return __ldcs(base + i);
+}
 
 // Resolved premultiplied colour to the RGBA8 sRGB output (alpha stays
 // linear), plus the optional linear copy.

@@ -100,6 +100,7 @@ struct RasterParams {
   int has_opaque;                // 0: depth 1.0 and background colour everywhere
   float4 background;
   float4* color;                 // [ssn][P] colour target after tail blend (sample average unless sample shading)
+  int color_half;                // the colour target holds four halves per element
   // algorithm state
   uint32_t* abuf;
   uint32_t* aux;
@@ -135,6 +136,7 @@ struct CompositeParams {
   const uint32_t* abuf;
   const uint32_t* aux;
   const float4* color;           // [ssn][P] (A-buffer algorithms) colour after tail blend
+  int color_half;                // four halves per element
   const float4* opaque_color;    // [S][P] (WBOIT) or null
   int has_opaque;
   float4 background;
@@ -155,6 +157,7 @@ struct ResolveView {
   const uint8_t* lens;           // [mty][mtx] per 8x4 micro-tile fragment counts
   uint32_t P, capacity;
   int W, H, L, kind, tail, mtx, mty;
+  int color_half;
   uint32_t tile_base;            // first global micro-tile index of this view
 };
 
@@ -182,13 +185,12 @@ cudaError_t launch_raster_c(Alg alg, const RasterParams& p, cudaStream_t s);  //
 cudaError_t launch_composite(Alg alg, const CompositeParams& p, cudaStream_t s);
 // Batched resolve: bin the micro-tiles of every view by cost (costliest
 // first), then one persistent launch resolves them all.
-// Kernel variants: Loop64 views, or linked-list views with 0, 4 or 8 register
-// slots for the first sort entries (the rest in local memory).
+// Kernel variants: Loop64 views; linked-list views with their sort arrays in
+// local memory, or with the first 8 entries in a shared-memory column.
 enum ResolveVariant : int {
   kResolveVariantLoop64 = 0,
-  kResolveVariantList0 = 1,
-  kResolveVariantList4 = 2,
-  kResolveVariantList8 = 3,
+  kResolveVariantList = 1,
+  kResolveVariantListShared = 2,
 };
 cudaError_t resolve_bin(const ResolveBatch& b, cudaStream_t s, uint64_t* launches);
 cudaError_t resolve_run(const ResolveBatch& b, int variant, int threads, int blocks, cudaStream_t s);

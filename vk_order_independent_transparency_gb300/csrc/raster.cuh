@@ -796,7 +796,7 @@ __global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
       c.w += tg.col[s].w;
     }
     const float k = 1.0f / (float)S;
-    p.color[elem] = make_float4(c.x * k, c.y * k, c.z * k, c.w * k);
+    store_color(p.color, p.color_half != 0, elem, make_float4(c.x * k, c.y * k, c.z * k, c.w * k));
   }
   if (w.lane == 0 && nfrag && p.frag_count) atomicAdd(p.frag_count, (unsigned long long)nfrag);
   if (SSN == 1 && p.lens) {

@@ -7,21 +7,15 @@
 //                                  the most fragments any of its pixels
 //                                  received (the transparent raster writes
 //                                  it), i.e. the longest list its warp walks.
-//   k_resolve_list<K> /            persistent: every warp resolves micro-tiles
-//   k_resolve_loop64               (one lane per pixel) of one view kind from
-//                                  the work list in a static cyclic order;
-//                                  K = register slots for the first sort
-//                                  entries of a list (0, 4 or 8: the
-//                                  autotuner picks).
+//   k_resolve_list / k_resolve_loop64  persistent: every warp resolves
+//                                  micro-tiles (one lane per pixel) of one
+//                                  view kind from the work list in a static
+//                                  cyclic order.
 //
-// Per pixel the result equals the per-view composite (composite.cu): the
-// linked list's kept entries are the first OIT_LAYERS nodes in list order,
-// ordered as bubbleSort orders them (oitCompositeDefines.glsl:51-89), the
-// rest go through insertionSortTail (:94-139) and are tail blended in
-// eviction order. Here the kept entries are sorted on insertion in a per-
-// thread local array; bubbleSort's swap-on-equal makes its order of equal
-// depths depend on the passes, so a pixel with equal depths among its first
-// OIT_LAYERS nodes re-reads them and runs bubbleSort itself.
+// Per pixel the result equals the per-view composite (composite.cu, the same
+// list walk, list_walk.cuh).
+#include <type_traits>
+
 #include "list_walk.cuh"
 #include "oit_device.cuh"
 #include "oit_internal.h"
@@ -139,16 +133,23 @@ __device__ __forceinline__ float4 resolve_loop64(const ResolveView& v, uint32_t 
   return sum;
 }
 
-// The pixel of lane `lane` in work item `it`, or false outside the view.
+// The pixel of lane `lane` in work item `it`, or false outside the view. A
+// warp's items only move forward through the views, so the view index `vi`
+// (start at 0) is advanced instead of searched unless the list is binned.
 struct ItemPixel {
   const ResolveView* v;
   uint32_t tile, pixel;
 };
 
-__device__ __forceinline__ bool item_pixel(const ResolveBatch& b, const uint32_t* tb, uint32_t it, int lane,
+__device__ __forceinline__ bool item_pixel(const ResolveBatch& b, const uint32_t* tb, uint32_t it, int lane, int& vi,
                                            ItemPixel& o) {
-  const uint32_t g = b.items ? __ldg(b.items + it) : it;
-  const int vi = find_view(tb, b.num_views, g);
+  uint32_t g = it;
+  if (b.items) {
+    g = __ldg(b.items + it);
+    vi = find_view(tb, b.num_views, g);
+  } else {
+    while (vi + 1 < b.num_views && tb[vi + 1] <= g) ++vi;
+  }
   const ResolveView& v = b.views[vi];
   o.v = &v;
   o.tile = g - tb[vi];
@@ -162,21 +163,32 @@ __device__ __forceinline__ bool item_pixel(const ResolveBatch& b, const uint32_t
 // Persistent: every warp resolves micro-tiles (one lane per pixel) from the
 // work list in static cyclic order. One kernel per view kind, so each gets the
 // registers (and the occupancy) its own per-pixel work needs; the linked-list
-// kernel comes with K register slots for the first sort entries.
-template <int K>
+// kernel keeps its sort arrays in local memory, or the first kSplitSlots
+// entries in a shared-memory column (Split).
+constexpr int kSplitSlots = 8;
+
+template <bool Split>
 __global__ void __launch_bounds__(256) k_resolve_list(ResolveBatch b) {
   extern __shared__ __align__(16) uint32_t rsm[];
   load_bases(b, rsm);
   const int lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-  WalkArrays<false> a;
+  using Arrays = typename std::conditional<Split, SplitArrays<kSplitSlots>, WalkArrays<false>>::type;
+  Arrays a;
+  if constexpr (Split) {
+    uint32_t* col = rsm + ((b.num_views + 3) & ~3);
+    a.sc = col + threadIdx.x;
+    a.sd = col + kSplitSlots * blockDim.x + threadIdx.x;
+    a.T = blockDim.x;
+  }
+  int vi = 0;
   for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < b.total_tiles; it += warps) {
     ItemPixel ip;
-    if (!item_pixel(b, rsm, it, lane, ip)) continue;
+    if (!item_pixel(b, rsm, it, lane, vi, ip)) continue;
     const ResolveView& v = *ip.v;
-    float4 c = __ldcs(v.color + ip.pixel);  // read once: streaming
-    const float4 sum = walk_list<false, false, K>(reinterpret_cast<const uint4*>(v.abuf), __ldg(v.aux + ip.pixel),
-                                                   v.capacity, v.L, v.tail, 1, a);
+    float4 c = load_color(v.color, v.color_half != 0, ip.pixel);
+    const float4 sum = walk_list<false>(reinterpret_cast<const uint4*>(v.abuf), __ldg(v.aux + ip.pixel), v.capacity,
+                                        v.L, v.tail, 1, a);
     rop_over(c, sum);
     write_rgba8(v.out, v.out_linear, ip.pixel, c);
   }
@@ -187,11 +199,12 @@ __global__ void __launch_bounds__(256) k_resolve_loop64(ResolveBatch b) {
   load_bases(b, rsm);
   const int lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  int vi = 0;
   for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < b.total_tiles; it += warps) {
     ItemPixel ip;
-    if (!item_pixel(b, rsm, it, lane, ip)) continue;
+    if (!item_pixel(b, rsm, it, lane, vi, ip)) continue;
     const ResolveView& v = *ip.v;
-    float4 c = __ldcs(v.color + ip.pixel);
+    float4 c = load_color(v.color, v.color_half != 0, ip.pixel);
     const uint2 key0 = __ldg(reinterpret_cast<const uint2*>(v.abuf) + ip.pixel);
     const float4 sum = resolve_loop64(v, ip.pixel, key0, min((int)__ldg(v.lens + ip.tile) + 1, v.L));
     rop_over(c, sum);
@@ -199,15 +212,17 @@ __global__ void __launch_bounds__(256) k_resolve_loop64(ResolveBatch b) {
   }
 }
 
-size_t resolve_smem(const ResolveBatch& b) { return (size_t)((b.num_views + 3) & ~3) * 4; }
+size_t resolve_smem(const ResolveBatch& b, int variant, int threads) {
+  const size_t bases = (size_t)((b.num_views + 3) & ~3) * 4;
+  return bases + (variant == kResolveVariantListShared ? (size_t)threads * kSplitSlots * 8 : 0);
+}
 
 template <class F>
 cudaError_t with_kernel(int variant, F f) {
   switch (variant) {
     case kResolveVariantLoop64: return f(k_resolve_loop64);
-    case kResolveVariantList0: return f(k_resolve_list<0>);
-    case kResolveVariantList4: return f(k_resolve_list<4>);
-    case kResolveVariantList8: return f(k_resolve_list<8>);
+    case kResolveVariantList: return f(k_resolve_list<false>);
+    case kResolveVariantListShared: return f(k_resolve_list<true>);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -228,7 +243,7 @@ cudaError_t resolve_bin(const ResolveBatch& b, cudaStream_t s, uint64_t* launche
 }
 
 int resolve_blocks_per_sm(const ResolveBatch& b, int variant, int threads) {
-  const size_t smem = resolve_smem(b);
+  const size_t smem = resolve_smem(b, variant, threads);
   int n = 0;
   const cudaError_t e = with_kernel(variant, [&](auto kern) {
     if (smem > 48 * 1024) {
@@ -245,7 +260,7 @@ cudaError_t resolve_run(const ResolveBatch& b, int variant, int threads, int blo
   if (b.num_views > kResolveMaxViews || threads % 32 != 0 || threads < 32 || threads > 256 || blocks < 1)
     return cudaErrorInvalidValue;
   return with_kernel(variant, [&](auto kern) {
-    kern<<<blocks, threads, resolve_smem(b), s>>>(b);
+    kern<<<blocks, threads, resolve_smem(b, variant, threads), s>>>(b);
     return cudaGetLastError();
   });
 }
