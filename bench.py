@@ -1,9 +1,18 @@
-"""Benchmark of the transparent pass (one step = one whole frame).
+"""Benchmark of the transparent pass.
 
-Default workload: Loop64 k-buffer at 1920x1080, OIT_LAYERS=16, 1024 seeded
-spheres (radii 0.03-0.1) with the first 60% transparent over an opaque depth
-pre-pass, tail blending on. Metric: transparent fragments (after early depth)
-per second, in Mfragments/s; ms_per_step is ms/frame.
+Default workload: the batched multi-view case -- 64 seeded sphere scenes at
+square resolutions log-uniform in 256..2048 with 64..8192 spheres, Linked
+List and Loop64 views with OIT_LAYERS 4..32 -- rendered as one batch with
+RGBA8 records and an FP16 colour target (one CUDA graph, one persistent
+resolve per view kind), against the plain path: one oit_render_frame per view
+with RGBA32F records. One step = the whole batch of 64 frames. Metric:
+transparent fragments (after early depth) per second in Mfragments/s;
+ms_per_step is ms per batch. The line also carries the resolve alone (batched
+vs one FP32 composite launch per view) with its HBM roofline.
+
+Single-view workloads (--workload NAME): Loop64 / Spinlock at 1920x1080,
+Linked List at 640x480, Interlock / Simple with 8x MSAA at 2560x1440, WBOIT at
+3840x2160; one step = one frame.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl gb300|reference]
 
@@ -35,7 +44,7 @@ WORKLOADS = {
 ALGS = ['simple', 'linkedlist', 'loop', 'loop64', 'spinlock', 'interlock', 'weighted']
 SEED = 2
 BATCH_WORKLOAD = 'batch_64views_ll_loop64_mixed_vs_fp32'
-DEFAULT_WORKLOAD = 'loop64_1920x1080_L16_1024spheres_60pct'
+DEFAULT_WORKLOAD = BATCH_WORKLOAD
 
 
 def batch_views(seed=SEED, n=64):
@@ -63,6 +72,8 @@ def parse():
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=5)
     ap.add_argument('--workload', default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [BATCH_WORKLOAD])
+    ap.add_argument('--views', type=int, default=64,
+                    help='batch workload: the first N of its 64 views (smaller cases for profiling)')
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
     return ap.parse_args()
@@ -121,10 +132,39 @@ def cpu_baseline(wd, cores=1, frames=None, budget_s=15.0):
     return frags, wall, res
 
 
+def cpu_baseline_views(views, budget_s=15.0):
+    """Oracle throughput (one process, one core) on whole frames of batch
+    views, smallest first, until about budget_s of CPU work."""
+    import oracle  # noqa: F401
+    ctx = mp.get_context('spawn')
+    order = sorted(views, key=lambda vd: vd['width'] * vd['height'] + 1000 * vd['spheres'])
+    frags, busy, n = 0, 0.0, 0
+    with ctx.Pool(1) as pool:
+        for f, dt in pool.imap(_oracle_frame, [(vd, 1) for vd in order]):
+            frags += f
+            busy += dt
+            n += 1
+            if busy >= budget_s:
+                break
+        pool.terminate()
+    return frags, busy, n
+
+
+def reference_views(step, cores):
+    """The views the reference arm renders in one step of the batch workload:
+    one per core, cycling through the 64."""
+    vs = batch_views(SEED)
+    return [vs[(step * cores + j) % len(vs)] for j in range(cores)]
+
+
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
 class Clocks:
+    """nvidia-smi samples (every 20 ms) of SM clocks and throttle reasons.
+    Started before the warm-up; mark() before and after the timed region
+    delimits the samples that stop() summarises (if the region is shorter
+    than one interval, the first sample after it began)."""
     Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
          'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
          'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
@@ -134,39 +174,56 @@ class Clocks:
         self.proc = None
         self.path = None
 
+    def _rows(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [p.strip() for p in line.split(',')]
+                    if len(parts) >= 9 and line.endswith('\n'):
+                        rows.append(parts)
+        except OSError:
+            pass
+        return rows
+
     def start(self):
         try:
             fd, self.path = tempfile.mkstemp(suffix='.csv')
             os.close(fd)
             self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.dev), '--query-gpu=' + self.Q,
-                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                          '--format=csv,noheader,nounits', '-lms', '20'],
                                          stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        t0 = time.time()
+        while not self._rows() and time.time() - t0 < 5.0 and self.proc.poll() is None:
+            time.sleep(0.01)
 
-    def stop(self):
+    def mark(self):
+        return len(self._rows()) if self.proc else 0
+
+    def stop(self, begin=0, end=None):
         if not self.proc:
             return None
+        if end is not None and end <= begin:
+            time.sleep(0.05)  # region shorter than one interval: take the next sample
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        rows = []
-        with open(self.path) as f:
-            for line in f:
-                parts = [p.strip() for p in line.split(',')]
-                if len(parts) >= 9:
-                    rows.append(parts)
+        rows = self._rows()
         os.unlink(self.path)
-        if not rows:
+        sel = rows[begin:end] if end is not None and end > begin else rows[begin:begin + 1]
+        if not sel:
             return None
-        sm = sorted(float(r[1]) for r in rows if r[1].replace('.', '').isdigit())
-        mx = max((float(r[2]) for r in rows if r[2].replace('.', '').isdigit()), default=None)
+        sm = sorted(float(r[1]) for r in sel if r[1].replace('.', '').isdigit())
+        mx = max((float(r[2]) for r in sel if r[2].replace('.', '').isdigit()), default=None)
         names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
-        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith('active')})
+        reasons = sorted({names[k] for r in sel for k in range(4) if r[5 + k].lower().startswith('active')})
         return {'sm_mhz': sm[len(sm) // 2] if sm else None, 'sm_max_mhz': mx, 'reasons': reasons,
-                'samples': len(rows)}
+                'samples': len(sel), 'interval_ms': 20}
 
 
 # ---------------------------------------------------------------------------
@@ -316,6 +373,8 @@ def run_gpu(a, wd, rank, world):
     def step():
         r.render_frame(mesh, tpo, wd['percent_transparent'], None, stream)
 
+    clocks = Clocks(dev)
+    clocks.start()
     for _ in range(max(3, a.warmup)):
         step()
     torch.cuda.synchronize()
@@ -324,11 +383,10 @@ def run_gpu(a, wd, rank, world):
 
     # device-resident timing
     l0 = r.launch_count()
-    clocks = Clocks(dev)
-    clocks.start()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    m0 = clocks.mark()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record()
@@ -337,9 +395,9 @@ def run_gpu(a, wd, rank, world):
     ev1.record()
     torch.cuda.synchronize()
     elapsed_ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop(m0, clocks.mark())
     if world > 1:
         torch.distributed.barrier()
-    clk = clocks.stop()
     launches = r.launch_count() - l0
 
     # per-pass timing (CUDA events on the launching stream), separate run
@@ -349,23 +407,35 @@ def run_gpu(a, wd, rank, world):
     prof = r.profile_read()
     r.profile_enable(False)
 
-    # end to end through the C ABI with host buffers (pinned), copies inside
-    vh = torch.from_numpy(np.ascontiguousarray(v)).pin_memory().numpy()
-    ih = torch.from_numpy(np.ascontiguousarray(i)).pin_memory().numpy()
+    # end to end through the C ABI with host buffers (pinned), copies inside:
+    # the scene as a template sphere and instance table (what a sphere scene
+    # is), and as the flattened mesh the reference uploads
+    def pinned(x):
+        return torch.from_numpy(np.ascontiguousarray(x)).pin_memory().numpy()
+
+    tv, ti, inst = (pinned(x) for x in oit.make_scene_instanced(
+        wd['spheres'], seed=wd['seed'] + rank, radius_min=wd['radius_min'], radius_max=wd['radius_max']))
+    vh, ih = pinned(v), pinned(i)
     oh = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory().numpy()
-    for _ in range(2):
-        r.render_frame_host(vh, ih, tpo, wd['percent_transparent'], oh, stream)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(a.steps):
-        r.render_frame_host(vh, ih, tpo, wd['percent_transparent'], oh, stream)
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+
+    def e2e_time(frame):
+        for _ in range(2):
+            frame()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            frame()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    e2e_s = e2e_time(lambda: r.render_frame_instanced_host(tv, ti, inst, wd['percent_transparent'], oh, stream))
+    e2e_flat_s = e2e_time(lambda: r.render_frame_host(vh, ih, tpo, wd['percent_transparent'], oh, stream))
 
     kept = count_kept(wd, r)
     tris_t = (i.shape[0] // tpo) * wd['percent_transparent'] // 100 * tpo
     res = dict(elapsed_ms=elapsed_ms, frags=frags, launches=launches, clocks=clk, prof=prof, e2e_s=e2e_s,
-               h2d=int(vh.nbytes + ih.nbytes), d2h=int(oh.nbytes), kept=kept, tris_t=tris_t, r=r)
+               h2d=int(tv.nbytes + ti.nbytes + inst.nbytes), d2h=int(oh.nbytes), kept=kept, tris_t=tris_t, r=r,
+               e2e_flat_s=e2e_flat_s, h2d_flat=int(vh.nbytes + ih.nbytes))
     return res
 
 
@@ -379,7 +449,7 @@ def run_batch(a, rank):
     _build.build()
     torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
     stream = torch.cuda.current_stream().cuda_stream
-    vs = batch_views(SEED + rank)
+    vs = batch_views(SEED + rank)[:a.views]
     mixed, plain, meshes, host = [], [], [], []
     for vd in vs:
         v, i, tpo = oit.make_scene(vd['spheres'], seed=vd['seed'], radius_min=vd['radius_min'],
@@ -429,43 +499,81 @@ def run_batch(a, rank):
 
     clocks = Clocks(int(os.environ.get('LOCAL_RANK', '0')))
     clocks.start()
+    step_mixed()
+    torch.cuda.synchronize()
+    m0 = clocks.mark()
+    torch.cuda.nvtx.range_push('batched_frames')
     t_mixed = timed(step_mixed)
-    clk = clocks.stop()
+    torch.cuda.nvtx.range_pop()
+    clk = clocks.stop(m0, clocks.mark())
+    torch.cuda.nvtx.range_push('plain_frames')
     t_plain = timed(step_plain)
+    torch.cuda.nvtx.range_pop()
     launches = batch.launch_count() * a.steps
 
-    # per-pass times: every view rendered alone with section timing
+    # per-pass times: every view rendered alone with section timing, and the
+    # transparent raster's algorithmic bytes summed over the views
     sections = {}
-    for r, m, h in zip(mixed, meshes, host):
+    raster_bytes = 0
+    for r, m, h, vd in zip(mixed, meshes, host, vs):
         r.profile_enable(True)
         r.render_frame(m, h[2], 100, None, stream)
         for k, (ms, n) in r.profile_read().items():
             if n:
                 sections[k] = sections.get(k, 0.0) + ms / n
         r.profile_enable(False)
+        vw = dict(vd, workload=BATCH_WORKLOAD)
+        raster_bytes += kernel_bytes(vw, r, r.fragment_count(), 0, 0, h[1].shape[0])[0]
 
-    # end to end: every view's mesh from pinned host memory, the batch, every image back
+    # end to end: every view's scene from pinned host memory, the batch, every
+    # image back. The scene as template + instance table (what the sphere
+    # scenes are), and as flattened meshes (what the reference uploads)
+    outs = [torch.empty((vd['height'], vd['width'], 4), dtype=torch.uint8).pin_memory() for vd in vs]
+    d2h = sum(o.nbytes for o in outs)
+    inst_dev, inst_host = [], []
+    for vd in vs:
+        tmpl = oit.make_scene_instanced(vd['spheres'], seed=vd['seed'], radius_min=vd['radius_min'],
+                                        radius_max=vd['radius_max'])
+        inst_dev.append(oit.DeviceInstancedMesh(*tmpl))
+        inst_host.append(tuple(torch.from_numpy(np.ascontiguousarray(x).view(np.int32)).pin_memory() for x in tmpl))
+    batch_inst = oit.Batch(parallel_streams=8)
+    batch_inst.set_views([(r, m, 0, 100) for r, m in zip(mixed, inst_dev)])
+    h2d = sum(x.nbytes for t in inst_host for x in t)
     hv = [(torch.from_numpy(np.ascontiguousarray(v)).pin_memory(), torch.from_numpy(
         np.ascontiguousarray(i).view(np.int32)).pin_memory()) for v, i, _ in host]
-    outs = [torch.empty((vd['height'], vd['width'], 4), dtype=torch.uint8).pin_memory() for vd in vs]
-    h2d = sum(x.nbytes + y.nbytes for x, y in hv)
-    d2h = sum(o.nbytes for o in outs)
+    h2d_flat = sum(x.nbytes + y.nbytes for x, y in hv)
 
-    def step_e2e():
-        for (x, y), m in zip(hv, meshes):
-            m.vertices.copy_(x, non_blocking=True)
-            m.indices.copy_(y, non_blocking=True)
-        batch.render(stream)
-        for r, o, vd in zip(mixed, outs, vs):
+    def images_back():
+        for r, o in zip(mixed, outs):
             ptr, nb = r.buffer(oit.OIT_BUF_OUTPUT)
             _copy_d2h(o, ptr, nb, stream)
         torch.cuda.current_stream().synchronize()
 
-    step_e2e()
-    t0 = time.perf_counter()
-    for _ in range(a.steps):
-        step_e2e()
-    e2e_s = time.perf_counter() - t0
+    def step_e2e():
+        for (tv, ti, inst), m in zip(inst_host, inst_dev):
+            m.template_vertices.view(torch.int32).copy_(tv, non_blocking=True)
+            m.template_indices.copy_(ti, non_blocking=True)
+            m.instances.view(torch.int32).copy_(inst, non_blocking=True)
+        batch_inst.render(stream)
+        images_back()
+
+    def step_e2e_flat():
+        for (x, y), m in zip(hv, meshes):
+            m.vertices.copy_(x, non_blocking=True)
+            m.indices.copy_(y, non_blocking=True)
+        batch.render(stream)
+        images_back()
+
+    def e2e_time(step):
+        step()
+        step()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            step()
+        return time.perf_counter() - t0
+
+    e2e_s = e2e_time(step_e2e)
+    e2e_flat_s = e2e_time(step_e2e_flat)
 
     # resolve alone: the batched persistent resolve of the mixed views against
     # one FP32-record composite launch per view, on the frames rendered above
@@ -482,13 +590,19 @@ def run_batch(a, rank):
     for _ in range(max(3, a.warmup)):
         step_resolve_mixed()
         step_resolve_plain()
+    # NVTX ranges name the timed regions for profilers (ncu --nvtx-include)
+    torch.cuda.nvtx.range_push('batched_resolve')
     t_res_mixed = timed(step_resolve_mixed)
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.nvtx.range_push('plain_resolve')
     t_res_plain = timed(step_resolve_plain)
+    torch.cuda.nvtx.range_pop()
     res_cfg = batch.resolve_config()
     res_bytes = resolve_bytes(vs, mixed)
     return dict(frags=frags, t_mixed=t_mixed, t_plain=t_plain, launches=launches, clocks=clk, sections=sections,
                 e2e_s=e2e_s, h2d=h2d, d2h=d2h, views=vs, t_res_mixed=t_res_mixed, t_res_plain=t_res_plain,
-                res_cfg=res_cfg, res_bytes=res_bytes)
+                res_cfg=res_cfg, res_bytes=res_bytes, e2e_flat_s=e2e_flat_s, h2d_flat=h2d_flat,
+                raster_bytes=raster_bytes)
 
 
 def _copy_d2h(host_tensor, dev_ptr, nbytes, stream):
@@ -514,8 +628,13 @@ def reduce_replicas(maxes, sums, world, device='cuda'):
 
 def main_batch(a, rank, world):
     res = run_batch(a, rank)
-    (t_mixed, t_plain, e2e_s, t_res_mixed, t_res_plain), (total,) = reduce_replicas(
-        [res['t_mixed'], res['t_plain'], res['e2e_s'], res['t_res_mixed'], res['t_res_plain']],
+    cpu_line = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        f, busy, n = cpu_baseline_views(res['views'])
+        cpu_line = {'value': round(f / busy / 1e6, 4), 'unit': 'Mfragments/s', 'cores': 1, 'kind': 'port',
+                    'sample': '%d of the 64 views (the smallest), whole frames, single-threaded FP64 oracle' % n}
+    (t_mixed, t_plain, e2e_s, t_res_mixed, t_res_plain, e2e_flat_s), (total,) = reduce_replicas(
+        [res['t_mixed'], res['t_plain'], res['e2e_s'], res['t_res_mixed'], res['t_res_plain'], res['e2e_flat_s']],
         [res['frags'] * a.steps], world)
     if rank != 0:
         return
@@ -529,7 +648,7 @@ def main_batch(a, rank, world):
         'steps': a.steps, 'warmup': a.warmup, 'ms_per_step': round(t_mixed / a.steps, 4), 'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'rgba8 records, f16 colour target, f32 blend',
         'data': 'synthetic: 64 seeded UV-sphere scenes, inputs resident in HBM',
-        'config': dict(workload_dict(BATCH_WORKLOAD), fragments_per_batch=res['frags'],
+        'config': dict(workload_dict(BATCH_WORKLOAD), views=len(res['views']), fragments_per_batch=res['frags'],
                        parallelism='replicas' if world > 1 else 'single',
                        frame='all 64 views in one CUDA graph, 8 parallel streams',
                        l2='working set larger than L2, no flush'),
@@ -537,17 +656,35 @@ def main_batch(a, rank, world):
                        'path': 'one oit_render_frame per view, RGBA32F records, no graph'},
         'speedup_vs_plain_fp32': round(value / plain, 3),
         'e2e': {'value': round(total / e2e_s / 1e6, 3), 'unit': 'Mfragments/s', 'h2d_bytes_per_step': res['h2d'],
-                'd2h_bytes_per_step': res['d2h'], 'ms_per_step': round(e2e_s / a.steps * 1e3, 4)},
-        'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': None, 'peak': peak, 'unit': 'GB/s', 'frac': None,
-                     'traffic': None, 'peak_source': peak_kind, 'note': 'per-pass times summed over views; see the '
-                     'single-view workloads for per-kernel roofline fractions'},
+                'd2h_bytes_per_step': res['d2h'], 'ms_per_step': round(e2e_s / a.steps * 1e3, 4),
+                'path': 'oit_batch_render over instanced views: templates + instance tables in, 64 RGBA8 images out'},
+        'e2e_flat_mesh': {'value': round(total / e2e_flat_s / 1e6, 3), 'unit': 'Mfragments/s',
+                          'h2d_bytes_per_step': res['h2d_flat'], 'd2h_bytes_per_step': res['d2h'],
+                          'ms_per_step': round(e2e_flat_s / a.steps * 1e3, 4),
+                          'path': 'oit_batch_render over flattened meshes uploaded every step'},
+        'roofline': raster_roofline(res, sec, peak, peak_kind),
         'kernels': {k: {'ms_sum_over_views': round(v, 4)} for k, v in sec.items()},
         'resolve': resolve_line(res, a, world, total, t_res_mixed, t_res_plain, peak, peak_kind),
-        'cpu_baseline': None,
+        'cpu_baseline': cpu_line,
         'clocks': res['clocks'],
         'gpu_launches': int(res['launches']),
     }
     print(json.dumps(line))
+
+
+def raster_roofline(res, sec, peak, peak_kind):
+    """The batch's dominant kernel, the transparent raster: its algorithmic
+    bytes summed over the 64 views over its CUDA-event time summed over the
+    views (each rendered alone)."""
+    ms = sec.get('transparent_raster', 0.0)
+    gbs = res['raster_bytes'] / (ms * 1e-3) / 1e9 if ms else None
+    return {'bound': 'hbm', 'kernel': 'k_raster_transparent (summed over the 64 views)',
+            'achieved': round(gbs, 1) if gbs else None, 'peak': peak, 'unit': 'GB/s',
+            'frac': round(gbs / peak, 4) if gbs else None, 'traffic': None,
+            'bytes_per_step': int(res['raster_bytes']), 'ms_per_step_summed': round(ms, 4),
+            'peak_source': peak_kind,
+            'note': 'an integer/float raster bound by issue and latency, not by HBM; the resolve below is the '
+                    'HBM-bound pass'}
 
 
 def resolve_line(res, a, world, total, t_mixed, t_plain, peak, peak_kind):
@@ -583,13 +720,24 @@ def main():
         if rank != 0:
             return
         cores = os.cpu_count() or 1
-        # one step = every core renders one whole frame of the workload
-        for _ in range(max(0, min(a.warmup, 1))):
-            cpu_baseline(wd, cores=cores, frames=cores)
+        batch = a.workload == BATCH_WORKLOAD
+
+        def ref_step(k):
+            # one step = every core renders one whole frame of the workload
+            # (batch: one view of the batch per core)
+            import oracle  # noqa: F401
+            args = [(vd, 1) for vd in reference_views(k, cores)] if batch else [(wd, 1)] * cores
+            t0 = time.perf_counter()
+            with mp.get_context('spawn').Pool(cores) as pool:
+                res = pool.map(_oracle_frame, args)
+            return sum(r[0] for r in res), time.perf_counter() - t0
+
+        for k in range(max(0, min(a.warmup, 1))):
+            ref_step(k)
         frags = 0
         wall = 0.0
-        for _ in range(a.steps):
-            f, w, _ = cpu_baseline(wd, cores=cores, frames=cores)
+        for k in range(a.steps):
+            f, w = ref_step(k)
             frags += f
             wall += w
         value = frags / wall / 1e6
@@ -599,7 +747,8 @@ def main():
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64 blend',
             'data': 'synthetic: seeded UV-sphere scene', 'config': wd,
             'cpu_baseline': {'value': round(value, 4), 'unit': 'Mfragments/s', 'cores': cores, 'kind': 'port',
-                             'sample': '%d whole frames per step, one per core' % cores},
+                             'sample': '%d whole frames per step, one per core%s' % (
+                                 cores, ' (batch views in turn)' if batch else '')},
             'e2e': {'value': round(value, 4), 'unit': 'Mfragments/s', 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0},
             'note': 'reference Vulkan build unavailable on this box (no graphics stack); CPU restatement of the '
@@ -617,7 +766,8 @@ def main():
             torch.distributed.destroy_process_group()
         return
     res = run_gpu(a, wd, rank, world)
-    (t_ms, e2e_s), (frags_all,) = reduce_replicas([res['elapsed_ms'], res['e2e_s']], [res['frags'] * a.steps], world)
+    (t_ms, e2e_s, e2e_flat_s), (frags_all,) = reduce_replicas([res['elapsed_ms'], res['e2e_s'], res['e2e_flat_s']],
+                                                              [res['frags'] * a.steps], world)
     if rank != 0:
         torch.distributed.destroy_process_group()
         return
@@ -663,7 +813,12 @@ def main():
                        frame='one CUDA graph per frame (opaque + transparent binning, rasters, composite)',
                        l2='working set larger than L2 (A-buffer + triangle setup > 129 MB), no flush'),
         'e2e': {'value': round(e2e_value, 3), 'unit': 'Mfragments/s', 'h2d_bytes_per_step': res['h2d'],
-                'd2h_bytes_per_step': res['d2h'], 'ms_per_step': round(e2e_s / a.steps * 1e3, 4)},
+                'd2h_bytes_per_step': res['d2h'], 'ms_per_step': round(e2e_s / a.steps * 1e3, 4),
+                'path': 'oit_render_frame_instanced_host: template sphere + instance table in, RGBA8 out'},
+        'e2e_flat_mesh': {'value': round(frags_all / e2e_flat_s / 1e6, 3), 'unit': 'Mfragments/s',
+                          'h2d_bytes_per_step': res['h2d_flat'], 'd2h_bytes_per_step': res['d2h'],
+                          'ms_per_step': round(e2e_flat_s / a.steps * 1e3, 4),
+                          'path': 'oit_render_frame_host: flattened vertex + index buffers in, RGBA8 out'},
         'roofline': roofline,
         'kernels': kernels,
         'cpu_baseline': cpu,

@@ -247,13 +247,16 @@ int oit_render_frame_noalloc(const oit_state* state, const oit_scene_data* scene
 /* ---- batched views ----------------------------------------------------- */
 
 /* One view of a batch: a context (own resolution, algorithm, OIT_LAYERS, record
- * format), its mesh and the frame parameters of oit_render_frame. */
+ * format), its mesh and the frame parameters of oit_render_frame. A view with
+ * an instanced mesh sets instanced_mesh (and leaves mesh NULL); its objects
+ * are its instances and triangles_per_object is ignored. */
 typedef struct oit_view_frame {
   oit_context* ctx;
   const oit_mesh* mesh;
   uint32_t triangles_per_object;
   int32_t percent_transparent;
   uint8_t* out_rgba8_device;  /* NULL = the view context's OIT_BUF_OUTPUT */
+  const oit_instanced_mesh* instanced_mesh;
 } oit_view_frame;
 
 typedef struct oit_batch oit_batch;
@@ -287,11 +290,12 @@ int oit_batch_resolve(oit_batch* batch, const oit_view_frame* views, uint32_t nu
 
 /* The shape the autotuner picked for one part of the batched resolve (part 0:
  * linked-list views, 1: Loop64 views): threads per block, blocks, binned (1)
- * or view-order (0) work list, and the sort-array entries per thread held in
- * shared memory (0 or 8; the rest live in local memory). A part without views
- * reports zeros. OIT_ERR_STATE before the first resolve. */
+ * or view-order (0) work list, the sort-array entries per thread held in
+ * shared memory (0 or 8; the rest live in local memory), and the micro-tiles a
+ * warp takes per step (1 or 2). A part without views reports zeros.
+ * OIT_ERR_STATE before the first resolve. */
 int oit_batch_resolve_config(oit_batch* batch, uint32_t part, uint32_t* threads_per_block, uint32_t* blocks,
-                             int32_t* binned, int32_t* shared_slots);
+                             int32_t* binned, int32_t* shared_slots, int32_t* items_per_step);
 
 /* ---- inspection -------------------------------------------------------- */
 

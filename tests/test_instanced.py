@@ -115,3 +115,26 @@ def test_instanced_invalid_arguments():
         assert lib.oit_render_frame_instanced(r._ctx, None, 100, None, None) == oit.OIT_ERR_INVALID_ARGUMENT
         r.render_frame_instanced(m)
         assert r.get_error() == 0
+
+
+@pytest.mark.gpu
+def test_batch_with_instanced_views():
+    """Batch views may carry instanced meshes: each view's image equals its
+    flattened mesh rendered alone."""
+    specs = [(oit.OIT_LINKEDLIST, 120, 90, 8, 0), (oit.OIT_LOOP64, 96, 96, 4, 0),
+             (oit.OIT_INTERLOCK, 80, 64, 8, oit.OIT_AA_MSAA_4X)]
+    views, refs = [], []
+    for k, (alg, W, H, L, aa) in enumerate(specs):
+        kw = dict(seed=40 + k, radius_min=0.05, radius_max=0.2)
+        flat = oit.make_scene(60, **kw)
+        refs.append(_frame(alg, W, H, flat, False, 80, aa_type=aa, oit_layers=L, nodes_per_pixel=10)['out'])
+        r = oit.Renderer(oit.make_state(alg, W, H, aa_type=aa, oit_layers=L, nodes_per_pixel=10))
+        r.update_scene(oit.make_camera(W, H))
+        views.append((r, oit.DeviceInstancedMesh(*oit.make_scene_instanced(60, **kw)), 0, 80))
+    batch = oit.Batch(parallel_streams=2)
+    batch.set_views(views)
+    for _ in range(3):
+        batch.render()
+        for (r, _, _, _), ref in zip(views, refs):
+            np.testing.assert_array_equal(r.read_buffer(oit.OIT_BUF_OUTPUT), ref)
+            assert r.get_error() == 0

@@ -90,7 +90,8 @@ class OitSceneDesc(ctypes.Structure):
 
 class OitViewFrame(ctypes.Structure):
     _fields_ = [('ctx', ctypes.c_void_p), ('mesh', ctypes.POINTER(OitMesh)), ('triangles_per_object', ctypes.c_uint32),
-                ('percent_transparent', ctypes.c_int32), ('out_rgba8_device', ctypes.c_void_p)]
+                ('percent_transparent', ctypes.c_int32), ('out_rgba8_device', ctypes.c_void_p),
+                ('instanced_mesh', ctypes.POINTER(OitInstancedMesh))]
 
 
 class OitError(RuntimeError):
@@ -153,7 +154,7 @@ def library():
         'oit_scene_generate_instanced': (I, [ctypes.POINTER(OitSceneDesc), P, P, P]),
         'oit_batch_resolve': (I, [P, ctypes.POINTER(OitViewFrame), U, P]),
         'oit_batch_resolve_config': (I, [P, U, ctypes.POINTER(U), ctypes.POINTER(U), ctypes.POINTER(ctypes.c_int32),
-                                         ctypes.POINTER(ctypes.c_int32)]),
+                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -441,11 +442,15 @@ class Batch:
             pass
 
     def set_views(self, views):
-        """views: list of (Renderer, DeviceMesh, triangles_per_object, percent_transparent)."""
+        """views: list of (Renderer, DeviceMesh or DeviceInstancedMesh,
+        triangles_per_object, percent_transparent)."""
         arr = (OitViewFrame * len(views))()
         for k, (r, mesh, tpo, pct) in enumerate(views):
             arr[k].ctx = r._ctx.value
-            arr[k].mesh = ctypes.pointer(mesh.c)
+            if isinstance(mesh, DeviceInstancedMesh):
+                arr[k].instanced_mesh = ctypes.pointer(mesh.c)
+            else:
+                arr[k].mesh = ctypes.pointer(mesh.c)
             arr[k].triangles_per_object = tpo
             arr[k].percent_transparent = pct
             arr[k].out_rgba8_device = None
@@ -471,11 +476,11 @@ class Batch:
         list, register slots for the first sort entries)."""
         out = {}
         for part, name in ((0, 'linkedlist'), (1, 'loop64')):
-            t, n, b, k = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_int32(), ctypes.c_int32()
+            t, n, b, k, u = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
             _check(self.lib.oit_batch_resolve_config(self._b, part, ctypes.byref(t), ctypes.byref(n), ctypes.byref(b),
-                                                     ctypes.byref(k)), 'oit_batch_resolve_config')
+                                                     ctypes.byref(k), ctypes.byref(u)), 'oit_batch_resolve_config')
             out[name] = {'threads_per_block': t.value, 'blocks': n.value, 'binned': bool(b.value),
-                         'shared_slots': k.value}
+                         'shared_slots': k.value, 'items_per_step': u.value}
         return out
 
 

@@ -878,7 +878,8 @@ int batch_resolve_launch(oit_batch* b, cudaStream_t s, uint64_t* launches) {
 }
 
 // The autotuner, per part: kernel variant (linked lists: sort arrays in local
-// memory, or the first 8 entries in shared memory), block size and binned versus view-order
+// memory, or the first 8 entries in shared memory; one or two micro-tiles per
+// warp step), block size and binned versus view-order
 // work lists, each timed with CUDA events on the batch's current frames (the
 // resolve only writes the outputs, so reruns are harmless); the grid holds
 // every block that fits. The fastest shape is kept for the batch's views.
@@ -893,8 +894,8 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
     if (rp.rb.num_views == 0) continue;
     float best = 1e30f;
     std::vector<int> variants;
-    if (part == 0) variants = {oit::kResolveVariantList, oit::kResolveVariantListShared};
-    else variants = {oit::kResolveVariantLoop64};
+    if (part == 0) variants = {oit::kResolveVariantList, oit::kResolveVariantListShared, oit::kResolveVariantListx2};
+    else variants = {oit::kResolveVariantLoop64, oit::kResolveVariantLoop64x2};
     for (int variant : variants) {
       for (int threads : {64, 128, 256}) {
         const int bps = oit::resolve_blocks_per_sm(rp.rb, variant, threads);
@@ -1107,6 +1108,14 @@ int oit_render_frame_host(oit_context* ctx, const float* vertices, uint32_t num_
   return OIT_OK;
 }
 
+static oit::MeshRef view_mesh(const oit_view_frame& v) {
+  return v.instanced_mesh ? instanced_ref(v.instanced_mesh) : mesh_ref(v.mesh);
+}
+
+static uint32_t view_tpo(const oit_view_frame& v) {
+  return v.instanced_mesh ? v.instanced_mesh->template_triangles : v.triangles_per_object;
+}
+
 int oit_render_frame_instanced(oit_context* ctx, const oit_instanced_mesh* mesh, int32_t percent, uint8_t* out,
                                void* stream) {
   if (!ctx || !instanced_ok(mesh)) return OIT_ERR_INVALID_ARGUMENT;
@@ -1187,14 +1196,17 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
   uint64_t sig = 1469598103934665603ull;
   for (uint32_t i = 0; i < n; ++i) {
     const oit_view_frame& v = views[i];
-    if (!v.ctx || !v.mesh || !v.triangles_per_object || v.percent_transparent < 0) return OIT_ERR_INVALID_ARGUMENT;
+    if (!v.ctx || v.percent_transparent < 0) return OIT_ERR_INVALID_ARGUMENT;
+    if (v.instanced_mesh ? !instanced_ok(v.instanced_mesh) : (!v.mesh || !v.triangles_per_object))
+      return OIT_ERR_INVALID_ARGUMENT;
     if (!v.ctx->has_scene) return OIT_ERR_STATE;
-    if (!mesh_ok(v.mesh, 0, v.mesh->num_triangles)) return OIT_ERR_INVALID_ARGUMENT;
+    if (!v.instanced_mesh && !mesh_ok(v.mesh, 0, v.mesh->num_triangles)) return OIT_ERR_INVALID_ARGUMENT;
     for (uint32_t j = 0; j < i; ++j)
       if (views[j].ctx == v.ctx) return OIT_ERR_INVALID_ARGUMENT;  // one frame per context
-    const uint64_t parts[] = {(uint64_t)(uintptr_t)v.ctx, (uint64_t)(uintptr_t)v.mesh->vertices_device,
-                              (uint64_t)(uintptr_t)v.mesh->indices_device, v.mesh->num_triangles,
-                              v.triangles_per_object, (uint64_t)v.percent_transparent,
+    const oit::MeshRef m = view_mesh(v);
+    const uint64_t parts[] = {(uint64_t)(uintptr_t)v.ctx, (uint64_t)(uintptr_t)m.vertices,
+                              (uint64_t)(uintptr_t)m.indices, (uint64_t)(uintptr_t)m.instances, m.num_triangles,
+                              view_tpo(v), (uint64_t)v.percent_transparent,
                               (uint64_t)(uintptr_t)v.out_rgba8_device};
     for (uint64_t x : parts) sig = (sig ^ x) * 1099511628211ull;
   }
@@ -1207,7 +1219,7 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
     // batched resolve handles are resolved together afterwards
     for (uint32_t i = 0; i < n; ++i) {
       const oit_view_frame& v = views[i];
-      int r = v.ctx->render_frame_body(mesh_ref(v.mesh), v.triangles_per_object, v.percent_transparent,
+      int r = v.ctx->render_frame_body(view_mesh(v), view_tpo(v), v.percent_transparent,
                                        v.out_rgba8_device, s, !v.ctx->batch_resolvable());
       if (r != OIT_OK) return r;
     }
@@ -1231,7 +1243,7 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
       const uint64_t l0 = c->launches;
       c->graph_stats.clear();
       c->capturing = true;
-      r = c->render_frame_body(mesh_ref(v.mesh), v.triangles_per_object, v.percent_transparent, v.out_rgba8_device,
+      r = c->render_frame_body(view_mesh(v), view_tpo(v), v.percent_transparent, v.out_rgba8_device,
                                b->lanes[i % K], !c->batch_resolvable());
       c->capturing = false;
       nodes += c->launches - l0;
@@ -1300,8 +1312,9 @@ int oit_batch_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n, voi
 }
 
 int oit_batch_resolve_config(oit_batch* b, uint32_t part, uint32_t* threads_per_block, uint32_t* blocks,
-                             int32_t* binned, int32_t* shared_slots) {
-  if (!b || part > 1 || !threads_per_block || !blocks || !binned || !shared_slots) return OIT_ERR_INVALID_ARGUMENT;
+                             int32_t* binned, int32_t* shared_slots, int32_t* items_per_step) {
+  if (!b || part > 1 || !threads_per_block || !blocks || !binned || !shared_slots || !items_per_step)
+    return OIT_ERR_INVALID_ARGUMENT;
   if (!b->r_tuned) return OIT_ERR_STATE;
   const oit_batch::ResolvePart& rp = b->rparts[part];
   const bool any = rp.rb.num_views > 0;
@@ -1309,6 +1322,7 @@ int oit_batch_resolve_config(oit_batch* b, uint32_t part, uint32_t* threads_per_
   *blocks = any ? (uint32_t)rp.blocks : 0u;
   *binned = any && rp.binned ? 1 : 0;
   *shared_slots = rp.variant == oit::kResolveVariantListShared ? 8 : 0;
+  *items_per_step = (rp.variant == oit::kResolveVariantListx2 || rp.variant == oit::kResolveVariantLoop64x2) ? 2 : 1;
   return OIT_OK;
 }
 

@@ -186,11 +186,14 @@ cudaError_t launch_composite(Alg alg, const CompositeParams& p, cudaStream_t s);
 // Batched resolve: bin the micro-tiles of every view by cost (costliest
 // first), then one persistent launch resolves them all.
 // Kernel variants: Loop64 views; linked-list views with their sort arrays in
-// local memory, or with the first 8 entries in a shared-memory column.
+// local memory, or with the first 8 entries in a shared-memory column; one or
+// two micro-tiles per warp step.
 enum ResolveVariant : int {
   kResolveVariantLoop64 = 0,
   kResolveVariantList = 1,
   kResolveVariantListShared = 2,
+  kResolveVariantListx2 = 3,    // two micro-tiles per warp step
+  kResolveVariantLoop64x2 = 4,  // two micro-tiles per warp step
 };
 cudaError_t resolve_bin(const ResolveBatch& b, cudaStream_t s, uint64_t* launches);
 cudaError_t resolve_run(const ResolveBatch& b, int variant, int threads, int blocks, cudaStream_t s);

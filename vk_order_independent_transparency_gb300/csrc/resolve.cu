@@ -167,7 +167,9 @@ __device__ __forceinline__ bool item_pixel(const ResolveBatch& b, const uint32_t
 // entries in a shared-memory column (Split).
 constexpr int kSplitSlots = 8;
 
-template <bool Split>
+// U micro-tiles per step: the independent first loads of all U (colour
+// target, list head) are issued before any list is walked.
+template <bool Split, int U>
 __global__ void __launch_bounds__(256) k_resolve_list(ResolveBatch b) {
   extern __shared__ __align__(16) uint32_t rsm[];
   load_bases(b, rsm);
@@ -182,33 +184,64 @@ __global__ void __launch_bounds__(256) k_resolve_list(ResolveBatch b) {
     a.T = blockDim.x;
   }
   int vi = 0;
-  for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < b.total_tiles; it += warps) {
-    ItemPixel ip;
-    if (!item_pixel(b, rsm, it, lane, vi, ip)) continue;
-    const ResolveView& v = *ip.v;
-    float4 c = load_color(v.color, v.color_half != 0, ip.pixel);
-    const float4 sum = walk_list<false>(reinterpret_cast<const uint4*>(v.abuf), __ldg(v.aux + ip.pixel), v.capacity,
-                                        v.L, v.tail, 1, a);
-    rop_over(c, sum);
-    write_rgba8(v.out, v.out_linear, ip.pixel, c);
+  for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < b.total_tiles; it += U * warps) {
+    ItemPixel ip[U];
+    bool ok[U];
+    float4 c[U];
+    uint32_t head[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t iu = it + u * warps;
+      ok[u] = iu < b.total_tiles && item_pixel(b, rsm, iu, lane, vi, ip[u]);
+      if (ok[u]) {
+        c[u] = load_color(ip[u].v->color, ip[u].v->color_half != 0, ip[u].pixel);
+        head[u] = __ldg(ip[u].v->aux + ip[u].pixel);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (!ok[u]) continue;
+      const ResolveView& v = *ip[u].v;
+      const float4 sum =
+          walk_list<false>(reinterpret_cast<const uint4*>(v.abuf), head[u], v.capacity, v.L, v.tail, 1, a);
+      rop_over(c[u], sum);
+      write_rgba8(v.out, v.out_linear, ip[u].pixel, c[u]);
+    }
   }
 }
 
+template <int U>
 __global__ void __launch_bounds__(256) k_resolve_loop64(ResolveBatch b) {
   extern __shared__ __align__(16) uint32_t rsm[];
   load_bases(b, rsm);
   const int lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   int vi = 0;
-  for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < b.total_tiles; it += warps) {
-    ItemPixel ip;
-    if (!item_pixel(b, rsm, it, lane, vi, ip)) continue;
-    const ResolveView& v = *ip.v;
-    float4 c = load_color(v.color, v.color_half != 0, ip.pixel);
-    const uint2 key0 = __ldg(reinterpret_cast<const uint2*>(v.abuf) + ip.pixel);
-    const float4 sum = resolve_loop64(v, ip.pixel, key0, min((int)__ldg(v.lens + ip.tile) + 1, v.L));
-    rop_over(c, sum);
-    write_rgba8(v.out, v.out_linear, ip.pixel, c);
+  for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < b.total_tiles; it += U * warps) {
+    ItemPixel ip[U];
+    bool ok[U];
+    float4 c[U];
+    uint2 key0[U];
+    int nmax[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t iu = it + u * warps;
+      ok[u] = iu < b.total_tiles && item_pixel(b, rsm, iu, lane, vi, ip[u]);
+      if (ok[u]) {
+        const ResolveView& v = *ip[u].v;
+        c[u] = load_color(v.color, v.color_half != 0, ip[u].pixel);
+        key0[u] = __ldg(reinterpret_cast<const uint2*>(v.abuf) + ip[u].pixel);
+        nmax[u] = min((int)__ldg(v.lens + ip[u].tile) + 1, v.L);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (!ok[u]) continue;
+      const ResolveView& v = *ip[u].v;
+      const float4 sum = resolve_loop64(v, ip[u].pixel, key0[u], nmax[u]);
+      rop_over(c[u], sum);
+      write_rgba8(v.out, v.out_linear, ip[u].pixel, c[u]);
+    }
   }
 }
 
@@ -220,9 +253,11 @@ size_t resolve_smem(const ResolveBatch& b, int variant, int threads) {
 template <class F>
 cudaError_t with_kernel(int variant, F f) {
   switch (variant) {
-    case kResolveVariantLoop64: return f(k_resolve_loop64);
-    case kResolveVariantList: return f(k_resolve_list<false>);
-    case kResolveVariantListShared: return f(k_resolve_list<true>);
+    case kResolveVariantLoop64: return f(k_resolve_loop64<1>);
+    case kResolveVariantLoop64x2: return f(k_resolve_loop64<2>);
+    case kResolveVariantList: return f(k_resolve_list<false, 1>);
+    case kResolveVariantListShared: return f(k_resolve_list<true, 1>);
+    case kResolveVariantListx2: return f(k_resolve_list<false, 2>);
     default: return cudaErrorInvalidValue;
   }
 }
