@@ -719,6 +719,9 @@ struct oit_batch {
     bool binned = false;
   };
   ResolvePart rparts[2];
+  // share of its resident blocks the linked-list part launches while the
+  // Loop64 part takes the rest (both run side by side); 1 = both full
+  float r_share = 1.0f;
   uint64_t rsig = 0;
   bool r_tuned = false;
   int num_sms = 0;
@@ -802,6 +805,7 @@ int batch_prepare_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n)
   if (sig == b->rsig) return OIT_OK;
   b->rsig = 0;
   b->r_tuned = false;
+  b->r_share = 1.0f;
   if (b->num_sms == 0) OIT_TRY_CUDA(cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, 0), "attr");
   for (int part = 0; part < 2; ++part) {
     const int kind = part == 0 ? oit::kResolveList : oit::kResolveLoop64;
@@ -869,7 +873,9 @@ int batch_resolve_launch(oit_batch* b, cudaStream_t s, uint64_t* launches) {
   for (int k = 0; k < 2; ++k) {
     const oit_batch::ResolvePart& rp = b->rparts[k];
     OIT_TRY_CUDA(cudaStreamWaitEvent(b->lanes[k], b->rfork, 0), "wait");
-    const int r = part_launch(rp, b->lanes[k], rp.variant, rp.binned, rp.threads, rp.blocks, launches);
+    const float share = b->r_share >= 1.0f ? 1.0f : (k == 0 ? b->r_share : 1.0f - b->r_share);
+    const int blocks = std::max(1, (int)((float)rp.blocks * share));
+    const int r = part_launch(rp, b->lanes[k], rp.variant, rp.binned, rp.threads, blocks, launches);
     if (r != OIT_OK) return r;
     OIT_TRY_CUDA(cudaEventRecord(b->rjoin[k], b->lanes[k]), "event");
     OIT_TRY_CUDA(cudaStreamWaitEvent(s, b->rjoin[k], 0), "wait");
@@ -883,6 +889,8 @@ int batch_resolve_launch(oit_batch* b, cudaStream_t s, uint64_t* launches) {
 // work lists, each timed with CUDA events on the batch's current frames (the
 // resolve only writes the outputs, so reruns are harmless); the grid holds
 // every block that fits. The fastest shape is kept for the batch's views.
+// Then, with both parts present, the share of the machine each takes when they
+// run side by side is timed the same way.
 int batch_autotune(oit_batch* b, cudaStream_t s) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   OIT_TRY_CUDA(cudaEventCreate(&e0), "event");
@@ -927,6 +935,31 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
       if (r != OIT_OK) break;
     }
     if (r == OIT_OK && best >= 1e30f) r = OIT_ERR_UNSUPPORTED;
+  }
+  // both parts together: the share of the machine the linked-list part takes
+  if (r == OIT_OK && b->rparts[0].rb.num_views > 0 && b->rparts[1].rb.num_views > 0 && b->lanes.size() >= 2) {
+    float best = 1e30f;
+    float pick = 1.0f;
+    for (float share : {1.0f, 0.7f, 0.5f, 0.3f}) {
+      b->r_share = share;
+      r = batch_resolve_launch(b, s, &scratch);  // warm-up
+      if (r != OIT_OK) break;
+      cudaEventRecord(e0, s);
+      for (int k = 0; k < 3 && r == OIT_OK; ++k) r = batch_resolve_launch(b, s, &scratch);
+      cudaEventRecord(e1, s);
+      if (r != OIT_OK) break;
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        r = OIT_ERR_CUDA;
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        pick = share;
+      }
+    }
+    b->r_share = pick;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -1323,6 +1356,10 @@ int oit_batch_resolve_config(oit_batch* b, uint32_t part, uint32_t* threads_per_
   *binned = any && rp.binned ? 1 : 0;
   *shared_slots = rp.variant == oit::kResolveVariantListShared ? 8 : 0;
   *items_per_step = (rp.variant == oit::kResolveVariantListx2 || rp.variant == oit::kResolveVariantLoop64x2) ? 2 : 1;
+  // blocks actually launched when both parts run side by side
+  const bool two = b->rparts[0].rb.num_views > 0 && b->rparts[1].rb.num_views > 0 && b->lanes.size() >= 2;
+  if (any && two && b->r_share < 1.0f)
+    *blocks = (uint32_t)std::max(1, (int)((float)rp.blocks * (part == 0 ? b->r_share : 1.0f - b->r_share)));
   return OIT_OK;
 }
 
