@@ -150,10 +150,15 @@ def cpu_baseline_views(views, budget_s=15.0):
     return frags, busy, n
 
 
+REFERENCE_SAMPLE_VIEWS = 48
+
+
 def reference_views(step, cores):
     """The views the reference arm renders in one step of the batch workload:
-    one per core, cycling through the 64."""
-    vs = batch_views(SEED)
+    one per core, cycling through the 48 cheapest of the 64 (a bounded sample:
+    the largest views take the oracle several seconds each)."""
+    vs = sorted(batch_views(SEED), key=lambda vd: vd['width'] * vd['height'] + 1000 * vd['spheres'])
+    vs = vs[:REFERENCE_SAMPLE_VIEWS]
     return [vs[(step * cores + j) % len(vs)] for j in range(cores)]
 
 
@@ -748,7 +753,7 @@ def main():
             'data': 'synthetic: seeded UV-sphere scene', 'config': wd,
             'cpu_baseline': {'value': round(value, 4), 'unit': 'Mfragments/s', 'cores': cores, 'kind': 'port',
                              'sample': '%d whole frames per step, one per core%s' % (
-                                 cores, ' (batch views in turn)' if batch else '')},
+                                 cores, ' (the 48 cheapest batch views in turn)' if batch else '')},
             'e2e': {'value': round(value, 4), 'unit': 'Mfragments/s', 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0},
             'note': 'reference Vulkan build unavailable on this box (no graphics stack); CPU restatement of the '

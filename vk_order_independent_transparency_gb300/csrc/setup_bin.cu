@@ -10,7 +10,7 @@
 //                 written in triangle order;
 //   radix sort    stable LSD sort of the pairs by tile id, so every tile's list
 //                 keeps primitive order;
-//   k_tile_ranges begin/end of each tile's list.
+//   k_tile_bounds begin/end of each tile's list (where the sorted key changes).
 #include <algorithm>
 #include <cstdio>
 
@@ -389,27 +389,21 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t*
   }
 }
 
-// [begin, end) of every tile's pair range in the sorted keys (binary search).
-__global__ void __launch_bounds__(256) k_tile_ranges(const uint32_t* __restrict__ keys,
+// [begin, end) of every tile's pair range in the sorted keys: every position
+// where the key changes ends the previous key's range and begins the next
+// one's. Both arrays start at zero, so tiles without pairs read an empty range.
+__global__ void __launch_bounds__(256) k_tile_bounds(const uint32_t* __restrict__ keys,
                                                      const uint32_t* __restrict__ total, size_t capacity,
-                                                     int num_tiles, uint32_t* __restrict__ begin,
+                                                     uint32_t num_keys, uint32_t* __restrict__ begin,
                                                      uint32_t* __restrict__ end) {
-  const int tile = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tile >= num_tiles) return;
   const uint32_t n = (uint32_t)pair_count_of(total, capacity);
-  uint32_t lo = 0, hi = n;
-  while (lo < hi) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (keys[mid] < (uint32_t)tile) lo = mid + 1; else hi = mid;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
+    const uint32_t cur = i < n ? keys[i] : num_keys;
+    const uint32_t prev = i > 0 ? keys[i - 1] : 0xFFFFFFFFu;
+    if (cur == prev) continue;
+    if (i > 0 && prev < num_keys) end[prev] = i;
+    if (cur < num_keys) begin[cur] = i;
   }
-  const uint32_t b = lo;
-  hi = n;
-  while (lo < hi) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (keys[mid] <= (uint32_t)tile) lo = mid + 1; else hi = mid;
-  }
-  begin[tile] = b;
-  end[tile] = lo;
 }
 
 __global__ void k_fill_u32(uint32_t* dst, uint32_t v, size_t n) {
@@ -489,8 +483,13 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles
     std::swap(b.tris, b.tris_alt);
   }
   // ranges of both kinds: [0, num_tiles) opaque, [num_tiles, 2 num_tiles) transparent
-  k_tile_ranges<<<(2 * num_tiles + 255) / 256, 256, 0, s>>>(b.keys, b.total, b.capacity, 2 * num_tiles,
-                                                             b.tile_begin, b.tile_end);
+  const size_t range_bytes = (size_t)2 * num_tiles * sizeof(uint32_t);
+  if ((e = cudaMemsetAsync(b.tile_begin, 0, range_bytes, s)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(b.tile_end, 0, range_bytes, s)) != cudaSuccess) return e;
+  const size_t nb = std::min<size_t>((b.capacity + 256) / 256, 152 * 16);
+  k_tile_bounds<<<(unsigned)std::max<size_t>(nb, 1), 256, 0, s>>>(b.keys, b.total, b.capacity,
+                                                                  (uint32_t)(2 * num_tiles), b.tile_begin,
+                                                                  b.tile_end);
   ++*launches;
   return cudaGetLastError();
 }
