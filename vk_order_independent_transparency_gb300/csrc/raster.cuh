@@ -538,8 +538,11 @@ constexpr size_t kWarpStageBytes =
 // ---------------------------------------------------------------------------
 // S: samples each lane evaluates (MSAA coverage); SSN: samples mapped to
 // lanes (sample shading, S = 1 then).
+// Four resident CTAs per SM for one coverage sample per lane (64 registers,
+// spill-free for every policy; shared memory still limits Loop64 and Loop32
+// at large OIT_LAYERS), three for MSAA lanes, whose per-sample state needs more.
 template <template <int> class Policy, int S, int SSN>
-__global__ void __launch_bounds__(256, 3) k_raster_transparent(RasterParams p) {
+__global__ void __launch_bounds__(256, S == 1 ? 4 : 3) k_raster_transparent(RasterParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using Pol = Policy<S>;
   using M = LaneMap<SSN>;
