@@ -432,6 +432,7 @@ struct oit_context {
     v.tail = st.tail_blend ? 1 : 0;
     v.mtx = lens_stride();
     v.mty = lens_rows();
+    v.mtx_recip = ((1ull << 40) + (uint64_t)v.mtx - 1) / (uint64_t)v.mtx;  // exact: mtx <= 2048, tiles < 2^26
     return v;
   }
 

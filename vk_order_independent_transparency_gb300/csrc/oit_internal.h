@@ -158,6 +158,7 @@ struct ResolveView {
   uint32_t P, capacity;
   int W, H, L, kind, tail, mtx, mty;
   int color_half;
+  uint64_t mtx_recip;            // ceil(2^40 / mtx): tile / mtx = (tile * mtx_recip) >> 40 for tile < 2^26
   uint32_t tile_base;            // first global micro-tile index of this view
 };
 

@@ -153,8 +153,9 @@ __device__ __forceinline__ bool item_pixel(const ResolveBatch& b, const uint32_t
   const ResolveView& v = b.views[vi];
   o.v = &v;
   o.tile = g - tb[vi];
-  const int mtx = v.mtx;
-  const int x = (int)(o.tile % (uint32_t)mtx) * 8 + (lane & 7), y = (int)(o.tile / (uint32_t)mtx) * 4 + (lane >> 3);
+  const uint32_t my = (uint32_t)(((uint64_t)o.tile * v.mtx_recip) >> 40);
+  const uint32_t mx = o.tile - my * (uint32_t)v.mtx;
+  const int x = (int)mx * 8 + (lane & 7), y = (int)my * 4 + (lane >> 3);
   if (x >= v.W || y >= v.H) return false;
   o.pixel = (uint32_t)y * (uint32_t)v.W + (uint32_t)x;
   return true;
