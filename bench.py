@@ -102,7 +102,9 @@ def dtype_of(alg):
 # CPU leg (the oracle): a bounded sample of the same workload
 # ---------------------------------------------------------------------------
 def _oracle_frame(args):
-    wd, scale = args
+    """(fragments, seconds[, RGBA8 image]) of one oracle frame of a workload;
+    args = (workload, want_image)."""
+    wd, want_image = args
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
     import oracle as orc
     import vk_order_independent_transparency_gb300 as oit
@@ -114,8 +116,10 @@ def _oracle_frame(args):
     fr = orc.render(ALGS.index(wd['algorithm']), W, H, sd, v, i, tpo, wd['percent_transparent'],
                     oit_layers=wd['oit_layers'], nodes_per_pixel=wd['nodes_per_pixel'], aa_type=wd['aa_type'],
                     alpha_min=wd['alpha_min'], alpha_width=wd['alpha_width'])
-    fr.composite()
+    img, _ = fr.composite()
     dt = time.perf_counter() - t
+    if want_image == 'image':
+        return fr.fragment_count(), dt, img
     return fr.fragment_count(), dt
 
 
@@ -134,20 +138,70 @@ def cpu_baseline(wd, cores=1, frames=None, budget_s=15.0):
 
 def cpu_baseline_views(views, budget_s=15.0):
     """Oracle throughput (one process, one core) on whole frames of batch
-    views, smallest first, until about budget_s of CPU work."""
+    views, smallest first, until about budget_s of CPU work; also returns
+    the oracle's images by view index."""
     import oracle  # noqa: F401
     ctx = mp.get_context('spawn')
-    order = sorted(views, key=lambda vd: vd['width'] * vd['height'] + 1000 * vd['spheres'])
-    frags, busy, n = 0, 0.0, 0
+    order = sorted(range(len(views)), key=lambda k: views[k]['width'] * views[k]['height'] + 1000 * views[k]['spheres'])
+    frags, busy, n, images = 0, 0.0, 0, {}
     with ctx.Pool(1) as pool:
-        for f, dt in pool.imap(_oracle_frame, [(vd, 1) for vd in order]):
+        for k, (f, dt, img) in zip(order, pool.imap(_oracle_frame, [(views[k], 'image') for k in order])):
             frags += f
             busy += dt
             n += 1
+            images[k] = img
             if busy >= budget_s:
                 break
         pool.terminate()
-    return frags, busy, n
+    return frags, busy, n, images
+
+
+def weighted_precision(wd, width=960, height=540):
+    """The WBOIT precision study: the workload's scene at width x height with
+    FP16 and FP32 accumulators on the GPU against the FP64 oracle; per-pixel
+    relative error of the accumulation (RGBA, where the oracle's magnitude is
+    above 1e-3) and of the revealage."""
+    import importlib.util
+    import numpy as np
+    import vk_order_independent_transparency_gb300 as oit
+    spec = importlib.util.spec_from_file_location('oit_checker_oracle', os.path.join(ROOT, 'oracle', 'oracle.py'))
+    orc = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(orc)
+    v, i, tpo = oit.make_scene(wd['spheres'], seed=wd['seed'], radius_min=wd['radius_min'], radius_max=wd['radius_max'])
+    sd = oit.make_camera(width, height)
+    fr = orc.render(orc.WEIGHTED, width, height, sd, v, i, tpo, wd['percent_transparent'],
+                    alpha_min=wd['alpha_min'], alpha_width=wd['alpha_width'])
+    acc_o = fr.buffer(orc.BUF_ACCUM, np.float64).reshape(-1, 4)
+    rev_o = fr.buffer(orc.BUF_REVEAL, np.float64)
+    mesh = oit.DeviceMesh(v, i)
+    out = {'size': '%dx%d' % (width, height), 'reference': 'FP64 oracle'}
+    for name, prec, dt in (('fp16', oit.OIT_WEIGHTED_FP16, np.float16), ('fp32', oit.OIT_WEIGHTED_FP32, np.float32)):
+        with oit.Renderer(oit.make_state(oit.OIT_WEIGHTED, width, height, alpha_min=wd['alpha_min'],
+                                         alpha_width=wd['alpha_width'], weighted_precision=prec)) as r:
+            r.update_scene(sd)
+            r.render_frame(mesh, tpo, wd['percent_transparent'])
+            acc = r.read_buffer(oit.OIT_BUF_ACCUM, dt).astype(np.float64).reshape(-1, 4)
+            rev = r.read_buffer(oit.OIT_BUF_REVEAL, dt).astype(np.float64)
+        m = np.abs(acc_o) > 1e-3
+        ra = np.abs(acc - acc_o)[m] / np.abs(acc_o)[m]
+        rr = np.abs(rev - rev_o) / np.maximum(rev_o, 1e-3)
+        out[name] = {'accum_rel_max': float(ra.max()), 'accum_rel_mean': float(ra.mean()),
+                     'reveal_rel_max': float(rr.max()), 'reveal_rel_mean': float(rr.mean())}
+    return out
+
+
+def image_error(gpu_images, oracle_images):
+    """Max and mean absolute RGBA8 difference (LSB) over the views both have."""
+    import numpy as np
+    mx, tot, cnt, over = 0, 0.0, 0, 0
+    for k, ref in oracle_images.items():
+        d = np.abs(gpu_images[k].astype(np.int32) - ref.astype(np.int32))
+        mx = max(mx, int(d.max()))
+        tot += float(d.sum())
+        cnt += d.size
+        over += int((d > 1).sum())
+    return {'views_compared': len(oracle_images), 'max_lsb': mx, 'mean_lsb': round(tot / max(cnt, 1), 6),
+            'channels_over_1_lsb': over, 'reference': 'FP64 oracle, same scenes'}
 
 
 REFERENCE_SAMPLE_VIEWS = 48
@@ -604,10 +658,12 @@ def run_batch(a, rank):
     torch.cuda.nvtx.range_pop()
     res_cfg = batch.resolve_config()
     res_bytes = resolve_bytes(vs, mixed)
+    batch.render(stream)
+    images = [r.output() for r in mixed]
     return dict(frags=frags, t_mixed=t_mixed, t_plain=t_plain, launches=launches, clocks=clk, sections=sections,
                 e2e_s=e2e_s, h2d=h2d, d2h=d2h, views=vs, t_res_mixed=t_res_mixed, t_res_plain=t_res_plain,
                 res_cfg=res_cfg, res_bytes=res_bytes, e2e_flat_s=e2e_flat_s, h2d_flat=h2d_flat,
-                raster_bytes=raster_bytes)
+                raster_bytes=raster_bytes, images=images)
 
 
 def _copy_d2h(host_tensor, dev_ptr, nbytes, stream):
@@ -634,10 +690,13 @@ def reduce_replicas(maxes, sums, world, device='cuda'):
 def main_batch(a, rank, world):
     res = run_batch(a, rank)
     cpu_line = None
+    accuracy = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        f, busy, n = cpu_baseline_views(res['views'])
+        f, busy, n, oracle_images = cpu_baseline_views(res['views'])
         cpu_line = {'value': round(f / busy / 1e6, 4), 'unit': 'Mfragments/s', 'cores': 1, 'kind': 'port',
-                    'sample': '%d of the 64 views (the smallest), whole frames, single-threaded FP64 oracle' % n}
+                    'sample': '%d of the %d views (the smallest), whole frames, single-threaded FP64 oracle' % (
+                        n, len(res['views']))}
+        accuracy = image_error(res['images'], oracle_images)
     (t_mixed, t_plain, e2e_s, t_res_mixed, t_res_plain, e2e_flat_s), (total,) = reduce_replicas(
         [res['t_mixed'], res['t_plain'], res['e2e_s'], res['t_res_mixed'], res['t_res_plain'], res['e2e_flat_s']],
         [res['frags'] * a.steps], world)
@@ -671,6 +730,7 @@ def main_batch(a, rank, world):
         'kernels': {k: {'ms_sum_over_views': round(v, 4)} for k, v in sec.items()},
         'resolve': resolve_line(res, a, world, total, t_res_mixed, t_res_plain, peak, peak_kind),
         'cpu_baseline': cpu_line,
+        'accuracy': accuracy,
         'clocks': res['clocks'],
         'gpu_launches': int(res['launches']),
     }
@@ -800,6 +860,7 @@ def main():
                 'peak_source': peak_kind + ' (MEASURED_PEAKS.json hbm_gbs)' if peak_kind == 'measured' else peak_kind,
                 'dominant_pass': dom}
     cpu = None
+    precision = None
     if not a.no_cpu_baseline:
         f, w, runs = cpu_baseline(wd, cores=1, frames=1)
         n_more = max(0, min(4, int(12.0 / max(w, 1e-3)) - 1))
@@ -809,6 +870,8 @@ def main():
             w += w2
         cpu = {'value': round(f / w / 1e6, 4), 'unit': 'Mfragments/s', 'cores': 1, 'kind': 'port',
                'sample': '%d whole frame(s) of the workload, single-threaded FP64 oracle' % (1 + n_more)}
+        if wd['algorithm'] == 'weighted':
+            precision = weighted_precision(wd)
     line = {
         'metric': 'Mfragments/s', 'value': round(value, 3), 'unit': 'Mfragments/s', 'n_gpus': world,
         'steps': a.steps, 'warmup': a.warmup, 'ms_per_step': round(t_ms / a.steps, 4), 'higher_is_better': True,
@@ -830,6 +893,8 @@ def main():
         'clocks': res['clocks'],
         'gpu_launches': int(res['launches']),
     }
+    if precision:
+        line['precision'] = precision
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
