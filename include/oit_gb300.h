@@ -291,11 +291,13 @@ int oit_batch_resolve(oit_batch* batch, const oit_view_frame* views, uint32_t nu
 /* The shape the autotuner picked for one part of the batched resolve (part 0:
  * linked-list views, 1: Loop64 views): threads per block, blocks, binned (1)
  * or view-order (0) work list, the sort-array entries per thread held in
- * shared memory (0 or 8; the rest live in local memory), and the micro-tiles a
- * warp takes per step (1 or 2). A part without views reports zeros.
+ * shared memory (0 or 8; the rest live in local memory), the micro-tiles a
+ * warp takes per step (1 or 2), and the register slots for lists short enough
+ * to be sorted in registers (0, 4 or 8). A part without views reports zeros.
  * OIT_ERR_STATE before the first resolve. */
 int oit_batch_resolve_config(oit_batch* batch, uint32_t part, uint32_t* threads_per_block, uint32_t* blocks,
-                             int32_t* binned, int32_t* shared_slots, int32_t* items_per_step);
+                             int32_t* binned, int32_t* shared_slots, int32_t* items_per_step,
+                             int32_t* register_slots);
 
 /* ---- inspection -------------------------------------------------------- */
 

@@ -154,7 +154,8 @@ def library():
         'oit_scene_generate_instanced': (I, [ctypes.POINTER(OitSceneDesc), P, P, P]),
         'oit_batch_resolve': (I, [P, ctypes.POINTER(OitViewFrame), U, P]),
         'oit_batch_resolve_config': (I, [P, U, ctypes.POINTER(U), ctypes.POINTER(U), ctypes.POINTER(ctypes.c_int32),
-                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
+                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.POINTER(ctypes.c_int32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -476,11 +477,13 @@ class Batch:
         list, register slots for the first sort entries)."""
         out = {}
         for part, name in ((0, 'linkedlist'), (1, 'loop64')):
-            t, n, b, k, u = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+            t, n = ctypes.c_uint32(), ctypes.c_uint32()
+            b, k, u, g = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
             _check(self.lib.oit_batch_resolve_config(self._b, part, ctypes.byref(t), ctypes.byref(n), ctypes.byref(b),
-                                                     ctypes.byref(k), ctypes.byref(u)), 'oit_batch_resolve_config')
+                                                     ctypes.byref(k), ctypes.byref(u), ctypes.byref(g)),
+                   'oit_batch_resolve_config')
             out[name] = {'threads_per_block': t.value, 'blocks': n.value, 'binned': bool(b.value),
-                         'shared_slots': k.value, 'items_per_step': u.value}
+                         'shared_slots': k.value, 'items_per_step': u.value, 'register_slots': g.value}
         return out
 
 

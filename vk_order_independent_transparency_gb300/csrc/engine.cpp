@@ -885,8 +885,9 @@ int batch_resolve_launch(oit_batch* b, cudaStream_t s, uint64_t* launches) {
 }
 
 // The autotuner, per part: kernel variant (linked lists: sort arrays in local
-// memory, or the first 8 entries in shared memory; one or two micro-tiles per
-// warp step), block size and binned versus view-order
+// memory, or the first 8 entries in shared memory; short lists in 4 or 8
+// registers; one or two micro-tiles per warp step), block size and binned
+// versus view-order
 // work lists, each timed with CUDA events on the batch's current frames (the
 // resolve only writes the outputs, so reruns are harmless); the grid holds
 // every block that fits. The fastest shape is kept for the batch's views.
@@ -903,7 +904,9 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
     if (rp.rb.num_views == 0) continue;
     float best = 1e30f;
     std::vector<int> variants;
-    if (part == 0) variants = {oit::kResolveVariantList, oit::kResolveVariantListShared, oit::kResolveVariantListx2};
+    if (part == 0)
+      variants = {oit::kResolveVariantList, oit::kResolveVariantListShared, oit::kResolveVariantListx2,
+                  oit::kResolveVariantListShort4, oit::kResolveVariantListShort8};
     else variants = {oit::kResolveVariantLoop64, oit::kResolveVariantLoop64x2};
     for (int variant : variants) {
       for (int threads : {64, 128, 256}) {
@@ -1346,8 +1349,9 @@ int oit_batch_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n, voi
 }
 
 int oit_batch_resolve_config(oit_batch* b, uint32_t part, uint32_t* threads_per_block, uint32_t* blocks,
-                             int32_t* binned, int32_t* shared_slots, int32_t* items_per_step) {
-  if (!b || part > 1 || !threads_per_block || !blocks || !binned || !shared_slots || !items_per_step)
+                             int32_t* binned, int32_t* shared_slots, int32_t* items_per_step, int32_t* register_slots) {
+  if (!b || part > 1 || !threads_per_block || !blocks || !binned || !shared_slots || !items_per_step ||
+      !register_slots)
     return OIT_ERR_INVALID_ARGUMENT;
   if (!b->r_tuned) return OIT_ERR_STATE;
   const oit_batch::ResolvePart& rp = b->rparts[part];
@@ -1356,6 +1360,7 @@ int oit_batch_resolve_config(oit_batch* b, uint32_t part, uint32_t* threads_per_
   *blocks = any ? (uint32_t)rp.blocks : 0u;
   *binned = any && rp.binned ? 1 : 0;
   *shared_slots = rp.variant == oit::kResolveVariantListShared ? 8 : 0;
+  *register_slots = rp.variant == oit::kResolveVariantListShort4 ? 4 : (rp.variant == oit::kResolveVariantListShort8 ? 8 : 0);
   *items_per_step = (rp.variant == oit::kResolveVariantListx2 || rp.variant == oit::kResolveVariantLoop64x2) ? 2 : 1;
   // blocks actually launched when both parts run side by side
   const bool two = b->rparts[0].rb.num_views > 0 && b->rparts[1].rb.num_views > 0 && b->lanes.size() >= 2;

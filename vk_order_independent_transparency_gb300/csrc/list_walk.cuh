@@ -215,4 +215,50 @@ __device__ __forceinline__ float4 walk_list(const uint4* __restrict__ pool, uint
   return sum;
 }
 
+// walk_list for lists of at most min(K, OIT_LAYERS) nodes without coverage
+// masks: the nodes are appended to K registers (static indices), then ordered
+// by bubbleSort itself (swap on >=, unrolled over K) and blended; there is no
+// tail. A longer list is walked again by walk_list with the arrays `a`.
+template <bool F32, int K, class A>
+__device__ __forceinline__ float4 walk_list_short(const uint4* __restrict__ pool, uint32_t head, uint32_t cap, int L,
+                                                  int tail, int S, A& a) {
+  uint32_t rc[K], rd[K];
+  const int lim = L < K ? L : K;
+  uint32_t off = head < cap ? head : 0u;
+  int k = 0;
+#pragma unroll 1
+  while (off != 0) {
+    if (k == lim) return walk_list<F32>(pool, head, cap, L, tail, S, a);
+    const WalkNode n = load_node<F32>(pool, off);
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+      if (i == k) {
+        rc[i] = n.c;
+        rd[i] = n.d;
+      }
+    ++k;
+    off = n.next < cap ? n.next : 0u;
+  }
+#pragma unroll
+  for (int i = K - 2; i >= 0; --i) {
+    if (i <= k - 2) {
+#pragma unroll
+      for (int j = 0; j <= i; ++j) {
+        if (walk_dge(rd[j], rd[j + 1])) {
+          const uint32_t tc = rc[j], td = rd[j];
+          rc[j] = rc[j + 1];
+          rd[j] = rd[j + 1];
+          rc[j + 1] = tc;
+          rd[j + 1] = td;
+        }
+      }
+    }
+  }
+  float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < K; ++i)
+    if (i < k) blend_under(sum, node_colour<F32>(pool, rc[i]));
+  return sum;
+}
+
 }  // namespace oitd

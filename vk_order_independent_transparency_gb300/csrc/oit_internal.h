@@ -195,6 +195,8 @@ enum ResolveVariant : int {
   kResolveVariantListShared = 2,
   kResolveVariantListx2 = 3,    // two micro-tiles per warp step
   kResolveVariantLoop64x2 = 4,  // two micro-tiles per warp step
+  kResolveVariantListShort4 = 5,  // lists of up to 4 (8) nodes in registers, bubble-sorted;
+  kResolveVariantListShort8 = 6,  // longer ones walked again with the local arrays
 };
 cudaError_t resolve_bin(const ResolveBatch& b, cudaStream_t s, uint64_t* launches);
 cudaError_t resolve_run(const ResolveBatch& b, int variant, int threads, int blocks, cudaStream_t s);

@@ -170,7 +170,7 @@ constexpr int kSplitSlots = 8;
 
 // U micro-tiles per step: the independent first loads of all U (colour
 // target, list head) are issued before any list is walked.
-template <bool Split, int U>
+template <bool Split, int U, int Short = 0>
 __global__ void __launch_bounds__(256) k_resolve_list(ResolveBatch b) {
   extern __shared__ __align__(16) uint32_t rsm[];
   load_bases(b, rsm);
@@ -203,8 +203,10 @@ __global__ void __launch_bounds__(256) k_resolve_list(ResolveBatch b) {
     for (int u = 0; u < U; ++u) {
       if (!ok[u]) continue;
       const ResolveView& v = *ip[u].v;
-      const float4 sum =
-          walk_list<false>(reinterpret_cast<const uint4*>(v.abuf), head[u], v.capacity, v.L, v.tail, 1, a);
+      const uint4* pool = reinterpret_cast<const uint4*>(v.abuf);
+      float4 sum;
+      if constexpr (Short > 0) sum = walk_list_short<false, Short>(pool, head[u], v.capacity, v.L, v.tail, 1, a);
+      else sum = walk_list<false>(pool, head[u], v.capacity, v.L, v.tail, 1, a);
       rop_over(c[u], sum);
       write_rgba8(v.out, v.out_linear, ip[u].pixel, c[u]);
     }
@@ -259,6 +261,8 @@ cudaError_t with_kernel(int variant, F f) {
     case kResolveVariantList: return f(k_resolve_list<false, 1>);
     case kResolveVariantListShared: return f(k_resolve_list<true, 1>);
     case kResolveVariantListx2: return f(k_resolve_list<false, 2>);
+    case kResolveVariantListShort4: return f(k_resolve_list<false, 1, 4>);
+    case kResolveVariantListShort8: return f(k_resolve_list<false, 1, 8>);
     default: return cudaErrorInvalidValue;
   }
 }
