@@ -392,7 +392,7 @@ def resolve_bytes(views, renderers, color_bytes=8):
     for vd, r in zip(views, renderers):
         W, H, L = vd['width'], vd['height'], vd['oit_layers']
         P = W * H
-        tiles += ((W + 7) // 8) * ((H + 3) // 4)
+        tiles += 8 * ((W + 15) // 16) * ((H + 15) // 16)  # work items: the micro-tiles of whole 16x16 tiles
         b = P * (color_bytes + 4)
         if vd['algorithm'] == 'linkedlist':
             b += P * 4 + 16 * min(r.fragment_count(), vd['nodes_per_pixel'] * P - 1)

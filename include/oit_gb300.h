@@ -288,16 +288,21 @@ int oit_batch_launch_count(oit_batch* batch, uint64_t* launches);
  * oit_batch_resolve_config) and keeps the fastest. */
 int oit_batch_resolve(oit_batch* batch, const oit_view_frame* views, uint32_t num_views, void* stream);
 
-/* The shape the autotuner picked for one part of the batched resolve (part 0:
- * linked-list views, 1: Loop64 views): threads per block, blocks, binned (1)
- * or view-order (0) work list, the sort-array entries per thread held in
- * shared memory (0 or 8; the rest live in local memory), the micro-tiles a
- * warp takes per step (1 or 2), and the register slots for lists short enough
- * to be sorted in registers (0, 4 or 8). A part without views reports zeros.
- * OIT_ERR_STATE before the first resolve. */
-int oit_batch_resolve_config(oit_batch* batch, uint32_t part, uint32_t* threads_per_block, uint32_t* blocks,
-                             int32_t* binned, int32_t* shared_slots, int32_t* items_per_step,
-                             int32_t* register_slots);
+/* The shape the autotuner picked for one part of the batched resolve. */
+typedef struct oit_resolve_shape {
+  uint32_t threads_per_block;
+  uint32_t blocks;          /* launched (with both parts present: this part's share of the machine) */
+  int32_t binned;           /* 1: micro-tiles binned by list length, costliest first; 0: in order */
+  int32_t tile_order;       /* 0: micro-tiles row by row; 1: the 8 micro-tiles of each 16x16 tile together */
+  int32_t shared_slots;     /* sort-array entries per thread in shared memory (0 or 8; the rest local) */
+  int32_t items_per_step;   /* micro-tiles a warp takes per step (1 or 2) */
+  int32_t register_slots;   /* lists short enough to be sorted in registers (0, 4 or 8 entries) */
+  int32_t dense;            /* 1: at most 32 registers per thread (eight 256-thread blocks per SM) */
+} oit_resolve_shape;
+
+/* Part 0: linked-list views, 1: Loop64 views. A part without views reports
+ * zeros. OIT_ERR_STATE before the first resolve. */
+int oit_batch_resolve_config(oit_batch* batch, uint32_t part, oit_resolve_shape* shape);
 
 /* ---- inspection -------------------------------------------------------- */
 

@@ -82,6 +82,12 @@ class OitInstancedMesh(ctypes.Structure):
                 ('template_triangles', ctypes.c_uint32), ('num_instances', ctypes.c_uint32)]
 
 
+class OitResolveShape(ctypes.Structure):
+    _fields_ = [('threads_per_block', ctypes.c_uint32), ('blocks', ctypes.c_uint32), ('binned', ctypes.c_int32),
+                ('tile_order', ctypes.c_int32), ('shared_slots', ctypes.c_int32), ('items_per_step', ctypes.c_int32),
+                ('register_slots', ctypes.c_int32), ('dense', ctypes.c_int32)]
+
+
 class OitSceneDesc(ctypes.Structure):
     _fields_ = [('seed', ctypes.c_uint64), ('num_objects', ctypes.c_uint32), ('stacks', ctypes.c_uint32),
                 ('slices', ctypes.c_uint32), ('half_extent', ctypes.c_float), ('radius_min', ctypes.c_float),
@@ -153,9 +159,7 @@ def library():
         'oit_render_frame_instanced_host': (I, [P, P, U, P, U, P, U, ctypes.c_int32, P, P]),
         'oit_scene_generate_instanced': (I, [ctypes.POINTER(OitSceneDesc), P, P, P]),
         'oit_batch_resolve': (I, [P, ctypes.POINTER(OitViewFrame), U, P]),
-        'oit_batch_resolve_config': (I, [P, U, ctypes.POINTER(U), ctypes.POINTER(U), ctypes.POINTER(ctypes.c_int32),
-                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
-                                         ctypes.POINTER(ctypes.c_int32)]),
+        'oit_batch_resolve_config': (I, [P, U, ctypes.POINTER(OitResolveShape)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -472,18 +476,14 @@ class Batch:
         _check(self.lib.oit_batch_resolve(self._b, self._frames, len(self._frames), stream), 'oit_batch_resolve')
 
     def resolve_config(self):
-        """{'linkedlist': ..., 'loop64': ...}: per part of the batched resolve,
-        the shape the autotuner picked (threads per block, blocks, binned work
-        list, register slots for the first sort entries)."""
+        """{'linkedlist': {...}, 'loop64': {...}}: per part of the batched
+        resolve, the shape the autotuner picked (oit_resolve_shape's fields)."""
         out = {}
         for part, name in ((0, 'linkedlist'), (1, 'loop64')):
-            t, n = ctypes.c_uint32(), ctypes.c_uint32()
-            b, k, u, g = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
-            _check(self.lib.oit_batch_resolve_config(self._b, part, ctypes.byref(t), ctypes.byref(n), ctypes.byref(b),
-                                                     ctypes.byref(k), ctypes.byref(u), ctypes.byref(g)),
-                   'oit_batch_resolve_config')
-            out[name] = {'threads_per_block': t.value, 'blocks': n.value, 'binned': bool(b.value),
-                         'shared_slots': k.value, 'items_per_step': u.value, 'register_slots': g.value}
+            sh = OitResolveShape()
+            _check(self.lib.oit_batch_resolve_config(self._b, part, ctypes.byref(sh)), 'oit_batch_resolve_config')
+            out[name] = {f: (bool(getattr(sh, f)) if f in ('binned', 'tile_order', 'dense') else getattr(sh, f))
+                         for f, _ in OitResolveShape._fields_}
         return out
 
 

@@ -173,6 +173,8 @@ struct oit_context {
   int lens_stride() const { return (RW + 7) / 8; }
   int lens_rows() const { return (RH + 3) / 4; }
   size_t lens_count() const { return (size_t)lens_stride() * (size_t)lens_rows(); }
+  // batched-resolve work items: the 8 micro-tiles of every 16x16 tile
+  size_t resolve_items() const { return (size_t)8 * (size_t)num_tiles; }
 
   // ---- Sample::createFrameImages (oit.cpp:45-220) ----
   int create() {
@@ -432,7 +434,10 @@ struct oit_context {
     v.tail = st.tail_blend ? 1 : 0;
     v.mtx = lens_stride();
     v.mty = lens_rows();
-    v.mtx_recip = ((1ull << 40) + (uint64_t)v.mtx - 1) / (uint64_t)v.mtx;  // exact: mtx <= 2048, tiles < 2^26
+    v.tiles_x = tiles_x;
+    v.ptx = 2 * tiles_x;
+    v.tx_recip = ((1ull << 40) + (uint64_t)v.tiles_x - 1) / (uint64_t)v.tiles_x;  // exact: tiles_x <= 1024
+    v.ptx_recip = ((1ull << 40) + (uint64_t)v.ptx - 1) / (uint64_t)v.ptx;
     return v;
   }
 
@@ -716,7 +721,7 @@ struct oit_batch {
   struct ResolvePart {
     DevBuf views, base, hist, items;
     oit::ResolveBatch rb{};
-    int variant = 0, threads = 128, blocks = 0;
+    int variant = 0, threads = 128, blocks = 0, order = 0;
     bool binned = false;
   };
   ResolvePart rparts[2];
@@ -818,8 +823,8 @@ int batch_prepare_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n)
       if (!c->batch_resolvable()) continue;
       oit::ResolveView v = c->resolve_view(views[i].out_rgba8_device);
       if (v.kind != kind) continue;
-      v.tile_base = (uint32_t)total;
-      total += c->lens_count();
+        v.tile_base = (uint32_t)total;
+      total += c->resolve_items();
       hv.push_back(v);
       base.push_back(v.tile_base);
     }
@@ -849,10 +854,11 @@ int batch_prepare_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n)
 }
 
 int part_launch(const oit_batch::ResolvePart& rp, cudaStream_t s, int variant, bool binned, int threads, int blocks,
-                uint64_t* launches) {
+                int order, uint64_t* launches) {
   oit::ResolveBatch rb = rp.rb;
   if (rb.num_views == 0) return OIT_OK;
   if (!binned) rb.items = nullptr;
+  rb.order = order;
   OIT_TRY_CUDA(oit::resolve_bin(rb, s, launches), "resolve bin");
   OIT_TRY_CUDA(oit::resolve_run(rb, variant, threads, blocks, s), "resolve");
   ++*launches;
@@ -865,7 +871,7 @@ int batch_resolve_launch(oit_batch* b, cudaStream_t s, uint64_t* launches) {
   const bool two = b->rparts[0].rb.num_views > 0 && b->rparts[1].rb.num_views > 0 && b->lanes.size() >= 2;
   if (!two) {
     for (const oit_batch::ResolvePart& rp : b->rparts) {
-      const int r = part_launch(rp, s, rp.variant, rp.binned, rp.threads, rp.blocks, launches);
+      const int r = part_launch(rp, s, rp.variant, rp.binned, rp.threads, rp.blocks, rp.order, launches);
       if (r != OIT_OK) return r;
     }
     return OIT_OK;
@@ -876,7 +882,7 @@ int batch_resolve_launch(oit_batch* b, cudaStream_t s, uint64_t* launches) {
     OIT_TRY_CUDA(cudaStreamWaitEvent(b->lanes[k], b->rfork, 0), "wait");
     const float share = b->r_share >= 1.0f ? 1.0f : (k == 0 ? b->r_share : 1.0f - b->r_share);
     const int blocks = std::max(1, (int)((float)rp.blocks * share));
-    const int r = part_launch(rp, b->lanes[k], rp.variant, rp.binned, rp.threads, blocks, launches);
+    const int r = part_launch(rp, b->lanes[k], rp.variant, rp.binned, rp.threads, blocks, rp.order, launches);
     if (r != OIT_OK) return r;
     OIT_TRY_CUDA(cudaEventRecord(b->rjoin[k], b->lanes[k]), "event");
     OIT_TRY_CUDA(cudaStreamWaitEvent(s, b->rjoin[k], 0), "wait");
@@ -906,34 +912,37 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
     std::vector<int> variants;
     if (part == 0)
       variants = {oit::kResolveVariantList, oit::kResolveVariantListShared, oit::kResolveVariantListx2,
-                  oit::kResolveVariantListShort4, oit::kResolveVariantListShort8};
+                  oit::kResolveVariantListShort4, oit::kResolveVariantListShort8, oit::kResolveVariantListDense};
     else variants = {oit::kResolveVariantLoop64, oit::kResolveVariantLoop64x2};
     for (int variant : variants) {
       for (int threads : {64, 128, 256}) {
         const int bps = oit::resolve_blocks_per_sm(rp.rb, variant, threads);
         if (bps <= 0) continue;
         const int blocks = bps * b->num_sms;
-        for (bool binned : {true, false}) {
-          r = part_launch(rp, s, variant, binned, threads, blocks, &scratch);  // warm-up
-          if (r != OIT_OK) break;
-          cudaEventRecord(e0, s);
-          for (int k = 0; k < 3 && r == OIT_OK; ++k) r = part_launch(rp, s, variant, binned, threads, blocks, &scratch);
-          cudaEventRecord(e1, s);
-          if (r != OIT_OK) break;
-          if (cudaEventSynchronize(e1) != cudaSuccess) {
-            r = OIT_ERR_CUDA;
-            break;
+        for (int order : {0, 1})
+          for (bool binned : {true, false}) {
+            r = part_launch(rp, s, variant, binned, threads, blocks, order, &scratch);  // warm-up
+            if (r != OIT_OK) break;
+            cudaEventRecord(e0, s);
+            for (int k = 0; k < 3 && r == OIT_OK; ++k)
+              r = part_launch(rp, s, variant, binned, threads, blocks, order, &scratch);
+            cudaEventRecord(e1, s);
+            if (r != OIT_OK) break;
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+              r = OIT_ERR_CUDA;
+              break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+              best = ms;
+              rp.variant = variant;
+              rp.threads = threads;
+              rp.blocks = blocks;
+              rp.binned = binned;
+              rp.order = order;
+            }
           }
-          float ms = 0.f;
-          cudaEventElapsedTime(&ms, e0, e1);
-          if (ms < best) {
-            best = ms;
-            rp.variant = variant;
-            rp.threads = threads;
-            rp.blocks = blocks;
-            rp.binned = binned;
-          }
-        }
         if (r != OIT_OK) break;
       }
       if (r != OIT_OK) break;
@@ -1348,24 +1357,25 @@ int oit_batch_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n, voi
   return r;
 }
 
-int oit_batch_resolve_config(oit_batch* b, uint32_t part, uint32_t* threads_per_block, uint32_t* blocks,
-                             int32_t* binned, int32_t* shared_slots, int32_t* items_per_step, int32_t* register_slots) {
-  if (!b || part > 1 || !threads_per_block || !blocks || !binned || !shared_slots || !items_per_step ||
-      !register_slots)
-    return OIT_ERR_INVALID_ARGUMENT;
+int oit_batch_resolve_config(oit_batch* b, uint32_t part, oit_resolve_shape* out) {
+  if (!b || part > 1 || !out) return OIT_ERR_INVALID_ARGUMENT;
   if (!b->r_tuned) return OIT_ERR_STATE;
   const oit_batch::ResolvePart& rp = b->rparts[part];
-  const bool any = rp.rb.num_views > 0;
-  *threads_per_block = any ? (uint32_t)rp.threads : 0u;
-  *blocks = any ? (uint32_t)rp.blocks : 0u;
-  *binned = any && rp.binned ? 1 : 0;
-  *shared_slots = rp.variant == oit::kResolveVariantListShared ? 8 : 0;
-  *register_slots = rp.variant == oit::kResolveVariantListShort4 ? 4 : (rp.variant == oit::kResolveVariantListShort8 ? 8 : 0);
-  *items_per_step = (rp.variant == oit::kResolveVariantListx2 || rp.variant == oit::kResolveVariantLoop64x2) ? 2 : 1;
+  *out = oit_resolve_shape{};
+  if (rp.rb.num_views == 0) return OIT_OK;
+  out->threads_per_block = (uint32_t)rp.threads;
+  out->blocks = (uint32_t)rp.blocks;
   // blocks actually launched when both parts run side by side
   const bool two = b->rparts[0].rb.num_views > 0 && b->rparts[1].rb.num_views > 0 && b->lanes.size() >= 2;
-  if (any && two && b->r_share < 1.0f)
-    *blocks = (uint32_t)std::max(1, (int)((float)rp.blocks * (part == 0 ? b->r_share : 1.0f - b->r_share)));
+  if (two && b->r_share < 1.0f)
+    out->blocks = (uint32_t)std::max(1, (int)((float)rp.blocks * (part == 0 ? b->r_share : 1.0f - b->r_share)));
+  out->binned = rp.binned ? 1 : 0;
+  out->tile_order = rp.order;
+  out->shared_slots = rp.variant == oit::kResolveVariantListShared ? 8 : 0;
+  out->items_per_step = (rp.variant == oit::kResolveVariantListx2 || rp.variant == oit::kResolveVariantLoop64x2) ? 2 : 1;
+  out->register_slots =
+      rp.variant == oit::kResolveVariantListShort4 ? 4 : (rp.variant == oit::kResolveVariantListShort8 ? 8 : 0);
+  out->dense = rp.variant == oit::kResolveVariantListDense ? 1 : 0;
   return OIT_OK;
 }
 

@@ -158,7 +158,11 @@ struct ResolveView {
   uint32_t P, capacity;
   int W, H, L, kind, tail, mtx, mty;
   int color_half;
-  uint64_t mtx_recip;            // ceil(2^40 / mtx): tile / mtx = (tile * mtx_recip) >> 40 for tile < 2^26
+  // work items: the micro-tiles of the view's 16x16 tiles, 8 per tile, padded
+  // to ptx = 2 * tiles_x columns; x / d = (x * recip) >> 40 with
+  // recip = ceil(2^40 / d), exact for x < 2^26 and d <= 2^12
+  int tiles_x, ptx;
+  uint64_t tx_recip, ptx_recip;
   uint32_t tile_base;            // first global micro-tile index of this view
 };
 
@@ -169,7 +173,8 @@ struct ResolveBatch {
   const ResolveView* views;      // [num_views] (device)
   const uint32_t* tile_base;     // [num_views] (device) copy of views[i].tile_base
   int num_views;
-  uint32_t total_tiles;          // micro-tiles over all views
+  uint32_t total_tiles;          // work items (micro-tiles, padded to whole tiles) over all views
+  int order;                     // 0: micro-tiles row by row; 1: tile by tile (8 micro-tiles of a tile in a row)
   uint32_t* hist;                // [kResolveBuckets] (device)
   uint32_t* fill;                // [kResolveBuckets] (device)
   uint32_t* items;               // [total_tiles] work list, costliest bucket first; null = view order
@@ -197,6 +202,7 @@ enum ResolveVariant : int {
   kResolveVariantLoop64x2 = 4,  // two micro-tiles per warp step
   kResolveVariantListShort4 = 5,  // lists of up to 4 (8) nodes in registers, bubble-sorted;
   kResolveVariantListShort8 = 6,  // longer ones walked again with the local arrays
+  kResolveVariantListDense = 7,   // local arrays, at most 32 registers (eight 256-thread blocks per SM)
 };
 cudaError_t resolve_bin(const ResolveBatch& b, cudaStream_t s, uint64_t* launches);
 cudaError_t resolve_run(const ResolveBatch& b, int variant, int threads, int blocks, cudaStream_t s);

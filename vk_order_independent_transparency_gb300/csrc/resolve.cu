@@ -40,13 +40,31 @@ __device__ __forceinline__ int find_view(const uint32_t* tb, int n, uint32_t g) 
   return lo;
 }
 
+// Micro-tile (mx, my) of work item t of a view in the batch's order; false
+// for the padding beyond the view's micro-tiles.
+__device__ __forceinline__ bool item_microtile(const ResolveView& v, uint32_t t, int order, uint32_t& mx,
+                                               uint32_t& my) {
+  if (order == 0) {
+    my = (uint32_t)(((uint64_t)t * v.ptx_recip) >> 40);
+    mx = t - my * (uint32_t)v.ptx;
+  } else {
+    const uint32_t tile = t >> 3, sub = t & 7u;
+    const uint32_t ty = (uint32_t)(((uint64_t)tile * v.tx_recip) >> 40);
+    mx = 2u * (tile - ty * (uint32_t)v.tiles_x) + (sub & 1u);
+    my = 4u * ty + (sub >> 1);
+  }
+  return mx < (uint32_t)v.mtx && my < (uint32_t)v.mty;
+}
+
 // Cost bucket of a micro-tile: 0 for no node reads, else 1 + floor(log2(cost)),
 // at most kResolveBuckets - 1. A list pixel reads one node per fragment; a
 // Loop64 pixel reads its kept keys plus the terminating empty key.
 __device__ __forceinline__ int tile_bucket(const ResolveView* __restrict__ views, const uint32_t* tb, int nv,
-                                           uint32_t g) {
+                                           uint32_t g, int order) {
   const int v = find_view(tb, nv, g);
-  const uint32_t len = __ldg(views[v].lens + (g - tb[v]));
+  uint32_t mx, my;
+  if (!item_microtile(views[v], g - tb[v], order, mx, my)) return 0;
+  const uint32_t len = __ldg(views[v].lens + (size_t)my * views[v].mtx + mx);
   const int L = views[v].L;
   const uint32_t cost = views[v].kind == kResolveList ? len : min(len, (uint32_t)L) + (len < (uint32_t)L ? 1u : 0u);
   if (cost == 0) return 0;
@@ -66,7 +84,7 @@ __global__ void __launch_bounds__(kBinThreads) k_rbin_count(ResolveBatch b) {
   const uint32_t lane = threadIdx.x & 31;
   for (int i = 0; i < kBinPerThread; ++i) {
     const uint32_t g = blockIdx.x * kBinChunk + i * kBinThreads + threadIdx.x;
-    const int bk = g < b.total_tiles ? tile_bucket(b.views, tb, b.num_views, g) : -1;
+    const int bk = g < b.total_tiles ? tile_bucket(b.views, tb, b.num_views, g, b.order) : -1;
     const uint32_t peers = __match_any_sync(0xffffffffu, bk);
     if (bk >= 0 && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&cnt[bk], (uint32_t)__popc(peers));
   }
@@ -86,7 +104,7 @@ __global__ void __launch_bounds__(kBinThreads) k_rbin_scatter(ResolveBatch b) {
 #pragma unroll
   for (int i = 0; i < kBinPerThread; ++i) {
     const uint32_t g = blockIdx.x * kBinChunk + i * kBinThreads + threadIdx.x;
-    bk[i] = g < b.total_tiles ? tile_bucket(b.views, tb, b.num_views, g) : -1;
+    bk[i] = g < b.total_tiles ? tile_bucket(b.views, tb, b.num_views, g, b.order) : -1;
     const uint32_t peers = __match_any_sync(0xffffffffu, bk[i]);
     const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
     uint32_t r = 0;
@@ -152,9 +170,9 @@ __device__ __forceinline__ bool item_pixel(const ResolveBatch& b, const uint32_t
   }
   const ResolveView& v = b.views[vi];
   o.v = &v;
-  o.tile = g - tb[vi];
-  const uint32_t my = (uint32_t)(((uint64_t)o.tile * v.mtx_recip) >> 40);
-  const uint32_t mx = o.tile - my * (uint32_t)v.mtx;
+  uint32_t mx, my;
+  if (!item_microtile(v, g - tb[vi], b.order, mx, my)) return false;
+  o.tile = my * (uint32_t)v.mtx + mx;  // the micro-tile's index in the view's lengths
   const int x = (int)mx * 8 + (lane & 7), y = (int)my * 4 + (lane >> 3);
   if (x >= v.W || y >= v.H) return false;
   o.pixel = (uint32_t)y * (uint32_t)v.W + (uint32_t)x;
@@ -170,8 +188,8 @@ constexpr int kSplitSlots = 8;
 
 // U micro-tiles per step: the independent first loads of all U (colour
 // target, list head) are issued before any list is walked.
-template <bool Split, int U, int Short = 0>
-__global__ void __launch_bounds__(256) k_resolve_list(ResolveBatch b) {
+template <bool Split, int U, int Short = 0, int MinBlocks = 1>
+__global__ void __launch_bounds__(256, MinBlocks) k_resolve_list(ResolveBatch b) {
   extern __shared__ __align__(16) uint32_t rsm[];
   load_bases(b, rsm);
   const int lane = threadIdx.x & 31;
@@ -263,6 +281,7 @@ cudaError_t with_kernel(int variant, F f) {
     case kResolveVariantListx2: return f(k_resolve_list<false, 2>);
     case kResolveVariantListShort4: return f(k_resolve_list<false, 1, 4>);
     case kResolveVariantListShort8: return f(k_resolve_list<false, 1, 8>);
+    case kResolveVariantListDense: return f(k_resolve_list<false, 1, 0, 8>);
     default: return cudaErrorInvalidValue;
   }
 }
