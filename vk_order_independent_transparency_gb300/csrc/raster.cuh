@@ -737,7 +737,13 @@ __global__ void __launch_bounds__(256, S == 1 ? 4 : 3) k_raster_transparent(Rast
         const int owner = act ? (py - w.ry0) * M::kW + (px - w.rx0) : 0;
         uint32_t od[S];
 #pragma unroll
-        for (int s = 0; s < S; ++s) od[s] = __shfl_sync(kFull, tg.depth[s], owner);
+        if (p.has_opaque) {
+#pragma unroll
+          for (int s = 0; s < S; ++s) od[s] = __shfl_sync(kFull, tg.depth[s], owner);
+        } else {
+#pragma unroll
+          for (int s = 0; s < S; ++s) od[s] = 0x3F800000u;  // no opaque pass: depth 1.0 everywhere
+        }
         uint32_t cover = 0;
         float zcen = 0.f;
         if (act) {
