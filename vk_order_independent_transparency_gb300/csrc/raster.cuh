@@ -736,7 +736,6 @@ __global__ void __launch_bounds__(256, S == 1 ? 4 : 3) k_raster_transparent(Rast
         const int px = w.rx0 + (int)((hk >> 11) & 7u) + r - row * wdt, py = w.ry0 + (int)((hk >> 14) & 3u) + row;
         const int owner = act ? (py - w.ry0) * M::kW + (px - w.rx0) : 0;
         uint32_t od[S];
-#pragma unroll
         if (p.has_opaque) {
 #pragma unroll
           for (int s = 0; s < S; ++s) od[s] = __shfl_sync(kFull, tg.depth[s], owner);
