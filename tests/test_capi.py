@@ -115,13 +115,21 @@ def test_srgb_table_file_is_current():
 
 @pytest.mark.parametrize('field,value', [('algorithm', 7), ('oit_layers', 3), ('oit_layers', 64), ('aa_type', 6),
                                          ('width', 0), ('linked_list_allocated_per_element', 0),
-                                         ('record_format', 5), ('width', 20000)])
+                                         ('record_format', 5), ('width', 20000), ('width', 16385),
+                                         ('height', 16385)])
 def test_create_rejects_invalid_state(lib, field, value):
     st = oit.make_state(oit.OIT_LINKEDLIST, 64, 64)
     setattr(st, field, value)
     ctx = ctypes.c_void_p()
     assert lib.oit_create(ctypes.byref(st), ctypes.byref(ctx)) == oit.OIT_ERR_INVALID_ARGUMENT
     assert not ctx.value
+
+
+def test_create_rejects_supersampled_size_past_the_limit(lib):
+    # 2x2 supersampling renders at twice the size: 8193 px wide is 16386 rendered
+    st = oit.make_state(oit.OIT_LOOP64, 8193, 64, aa_type=oit.OIT_AA_SUPER_4X)
+    ctx = ctypes.c_void_p()
+    assert lib.oit_create(ctypes.byref(st), ctypes.byref(ctx)) == oit.OIT_ERR_INVALID_ARGUMENT
 
 
 def test_null_arguments(lib):

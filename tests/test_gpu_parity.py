@@ -282,3 +282,30 @@ def test_half_colour_target(engine, alg, aa):
     kw = dict(oit_layers=L, nodes_per_pixel=6, aa_type=aa, flags=engine.OIT_FLAG_HALF_COLOR)
     g, o = run_pair(engine, alg, W, H, 40, percent=70, **kw)
     pu.check_pair(alg, g, o, W, H, L, aa, color_atol=1e-4, color_rtol=2.0 ** -11)
+
+
+@pytest.mark.parametrize('alg', ALGS)
+def test_empty_mesh_gives_background(engine, alg):
+    """No triangles at all: every pixel is the cleared background (0.2 linear,
+    oitRender.cpp:90) through every algorithm's composite."""
+    W, H = 40, 24
+    v = np.zeros((3, 10), np.float32)
+    i = np.zeros((0, 3), np.uint32)
+    r = engine.Renderer(engine.make_state(alg, W, H, oit_layers=4))
+    r.update_scene(engine.make_camera(W, H))
+    mesh = engine.DeviceMesh(v, np.zeros((1, 3), np.uint32))
+    mesh.c.num_triangles = 0
+    r.render_frame(mesh, 1, 100)
+    img = r.output()
+    assert r.get_error() == 0
+    thr, _ = engine.srgb_tables()
+    code = int(np.searchsorted(thr, np.float32(0.2), side='right'))
+    alpha = int(np.rint(np.float32(0.2) * np.float32(255.0)))
+    np.testing.assert_array_equal(img[..., :3], np.full((H, W, 3), code, np.uint8))
+    np.testing.assert_array_equal(img[..., 3], np.full((H, W), alpha, np.uint8))
+
+
+@pytest.mark.parametrize('alg', ALGS)
+def test_one_pixel_viewport(engine, alg):
+    g, o = run_pair(engine, alg, 1, 1, 20, seed=21, rmin=0.3, rmax=0.6, oit_layers=4, nodes_per_pixel=8)
+    check(engine, alg, g, o, 1, 1, 4)
