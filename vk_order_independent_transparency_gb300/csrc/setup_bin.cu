@@ -248,6 +248,36 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const uint32_t* __r
   if (grand_total && blockIdx.x == gridDim.x - 1 && threadIdx.x == kScanThreads - 1) *grand_total = pre;
 }
 
+// One block walks the tiles of a short array in order, carrying the running
+// sum: one launch instead of three for up to kScanLoopTiles tiles.
+constexpr int kScanLoopTiles = 8;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_loop(const uint32_t* __restrict__ in,
+                                                            uint32_t* __restrict__ out, size_t n,
+                                                            uint32_t* __restrict__ grand_total) {
+  __shared__ uint32_t smem[64];
+  uint32_t carry = 0;
+  for (size_t tile = 0; tile * kScanTile < n; ++tile) {
+    const size_t base = tile * kScanTile + (size_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+      v[i] = (base + i < n) ? in[base + i] : 0u;
+      s += v[i];
+    }
+    uint32_t total;
+    uint32_t pre = block_exclusive_scan(s, &total, smem) + carry;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+      if (base + i < n) out[base + i] = pre;
+      pre += v[i];
+    }
+    carry += total;
+  }
+  if (grand_total && threadIdx.x == 0) *grand_total = carry;
+}
+
 size_t blocks_for(size_t n) { return (n + kScanTile - 1) / kScanTile; }
 
 // Exclusive scan of n u32 values; grand_total (device, may be null) receives the sum.
@@ -260,6 +290,11 @@ cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, size_t n, uint32_t
   const size_t nb = blocks_for(n);
   if (nb == 1) {
     k_scan_apply<<<1, kScanThreads, 0, s>>>(in, out, n, nullptr, grand_total);
+    ++*launches;
+    return cudaGetLastError();
+  }
+  if (nb <= (size_t)kScanLoopTiles) {
+    k_scan_loop<<<1, kScanThreads, 0, s>>>(in, out, n, grand_total);
     ++*launches;
     return cudaGetLastError();
   }
