@@ -588,16 +588,36 @@ def run_batch(a, rank):
     # image back. The scene as template + instance table (what the sphere
     # scenes are), and as flattened meshes (what the reference uploads)
     outs = [torch.empty((vd['height'], vd['width'], 4), dtype=torch.uint8).pin_memory() for vd in vs]
-    d2h = sum(o.nbytes for o in outs)
-    inst_dev, inst_host = [], []
-    for vd in vs:
-        tmpl = oit.make_scene_instanced(vd['spheres'], seed=vd['seed'], radius_min=vd['radius_min'],
-                                        radius_max=vd['radius_max'])
-        inst_dev.append(oit.DeviceInstancedMesh(*tmpl))
-        inst_host.append(tuple(torch.from_numpy(np.ascontiguousarray(x).view(np.int32)).pin_memory() for x in tmpl))
+    # instanced scenes: every view's spheres share one template (same stacks
+    # and slices); the views' instance tables are packed in one buffer and
+    # their images land in one buffer, so a step is one copy in and one out
+    scenes = [oit.make_scene_instanced(vd['spheres'], seed=vd['seed'], radius_min=vd['radius_min'],
+                                       radius_max=vd['radius_max']) for vd in vs]
+    tv, ti = scenes[0][0], scenes[0][1]
+    counts = [sc[2].shape[0] for sc in scenes]
+    starts = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    # offsets in 4-byte words; the instance tables start 16-byte aligned
+    inst_at = (tv.size + ti.size + 3) // 4 * 4
+    scene_host = torch.zeros(inst_at + int(starts[-1]) * 8, dtype=torch.int32).pin_memory()
+    scene_np = scene_host.numpy()
+    scene_np[:tv.size] = tv.reshape(-1).view(np.int32)
+    scene_np[tv.size:tv.size + ti.size] = ti.reshape(-1).view(np.int32)
+    for sc, st in zip(scenes, starts[:-1]):
+        scene_np[inst_at + 8 * st:inst_at + 8 * (st + sc[2].shape[0])] = sc[2].reshape(-1).view(np.int32)
+    scene_dev = torch.empty_like(scene_host, device='cuda')
+    scene_dev.copy_(scene_host)
+    tv_dev = scene_dev[:tv.size].view(torch.float32).view(-1, 6)
+    ti_dev = scene_dev[tv.size:tv.size + ti.size].view(-1, 3)
+    inst_views = [oit.DeviceInstancedMesh.from_tensors(
+        tv_dev, ti_dev, scene_dev[inst_at + 8 * st:inst_at + 8 * (st + n)].view(torch.float32).view(-1, 8))
+        for st, n in zip(starts[:-1], counts)]
+    sizes = [vd['width'] * vd['height'] * 4 for vd in vs]
+    out_at = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    out_dev = torch.empty(int(out_at[-1]), dtype=torch.uint8, device='cuda')
+    out_host = torch.empty(int(out_at[-1]), dtype=torch.uint8).pin_memory()
     batch_inst = oit.Batch(parallel_streams=8)
-    batch_inst.set_views([(r, m, 0, 100) for r, m in zip(mixed, inst_dev)])
-    h2d = sum(x.nbytes for t in inst_host for x in t)
+    batch_inst.set_views([(r, m, 0, 100, out_dev.data_ptr() + int(o)) for r, m, o in zip(mixed, inst_views, out_at)])
+    h2d, d2h = scene_host.nbytes, out_host.nbytes
     hv = [(torch.from_numpy(np.ascontiguousarray(v)).pin_memory(), torch.from_numpy(
         np.ascontiguousarray(i).view(np.int32)).pin_memory()) for v, i, _ in host]
     h2d_flat = sum(x.nbytes + y.nbytes for x, y in hv)
@@ -609,12 +629,10 @@ def run_batch(a, rank):
         torch.cuda.current_stream().synchronize()
 
     def step_e2e():
-        for (tv, ti, inst), m in zip(inst_host, inst_dev):
-            m.template_vertices.view(torch.int32).copy_(tv, non_blocking=True)
-            m.template_indices.copy_(ti, non_blocking=True)
-            m.instances.view(torch.int32).copy_(inst, non_blocking=True)
+        scene_dev.copy_(scene_host, non_blocking=True)
         batch_inst.render(stream)
-        images_back()
+        out_host.copy_(out_dev, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
 
     def step_e2e_flat():
         for (x, y), m in zip(hv, meshes):
@@ -633,6 +651,9 @@ def run_batch(a, rank):
 
     e2e_s = e2e_time(step_e2e)
     e2e_flat_s = e2e_time(step_e2e_flat)
+    # the packed instanced step's images are the flattened meshes' bit for bit
+    e2e_same = all(torch.equal(out_host[int(o0):int(o1)], o.reshape(-1))
+                   for o, o0, o1 in zip(outs, out_at[:-1], out_at[1:]))
 
     # resolve alone: the batched persistent resolve of the mixed views against
     # one FP32-record composite launch per view, on the frames rendered above
@@ -662,7 +683,7 @@ def run_batch(a, rank):
     images = [r.output() for r in mixed]
     return dict(frags=frags, t_mixed=t_mixed, t_plain=t_plain, launches=launches, clocks=clk, sections=sections,
                 e2e_s=e2e_s, h2d=h2d, d2h=d2h, views=vs, t_res_mixed=t_res_mixed, t_res_plain=t_res_plain,
-                res_cfg=res_cfg, res_bytes=res_bytes, e2e_flat_s=e2e_flat_s, h2d_flat=h2d_flat,
+                res_cfg=res_cfg, res_bytes=res_bytes, e2e_flat_s=e2e_flat_s, h2d_flat=h2d_flat, e2e_same=e2e_same,
                 raster_bytes=raster_bytes, images=images)
 
 
@@ -721,7 +742,9 @@ def main_batch(a, rank, world):
         'speedup_vs_plain_fp32': round(value / plain, 3),
         'e2e': {'value': round(total / e2e_s / 1e6, 3), 'unit': 'Mfragments/s', 'h2d_bytes_per_step': res['h2d'],
                 'd2h_bytes_per_step': res['d2h'], 'ms_per_step': round(e2e_s / a.steps * 1e3, 4),
-                'path': 'oit_batch_render over instanced views: templates + instance tables in, 64 RGBA8 images out'},
+                'path': 'oit_batch_render over instanced views: one template + the packed instance tables in, '
+                        'the 64 RGBA8 images out (one copy each way)',
+                'images_equal_flat_mesh': bool(res['e2e_same'])},
         'e2e_flat_mesh': {'value': round(total / e2e_flat_s / 1e6, 3), 'unit': 'Mfragments/s',
                           'h2d_bytes_per_step': res['h2d_flat'], 'd2h_bytes_per_step': res['d2h'],
                           'ms_per_step': round(e2e_flat_s / a.steps * 1e3, 4),

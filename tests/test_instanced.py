@@ -138,3 +138,42 @@ def test_batch_with_instanced_views():
         for (r, _, _, _), ref in zip(views, refs):
             np.testing.assert_array_equal(r.read_buffer(oit.OIT_BUF_OUTPUT), ref)
             assert r.get_error() == 0
+
+
+@pytest.mark.gpu
+def test_batch_packed_scene_and_outputs():
+    """One template shared by every view, the views' instance tables slices of
+    one device buffer, and every image written into one device buffer through
+    the views' output pointers: the images equal the views' flattened meshes
+    rendered alone."""
+    import torch
+    specs = [(oit.OIT_LINKEDLIST, 72, 56, 8, 40), (oit.OIT_LOOP64, 64, 48, 4, 25), (oit.OIT_SIMPLE, 40, 40, 1, 31)]
+    scenes = [oit.make_scene_instanced(n, seed=70 + k, radius_min=0.05, radius_max=0.2)
+              for k, (_, _, _, _, n) in enumerate(specs)]
+    tv, ti = scenes[0][0], scenes[0][1]
+    tv_dev = torch.from_numpy(tv).cuda()
+    ti_dev = torch.from_numpy(ti.view(np.int32)).cuda()
+    # odd object counts: slices after the first start at 16-byte multiples anyway (32-byte records)
+    inst_dev = torch.from_numpy(np.concatenate([s[2] for s in scenes])).cuda()
+    starts = np.concatenate([[0], np.cumsum([s[2].shape[0] for s in scenes])])
+    sizes = [W * H * 4 for _, W, H, _, _ in specs]
+    at = np.concatenate([[0], np.cumsum(sizes)])
+    out = torch.full((int(at[-1]),), 7, dtype=torch.uint8, device='cuda')
+    views, refs = [], []
+    for k, (alg, W, H, L, n) in enumerate(specs):
+        kw = dict(seed=70 + k, radius_min=0.05, radius_max=0.2)
+        refs.append(_frame(alg, W, H, oit.make_scene(n, **kw), False, 90, oit_layers=L, nodes_per_pixel=10)['out'])
+        r = oit.Renderer(oit.make_state(alg, W, H, oit_layers=L, nodes_per_pixel=10))
+        r.update_scene(oit.make_camera(W, H))
+        m = oit.DeviceInstancedMesh.from_tensors(tv_dev, ti_dev, inst_dev[int(starts[k]):int(starts[k + 1])])
+        views.append((r, m, 0, 90, out.data_ptr() + int(at[k])))
+    batch = oit.Batch(parallel_streams=2)
+    batch.set_views(views)
+    for _ in range(3):
+        out.fill_(7)
+        batch.render()
+        torch.cuda.synchronize()
+        host = out.cpu().numpy()
+        for k, ref in enumerate(refs):
+            np.testing.assert_array_equal(host[at[k]:at[k + 1]], np.ascontiguousarray(ref).view(np.uint8).reshape(-1))
+            assert views[k][0].get_error() == 0

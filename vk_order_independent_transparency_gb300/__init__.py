@@ -282,13 +282,23 @@ class DeviceInstancedMesh:
 
     def __init__(self, template_vertices, template_indices, instances, device='cuda'):
         import torch
-        self.template_vertices = torch.as_tensor(np.ascontiguousarray(template_vertices, np.float32)).to(device)
-        self.template_indices = torch.as_tensor(
-            np.ascontiguousarray(template_indices, np.uint32).view(np.int32)).to(device)
-        self.instances = torch.as_tensor(np.ascontiguousarray(instances, np.float32)).to(device)
-        self.c = OitInstancedMesh(self.template_vertices.data_ptr(), self.template_indices.data_ptr(),
-                                  self.instances.data_ptr(), int(template_vertices.shape[0]),
-                                  int(template_indices.shape[0]), int(instances.shape[0]))
+        self._set(torch.as_tensor(np.ascontiguousarray(template_vertices, np.float32)).to(device),
+                  torch.as_tensor(np.ascontiguousarray(template_indices, np.uint32).view(np.int32)).to(device),
+                  torch.as_tensor(np.ascontiguousarray(instances, np.float32)).to(device))
+
+    @classmethod
+    def from_tensors(cls, template_vertices, template_indices, instances):
+        """Views of existing device tensors (float32 [nv, 6], int32 [nt, 3],
+        float32 [n, 8]): meshes can share one template and slice one instance
+        buffer, so a batch's scenes upload in one copy."""
+        m = cls.__new__(cls)
+        m._set(template_vertices, template_indices, instances)
+        return m
+
+    def _set(self, tv, ti, inst):
+        self.template_vertices, self.template_indices, self.instances = tv, ti, inst
+        self.c = OitInstancedMesh(tv.data_ptr(), ti.data_ptr(), inst.data_ptr(), int(tv.shape[0]), int(ti.shape[0]),
+                                  int(inst.shape[0]))
 
 
 class Renderer:
@@ -448,9 +458,11 @@ class Batch:
 
     def set_views(self, views):
         """views: list of (Renderer, DeviceMesh or DeviceInstancedMesh,
-        triangles_per_object, percent_transparent)."""
+        triangles_per_object, percent_transparent[, output device pointer]);
+        without an output pointer a view writes its context's OIT_BUF_OUTPUT."""
         arr = (OitViewFrame * len(views))()
-        for k, (r, mesh, tpo, pct) in enumerate(views):
+        for k, view in enumerate(views):
+            r, mesh, tpo, pct = view[:4]
             arr[k].ctx = r._ctx.value
             if isinstance(mesh, DeviceInstancedMesh):
                 arr[k].instanced_mesh = ctypes.pointer(mesh.c)
@@ -458,7 +470,7 @@ class Batch:
                 arr[k].mesh = ctypes.pointer(mesh.c)
             arr[k].triangles_per_object = tpo
             arr[k].percent_transparent = pct
-            arr[k].out_rgba8_device = None
+            arr[k].out_rgba8_device = view[4] if len(view) > 4 else None
         self._frames = arr
         self._keep = views
 
