@@ -76,7 +76,25 @@ def parse():
                     help='batch workload: the first N of its 64 views (smaller cases for profiling)')
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--hbm-random', action='store_true',
+                    help='measure HBM throughput for sequential, random and dependent-chain reads (csrc/hbm_random.cu)')
     return ap.parse_args()
+
+
+def hbm_random():
+    """Build and run the random-access measurement program; its JSON line."""
+    from vk_order_independent_transparency_gb300 import _build
+    src = os.path.join(ROOT, 'vk_order_independent_transparency_gb300', 'csrc', 'hbm_random.cu')
+    exe = os.path.join(_build.BUILD, 'hbm_random')
+    os.makedirs(_build.BUILD, exist_ok=True)
+    subprocess.run([_build.nvcc(), '-gencode', 'arch=compute_103a,code=sm_103a', '-O3', '-std=c++17', '-o', exe, src],
+                   check=True)
+    r = subprocess.run([exe], check=True, capture_output=True, text=True)
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    line['what'] = ('HBM read throughput (GB/s of bytes requested): sequential; independent random reads of G bytes, '
+                    'a warp\'s 32 reads in one window of the 4 GiB buffer; dependent chains of 16-byte reads '
+                    '(64 warps per SM)')
+    return line
 
 
 def workload_dict(name):
@@ -800,6 +818,9 @@ def resolve_line(res, a, world, total, t_mixed, t_plain, peak, peak_kind):
 
 def main():
     a = parse()
+    if a.hbm_random:
+        print(json.dumps(hbm_random()))
+        return
     wd = workload_dict(a.workload)
     rank = int(os.environ.get('RANK', '0'))
     world = int(os.environ.get('WORLD_SIZE', '1'))

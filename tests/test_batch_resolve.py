@@ -63,7 +63,8 @@ def test_batch_render_and_resolve_match_single_frames():
         assert cfg[part]['threads_per_block'] in (64, 128, 256) and cfg[part]['blocks'] >= 1
     assert cfg['linkedlist']['shared_slots'] in (0, 8) and cfg['loop64']['shared_slots'] == 0
     assert cfg['linkedlist']['register_slots'] in (0, 4, 8) and cfg['loop64']['register_slots'] == 0
-    assert cfg['loop64']['items_per_step'] in (1, 2) and not cfg['loop64']['dense']
+    assert cfg['loop64']['items_per_step'] in (1, 2) and cfg['loop64']['dense'] in (0, 1)
+    assert cfg['loop64']['items_per_step'] == 1 or not cfg['loop64']['dense']
     # resolve alone, after clearing the outputs
     import torch
     for r, _, _, _ in views:

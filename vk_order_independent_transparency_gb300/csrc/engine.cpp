@@ -912,8 +912,9 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
     std::vector<int> variants;
     if (part == 0)
       variants = {oit::kResolveVariantList, oit::kResolveVariantListShared, oit::kResolveVariantListx2,
-                  oit::kResolveVariantListShort4, oit::kResolveVariantListShort8, oit::kResolveVariantListDense};
-    else variants = {oit::kResolveVariantLoop64, oit::kResolveVariantLoop64x2};
+                  oit::kResolveVariantListShort4, oit::kResolveVariantListShort8, oit::kResolveVariantListDense,
+                  oit::kResolveVariantListShort8Dense};
+    else variants = {oit::kResolveVariantLoop64, oit::kResolveVariantLoop64x2, oit::kResolveVariantLoop64Dense};
     for (int variant : variants) {
       for (int threads : {64, 128, 256}) {
         const int bps = oit::resolve_blocks_per_sm(rp.rb, variant, threads);
@@ -1373,9 +1374,15 @@ int oit_batch_resolve_config(oit_batch* b, uint32_t part, oit_resolve_shape* out
   out->tile_order = rp.order;
   out->shared_slots = rp.variant == oit::kResolveVariantListShared ? 8 : 0;
   out->items_per_step = (rp.variant == oit::kResolveVariantListx2 || rp.variant == oit::kResolveVariantLoop64x2) ? 2 : 1;
-  out->register_slots =
-      rp.variant == oit::kResolveVariantListShort4 ? 4 : (rp.variant == oit::kResolveVariantListShort8 ? 8 : 0);
-  out->dense = rp.variant == oit::kResolveVariantListDense ? 1 : 0;
+  out->register_slots = rp.variant == oit::kResolveVariantListShort4 ? 4
+                        : (rp.variant == oit::kResolveVariantListShort8 ||
+                           rp.variant == oit::kResolveVariantListShort8Dense)
+                            ? 8
+                            : 0;
+  out->dense = (rp.variant == oit::kResolveVariantListDense || rp.variant == oit::kResolveVariantListShort8Dense ||
+                rp.variant == oit::kResolveVariantLoop64Dense)
+                   ? 1
+                   : 0;
   return OIT_OK;
 }
 

@@ -215,50 +215,78 @@ __device__ __forceinline__ float4 walk_list(const uint4* __restrict__ pool, uint
   return sum;
 }
 
-// walk_list for lists of at most min(K, OIT_LAYERS) nodes without coverage
-// masks: the nodes are appended to K registers (static indices), then ordered
-// by bubbleSort itself (swap on >=, unrolled over K) and blended; there is no
-// tail. A longer list is walked again by walk_list with the arrays `a`.
-template <bool F32, int K, class A>
-__device__ __forceinline__ float4 walk_list_short(const uint4* __restrict__ pool, uint32_t head, uint32_t cap, int L,
-                                                  int tail, int S, A& a) {
-  uint32_t rc[K], rd[K];
-  const int lim = L < K ? L : K;
+// Sorting networks on (depth, colour) pairs, ascending depth: the 5- and
+// 19-comparator networks for 4 and 8 entries (each sorts all 2^K 0-1 inputs,
+// so every input). For distinct depths the order equals bubbleSort's.
+__device__ __forceinline__ void net_ce(uint32_t& da, uint32_t& ca, uint32_t& db, uint32_t& cb) {
+  const bool s = walk_dlt(db, da);
+  const uint32_t d0 = da, c0 = ca;
+  da = s ? db : da;
+  ca = s ? cb : ca;
+  db = s ? d0 : db;
+  cb = s ? c0 : cb;
+}
+
+template <int K>
+__device__ __forceinline__ void net_sort(uint32_t (&d)[K], uint32_t (&c)[K]) {
+  static_assert(K == 4 || K == 8, "networks for 4 and 8 entries");
+#define OIT_CE(a, b) net_ce(d[a], c[a], d[b], c[b])
+  if constexpr (K == 4) {
+    OIT_CE(0, 1); OIT_CE(2, 3); OIT_CE(0, 2); OIT_CE(1, 3); OIT_CE(1, 2);
+  } else {
+    OIT_CE(0, 2); OIT_CE(1, 3); OIT_CE(4, 6); OIT_CE(5, 7);
+    OIT_CE(0, 4); OIT_CE(1, 5); OIT_CE(2, 6); OIT_CE(3, 7);
+    OIT_CE(0, 1); OIT_CE(2, 3); OIT_CE(4, 5); OIT_CE(6, 7);
+    OIT_CE(2, 4); OIT_CE(3, 5);
+    OIT_CE(1, 4); OIT_CE(3, 6);
+    OIT_CE(1, 2); OIT_CE(3, 4); OIT_CE(5, 6);
+  }
+#undef OIT_CE
+}
+
+// Lists of at most K nodes, K <= OIT_LAYERS (all kept, no tail), 1x: the walk
+// only appends each node to the thread's shared-memory column (entry i at
+// col[i * 32], the columns of a warp's lanes side by side); the entries are sorted in registers by the network, which is
+// bubbleSort's order when the depths are distinct, and blended from the
+// column. Returns false, with nothing blended, for a list longer than K or
+// with equal depths (bubbleSort's order then depends on its passes: the
+// caller's full walk runs it).
+template <int K>
+__device__ __forceinline__ bool walk_list_staged(const uint4* __restrict__ pool, uint32_t head, uint32_t cap,
+                                                 uint32_t* sc, uint32_t* sd, float4& sum) {
+  constexpr int T = 32;  // the warp's columns: entry i of a lane at [i * 32 + lane]
   uint32_t off = head < cap ? head : 0u;
-  int k = 0;
+  int n = 0;
 #pragma unroll 1
   while (off != 0) {
-    if (k == lim) return walk_list<F32>(pool, head, cap, L, tail, S, a);
-    const WalkNode n = load_node<F32>(pool, off);
+    if (n == K) return false;
+    const WalkNode nd = load_node<false>(pool, off);
+    sc[n * T] = nd.c;
+    sd[n * T] = nd.d;
+    ++n;
+    off = nd.next < cap ? nd.next : 0u;
+  }
+  {
+    uint32_t d[K], c[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      d[i] = i < n ? sd[i * T] : 0x7f800000u;  // +inf after the entries
+      c[i] = i < n ? sc[i * T] : 0u;
+    }
+    net_sort<K>(d, c);
+    bool tie = false;
+#pragma unroll
+    for (int i = 0; i + 1 < K; ++i)
+      if (i + 1 < n) tie |= !walk_dlt(d[i], d[i + 1]);
+    if (tie) return false;
 #pragma unroll
     for (int i = 0; i < K; ++i)
-      if (i == k) {
-        rc[i] = n.c;
-        rd[i] = n.d;
-      }
-    ++k;
-    off = n.next < cap ? n.next : 0u;
+      if (i < n) sc[i * T] = c[i];
   }
-#pragma unroll
-  for (int i = K - 2; i >= 0; --i) {
-    if (i <= k - 2) {
-#pragma unroll
-      for (int j = 0; j <= i; ++j) {
-        if (walk_dge(rd[j], rd[j + 1])) {
-          const uint32_t tc = rc[j], td = rd[j];
-          rc[j] = rc[j + 1];
-          rd[j] = rd[j + 1];
-          rc[j + 1] = tc;
-          rd[j + 1] = td;
-        }
-      }
-    }
-  }
-  float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-  for (int i = 0; i < K; ++i)
-    if (i < k) blend_under(sum, node_colour<F32>(pool, rc[i]));
-  return sum;
+  sum = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+  for (int i = 0; i < n; ++i) blend_under(sum, decode_premult(sc[i * T]));
+  return true;
 }
 
 }  // namespace oitd

@@ -200,9 +200,11 @@ enum ResolveVariant : int {
   kResolveVariantListShared = 2,
   kResolveVariantListx2 = 3,    // two micro-tiles per warp step
   kResolveVariantLoop64x2 = 4,  // two micro-tiles per warp step
-  kResolveVariantListShort4 = 5,  // lists of up to 4 (8) nodes in registers, bubble-sorted;
-  kResolveVariantListShort8 = 6,  // longer ones walked again with the local arrays
+  kResolveVariantListShort4 = 5,  // micro-tiles whose lists hold at most 4 (8) nodes staged in shared
+  kResolveVariantListShort8 = 6,  // memory and sorted by a network; longer ones with the local arrays
   kResolveVariantListDense = 7,   // local arrays, at most 32 registers (eight 256-thread blocks per SM)
+  kResolveVariantListShort8Dense = 8,  // Short8 at most 32 registers
+  kResolveVariantLoop64Dense = 9,      // Loop64 at most 32 registers
 };
 cudaError_t resolve_bin(const ResolveBatch& b, cudaStream_t s, uint64_t* launches);
 cudaError_t resolve_run(const ResolveBatch& b, int variant, int threads, int blocks, cudaStream_t s);

@@ -129,20 +129,24 @@ __global__ void __launch_bounds__(kBinThreads) k_rbin_scatter(ResolveBatch b) {
 
 // oitLoop64.frag.glsl:162-183: the keys are sorted; blend until the first
 // empty one. key0 was fetched ahead; `nmax` bounds the keys to read (the
-// micro-tile's longest list plus its terminator), fetched four at a time
-// without waiting on each other (lanes of a row share every layer's sectors).
+// micro-tile's longest list plus its terminator), fetched kLoop64Batch at a
+// time without waiting on each other (lanes of a row share every layer's
+// sectors).
+constexpr int kLoop64Batch = 4;
+
 __device__ __forceinline__ float4 resolve_loop64(const ResolveView& v, uint32_t pixel, uint2 key0, int nmax) {
   const uint2* __restrict__ ab = reinterpret_cast<const uint2*>(v.abuf) + pixel;
   float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
   if (key0.y == kEmptyKey) return sum;
   blend_under(sum, decode_premult(key0.x));
-  for (int i0 = 1; i0 < nmax; i0 += 4) {
-    uint2 key[4];
+  for (int i0 = 1; i0 < nmax; i0 += kLoop64Batch) {
+    uint2 key[kLoop64Batch];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) key[j] = i0 + j < nmax ? __ldg(ab + (size_t)(i0 + j) * v.P) : make_uint2(0u, kEmptyKey);
+    for (int j = 0; j < kLoop64Batch; ++j)
+      key[j] = i0 + j < nmax ? __ldg(ab + (size_t)(i0 + j) * v.P) : make_uint2(0u, kEmptyKey);
     bool done = false;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < kLoop64Batch; ++j) {
       done |= key[j].y == kEmptyKey;
       if (!done) blend_under(sum, decode_premult(key[j].x));
     }
@@ -196,12 +200,17 @@ __global__ void __launch_bounds__(256, MinBlocks) k_resolve_list(ResolveBatch b)
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   using Arrays = typename std::conditional<Split, SplitArrays<kSplitSlots>, WalkArrays<false>>::type;
   Arrays a;
+  uint32_t* col = rsm + ((b.num_views + 3) & ~3);
   if constexpr (Split) {
-    uint32_t* col = rsm + ((b.num_views + 3) & ~3);
     a.sc = col + threadIdx.x;
     a.sd = col + kSplitSlots * blockDim.x + threadIdx.x;
     a.T = blockDim.x;
   }
+  // Short: the thread's staging columns for short lists, [warp][Short][32]
+  // colours then depths
+  constexpr int kStage = Short > 0 ? Short : 1;
+  uint32_t* stc = col + (threadIdx.x >> 5) * (2 * kStage * 32) + lane;
+  uint32_t* std_ = stc + kStage * 32;
   int vi = 0;
   for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < b.total_tiles; it += U * warps) {
     ItemPixel ip[U];
@@ -223,16 +232,27 @@ __global__ void __launch_bounds__(256, MinBlocks) k_resolve_list(ResolveBatch b)
       const ResolveView& v = *ip[u].v;
       const uint4* pool = reinterpret_cast<const uint4*>(v.abuf);
       float4 sum;
-      if constexpr (Short > 0) sum = walk_list_short<false, Short>(pool, head[u], v.capacity, v.L, v.tail, 1, a);
-      else sum = walk_list<false>(pool, head[u], v.capacity, v.L, v.tail, 1, a);
+      // Short: a micro-tile whose longest list (the raster's count of the
+      // fragments each pixel received, at least its list length) fits in 4
+      // or Short entries and in OIT_LAYERS is staged and sorted by a network;
+      // the choice is per warp
+      bool done = false;
+      if constexpr (Short > 0) {
+        const int len = (int)__ldg(v.lens + ip[u].tile);
+        if (len <= min(4, v.L))
+          done = walk_list_staged<4>(pool, head[u], v.capacity, stc, std_, sum);
+        else if (Short > 4 && len <= min(Short, v.L))
+          done = walk_list_staged<Short>(pool, head[u], v.capacity, stc, std_, sum);
+      }
+      if (!done) sum = walk_list<false>(pool, head[u], v.capacity, v.L, v.tail, 1, a);
       rop_over(c[u], sum);
       write_rgba8(v.out, v.out_linear, ip[u].pixel, c[u]);
     }
   }
 }
 
-template <int U>
-__global__ void __launch_bounds__(256) k_resolve_loop64(ResolveBatch b) {
+template <int U, int MinBlocks = 1>
+__global__ void __launch_bounds__(256, MinBlocks) k_resolve_loop64(ResolveBatch b) {
   extern __shared__ __align__(16) uint32_t rsm[];
   load_bases(b, rsm);
   const int lane = threadIdx.x & 31;
@@ -268,7 +288,12 @@ __global__ void __launch_bounds__(256) k_resolve_loop64(ResolveBatch b) {
 
 size_t resolve_smem(const ResolveBatch& b, int variant, int threads) {
   const size_t bases = (size_t)((b.num_views + 3) & ~3) * 4;
-  return bases + (variant == kResolveVariantListShared ? (size_t)threads * kSplitSlots * 8 : 0);
+  const int slots = variant == kResolveVariantListShared || variant == kResolveVariantListShort8 ||
+                            variant == kResolveVariantListShort8Dense
+                        ? 8
+                    : variant == kResolveVariantListShort4                                      ? 4
+                                                                                                : 0;
+  return bases + (size_t)threads * slots * 8;
 }
 
 template <class F>
@@ -282,6 +307,8 @@ cudaError_t with_kernel(int variant, F f) {
     case kResolveVariantListShort4: return f(k_resolve_list<false, 1, 4>);
     case kResolveVariantListShort8: return f(k_resolve_list<false, 1, 8>);
     case kResolveVariantListDense: return f(k_resolve_list<false, 1, 0, 8>);
+    case kResolveVariantListShort8Dense: return f(k_resolve_list<false, 1, 8, 8>);
+    case kResolveVariantLoop64Dense: return f(k_resolve_loop64<1, 8>);
     default: return cudaErrorInvalidValue;
   }
 }
