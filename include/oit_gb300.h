@@ -304,6 +304,16 @@ typedef struct oit_resolve_shape {
  * zeros. OIT_ERR_STATE before the first resolve. */
 int oit_batch_resolve_config(oit_batch* batch, uint32_t part, oit_resolve_shape* shape);
 
+/* Pins the shape of one part of the batched resolve (a shape reported by
+ * oit_batch_resolve_config, e.g. tuned once offline): the autotuner then
+ * skips that part. blocks 0: every block that fits on the GPU. Shapes the
+ * engine has no kernel for (for Loop64: shared or register slots; for linked
+ * lists: more than one of shared slots, register slots and two items per
+ * step, or dense with shared slots, register slots 4 or two items per step)
+ * return OIT_ERR_INVALID_ARGUMENT. NULL unpins. The next render or resolve
+ * of the batch uses it. */
+int oit_batch_set_resolve_config(oit_batch* batch, uint32_t part, const oit_resolve_shape* shape);
+
 /* ---- inspection -------------------------------------------------------- */
 
 /* Synchronises the context's last stream and returns the device error bits

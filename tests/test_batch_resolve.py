@@ -106,3 +106,70 @@ def test_batch_resolve_before_render_is_a_state_error():
     assert e.value.status == oit.OIT_ERR_STATE
     with pytest.raises(oit.OitError):
         batch.resolve_config()
+
+
+# every kernel the autotuner chooses from, pinned: (part, shape)
+PINNED = [
+    ('linkedlist', dict(threads_per_block=128)),
+    ('linkedlist', dict(threads_per_block=256, dense=1)),
+    ('linkedlist', dict(threads_per_block=64, shared_slots=8)),
+    ('linkedlist', dict(threads_per_block=128, items_per_step=2)),
+    ('linkedlist', dict(threads_per_block=64, register_slots=4)),
+    ('linkedlist', dict(threads_per_block=128, register_slots=8)),
+    ('linkedlist', dict(threads_per_block=256, register_slots=8, dense=1)),
+    ('loop64', dict(threads_per_block=256)),
+    ('loop64', dict(threads_per_block=128, items_per_step=2)),
+    ('loop64', dict(threads_per_block=256, dense=1)),
+]
+
+
+@pytest.mark.parametrize('order', [0, 1])
+@pytest.mark.parametrize('binned', [0, 1])
+def test_every_pinned_resolve_shape(binned, order):
+    """Each resolve kernel, in both work orders, binned or not, pinned
+    through oit_batch_set_resolve_config, gives every view the image its own
+    composite launch gives."""
+    import torch
+    views, refs, _ = _views(SPECS, 700)
+    batch = oit.Batch(parallel_streams=4)
+    batch.set_views(views)
+    batch.render()
+    for part, shape in PINNED:
+        batch.set_resolve_config(part, dict(shape, binned=binned, tile_order=order, blocks=37))
+        for r, _, _, _ in views:
+            ptr, nb = r.buffer(oit.OIT_BUF_OUTPUT)
+            oit._cudart().cudaMemset(ctypes.c_void_p(ptr), 0, ctypes.c_size_t(nb))
+        torch.cuda.synchronize()
+        batch.resolve()
+        got = batch.resolve_config()[part]
+        for f, v in shape.items():
+            assert got[f] == v, (part, shape, got)
+        assert got['binned'] == bool(binned) and got['tile_order'] == bool(order)
+        for k, ((r, _, _, _), ref) in enumerate(zip(views, refs)):
+            np.testing.assert_array_equal(r.output(), ref, err_msg='%s %s view %d' % (part, shape, k))
+        batch.set_resolve_config(part, None)
+    # pinned, the graph replays it too
+    batch.set_resolve_config('linkedlist', dict(threads_per_block=64, register_slots=8, blocks=0))
+    for _ in range(3):
+        batch.render()
+    assert batch.resolve_config()['linkedlist']['register_slots'] == 8
+    for (r, _, _, _), ref in zip(views, refs):
+        np.testing.assert_array_equal(r.output(), ref)
+
+
+def test_pinned_shape_validation():
+    batch = oit.Batch()
+    bad = [('loop64', dict(threads_per_block=128, shared_slots=8)), ('loop64', dict(threads_per_block=128,
+                                                                                    register_slots=4)),
+           ('loop64', dict(threads_per_block=128, items_per_step=2, dense=1)),
+           ('linkedlist', dict(threads_per_block=128, shared_slots=8, register_slots=8)),
+           ('linkedlist', dict(threads_per_block=128, register_slots=4, dense=1)),
+           ('linkedlist', dict(threads_per_block=128, items_per_step=3)),
+           ('linkedlist', dict(threads_per_block=48)), ('linkedlist', dict(threads_per_block=512)),
+           ('linkedlist', dict(threads_per_block=128, shared_slots=4))]
+    for part, shape in bad:
+        with pytest.raises(oit.OitError) as e:
+            batch.set_resolve_config(part, shape)
+        assert e.value.status == oit.OIT_ERR_INVALID_ARGUMENT
+    batch.set_resolve_config('linkedlist', dict(threads_per_block=128))
+    batch.set_resolve_config('linkedlist', None)

@@ -50,7 +50,7 @@ EXPORTS = [
     'oit_profile_enable', 'oit_profile_read', 'oit_render_frame_noalloc',
     'oit_batch_create', 'oit_batch_destroy', 'oit_batch_render', 'oit_batch_launch_count',
     'oit_render_frame_instanced', 'oit_render_frame_instanced_host', 'oit_scene_generate_instanced',
-    'oit_batch_resolve', 'oit_batch_resolve_config',
+    'oit_batch_resolve', 'oit_batch_resolve_config', 'oit_batch_set_resolve_config',
 ]
 PROF_SECTIONS = ['opaque_bin', 'opaque_raster', 'transparent_bin', 'transparent_raster', 'composite']
 
@@ -160,6 +160,7 @@ def library():
         'oit_scene_generate_instanced': (I, [ctypes.POINTER(OitSceneDesc), P, P, P]),
         'oit_batch_resolve': (I, [P, ctypes.POINTER(OitViewFrame), U, P]),
         'oit_batch_resolve_config': (I, [P, U, ctypes.POINTER(OitResolveShape)]),
+        'oit_batch_set_resolve_config': (I, [P, U, ctypes.POINTER(OitResolveShape)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -497,6 +498,16 @@ class Batch:
             out[name] = {f: (bool(getattr(sh, f)) if f in ('binned', 'tile_order', 'dense') else getattr(sh, f))
                          for f, _ in OitResolveShape._fields_}
         return out
+
+    def set_resolve_config(self, part, shape):
+        """Pins one part's shape ('linkedlist' or 'loop64'; a dict with the
+        fields resolve_config reports, missing ones 0), or unpins it (None)."""
+        idx = {'linkedlist': 0, 'loop64': 1}[part] if isinstance(part, str) else int(part)
+        if shape is None:
+            _check(self.lib.oit_batch_set_resolve_config(self._b, idx, None), 'oit_batch_set_resolve_config')
+            return
+        sh = OitResolveShape(**{f: int(shape.get(f, 0)) for f, _ in OitResolveShape._fields_})
+        _check(self.lib.oit_batch_set_resolve_config(self._b, idx, ctypes.byref(sh)), 'oit_batch_set_resolve_config')
 
 
 _cudart_lib = None

@@ -725,6 +725,13 @@ struct oit_batch {
     bool binned = false;
   };
   ResolvePart rparts[2];
+  // shapes pinned by oit_batch_set_resolve_config (blocks 0: all that fit)
+  struct Pin {
+    bool set = false;
+    int variant = 0, threads = 128, blocks = 0, order = 0;
+    bool binned = false;
+  };
+  Pin pin[2];
   // share of its resident blocks the linked-list part launches while the
   // Loop64 part takes the rest (both run side by side); 1 = both full
   float r_share = 1.0f;
@@ -908,6 +915,20 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
   for (int part = 0; part < 2 && r == OIT_OK; ++part) {
     oit_batch::ResolvePart& rp = b->rparts[part];
     if (rp.rb.num_views == 0) continue;
+    if (b->pin[part].set) {
+      const oit_batch::Pin& pn = b->pin[part];
+      const int bps = oit::resolve_blocks_per_sm(rp.rb, pn.variant, pn.threads);
+      if (bps <= 0) {
+        r = OIT_ERR_UNSUPPORTED;
+        break;
+      }
+      rp.variant = pn.variant;
+      rp.threads = pn.threads;
+      rp.blocks = pn.blocks > 0 ? pn.blocks : bps * b->num_sms;
+      rp.binned = pn.binned;
+      rp.order = pn.order;
+      continue;
+    }
     float best = 1e30f;
     std::vector<int> variants;
     if (part == 0)
@@ -1356,6 +1377,47 @@ int oit_batch_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n, voi
   r = b->r_tuned ? batch_resolve_launch(b, s, &launches) : batch_autotune(b, s);
   for (uint32_t i = 0; i < n; ++i) views[i].ctx->last_stream = s;
   return r;
+}
+
+int oit_batch_set_resolve_config(oit_batch* b, uint32_t part, const oit_resolve_shape* shape) {
+  if (!b || part > 1) return OIT_ERR_INVALID_ARGUMENT;
+  oit_batch::Pin pn;
+  if (shape) {
+    const oit_resolve_shape& sh = *shape;
+    if (sh.threads_per_block < 32 || sh.threads_per_block > 256 || sh.threads_per_block % 32 != 0)
+      return OIT_ERR_INVALID_ARGUMENT;
+    if ((sh.binned != 0 && sh.binned != 1) || (sh.tile_order != 0 && sh.tile_order != 1) ||
+        (sh.dense != 0 && sh.dense != 1) || (sh.items_per_step != 0 && sh.items_per_step != 1 && sh.items_per_step != 2))
+      return OIT_ERR_INVALID_ARGUMENT;
+    const bool x2 = sh.items_per_step == 2;
+    if (part == 1) {
+      if (sh.shared_slots != 0 || sh.register_slots != 0 || (x2 && sh.dense)) return OIT_ERR_INVALID_ARGUMENT;
+      pn.variant = x2 ? oit::kResolveVariantLoop64x2
+                      : (sh.dense ? oit::kResolveVariantLoop64Dense : oit::kResolveVariantLoop64);
+    } else {
+      if ((sh.shared_slots != 0 && sh.shared_slots != 8) ||
+          (sh.register_slots != 0 && sh.register_slots != 4 && sh.register_slots != 8))
+        return OIT_ERR_INVALID_ARGUMENT;
+      if ((sh.shared_slots != 0) + (sh.register_slots != 0) + (int)x2 > 1) return OIT_ERR_INVALID_ARGUMENT;
+      if (sh.dense && (sh.shared_slots != 0 || sh.register_slots == 4 || x2)) return OIT_ERR_INVALID_ARGUMENT;
+      if (sh.shared_slots) pn.variant = oit::kResolveVariantListShared;
+      else if (x2) pn.variant = oit::kResolveVariantListx2;
+      else if (sh.register_slots == 4) pn.variant = oit::kResolveVariantListShort4;
+      else if (sh.register_slots == 8)
+        pn.variant = sh.dense ? oit::kResolveVariantListShort8Dense : oit::kResolveVariantListShort8;
+      else pn.variant = sh.dense ? oit::kResolveVariantListDense : oit::kResolveVariantList;
+    }
+    pn.set = true;
+    pn.threads = (int)sh.threads_per_block;
+    pn.blocks = (int)std::min<uint32_t>(sh.blocks, 1u << 20);
+    pn.binned = sh.binned != 0;
+    pn.order = sh.tile_order;
+  }
+  b->pin[part] = pn;
+  // tune (or apply the pins) again on the next render or resolve, and capture again
+  b->r_tuned = false;
+  b->drop();
+  return OIT_OK;
 }
 
 int oit_batch_resolve_config(oit_batch* b, uint32_t part, oit_resolve_shape* out) {
