@@ -826,10 +826,10 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock, (S == 1 ? 32 : 24) 
 // Opaque pass: opaque.frag.glsl:30-35, depth LESS with write (main.cpp:542-547).
 // ---------------------------------------------------------------------------
 template <int S>
-__global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
-  __shared__ TriSetup stage_all[oit::kWarpsPerTile * 32];
-  __shared__ uint32_t stage_t_all[oit::kWarpsPerTile * 32];
-  __shared__ uint2 stage_bb_all[oit::kWarpsPerTile * 32];
+__global__ void __launch_bounds__(32 * kRasterWarpsPerBlock) k_raster_opaque(RasterParams p) {
+  __shared__ TriSetup stage_all[kRasterWarpsPerBlock * 32];
+  __shared__ uint32_t stage_t_all[kRasterWarpsPerBlock * 32];
+  __shared__ uint2 stage_bb_all[kRasterWarpsPerBlock * 32];
   const int warp = threadIdx.x >> 5;
   const WarpTile w = warp_tile<1>(p);
   TriSetup* stage = stage_all + warp * 32;
@@ -841,7 +841,7 @@ __global__ void __launch_bounds__(256) k_raster_opaque(RasterParams p) {
     dep[s] = w.valid ? p.depth[(size_t)s * p.P + w.pixel] : 0x3F800000u;
     col[s] = w.valid ? p.opaque_color[(size_t)s * p.P + w.pixel] : p.background;
   }
-  const int tile = blockIdx.x + p.tile_offset;
+  const int tile = (int)((blockIdx.x * kRasterWarpsPerBlock + warp) / oit::kWarpsPerTile) + p.tile_offset;
   walk_tile(p, w, stage, stage_t_all + warp * 32, stage_bb, p.tile_begin[tile], p.tile_end[tile], [&](int nh) {
     for (int k = 0; k < nh; ++k) {
       if (!lane_in_bbox(stage_bb[k], w)) continue;  // no warp-collective operation follows
@@ -932,11 +932,12 @@ cudaError_t launch_transparent(const RasterParams& p, cudaStream_t s) {
 }
 
 inline cudaError_t launch_opaque(const RasterParams& p, cudaStream_t s) {
-  const unsigned grid = (unsigned)(p.tiles_x * p.tiles_y);
+  const unsigned grid = (unsigned)(p.tiles_x * p.tiles_y * (oit::kWarpsPerTile / kRasterWarpsPerBlock));
+  constexpr int kThreads = 32 * kRasterWarpsPerBlock;
   switch (p.S) {
-    case 1: k_raster_opaque<1><<<grid, 256, 0, s>>>(p); break;
-    case 4: k_raster_opaque<4><<<grid, 256, 0, s>>>(p); break;
-    case 8: k_raster_opaque<8><<<grid, 256, 0, s>>>(p); break;
+    case 1: k_raster_opaque<1><<<grid, kThreads, 0, s>>>(p); break;
+    case 4: k_raster_opaque<4><<<grid, kThreads, 0, s>>>(p); break;
+    case 8: k_raster_opaque<8><<<grid, kThreads, 0, s>>>(p); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
