@@ -388,6 +388,7 @@ struct oit_context {
     p.tile_end = tile_end.as<uint32_t>();
     p.tile_offset = tile_offset;
     p.tile_tris = tris.as<uint32_t>();
+    p.tile_keys = keys.as<uint32_t>();
     p.bbox = bbox.as<uint2>();
     p.setup = setup.p;
     p.persp = persp.p;

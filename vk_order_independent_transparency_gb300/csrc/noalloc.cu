@@ -213,6 +213,7 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   p.tile_begin = b.tile_begin;
   p.tile_end = b.tile_end;
   p.tile_tris = b.tris;
+  p.tile_keys = b.keys;
   p.bbox = bbox;
   p.setup = setup;
   p.persp = persp;

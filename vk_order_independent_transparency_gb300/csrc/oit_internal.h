@@ -10,6 +10,9 @@ namespace oit {
 
 constexpr int kTile = 16;            // binning tile edge in pixels
 constexpr int kWarpsPerTile = 8;     // one warp per 8x4 micro-tile
+// pair keys: tile id in the low 24 bits (sorted), the micro-tile mask above
+constexpr int kMaskShift = 24;
+constexpr uint32_t kTileKeyMask = (1u << kMaskShift) - 1u;
 constexpr uint32_t kEmpty32 = 0xFFFFFFFFu;
 
 struct Mat4 {
@@ -91,6 +94,10 @@ struct RasterParams {
   const uint32_t* tile_end;
   int tile_offset;               // 0: opaque lists, num_tiles: transparent lists
   const uint32_t* tile_tris;
+  // the sorted pair keys beside tile_tris: tile id (bits 0-23) and the 8x4
+  // micro-tiles of the tile that the triangle's bbox overlaps (bit 24 + k for
+  // micro-tile k = 2 * row + column)
+  const uint32_t* tile_keys;
   const uint2* bbox;
   const void* setup;
   const void* persp;

@@ -412,6 +412,7 @@ struct WeightedPolicy {
 // and SSN CTAs cover the tile.
 struct WarpTile {
   int lane, px, py, rx0, ry0, rx1, ry1;
+  int mt;      // the warp's micro-tile (or sample group) within the tile
   int sample;  // the lane's sample with sample shading, else 0
   bool valid;
   uint32_t pixel;
@@ -435,6 +436,7 @@ __device__ __forceinline__ WarpTile warp_tile(const RasterParams& p) {
   const int gw = blockIdx.x * (int)(blockDim.x >> 5) + warp;   // warp within the pass
   const int tile = gw / (oit::kWarpsPerTile * SSN);
   const int mt = gw % (oit::kWarpsPerTile * SSN);           // micro-tile within the tile
+  w.mt = mt;
   const int tx = tile % p.tiles_x, ty = tile / p.tiles_x;
   w.rx0 = tx * 16 + (mt % (16 / M::kW)) * M::kW;
   w.ry0 = ty * 16 + (mt / (16 / M::kW)) * M::kH;
@@ -465,29 +467,40 @@ __device__ __forceinline__ bool bbox_hits(uint2 bb, const WarpTile& w) {
 }
 
 // Walks [beg, end) of the tile list in primitive order, 32 entries at a time:
-// the lanes test their triangle's bbox against the warp's micro-tile, the hits
-// copy their setup records into the warp's shared-memory stage in parallel
+// the lanes test their triangle against the warp's micro-tile, the hits copy
+// their setup records into the warp's shared-memory stage in parallel
 // (cp.async) with their triangle ids and bboxes, then chunk(nh) processes
 // stage slots 0..nh-1, which are in list order. chunk is warp-uniform.
-template <class Chunk>
+// Mask (8x4 micro-tiles, one lane per pixel): the test is the micro-tile's bit
+// in the pair's sorted key (the binning wrote the bbox's micro-tile overlap
+// there), so only hits gather their bbox; else the bbox itself is tested.
+template <bool Mask, class Chunk>
 __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile& w, TriSetup* stage,
                                           uint32_t* stage_t, uint2* stage_bb, uint32_t beg, uint32_t end,
                                           Chunk&& chunk) {
   const TriSetup* __restrict__ setup = reinterpret_cast<const TriSetup*>(p.setup);
   const uint32_t lt = (1u << w.lane) - 1u;
+  const uint32_t mbit = 1u << (oit::kMaskShift + (Mask ? w.mt : 0));
   uint32_t t_next = 0;
+  bool h_next = false;
   uint2 bb_next = make_uint2(0xFFFFFFFFu, 0u);  // empty bbox
   if (beg + w.lane < end) {
     t_next = __ldg(&p.tile_tris[beg + w.lane]);
-    bb_next = __ldg(&p.bbox[t_next]);
+    if (Mask) h_next = (__ldg(&p.tile_keys[beg + w.lane]) & mbit) != 0u;
+    if (!Mask || h_next) bb_next = __ldg(&p.bbox[t_next]);
   }
   for (uint32_t base = beg; base < end; base += 32) {
     const uint32_t t = t_next;
     const uint2 bb = bb_next;
-    const bool hit = (base + w.lane < end) && bbox_hits(bb, w);
+    const bool hit = (base + w.lane < end) && (Mask ? h_next : bbox_hits(bb, w));
     const uint32_t nb = base + 32;
     const bool more = nb + w.lane < end;
-    if (more) t_next = __ldg(&p.tile_tris[nb + w.lane]);
+    if (more) {
+      t_next = __ldg(&p.tile_tris[nb + w.lane]);
+      if (Mask) h_next = (__ldg(&p.tile_keys[nb + w.lane]) & mbit) != 0u;
+    } else {
+      h_next = false;
+    }
     const uint32_t m = __ballot_sync(kFull, hit);
     if (hit) {
       const int slot = __popc(m & lt);
@@ -498,7 +511,7 @@ __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile&
       stage_t[slot] = t;
       stage_bb[slot] = bb;
     }
-    bb_next = more ? __ldg(&p.bbox[t_next]) : make_uint2(0xFFFFFFFFu, 0u);
+    bb_next = more && (!Mask || h_next) ? __ldg(&p.bbox[t_next]) : make_uint2(0xFFFFFFFFu, 0u);
     cp_async_wait_all();
     __syncwarp();
     if (m) chunk(__popc(m));
@@ -790,7 +803,7 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock, (S == 1 ? 32 : 24) 
       __syncwarp();
     };
 
-    walk_tile(p, w, stage, stage_t, stage_bb, beg, end, [&](int nh) {
+    walk_tile<SSN == 1>(p, w, stage, stage_t, stage_bb, beg, end, [&](int nh) {
       if (SSN == 1) {
         cover_pairs(nh);
       } else {
@@ -842,7 +855,7 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock) k_raster_opaque(Ras
     col[s] = w.valid ? p.opaque_color[(size_t)s * p.P + w.pixel] : p.background;
   }
   const int tile = (int)((blockIdx.x * kRasterWarpsPerBlock + warp) / oit::kWarpsPerTile) + p.tile_offset;
-  walk_tile(p, w, stage, stage_t_all + warp * 32, stage_bb, p.tile_begin[tile], p.tile_end[tile], [&](int nh) {
+  walk_tile<true>(p, w, stage, stage_t_all + warp * 32, stage_bb, p.tile_begin[tile], p.tile_end[tile], [&](int nh) {
     for (int k = 0; k < nh; ++k) {
       if (!lane_in_bbox(stage_bb[k], w)) continue;  // no warp-collective operation follows
       const TriSetup& T = stage[k];

@@ -327,14 +327,22 @@ __global__ void __launch_bounds__(256) k_emit(const uint32_t* __restrict__ pair_
   const int tx0 = (bb.x & 0xFFFF) / kTile, ty0 = (bb.x >> 16) / kTile;
   const int tx1 = (bb.y & 0xFFFF) / kTile, ty1 = (bb.y >> 16) / kTile;
   const uint32_t tile_base = t < opaque_from ? num_tiles : 0u;
+  const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = bb.y >> 16;
   uint32_t j = 0;
-  for (int ty = ty0; ty <= ty1; ++ty)
+  for (int ty = ty0; ty <= ty1; ++ty) {
+    // rows of 8x4 micro-tiles the bbox overlaps in this tile row
+    const int ly0 = max(by0 - ty * kTile, 0), ly1 = min(by1 - ty * kTile, kTile - 1);
+    uint32_t rows = 0;
+    for (int r = ly0 >> 2; r <= (ly1 >> 2); ++r) rows |= 3u << (2 * r);
     for (int tx = tx0; tx <= tx1; ++tx, ++j) {
       const size_t pos = (size_t)off + j;
       if (pos >= capacity) return;
-      keys[pos] = tile_base + (uint32_t)(ty * tiles_x + tx);
+      const int lx0 = max(bx0 - tx * kTile, 0), lx1 = min(bx1 - tx * kTile, kTile - 1);
+      const uint32_t cols = (lx0 <= 7 ? 0x55u : 0u) | (lx1 >= 8 ? 0xAAu : 0u);
+      keys[pos] = (tile_base + (uint32_t)(ty * tiles_x + tx)) | ((rows & cols) << kMaskShift);
       tris[pos] = t;
     }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -433,8 +441,8 @@ __global__ void __launch_bounds__(256) k_tile_bounds(const uint32_t* __restrict_
                                                      uint32_t* __restrict__ end) {
   const uint32_t n = (uint32_t)pair_count_of(total, capacity);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
-    const uint32_t cur = i < n ? keys[i] : num_keys;
-    const uint32_t prev = i > 0 ? keys[i - 1] : 0xFFFFFFFFu;
+    const uint32_t cur = i < n ? keys[i] & kTileKeyMask : num_keys;
+    const uint32_t prev = i > 0 ? keys[i - 1] & kTileKeyMask : 0xFFFFFFFFu;
     if (cur == prev) continue;
     if (i > 0 && prev < num_keys) end[prev] = i;
     if (cur < num_keys) begin[cur] = i;
