@@ -121,8 +121,10 @@ def dtype_of(alg):
 # ---------------------------------------------------------------------------
 def _oracle_frame(args):
     """(fragments, seconds[, RGBA8 image]) of one oracle frame of a workload;
-    args = (workload, want_image)."""
-    wd, want_image = args
+    args = (workload, want_image[, oracle build: 'fp64' the checker, or
+    'fp32_omp' FP32 blending with OpenMP tile-parallel draws])."""
+    wd, want_image = args[0], args[1]
+    variant = args[2] if len(args) > 2 else 'fp64'
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
     import oracle as orc
     import vk_order_independent_transparency_gb300 as oit
@@ -133,7 +135,7 @@ def _oracle_frame(args):
     t = time.perf_counter()
     fr = orc.render(ALGS.index(wd['algorithm']), W, H, sd, v, i, tpo, wd['percent_transparent'],
                     oit_layers=wd['oit_layers'], nodes_per_pixel=wd['nodes_per_pixel'], aa_type=wd['aa_type'],
-                    alpha_min=wd['alpha_min'], alpha_width=wd['alpha_width'])
+                    alpha_min=wd['alpha_min'], alpha_width=wd['alpha_width'], variant=variant)
     img, _ = fr.composite()
     dt = time.perf_counter() - t
     if want_image == 'image':
@@ -172,6 +174,24 @@ def cpu_baseline_views(views, budget_s=15.0):
                 break
         pool.terminate()
     return frags, busy, n, images
+
+
+def cpu_baseline_omp(works, budget_s=10.0):
+    """The oracle's FP32 + OpenMP build (every host core, draws split over
+    screen tiles) on whole frames of `works` in order until about budget_s;
+    (fragments, seconds, frames, threads)."""
+    import oracle  # noqa: F401  (builds both oracle libraries if needed)
+    ctx = mp.get_context('spawn')
+    frags, busy, n = 0, 0.0, 0
+    with ctx.Pool(1) as pool:
+        for f, dt in pool.imap(_oracle_frame, [(w, 1, 'fp32_omp') for w in works]):
+            frags += f
+            busy += dt
+            n += 1
+            if busy >= budget_s:
+                break
+        pool.terminate()
+    return frags, busy, n, int(os.environ.get('OMP_NUM_THREADS', os.cpu_count() or 1))
 
 
 def weighted_precision(wd, width=960, height=540):
@@ -758,6 +778,7 @@ def reduce_replicas(maxes, sums, world, device='cuda'):
 def main_batch(a, rank, world):
     res = run_batch(a, rank)
     cpu_line = None
+    cpu_omp_line = None
     accuracy = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         f, busy, n, oracle_images = cpu_baseline_views(res['views'])
@@ -765,6 +786,12 @@ def main_batch(a, rank, world):
                     'sample': '%d of the %d views (the smallest), whole frames, single-threaded FP64 oracle' % (
                         n, len(res['views']))}
         accuracy = image_error(res['images'], oracle_images)
+        order = sorted(range(len(res['views'])), key=lambda k: res['views'][k]['width'] * res['views'][k]['height'] +
+                       1000 * res['views'][k]['spheres'])
+        fo, bo, no, th = cpu_baseline_omp([res['views'][k] for k in order])
+        cpu_omp_line = {'value': round(fo / bo / 1e6, 4), 'unit': 'Mfragments/s', 'cores': th, 'kind': 'port',
+                        'sample': '%d of the %d views (the smallest), whole frames, the oracle built with FP32 '
+                                  'blending and OpenMP tile-parallel draws' % (no, len(res['views']))}
     (t_mixed, t_plain, e2e_s, t_res_mixed, t_res_plain, e2e_flat_s), (total,) = reduce_replicas(
         [res['t_mixed'], res['t_plain'], res['e2e_s'], res['t_res_mixed'], res['t_res_plain'], res['e2e_flat_s']],
         [res['frags'] * a.steps], world)
@@ -801,6 +828,7 @@ def main_batch(a, rank, world):
         'kernels': {k: {'ms_sum_over_views': round(v, 4)} for k, v in sec.items()},
         'resolve': resolve_line(res, a, world, total, t_res_mixed, t_res_plain, peak, peak_kind),
         'cpu_baseline': cpu_line,
+        'cpu_baseline_fp32_omp': cpu_omp_line,
         'accuracy': accuracy,
         'clocks': res['clocks'],
         'gpu_launches': int(res['launches']),
@@ -937,8 +965,13 @@ def main():
                 'peak_source': peak_kind + ' (MEASURED_PEAKS.json hbm_gbs)' if peak_kind == 'measured' else peak_kind,
                 'dominant_pass': dom}
     cpu = None
+    cpu_omp = None
     precision = None
     if not a.no_cpu_baseline:
+        fo, bo, no, th = cpu_baseline_omp([wd] * 5)
+        cpu_omp = {'value': round(fo / bo / 1e6, 4), 'unit': 'Mfragments/s', 'cores': th, 'kind': 'port',
+                   'sample': '%d whole frame(s) of the workload, the oracle built with FP32 blending and OpenMP '
+                             'tile-parallel draws' % no}
         f, w, runs = cpu_baseline(wd, cores=1, frames=1)
         n_more = max(0, min(4, int(12.0 / max(w, 1e-3)) - 1))
         if n_more:
@@ -967,6 +1000,7 @@ def main():
         'roofline': roofline,
         'kernels': kernels,
         'cpu_baseline': cpu,
+        'cpu_baseline_fp32_omp': cpu_omp,
         'clocks': res['clocks'],
         'gpu_launches': int(res['launches']),
     }

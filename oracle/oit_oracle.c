@@ -8,12 +8,31 @@
  * multiply-add may be fused except where fmaf() is written explicitly.
  *
  * Reference files cited as path:line within nvpro-samples/vk_order_independent_transparency.
+ *
+ * Two builds of this file (oracle/Makefile): the checker (blending in FP64,
+ * single-threaded) and, as a CPU baseline only, OR_FP32 + OpenMP: blending in
+ * FP32 and the draws split over screen tiles (every triangle is set up, binned
+ * into 32x32 tiles in primitive order, and each thread rasterises whole tiles,
+ * so every pixel still sees its fragments in primitive order).
  */
 #include "oit_oracle.h"
 
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+
+#ifdef OR_FP32
+typedef float or_real;
+#else
+typedef double or_real;
+#endif
+
+#ifdef _OPENMP
+#include <omp.h>
+#define OR_OMP(x) _Pragma(x)
+#else
+#define OR_OMP(x)
+#endif
 
 #define EMPTY32 0xFFFFFFFFu
 #define EMPTY64 0xFFFFFFFFFFFFFFFFull
@@ -94,7 +113,7 @@ static uint32_t unorm8_double(double x) {
 /* ------------------------------------------------------------------------- */
 /* Frame state                                                               */
 /* ------------------------------------------------------------------------- */
-typedef struct { double r, g, b, a; } rgba_d;
+typedef struct { or_real r, g, b, a; } rgba_d;
 
 struct or_frame {
   or_params p;
@@ -115,7 +134,7 @@ struct or_frame {
   uint32_t* depth;   /* S*P opaque depth bits */
   rgba_d* color;     /* S*P colour target (premultiplied linear) */
   rgba_d* accum;     /* S*P WBOIT accumulation */
-  double* reveal;    /* S*P WBOIT revealage */
+  or_real* reveal;   /* S*P WBOIT revealage */
   const uint32_t* ll_limit;
   uint32_t* ll_stored;
   uint32_t ll_alloc;
@@ -129,7 +148,7 @@ static void* xcalloc(size_t n, size_t sz) {
 }
 
 or_frame* or_frame_create(const or_params* p) {
-  init_tables();
+  init_tables(); /* before any parallel region reads the tables */
   or_frame* f = (or_frame*)xcalloc(1, sizeof(or_frame));
   f->p = *p;
   int ss = p->supersample > 1 ? p->supersample : 1;
@@ -161,7 +180,7 @@ or_frame* or_frame_create(const or_params* p) {
   f->depth = (uint32_t*)xcalloc((size_t)f->S * f->P, 4);
   f->color = (rgba_d*)xcalloc((size_t)f->S * f->P, sizeof(rgba_d));
   f->accum = (rgba_d*)xcalloc((size_t)f->S * f->P, sizeof(rgba_d));
-  f->reveal = (double*)xcalloc((size_t)f->S * f->P, sizeof(double));
+  f->reveal = (or_real*)xcalloc((size_t)f->S * f->P, sizeof(or_real));
   or_begin(f);
   or_clear_transparent(f);
   return f;
@@ -176,6 +195,7 @@ void or_frame_destroy(or_frame* f) {
 
 void or_begin(or_frame* f) {
   const float* bg = f->p.background;
+  OR_OMP("omp parallel for schedule(static)")
   for (size_t i = 0; i < (size_t)f->S * f->P; ++i) {
     f->depth[i] = float_to_bits(1.0f);
     f->color[i].r = bg[0]; f->color[i].g = bg[1]; f->color[i].b = bg[2]; f->color[i].a = bg[3];
@@ -187,6 +207,7 @@ void or_clear_transparent(or_frame* f) {
    * 337-356 (Spinlock/Interlock); WBOIT targets are cleared by its render pass
    * (oitRender.cpp:394-397). */
   memset(f->aux, 0, f->E * 4);
+  OR_OMP("omp parallel for schedule(static)")
   for (size_t i = 0; i < f->E; ++i) f->auxdepth[i] = EMPTY32;
   memset(f->ll_stored, 0, f->E * 4);
   f->ll_alloc = 0;
@@ -197,8 +218,10 @@ void or_clear_transparent(or_frame* f) {
         for (size_t px = 0; px < f->P; ++px)
           f->abuf[((size_t)s * 2 * f->L + i) * f->P + px] = EMPTY32;
   } else if (f->p.algorithm == OR_LOOP64) {
+    OR_OMP("omp parallel for schedule(static)")
     for (size_t i = 0; i < f->abuf_words; ++i) f->abuf[i] = EMPTY32;
   }
+  OR_OMP("omp parallel for schedule(static)")
   for (size_t i = 0; i < (size_t)f->S * f->P; ++i) {
     f->accum[i].r = f->accum[i].g = f->accum[i].b = f->accum[i].a = 0.0;
     f->reveal[i] = 1.0;
@@ -387,14 +410,14 @@ static void shade(const tri_setup* T, const int64_t e[3], float rgb_out[3], floa
 /* Blending helpers                                                          */
 /* ------------------------------------------------------------------------- */
 static rgba_d premult_float(const float c[4]) {
-  rgba_d r = {(double)c[0] * c[3], (double)c[1] * c[3], (double)c[2] * c[3], (double)c[3]};
+  rgba_d r = {(or_real)c[0] * c[3], (or_real)c[1] * c[3], (or_real)c[2] * c[3], (or_real)c[3]};
   return r;
 }
 
 static rgba_d decode_packed(uint32_t packed) {
   /* unpackUnorm4x8 + unPremultSRGBToLinear, shaderCommon.glsl:117-124 (before premultiply) */
   rgba_d r = {g_dec[packed & 255], g_dec[(packed >> 8) & 255], g_dec[(packed >> 16) & 255],
-              (double)((packed >> 24) & 255) / 255.0};
+              (or_real)((packed >> 24) & 255) / (or_real)255.0};
   return r;
 }
 
@@ -405,7 +428,7 @@ static rgba_d premult(rgba_d c) {
 
 /* doBlend: color = color over base (shaderCommon.glsl:108-112) */
 static void do_blend(rgba_d* color, rgba_d base) {
-  double k = 1.0 - color->a;
+  or_real k = (or_real)1.0 - color->a;
   color->r += k * base.r; color->g += k * base.g; color->b += k * base.b; color->a += k * base.a;
 }
 
@@ -416,7 +439,7 @@ static void do_blend_packed(rgba_d* color, uint32_t packed) {
 
 /* Hardware blend ONE, ONE_MINUS_SRC_ALPHA (main.cpp:548-558): dst = src + (1-src.a) dst */
 static void rop_premultiplied(rgba_d* dst, rgba_d src) {
-  double k = 1.0 - src.a;
+  or_real k = (or_real)1.0 - src.a;
   dst->r = src.r + k * dst->r; dst->g = src.g + k * dst->g;
   dst->b = src.b + k * dst->b; dst->a = src.a + k * dst->a;
 }
@@ -463,13 +486,19 @@ static void frag_simple(or_frame* f, size_t pixel, int s, uint32_t cover, const 
 /* oitLinkedList.frag.glsl:51-85 */
 static void frag_linkedlist(or_frame* f, size_t pixel, int s, uint32_t cover, const frag_t* fr) {
   size_t e = (size_t)s * f->P + pixel;
-  uint32_t newOffset = f->counter++ + 1u;
+  uint32_t newOffset;
+  OR_OMP("omp atomic capture")
+  newOffset = f->counter++;
+  newOffset += 1u;
   int overflow = newOffset >= f->capacity;
   if (f->ll_limit) {
     /* replay: the caller decides how many nodes each element got; nodes are
      * numbered in this oracle's own order */
     overflow = f->ll_stored[e] >= f->ll_limit[e];
-    if (!overflow) newOffset = ++f->ll_alloc;
+    if (!overflow) {
+      OR_OMP("omp atomic capture")
+      newOffset = ++f->ll_alloc;
+    }
     if (newOffset >= f->capacity) overflow = 1;
   }
   if (overflow) {
@@ -599,17 +628,17 @@ static void frag_lock(or_frame* f, size_t pixel, int s, uint32_t cover, const fr
 /* oitWeighted.frag.glsl:53-79; blend state main.cpp:559-577 */
 static void frag_weighted(or_frame* f, size_t pixel, uint32_t cover, const frag_t* fr) {
   rgba_d c = premult_float(fr->rgba);
-  double depthZ = -(double)fr->view_z * 10.0;
-  double x = depthZ / 200.0;
-  double distWeight = 0.03 / (1e-5 + x * x * x * x);
+  or_real depthZ = -(or_real)fr->view_z * (or_real)10.0;
+  or_real x = depthZ / (or_real)200.0;
+  or_real distWeight = (or_real)0.03 / ((or_real)1e-5 + x * x * x * x);
   distWeight = distWeight < 1e-2 ? 1e-2 : (distWeight > 3e3 ? 3e3 : distWeight);
-  double m = c.r > c.g ? c.r : c.g;
-  double m2 = c.b > c.a ? c.b : c.a;
+  or_real m = c.r > c.g ? c.r : c.g;
+  or_real m2 = c.b > c.a ? c.b : c.a;
   m = m > m2 ? m : m2;
-  double alphaWeight = m * 40.0 + 0.01;
+  or_real alphaWeight = m * (or_real)40.0 + (or_real)0.01;
   alphaWeight = alphaWeight < 1.0 ? alphaWeight : 1.0;
   alphaWeight *= alphaWeight;
-  double w = alphaWeight * distWeight;
+  or_real w = alphaWeight * distWeight;
   for (int s = 0; s < f->S; ++s) {
     if (!(cover & (1u << s))) continue;
     size_t i = (size_t)s * f->P + pixel;
@@ -619,8 +648,8 @@ static void frag_weighted(or_frame* f, size_t pixel, uint32_t cover, const frag_
   }
 }
 
+/* The callers count fragments (Loop32 sees each twice: counted in its colour pass). */
 static void dispatch_fragment(or_frame* f, size_t pixel, int s, uint32_t cover, const frag_t* fr, int loop_pass) {
-  if (loop_pass == 1) f->fragments++; /* Loop32 sees each fragment twice; count it once */
   switch (f->p.algorithm) {
     case OR_SIMPLE: frag_simple(f, pixel, s, cover, fr); break;
     case OR_LINKEDLIST: frag_linkedlist(f, pixel, s, cover, fr); break;
@@ -654,16 +683,21 @@ void or_inject_fragments(or_frame* f, int n, const int32_t* xy, const int32_t* s
       size_t pixel = (size_t)xy[2 * (size_t)i + 1] * f->RW + (size_t)xy[2 * (size_t)i];
       uint32_t cover = f->p.sample_shading ? (1u << s) : (f->coverage ? m : 1u);
       dispatch_fragment(f, pixel, f->p.sample_shading ? s : 0, cover, &fr, loop_pass);
+      if (loop_pass == 1) f->fragments++;
     }
   }
 }
 
-/* Rasterises one triangle and calls the fragment body for each fragment. */
-static void raster_transparent(or_frame* f, const tri_setup* T, int loop_pass) {
+/* Rasterises one triangle over the pixels of [x0, x1] x [y0, y1] and calls
+ * the fragment body for each fragment; returns the fragments it counts. */
+static uint64_t raster_transparent(or_frame* f, const tri_setup* T, int loop_pass, int x0, int y0, int x1, int y1) {
   const int S = f->S;
   const int (*st)[2] = sample_table(S);
-  for (int py = T->by0; py <= T->by1; ++py) {
-    for (int px = T->bx0; px <= T->bx1; ++px) {
+  uint64_t n = 0;
+  const int ya = T->by0 > y0 ? T->by0 : y0, yb = T->by1 < y1 ? T->by1 : y1;
+  const int xa = T->bx0 > x0 ? T->bx0 : x0, xb = T->bx1 < x1 ? T->bx1 : x1;
+  for (int py = ya; py <= yb; ++py) {
+    for (int px = xa; px <= xb; ++px) {
       size_t pixel = (size_t)py * f->RW + px;
       int32_t bx = px * 256, by = py * 256;
       /* WBOIT never uses per-sample A-buffers: its COLOR shader does not read
@@ -685,6 +719,7 @@ static void raster_transparent(or_frame* f, const tri_setup* T, int loop_pass) {
           fr.depth = zb;
           fr.mask = 0;
           dispatch_fragment(f, pixel, s, 1u << s, &fr, loop_pass);
+          n += loop_pass == 1;
         }
       } else {
         uint32_t mask = 0;
@@ -707,20 +742,122 @@ static void raster_transparent(or_frame* f, const tri_setup* T, int loop_pass) {
         fr.depth = float_to_bits(depth_at(T, e));
         fr.mask = f->coverage ? mask : 0u;
         dispatch_fragment(f, pixel, 0, mask, &fr, loop_pass);
+        n += loop_pass == 1;
       }
     }
   }
+  return n;
 }
+
+#ifdef _OPENMP
+/* Tile-parallel draws: every triangle set up once, then binned into
+ * kOrTile x kOrTile pixel tiles in primitive order (CSR lists). */
+enum { kOrTile = 32 };
+typedef struct {
+  tri_setup* T;
+  unsigned char* ok;
+  uint32_t* start; /* [tiles + 1] */
+  uint32_t* list;  /* triangle slots, primitive order per tile */
+  int tx, ty;
+} or_bins;
+
+static void bins_free(or_bins* b) {
+  free(b->T);
+  free(b->ok);
+  free(b->start);
+  free(b->list);
+}
+
+static void bins_build(const or_frame* f, const float* pv, const float* view, const float* vertices,
+                       const uint32_t* indices, uint32_t first, uint32_t count, int opaque, or_bins* b) {
+  b->T = (tri_setup*)xcalloc(count ? count : 1, sizeof(tri_setup));
+  b->ok = (unsigned char*)xcalloc(count ? count : 1, 1);
+  OR_OMP("omp parallel for schedule(static)")
+  for (int64_t i = 0; i < (int64_t)count; ++i)
+    b->ok[i] = (unsigned char)setup_triangle(f, pv, view, vertices, indices, first + (uint32_t)i, opaque, &b->T[i]);
+  b->tx = (f->RW + kOrTile - 1) / kOrTile;
+  b->ty = (f->RH + kOrTile - 1) / kOrTile;
+  const size_t nt = (size_t)b->tx * b->ty;
+  b->start = (uint32_t*)xcalloc(nt + 1, sizeof(uint32_t));
+  for (uint32_t i = 0; i < count; ++i) {
+    if (!b->ok[i]) continue;
+    const tri_setup* T = &b->T[i];
+    for (int y = T->by0 / kOrTile; y <= T->by1 / kOrTile; ++y)
+      for (int x = T->bx0 / kOrTile; x <= T->bx1 / kOrTile; ++x) b->start[(size_t)y * b->tx + x + 1]++;
+  }
+  for (size_t k = 0; k < nt; ++k) b->start[k + 1] += b->start[k];
+  b->list = (uint32_t*)xcalloc(b->start[nt] ? b->start[nt] : 1, sizeof(uint32_t));
+  uint32_t* cur = (uint32_t*)xcalloc(nt ? nt : 1, sizeof(uint32_t));
+  memcpy(cur, b->start, nt * sizeof(uint32_t));
+  for (uint32_t i = 0; i < count; ++i) {
+    if (!b->ok[i]) continue;
+    const tri_setup* T = &b->T[i];
+    for (int y = T->by0 / kOrTile; y <= T->by1 / kOrTile; ++y)
+      for (int x = T->bx0 / kOrTile; x <= T->bx1 / kOrTile; ++x) b->list[cur[(size_t)y * b->tx + x]++] = i;
+  }
+  free(cur);
+}
+#endif
 
 void or_draw_transparent(or_frame* f, const float* pv, const float* view, const float* vertices,
                          const uint32_t* indices, uint32_t first, uint32_t count) {
   int passes = f->p.algorithm == OR_LOOP ? 2 : 1;
+#ifdef _OPENMP
+  or_bins b;
+  bins_build(f, pv, view, vertices, indices, first, count, 0, &b);
+  uint64_t frags = 0;
+  OR_OMP("omp parallel for schedule(dynamic, 1) reduction(+ : frags)")
+  for (int64_t k = 0; k < (int64_t)b.tx * b.ty; ++k) {
+    const int x0 = (int)(k % b.tx) * kOrTile, y0 = (int)(k / b.tx) * kOrTile;
+    for (int pass = 0; pass < passes; ++pass) {
+      int loop_pass = (f->p.algorithm == OR_LOOP) ? pass : 1;
+      for (uint32_t j = b.start[k]; j < b.start[k + 1]; ++j)
+        frags += raster_transparent(f, &b.T[b.list[j]], loop_pass, x0, y0, x0 + kOrTile - 1, y0 + kOrTile - 1);
+    }
+  }
+  f->fragments += frags;
+  bins_free(&b);
+#else
   for (int pass = 0; pass < passes; ++pass) {
     int loop_pass = (f->p.algorithm == OR_LOOP) ? pass : 1;
     for (uint32_t t = first; t < first + count; ++t) {
       tri_setup T;
       if (!setup_triangle(f, pv, view, vertices, indices, t, 0, &T)) continue;
-      raster_transparent(f, &T, loop_pass);
+      f->fragments += raster_transparent(f, &T, loop_pass, 0, 0, f->RW - 1, f->RH - 1);
+    }
+  }
+#endif
+}
+
+static void raster_opaque(or_frame* f, const tri_setup* T, int x0, int y0, int x1, int y1) {
+  const int S = f->S;
+  const int (*st)[2] = sample_table(S);
+  const int ya = T->by0 > y0 ? T->by0 : y0, yb = T->by1 < y1 ? T->by1 : y1;
+  const int xa = T->bx0 > x0 ? T->bx0 : x0, xb = T->bx1 < x1 ? T->bx1 : x1;
+  for (int py = ya; py <= yb; ++py) {
+    for (int px = xa; px <= xb; ++px) {
+      size_t pixel = (size_t)py * f->RW + px;
+      int32_t bx = px * 256, by = py * 256;
+      int shaded = 0;
+      rgba_d col = {0, 0, 0, 1};
+      for (int s = 0; s < S; ++s) {
+        int64_t e[3];
+        edges_at(T, bx + st[s][0], by + st[s][1], e);
+        if (!inside(T, e)) continue;
+        uint32_t zb = float_to_bits(depth_at(T, e));
+        size_t i = (size_t)s * f->P + pixel;
+        if (!(zb < f->depth[i])) continue;
+        if (!shaded) {
+          int64_t ec[3];
+          edges_at(T, bx + 128, by + 128, ec);
+          float rgb[3];
+          shade(T, ec, rgb, NULL);
+          col.r = rgb[0]; col.g = rgb[1]; col.b = rgb[2]; col.a = 1.0;
+          shaded = 1;
+        }
+        f->depth[i] = zb;
+        f->color[i] = col;
+      }
     }
   }
 }
@@ -728,38 +865,23 @@ void or_draw_transparent(or_frame* f, const float* pv, const float* view, const 
 /* opaque.frag.glsl:30-35 with depth LESS + write (main.cpp:542-547) */
 void or_draw_opaque(or_frame* f, const float* pv, const float* view, const float* vertices,
                     const uint32_t* indices, uint32_t first, uint32_t count) {
-  const int S = f->S;
-  const int (*st)[2] = sample_table(S);
+#ifdef _OPENMP
+  or_bins b;
+  bins_build(f, pv, view, vertices, indices, first, count, 1, &b);
+  OR_OMP("omp parallel for schedule(dynamic, 1)")
+  for (int64_t k = 0; k < (int64_t)b.tx * b.ty; ++k) {
+    const int x0 = (int)(k % b.tx) * kOrTile, y0 = (int)(k / b.tx) * kOrTile;
+    for (uint32_t j = b.start[k]; j < b.start[k + 1]; ++j)
+      raster_opaque(f, &b.T[b.list[j]], x0, y0, x0 + kOrTile - 1, y0 + kOrTile - 1);
+  }
+  bins_free(&b);
+#else
   for (uint32_t t = first; t < first + count; ++t) {
     tri_setup T;
     if (!setup_triangle(f, pv, view, vertices, indices, t, 1, &T)) continue;
-    for (int py = T.by0; py <= T.by1; ++py) {
-      for (int px = T.bx0; px <= T.bx1; ++px) {
-        size_t pixel = (size_t)py * f->RW + px;
-        int32_t bx = px * 256, by = py * 256;
-        int shaded = 0;
-        rgba_d col = {0, 0, 0, 1};
-        for (int s = 0; s < S; ++s) {
-          int64_t e[3];
-          edges_at(&T, bx + st[s][0], by + st[s][1], e);
-          if (!inside(&T, e)) continue;
-          uint32_t zb = float_to_bits(depth_at(&T, e));
-          size_t i = (size_t)s * f->P + pixel;
-          if (!(zb < f->depth[i])) continue;
-          if (!shaded) {
-            int64_t ec[3];
-            edges_at(&T, bx + 128, by + 128, ec);
-            float rgb[3];
-            shade(&T, ec, rgb, NULL);
-            col.r = rgb[0]; col.g = rgb[1]; col.b = rgb[2]; col.a = 1.0;
-            shaded = 1;
-          }
-          f->depth[i] = zb;
-          f->color[i] = col;
-        }
-      }
-    }
+    raster_opaque(f, &T, 0, 0, f->RW - 1, f->RH - 1);
   }
+#endif
 }
 
 /* ------------------------------------------------------------------------- */
@@ -923,10 +1045,11 @@ void or_composite(or_frame* f, uint8_t* out_rgba8, double* out_linear) {
   const int S = f->S;
   if (f->p.algorithm == OR_WEIGHTED) {
     /* oitWeighted.frag.glsl:98-108, blend main.cpp:578-588, per sample */
+    OR_OMP("omp parallel for schedule(static)")
     for (size_t i = 0; i < (size_t)S * f->P; ++i) {
       rgba_d a = f->accum[i];
-      double rv = f->reveal[i];
-      double d = a.a > 1e-5 ? a.a : 1e-5;
+      or_real rv = f->reveal[i];
+      or_real d = a.a > (or_real)1e-5 ? a.a : (or_real)1e-5;
       rgba_d* c = &f->color[i];
       c->r = (a.r / d) * (1.0 - rv) + c->r * rv;
       c->g = (a.g / d) * (1.0 - rv) + c->g * rv;
@@ -934,6 +1057,7 @@ void or_composite(or_frame* f, uint8_t* out_rgba8, double* out_linear) {
       c->a = rv * (1.0 - rv) + c->a * rv;
     }
   } else {
+    OR_OMP("omp parallel for schedule(dynamic, 1024)")
     for (size_t pixel = 0; pixel < f->P; ++pixel) {
       if (f->p.sample_shading) {
         for (int s = 0; s < S; ++s) {
@@ -950,6 +1074,7 @@ void or_composite(or_frame* f, uint8_t* out_rgba8, double* out_linear) {
    * of samples; supersample = 2x2 box downsample; both in linear space. */
   const int ss = f->p.supersample > 1 ? f->p.supersample : 1;
   const int W = f->p.width, H = f->p.height;
+  OR_OMP("omp parallel for schedule(static)")
   for (int y = 0; y < H; ++y) {
     for (int x = 0; x < W; ++x) {
       rgba_d acc = zero_rgba();
@@ -961,7 +1086,7 @@ void or_composite(or_frame* f, uint8_t* out_rgba8, double* out_linear) {
             acc.r += c.r; acc.g += c.g; acc.b += c.b; acc.a += c.a;
           }
         }
-      double k = 1.0 / (double)(ss * ss * S);
+      or_real k = (or_real)1.0 / (or_real)(ss * ss * S);
       acc.r *= k; acc.g *= k; acc.b *= k; acc.a *= k;
       size_t o = (size_t)y * W + x;
       if (out_linear) {
@@ -995,7 +1120,7 @@ const void* or_buffer(const or_frame* f, int which, size_t* bytes) {
     case OR_BUF_COUNTER: if (bytes) *bytes = 4; return &f->counter;
     case OR_BUF_DEPTH: if (bytes) *bytes = sp * 4; return f->depth;
     case OR_BUF_ACCUM: if (bytes) *bytes = sp * sizeof(rgba_d); return f->accum;
-    case OR_BUF_REVEAL: if (bytes) *bytes = sp * sizeof(double); return f->reveal;
+    case OR_BUF_REVEAL: if (bytes) *bytes = sp * sizeof(or_real); return f->reveal;
     case OR_BUF_COLOR: if (bytes) *bytes = sp * sizeof(rgba_d); return f->color;
     default: if (bytes) *bytes = 0; return NULL;
   }

@@ -2,6 +2,9 @@
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
 by bench.py's CPU-baseline leg as the checker; the engine never uses it.
+variant='fp32_omp' loads the same source built with FP32 blending and
+OpenMP tile-parallel draws (liboit_oracle_fp32_omp.so): a CPU baseline, not
+the checker.
 """
 import ctypes
 import os
@@ -11,6 +14,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'liboit_oracle.so')
+LIB_PATHS = {'fp64': LIB_PATH, 'fp32_omp': os.path.join(HERE, 'liboit_oracle_fp32_omp.so')}
 
 SIMPLE, LINKEDLIST, LOOP, LOOP64, SPINLOCK, INTERLOCK, WEIGHTED = range(7)
 BUF_ABUFFER, BUF_AUX, BUF_AUXDEPTH, BUF_COUNTER, BUF_DEPTH, BUF_ACCUM, BUF_REVEAL, BUF_COLOR = range(8)
@@ -30,15 +34,14 @@ def build():
     return LIB_PATH
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB_PATH):
+def lib(variant='fp64'):
+    if variant not in _libs:
+        if not os.path.exists(LIB_PATHS[variant]):
             build()
-        L = ctypes.CDLL(LIB_PATH)
+        L = ctypes.CDLL(LIB_PATHS[variant])
         P = ctypes.c_void_p
         L.or_frame_create.restype = P
         L.or_frame_create.argtypes = [ctypes.POINTER(OrParams)]
@@ -61,8 +64,8 @@ def lib():
         L.or_srgb_decode.argtypes = [ctypes.c_int]
         L.or_srgb_encode.restype = ctypes.c_uint32
         L.or_srgb_encode.argtypes = [ctypes.c_float]
-        _lib = L
-    return _lib
+        _libs[variant] = L
+    return _libs[variant]
 
 
 def aa_settings(aa_type):
@@ -73,7 +76,8 @@ class Frame:
     """One oracle frame: the reference's per-frame images plus the FP64 colour target."""
 
     def __init__(self, algorithm, width, height, oit_layers=8, nodes_per_pixel=8, aa_type=0, tail_blend=True,
-                 alpha_min=0.2, alpha_width=0.6, background=(0.2, 0.2, 0.2, 0.2), record_fp32=False):
+                 alpha_min=0.2, alpha_width=0.6, background=(0.2, 0.2, 0.2, 0.2), record_fp32=False,
+                 variant='fp64'):
         msaa, ss, sup = aa_settings(aa_type)
         p = OrParams()
         p.algorithm = algorithm
@@ -93,7 +97,7 @@ class Frame:
         self.msaa = msaa
         self.supersample = sup
         self.width, self.height = width, height
-        self.lib = lib()
+        self.lib = lib(variant)
         self.f = self.lib.or_frame_create(ctypes.byref(p))
         self._keep = []
 
