@@ -23,6 +23,10 @@ def _frame(variant, alg, aa, pct, L, W=96, H=72):
 
 @pytest.mark.parametrize('alg,aa,pct,L', CASES)
 def test_fp32_omp_matches_checker(alg, aa, pct, L):
+    import os
+    orc.build()
+    if not os.path.exists(orc.LIB_PATHS['fp32_omp']):
+        pytest.skip('the oracle baseline build needs OpenMP')
     f64, img64 = _frame('fp64', alg, aa, pct, L)
     f32, img32 = _frame('fp32_omp', alg, aa, pct, L)
     assert f32.fragment_count() == f64.fragment_count() > 0
