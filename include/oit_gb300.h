@@ -296,7 +296,8 @@ typedef struct oit_resolve_shape {
   int32_t tile_order;       /* 0: micro-tiles row by row; 1: the 8 micro-tiles of each 16x16 tile together */
   int32_t shared_slots;     /* sort-array entries per thread in shared memory (0 or 8; the rest local) */
   int32_t items_per_step;   /* micro-tiles a warp takes per step (1 or 2) */
-  int32_t register_slots;   /* lists short enough to be sorted in registers (0, 4 or 8 entries) */
+  int32_t register_slots;   /* micro-tiles whose lists hold at most this many nodes (0, 4 or 8) are staged
+                               in shared memory and sorted by a network in registers */
   int32_t dense;            /* 1: at most 32 registers per thread (eight 256-thread blocks per SM) */
 } oit_resolve_shape;
 

@@ -246,9 +246,9 @@ __device__ __forceinline__ void net_sort(uint32_t (&d)[K], uint32_t (&c)[K]) {
 
 // Lists of at most K nodes, K <= OIT_LAYERS (all kept, no tail), 1x: the walk
 // only appends each node to the thread's shared-memory column (entry i at
-// col[i * 32], the columns of a warp's lanes side by side); the entries are sorted in registers by the network, which is
-// bubbleSort's order when the depths are distinct, and blended from the
-// column. Returns false, with nothing blended, for a list longer than K or
+// col[i * 32], the columns of a warp's lanes side by side); the entries are
+// sorted in registers by the network, which is bubbleSort's order when the
+// depths are distinct, and blended from the column. Returns false, with nothing blended, for a list longer than K or
 // with equal depths (bubbleSort's order then depends on its passes: the
 // caller's full walk runs it).
 template <int K>
