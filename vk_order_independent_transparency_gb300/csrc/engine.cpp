@@ -1415,7 +1415,9 @@ int oit_batch_set_resolve_config(oit_batch* b, uint32_t part, const oit_resolve_
     pn.order = sh.tile_order;
   }
   b->pin[part] = pn;
-  // tune (or apply the pins) again on the next render or resolve, and capture again
+  // tune (or apply the pins) again on the next render or resolve, and capture
+  // again; a replay of the old graph may still be running on the batch stream
+  if (b->stream) OIT_TRY_CUDA(cudaStreamSynchronize(b->stream), "sync");
   b->r_tuned = false;
   b->drop();
   return OIT_OK;
