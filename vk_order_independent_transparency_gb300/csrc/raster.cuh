@@ -63,6 +63,9 @@ template <int S>
 struct SimplePolicy {
   static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
+  // resident warps per SM with one coverage sample per lane (sets the register
+  // budget: 36 -> 56 registers, spill-free or nearly; 32 -> 64 where 56 spills)
+  static constexpr int kWarpsPerSM = 36;
   static constexpr bool kViewZ = false;
   static __host__ __device__ size_t smem_bytes_per_warp(int, int, int = 0) { return 0; }
   uint32_t count;
@@ -97,6 +100,9 @@ struct SimplePolicy {
 template <int S>
 struct LinkedListPolicy {
   static constexpr int kPasses = 1;
+  // resident warps per SM with one coverage sample per lane (sets the register
+  // budget: 36 -> 56 registers, spill-free or nearly; 32 -> 64 where 56 spills)
+  static constexpr int kWarpsPerSM = 36;
   static constexpr bool kViewZ = false;
   static constexpr bool kNodes = true;
   static __host__ __device__ size_t smem_bytes_per_warp(int, int, int = 0) { return 0; }
@@ -136,6 +142,9 @@ template <int S>
 struct Loop64Policy {
   static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
+  // resident warps per SM with one coverage sample per lane (sets the register
+  // budget: 36 -> 56 registers, spill-free or nearly; 32 -> 64 where 56 spills)
+  static constexpr int kWarpsPerSM = 36;
   static constexpr bool kViewZ = false;
   // keys, plus a float4 colour per slot with RGBA32F records
   static __host__ __device__ size_t smem_bytes_per_warp(int L, int, int fp32 = 0) {
@@ -197,6 +206,9 @@ template <int S>
 struct LoopPolicy {
   static constexpr bool kNodes = false;
   static constexpr int kPasses = 2;
+  // resident warps per SM with one coverage sample per lane (sets the register
+  // budget: 36 -> 56 registers, spill-free or nearly; 32 -> 64 where 56 spills)
+  static constexpr int kWarpsPerSM = 32;
   static constexpr bool kViewZ = false;
   static __host__ __device__ size_t smem_bytes_per_warp(int L, int, int = 0) { return (size_t)L * 32 * 8; }
   uint32_t* dep;
@@ -255,6 +267,9 @@ template <int S>
 struct LockPolicy {
   static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
+  // resident warps per SM with one coverage sample per lane (sets the register
+  // budget: 36 -> 56 registers, spill-free or nearly; 32 -> 64 where 56 spills)
+  static constexpr int kWarpsPerSM = 36;
   static constexpr bool kViewZ = false;
   static __host__ __device__ size_t smem_bytes_per_warp(int L, int coverage, int = 0) {
     return (size_t)L * 32 * (coverage ? 16 : 8);
@@ -337,6 +352,9 @@ template <int S>
 struct WeightedPolicy {
   static constexpr bool kNodes = false;
   static constexpr int kPasses = 1;
+  // resident warps per SM with one coverage sample per lane (sets the register
+  // budget: 36 -> 56 registers, spill-free or nearly; 32 -> 64 where 56 spills)
+  static constexpr int kWarpsPerSM = 32;
   static constexpr bool kViewZ = true;
   static __host__ __device__ size_t smem_bytes_per_warp(int, int, int = 0) { return 0; }
   float4 acc[S];
@@ -565,11 +583,13 @@ constexpr size_t kWarpStageBytes = kStageSlots * (sizeof(TriSetup) + sizeof(uint
 // one tile differ in work (2 warps per CTA: the 64-view batch 5.6% faster
 // than 8; Loop64 k-buffers at large OIT_LAYERS pack shared memory better).
 constexpr int kRasterWarpsPerBlock = 2;
-// 32 resident warps per SM for one coverage sample per lane (64 registers,
-// spill-free for every policy; shared memory still limits Loop64 and Loop32
-// at large OIT_LAYERS), 24 for MSAA lanes, whose per-sample state needs more.
+// Policy::kWarpsPerSM resident warps per SM for one coverage sample per lane
+// (36 at 56 registers: the 64-view batch 19.28 -> 18.96 ms against 32 at 64;
+// shared memory still limits Loop64 and Loop32 at large OIT_LAYERS), 24 for
+// MSAA lanes, whose per-sample state needs more.
 template <template <int> class Policy, int S, int SSN>
-__global__ void __launch_bounds__(32 * kRasterWarpsPerBlock, (S == 1 ? 32 : 24) / kRasterWarpsPerBlock)
+__global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
+                                  (S == 1 ? Policy<S>::kWarpsPerSM : 24) / kRasterWarpsPerBlock)
     k_raster_transparent(RasterParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using Pol = Policy<S>;
