@@ -7,10 +7,12 @@
 //   k_setup       one thread per triangle: transform, cull, snap to 1/256 px,
 //                 bbox, interpolation constants (the raster specification);
 //   scan + emit   one (tile, triangle) pair per 16x16 tile the bbox touches,
-//                 written in triangle order;
+//                 written in triangle order; the key holds the tile id (bits
+//                 0-23) and the 8x4 micro-tiles the bbox overlaps (bits 24-31);
 //   radix sort    stable LSD sort of the pairs by tile id, so every tile's list
-//                 keeps primitive order;
-//   k_tile_bounds begin/end of each tile's list (where the sorted key changes).
+//                 keeps primitive order (the mask bits ride along unsorted);
+//   k_tile_bounds begin/end of each tile's list (where the sorted tile id
+//                 changes).
 #include <algorithm>
 #include <cstdio>
 
