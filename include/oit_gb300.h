@@ -317,6 +317,12 @@ int oit_batch_set_resolve_config(oit_batch* batch, uint32_t part, const oit_reso
 
 /* ---- inspection -------------------------------------------------------- */
 
+/* Testing aid for the error paths: the device allocation `after` allocations
+ * from now (0: the next one) fails once with OIT_ERR_OUT_OF_MEMORY, as an
+ * exhausted device would; -1 disarms it. Process-wide. The call that meets
+ * the failure returns the error and leaves the context usable. */
+int oit_debug_fail_allocations(int32_t after);
+
 /* Synchronises the context's last stream and returns the device error bits
  * (OIT_DEVERR_*) accumulated since the last call, then clears them. */
 int oit_get_error(oit_context* ctx, uint32_t* device_error_bits);

@@ -50,7 +50,7 @@ EXPORTS = [
     'oit_profile_enable', 'oit_profile_read', 'oit_render_frame_noalloc',
     'oit_batch_create', 'oit_batch_destroy', 'oit_batch_render', 'oit_batch_launch_count',
     'oit_render_frame_instanced', 'oit_render_frame_instanced_host', 'oit_scene_generate_instanced',
-    'oit_batch_resolve', 'oit_batch_resolve_config', 'oit_batch_set_resolve_config',
+    'oit_batch_resolve', 'oit_batch_resolve_config', 'oit_batch_set_resolve_config', 'oit_debug_fail_allocations',
 ]
 PROF_SECTIONS = ['opaque_bin', 'opaque_raster', 'transparent_bin', 'transparent_raster', 'composite']
 
@@ -161,6 +161,7 @@ def library():
         'oit_batch_resolve': (I, [P, ctypes.POINTER(OitViewFrame), U, P]),
         'oit_batch_resolve_config': (I, [P, U, ctypes.POINTER(OitResolveShape)]),
         'oit_batch_set_resolve_config': (I, [P, U, ctypes.POINTER(OitResolveShape)]),
+        'oit_debug_fail_allocations': (I, [ctypes.c_int32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -257,6 +258,12 @@ def make_camera(width, height, eye=(0.0, 0.0, 3.0), target=(0.0, 0.0, 0.0), fov_
     _check(library().oit_camera(width, height, ctypes.byref(e), ctypes.byref(t), fov_y, z_near, z_far,
                                 ctypes.byref(sd)), 'oit_camera')
     return sd
+
+
+def debug_fail_allocations(after):
+    """Testing aid: the device allocation `after` allocations from now fails
+    once with OIT_ERR_OUT_OF_MEMORY (-1 disarms)."""
+    _check(library().oit_debug_fail_allocations(int(after)), 'oit_debug_fail_allocations')
 
 
 def srgb_tables():

@@ -7,6 +7,7 @@
 // to the back buffer (copyOffscreenToBackBuffer, main.cpp:645-774). Every
 // entry point returns a status and never aborts.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -19,6 +20,10 @@
 
 namespace {
 
+// Test aid (oit_debug_fail_allocations): the device allocation this many
+// allocations from now fails once, as an exhausted cudaMalloc would; -1: off.
+std::atomic<int> g_fail_alloc_countdown{-1};
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -28,6 +33,10 @@ struct DevBuf {
     p = nullptr;
     bytes = 0;
     if (n == 0) n = 16;
+    int c = g_fail_alloc_countdown.load();
+    while (c >= 0 && !g_fail_alloc_countdown.compare_exchange_weak(c, c - 1)) {
+    }
+    if (c == 0) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(&p, n);
     if (e != cudaSuccess) {
       p = nullptr;
@@ -1448,6 +1457,12 @@ int oit_batch_resolve_config(oit_batch* b, uint32_t part, oit_resolve_shape* out
                 rp.variant == oit::kResolveVariantLoop64Dense)
                    ? 1
                    : 0;
+  return OIT_OK;
+}
+
+int oit_debug_fail_allocations(int32_t after) {
+  if (after < -1) return OIT_ERR_INVALID_ARGUMENT;
+  g_fail_alloc_countdown.store(after);
   return OIT_OK;
 }
 
