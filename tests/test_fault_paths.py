@@ -10,6 +10,13 @@ import vk_order_independent_transparency_gb300 as oit
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True)
+def _disarm():
+    """However a test ends, no armed failure reaches the next test."""
+    yield
+    oit.debug_fail_allocations(-1)
+
+
 @pytest.mark.parametrize('alg', [oit.OIT_LINKEDLIST, oit.OIT_LOOP64, oit.OIT_WEIGHTED])
 @pytest.mark.parametrize('after', [0, 1, 3])
 def test_allocation_failure_recovers(alg, after):
