@@ -41,3 +41,34 @@ def test_fp32_omp_matches_checker(alg, aa, pct, L):
     d = np.abs(img32.astype(np.int32) - img64.astype(np.int32))
     assert d.max() <= 2, d.max()  # FP32 vs FP64 blending before the sRGB8 encode
     assert (d > 1).mean() < 1e-3
+
+
+@pytest.mark.parametrize('alg', [orc.LOOP64, orc.INTERLOCK, orc.WEIGHTED])
+def test_fp32_omp_same_result_on_any_thread_count(alg, tmp_path):
+    """Each pixel belongs to one thread's tile and sees its fragments in
+    primitive order: 1, 3 and 8 threads give the same images and k-buffers."""
+    import hashlib
+    import os
+    import subprocess
+    import sys
+    orc.build()
+    if not os.path.exists(orc.LIB_PATHS['fp32_omp']):
+        pytest.skip('the oracle baseline build needs OpenMP')
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = (
+        "import sys, hashlib; sys.path[:0] = [%r, %r, %r]\n"
+        "import oracle as orc, parity_util as pu\n"
+        "v, i, tpo, sd = pu.scene(80, 120, 90, seed=4, radius_min=0.05, radius_max=0.25)\n"
+        "fr = orc.render(%d, 120, 90, sd, v, i, tpo, 80, oit_layers=4, aa_type=4 if %d == orc.INTERLOCK else 0,"
+        " variant='fp32_omp')\n"
+        "img, _ = fr.composite()\n"
+        "h = hashlib.sha256(img.tobytes() + (fr.buffer(orc.BUF_ABUFFER).tobytes() if %d != orc.WEIGHTED else b''))\n"
+        "print(h.hexdigest(), fr.fragment_count())\n" % (os.path.join(here, '..', 'oracle'), here,
+                                                      os.path.join(here, '..'), alg, alg, alg))
+    outs = set()
+    for n in (1, 3, 8):
+        env = dict(os.environ, OMP_NUM_THREADS=str(n))
+        r = subprocess.run([sys.executable, '-c', code], env=env, capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, r.stderr[-2000:]
+        outs.add(r.stdout.strip().splitlines()[-1])
+    assert len(outs) == 1, outs
