@@ -76,25 +76,7 @@ def parse():
                     help='batch workload: the first N of its 64 views (smaller cases for profiling)')
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
-    ap.add_argument('--hbm-random', action='store_true',
-                    help='measure HBM throughput for sequential, random and dependent-chain reads (csrc/hbm_random.cu)')
     return ap.parse_args()
-
-
-def hbm_random():
-    """Build and run the random-access measurement program; its JSON line."""
-    from vk_order_independent_transparency_gb300 import _build
-    src = os.path.join(ROOT, 'vk_order_independent_transparency_gb300', 'csrc', 'hbm_random.cu')
-    exe = os.path.join(_build.BUILD, 'hbm_random')
-    os.makedirs(_build.BUILD, exist_ok=True)
-    subprocess.run([_build.nvcc(), '-gencode', 'arch=compute_103a,code=sm_103a', '-O3', '-std=c++17', '-o', exe, src],
-                   check=True)
-    r = subprocess.run([exe], check=True, capture_output=True, text=True)
-    line = json.loads(r.stdout.strip().splitlines()[-1])
-    line['what'] = ('HBM read throughput (GB/s of bytes requested): sequential; independent random reads of G bytes, '
-                    'a warp\'s 32 reads in one window of the 4 GiB buffer; dependent chains of 16-byte reads '
-                    '(64 warps per SM)')
-    return line
 
 
 def workload_dict(name):
@@ -350,8 +332,16 @@ def ncu_traffic(kernel, workload):
     return None
 
 
-def kernel_bytes(wd, r, frags, kept_entries, pairs_t, tris_t):
-    """Algorithmic bytes per launch of the transparent raster and the composite."""
+def kernel_bytes(wd, r, frags, kept_entries, pairs_t, tris_t, color_bytes=16):
+    """Algorithmic bytes per launch of the transparent raster (the A-buffer
+    build) and of the composite, after the byte model of the pass: records
+    written once and read once, aux words, the tail-blended colour target
+    (16 B per pixel, 8 B with the FP16 colour target), the output, the opaque
+    depth and colour the passes read. Returns (raster, composite,
+    intermediate): `intermediate` is the pipeline's own traffic that the
+    model does not count -- the raster's reads of the 96-byte setup records
+    (+ 32 B perspective terms for WBOIT and the 8-byte bbox) once per
+    triangle, and its 4-byte tile-list entries."""
     import vk_order_independent_transparency_gb300 as oit
     alg = wd['algorithm']
     msaa, _, ss = oit.aa_settings(wd['aa_type'])
@@ -359,33 +349,34 @@ def kernel_bytes(wd, r, frags, kept_entries, pairs_t, tris_t):
     S = msaa
     L = wd['oit_layers']
     opaque = wd['percent_transparent'] < 100
-    # raster: opaque depth + colour in, colour target out, triangle setup once, tile lists
-    rb = (S * P * 20 if opaque else 0) + P * 16 + tris_t * 136 + pairs_t * 4
+    # raster: opaque depth + colour in (with an opaque pass), colour target out
+    rb = (S * P * 20 if opaque else 0) + P * color_bytes
     if alg == 'loop64':
-        rb += P * L * 8
+        rb += P * L * 8  # every layer written (kept keys and the cleared ones)
     elif alg == 'loop':
-        rb += P * L * 8
+        rb += P * L * 8  # depth and colour layers
     elif alg == 'linkedlist':
-        rb += frags * 16 + P * 4
+        rb += frags * 16 + P * 4  # nodes + heads
     elif alg in ('simple', 'spinlock', 'interlock'):
         rec = 16 if msaa > 1 else 8
         rb += kept_entries * rec + P * (4 if alg == 'simple' else 8)
     elif alg == 'weighted':
         rb += S * P * 10
+    intermediate = tris_t * (96 + 8 + (32 if alg == 'weighted' else 0)) + pairs_t * 4
     # composite: A-buffer entries actually read + colour target + output
     out = wd['width'] * wd['height'] * 4
     if alg == 'loop64':
-        cb = kept_entries * 8 + P * 16 + out
+        cb = kept_entries * 8 + P * color_bytes + out
     elif alg == 'loop':
-        cb = kept_entries * 8 + P * 16 + out
+        cb = kept_entries * 8 + P * color_bytes + out
     elif alg == 'linkedlist':
-        cb = frags * 16 + P * 4 + P * 16 + out
+        cb = frags * 16 + P * 4 + P * color_bytes + out
     elif alg == 'weighted':
         cb = S * P * (10 + (16 if opaque else 0)) + out
     else:
         rec = 16 if msaa > 1 else 8
-        cb = kept_entries * rec + P * 4 + P * 16 + out
-    return rb, cb
+        cb = kept_entries * rec + P * 4 + P * color_bytes + out
+    return rb, cb, intermediate
 
 
 def count_kept(wd, r):
@@ -612,6 +603,7 @@ def run_batch(a, rank):
     # transparent raster's algorithmic bytes summed over the views
     sections = {}
     raster_bytes = 0
+    raster_intermediate = 0
     for r, m, h, vd in zip(mixed, meshes, host, vs):
         r.profile_enable(True)
         r.render_frame(m, h[2], 100, None, stream)
@@ -620,7 +612,9 @@ def run_batch(a, rank):
                 sections[k] = sections.get(k, 0.0) + ms / n
         r.profile_enable(False)
         vw = dict(vd, workload=BATCH_WORKLOAD)
-        raster_bytes += kernel_bytes(vw, r, r.fragment_count(), 0, 0, h[1].shape[0])[0]
+        rb, _, ib = kernel_bytes(vw, r, r.fragment_count(), 0, 0, h[1].shape[0], color_bytes=8)
+        raster_bytes += rb
+        raster_intermediate += ib
 
     # end to end: every view's scene from pinned host memory, the batch, every
     # image back. The scene as template + instance table (what the sphere
@@ -751,7 +745,7 @@ def run_batch(a, rank):
     return dict(frags=frags, t_mixed=t_mixed, t_plain=t_plain, launches=launches, clocks=clk, sections=sections,
                 e2e_s=e2e_s, h2d=h2d, d2h=d2h, views=vs, t_res_mixed=t_res_mixed, t_res_plain=t_res_plain,
                 res_cfg=res_cfg, res_bytes=res_bytes, e2e_flat_s=e2e_flat_s, h2d_flat=h2d_flat, e2e_same=e2e_same,
-                raster_bytes=raster_bytes, images=images)
+                raster_bytes=raster_bytes, raster_intermediate=raster_intermediate, images=images)
 
 
 def _copy_d2h(host_tensor, dev_ptr, nbytes, stream):
@@ -804,7 +798,7 @@ def main_batch(a, rank, world):
     plain = total / (t_plain * 1e-3) / 1e6
     peak, peak_kind = peaks()
     sec = res['sections']
-    dom = max(sec, key=sec.get)
+    resolve = resolve_line(res, a, world, total, t_res_mixed, t_res_plain, peak, peak_kind)
     line = {
         'metric': 'Mfragments/s', 'value': round(value, 3), 'unit': 'Mfragments/s', 'n_gpus': world,
         'steps': a.steps, 'warmup': a.warmup, 'ms_per_step': round(t_mixed / a.steps, 4), 'higher_is_better': True,
@@ -827,9 +821,10 @@ def main_batch(a, rank, world):
                           'h2d_bytes_per_step': res['h2d_flat'], 'd2h_bytes_per_step': res['d2h'],
                           'ms_per_step': round(e2e_flat_s / a.steps * 1e3, 4),
                           'path': 'oit_batch_render over flattened meshes uploaded every step'},
-        'roofline': raster_roofline(res, sec, peak, peak_kind),
+        'roofline': resolve['roofline'],
+        'raster_roofline': raster_roofline(res, sec, peak, peak_kind),
         'kernels': {k: {'ms_sum_over_views': round(v, 4)} for k, v in sec.items()},
-        'resolve': resolve_line(res, a, world, total, t_res_mixed, t_res_plain, peak, peak_kind),
+        'resolve': resolve,
         'cpu_baseline': cpu_line,
         'cpu_baseline_fp32_omp': cpu_omp_line,
         'accuracy': accuracy,
@@ -840,18 +835,21 @@ def main_batch(a, rank, world):
 
 
 def raster_roofline(res, sec, peak, peak_kind):
-    """The batch's dominant kernel, the transparent raster: its algorithmic
-    bytes summed over the 64 views over its CUDA-event time summed over the
-    views (each rendered alone)."""
+    """The batch's longest pass, the transparent raster (A-buffer build):
+    the algorithmic bytes it writes and reads (records, aux words, the FP16
+    colour target), summed over the 64 views, over its CUDA-event time summed
+    over the views (each rendered alone). The setup-record reads, which the
+    byte model does not count, are reported beside it."""
     ms = sec.get('transparent_raster', 0.0)
     gbs = res['raster_bytes'] / (ms * 1e-3) / 1e9 if ms else None
-    return {'bound': 'hbm', 'kernel': 'k_raster_transparent (summed over the 64 views)',
+    return {'bound': 'issue/latency (integer edge tests, shading, per-pixel k-buffer steps)',
+            'kernel': 'k_raster_transparent (summed over the 64 views)',
             'achieved': round(gbs, 1) if gbs else None, 'peak': peak, 'unit': 'GB/s',
             'frac': round(gbs / peak, 4) if gbs else None, 'traffic': None,
             'bytes_per_step': int(res['raster_bytes']), 'ms_per_step_summed': round(ms, 4),
-            'peak_source': peak_kind,
-            'note': 'an integer/float raster bound by issue and latency, not by HBM; the resolve below is the '
-                    'HBM-bound pass'}
+            'intermediate_bytes': int(res['raster_intermediate']),
+            'intermediate': 'setup records (96 B) and bboxes (8 B) read once per triangle; not algorithmic bytes',
+            'peak_source': peak_kind}
 
 
 def resolve_line(res, a, world, total, t_mixed, t_plain, peak, peak_kind):
@@ -868,8 +866,8 @@ def resolve_line(res, a, world, total, t_mixed, t_plain, peak, peak_kind):
         'plain_fp32': {'value': round(plain, 3), 'unit': 'Mfragments/s', 'ms_per_step': round(t_plain / a.steps, 4),
                        'path': 'oit_composite per view, RGBA32F records'},
         'speedup_vs_plain_fp32': round(value / plain, 3),
-        'roofline': {'bound': 'hbm', 'kernel': 'k_resolve_list + k_resolve_loop64 side by side (+ binning)',
-                     'achieved': round(gbs, 1),
+        'roofline': {'bound': 'hbm', 'kernel': 'batched resolve: k_resolve_list + k_resolve_loop64 side by side '
+                               '(+ work-list binning), per step', 'achieved': round(gbs, 1),
                      'peak': peak, 'unit': 'GB/s', 'frac': round(gbs / peak, 4),
                      'traffic': ncu_traffic('resolve', BATCH_WORKLOAD), 'bytes_per_step': int(res['res_bytes']),
                      'peak_source': peak_kind},
@@ -879,9 +877,6 @@ def resolve_line(res, a, world, total, t_mixed, t_plain, peak, peak_kind):
 
 def main():
     a = parse()
-    if a.hbm_random:
-        print(json.dumps(hbm_random()))
-        return
     wd = workload_dict(a.workload)
     rank = int(os.environ.get('RANK', '0'))
     world = int(os.environ.get('WORLD_SIZE', '1'))
@@ -949,13 +944,15 @@ def main():
 
     peak, peak_kind = peaks()
     prof = res['prof']
-    rbytes, cbytes = kernel_bytes(wd, res['r'], res['frags'], res['kept'], 0, res['tris_t'])
+    rbytes, cbytes, ibytes = kernel_bytes(wd, res['r'], res['frags'], res['kept'], 0, res['tris_t'])
     kernels = {}
     for name, b in (('transparent_raster', rbytes), ('composite', cbytes)):
         ms, n = prof[name]
         if n:
             per = ms / n
             kernels[name] = {'ms': round(per, 4), 'bytes': int(b), 'gbs': round(b / (per * 1e-3) / 1e9, 1)}
+            if name == 'transparent_raster':
+                kernels[name]['intermediate_bytes'] = int(ibytes)
     for name in ('opaque_bin', 'opaque_raster', 'transparent_bin'):
         ms, n = prof[name]
         if n:

@@ -135,7 +135,14 @@ int oit_create(const oit_state* state, oit_context** out_ctx);
 /* Frees the context. Replaces Sample::onDetach / destroyFrameImages (oit.cpp:30-43). */
 int oit_destroy(oit_context* ctx);
 
-/* Uploads the per-frame constants. Replaces Sample::updateUniformBuffer (main.cpp:625-643). */
+/* Sets the per-frame constants. Replaces Sample::updateUniformBuffer
+ * (main.cpp:625-643), which records the upload into the frame's command
+ * buffer: here the next frame call (oit_render_frame*, oit_draw_*,
+ * oit_batch_render) copies them into the context's device scene buffer on
+ * its own stream before its first kernel, so frames already queued keep the
+ * constants they were called with and a replayed CUDA graph renders with the
+ * newest ones. The host copy goes through a ring of 4 pinned slots: the call
+ * blocks only when the copy made 4 updates ago has not run yet. */
 int oit_update_scene(oit_context* ctx, const oit_scene_data* scene);
 
 /* ---- per frame (the transparent pass) ---------------------------------- */
@@ -230,16 +237,22 @@ int oit_render_frame_instanced_host(oit_context* ctx, const float* template_vert
  * may synchronise the device and stall other streams, and processes near a
  * device-memory limit where a mid-frame allocation can fail.
  * All per-frame scratch (setup records, tile bins, sort scratch, A-buffer,
- * colour and depth targets) lives in one 64 MiB device array that every
- * device loading the library holds until the process exits; frames that do
- * not fit return OIT_ERR_TOO_LARGE. The caller passes the state, scene, mesh
- * (device) and width*height*4 bytes of device output. 1x and MSAA modes with
- * RGBA8 records only (supersampling and sample shading return
- * OIT_ERR_UNSUPPORTED). The call is synchronous on `stream`. The first call
- * on a device looks up the array's device address (once per device, with
- * that device current); make it before any stream capture. Every call reuses
- * the same array, so calls that overlap on the GPU (other host threads,
- * other streams) race and must be serialised by the caller. */
+ * colour and depth targets, the scene constants) lives in one 64 MiB device
+ * array that every device loading the library holds until the process exits;
+ * frames that do not fit return OIT_ERR_TOO_LARGE. The caller passes the
+ * state, scene (host memory), mesh (device) and width*height*4 bytes of
+ * device output. 1x and MSAA modes with RGBA8 records only (supersampling and
+ * sample shading return OIT_ERR_UNSUPPORTED). Flags: OIT_FLAG_HALF_COLOR is
+ * honoured (the image equals oit_render_frame's with the same flag),
+ * OIT_FLAG_LINEAR_OUTPUT returns OIT_ERR_UNSUPPORTED (no linear image is
+ * passed in) and OIT_FLAG_CUDA_GRAPH is ignored. The call is synchronous on
+ * `stream`. The first call on a device looks up the array's device address
+ * (once per device, with that device current; concurrent first calls on
+ * several host threads each look it up and store the same value); make it
+ * before any stream capture, and do not use the entry point across a
+ * cudaDeviceReset (the address is not looked up again). Every call reuses the
+ * same array, so calls that overlap on the GPU (other host threads, other
+ * streams) race and must be serialised by the caller. */
 int oit_render_frame_noalloc(const oit_state* state, const oit_scene_data* scene, const oit_mesh* mesh,
                              uint32_t triangles_per_object, int32_t percent_transparent,
                              uint8_t* out_rgba8_device, void* stream);

@@ -22,6 +22,15 @@ def render_gpu(algorithm, width, height, v, i, tpo, sd, percent=100, **kw):
     mesh = oit.DeviceMesh(v, i)
     r.update_scene(sd)
     r.render_frame(mesh, tpo, percent)
+    res = collect(r, algorithm, **kw)
+    res['mesh'] = mesh
+    return res
+
+
+def collect(r, algorithm, **kw):
+    """The frame state of a Renderer after a frame: image, A-buffer, aux
+    words, colour target, depth, fragment count, error bits (and the WBOIT
+    accumulators)."""
     res = {
         'image': r.output(),
         'abuf': r.read_buffer(oit.OIT_BUF_ABUFFER),
@@ -35,7 +44,6 @@ def render_gpu(algorithm, width, height, v, i, tpo, sd, percent=100, **kw):
         'fragments': r.fragment_count(),
         'error': r.get_error(),
         'renderer': r,
-        'mesh': mesh,
     }
     if algorithm == oit.OIT_WEIGHTED:
         if kw.get('weighted_precision', 0) == oit.OIT_WEIGHTED_FP32:

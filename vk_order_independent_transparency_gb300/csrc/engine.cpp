@@ -86,14 +86,27 @@ struct oit_context {
   int ssn = 1;  // samples with their own A-buffer (sample shading); WBOIT never uses them
   int tiles_x = 0, tiles_y = 0, num_tiles = 0, key_bits = 1;
   uint32_t capacity = 0;
-  oit::Mat4 pv{}, view{};
   bool has_scene = false;
+
+  // Scene constants (SceneData): oit_update_scene writes them into the next
+  // slot of a pinned host ring; the next frame call copies the newest slot
+  // into scene_dev on its stream before any kernel reads it, so a captured
+  // graph reads the camera of the frame it renders. A slot is rewritten only
+  // after the copy that last read it has run (its event).
+  static constexpr int kSceneSlots = 4;
+  static constexpr size_t kSceneBytes = 32 * sizeof(float);
+  float* scene_ring = nullptr;  // pinned, kSceneSlots x 32 floats
+  cudaEvent_t scene_ev[kSceneSlots] = {};
+  bool scene_ev_used[kSceneSlots] = {};
+  int scene_slot = 0;
+  bool scene_dirty = false;
   float4 background = make_float4(0.2f, 0.2f, 0.2f, 0.2f);
 
   DevBuf depth, opaque_color, color, abuf, aux, auxdepth, counter, accum, reveal, out, out_linear, err, frag;
   DevBuf bbox, setup, persp, pair_count, pair_offset, scan_tmp, total;
   DevBuf keys, tris, keys_alt, tris_alt, hist, tile_begin, tile_end;
   DevBuf mesh_v, mesh_i;
+  DevBuf scene_dev;  // proj_view then view, read by k_setup
   DevBuf lens;  // per 8x4 micro-tile fragment counts for the batched resolve
   size_t tri_cap = 0, pair_cap = 0;
   bool opaque_valid = false;
@@ -163,10 +176,13 @@ struct oit_context {
       if (p.ev) cudaEventDestroy(p.ev);
       if (p.host_total) cudaFreeHost(p.host_total);
     }
+    for (cudaEvent_t e : scene_ev)
+      if (e) cudaEventDestroy(e);
+    if (scene_ring) cudaFreeHost(scene_ring);
     DevBuf* all[] = {&depth, &opaque_color, &color, &abuf, &aux, &auxdepth, &counter, &accum, &reveal, &out,
                      &out_linear, &err, &frag, &bbox, &setup, &persp, &pair_count, &pair_offset, &scan_tmp, &total,
                      &keys, &tris, &keys_alt, &tris_alt, &hist, &tile_begin, &tile_end, &mesh_v, &mesh_i,
-                     &lens};
+                     &scene_dev, &lens};
     for (DevBuf* b : all) b->release();
   }
 
@@ -225,6 +241,9 @@ struct oit_context {
     OIT_TRY_CUDA(tile_begin.ensure((size_t)2 * num_tiles * 4), "alloc bins");
     OIT_TRY_CUDA(tile_end.ensure((size_t)2 * num_tiles * 4), "alloc bins");
     OIT_TRY_CUDA(total.ensure(4), "alloc total");
+    OIT_TRY_CUDA(scene_dev.ensure(kSceneBytes), "alloc scene");
+    OIT_TRY_CUDA(cudaMallocHost(&scene_ring, kSceneSlots * kSceneBytes), "alloc pinned scene");
+    for (cudaEvent_t& e : scene_ev) OIT_TRY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
     OIT_TRY_CUDA(cudaMemset(err.p, 0, 4), "memset");
     OIT_TRY_CUDA(cudaMemset(frag.p, 0, 8), "memset");
     OIT_TRY_CUDA(cudaMemset(counter.p, 0, 4), "memset");
@@ -270,6 +289,33 @@ struct oit_context {
     return OIT_OK;
   }
 
+  // oit_update_scene: the newest constants go to the next ring slot, once the
+  // copy that last read that slot has run.
+  int set_scene(const oit_scene_data* scene) {
+    const int k = (scene_slot + 1) % kSceneSlots;
+    if (scene_ev_used[k]) OIT_TRY_CUDA(cudaEventSynchronize(scene_ev[k]), "scene slot");
+    float* dst = scene_ring + 32 * k;
+    std::memcpy(dst, scene->proj_view_matrix, 16 * sizeof(float));
+    std::memcpy(dst + 16, scene->view_matrix, 16 * sizeof(float));
+    scene_slot = k;
+    scene_dirty = true;
+    has_scene = true;
+    return OIT_OK;
+  }
+
+  // Stream-ordered copy of the newest scene constants into scene_dev, before
+  // the frame's first kernel; nothing to do when they have not changed. Never
+  // captured: a graph reads scene_dev, and this copy precedes its launch.
+  int upload_scene(cudaStream_t s) {
+    if (!scene_dirty || capturing) return OIT_OK;
+    OIT_TRY_CUDA(cudaMemcpyAsync(scene_dev.p, scene_ring + 32 * scene_slot, kSceneBytes, cudaMemcpyHostToDevice, s),
+                 "scene h2d");
+    OIT_TRY_CUDA(cudaEventRecord(scene_ev[scene_slot], s), "event");
+    scene_ev_used[scene_slot] = true;
+    scene_dirty = false;
+    return OIT_OK;
+  }
+
   oit::SetupParams setup_params(const oit::MeshRef& mesh, uint32_t first, uint32_t count, uint32_t opaque_from) {
     oit::SetupParams sp{};
     sp.vertices = mesh.vertices;
@@ -278,8 +324,7 @@ struct oit_context {
     sp.template_triangles = mesh.template_triangles;
     sp.first_triangle = first;
     sp.num_triangles = count;
-    sp.proj_view = pv;
-    sp.view = view;
+    sp.scene = scene_dev.as<float>();
     sp.RW = RW;
     sp.RH = RH;
     sp.alpha_min = st.alpha_min;
@@ -334,7 +379,9 @@ struct oit_context {
   // Triangles [first, first + opaque_from) are transparent, the rest of the
   // range opaque; one setup, scan and sort bins both kinds.
   int bin(const oit::MeshRef& mesh, uint32_t first, uint32_t count, uint32_t opaque_from, cudaStream_t s) {
-    int r = ensure_triangles(count);
+    int r = upload_scene(s);
+    if (r != OIT_OK) return r;
+    r = ensure_triangles(count);
     if (r != OIT_OK) return r;
     const uint64_t key = ((uint64_t)first << 32) ^ ((uint64_t)count << 1) ^ ((uint64_t)opaque_from * 0x9E3779B1ull) ^
                          ((uint64_t)(uintptr_t)mesh.indices << 7) ^ ((uint64_t)(uintptr_t)mesh.instances << 3);
@@ -696,6 +743,8 @@ struct oit_context {
       launches = l0;
       return OIT_OK;  // the plain frame above produced this call's image
     }
+    int ur = upload_scene(s);  // the replay reads the newest scene constants
+    if (ur != OIT_OK) return ur;
     OIT_TRY_CUDA(cudaEventRecord(graph_in, s), "event");
     OIT_TRY_CUDA(cudaStreamWaitEvent(graph_stream, graph_in, 0), "wait");
     OIT_TRY_CUDA(cudaGraphLaunch(graph_exec, graph_stream), "graph launch");
@@ -1096,10 +1145,7 @@ int oit_destroy(oit_context* ctx) {
 
 int oit_update_scene(oit_context* ctx, const oit_scene_data* scene) {
   if (!ctx || !scene) return OIT_ERR_INVALID_ARGUMENT;
-  std::memcpy(ctx->pv.m, scene->proj_view_matrix, sizeof(ctx->pv.m));
-  std::memcpy(ctx->view.m, scene->view_matrix, sizeof(ctx->view.m));
-  ctx->has_scene = true;
-  return OIT_OK;
+  return ctx->set_scene(scene);
 }
 
 int oit_begin_frame(oit_context* ctx, void* stream) {
@@ -1348,6 +1394,10 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
     b->sig = sig;
     b->graph_launches = nodes;
     return OIT_OK;  // the plain frames produced this call's images
+  }
+  for (uint32_t i = 0; i < n; ++i) {  // each view's newest scene constants, before the replay
+    const int ur = views[i].ctx->upload_scene(s);
+    if (ur != OIT_OK) return ur;
   }
   OIT_TRY_CUDA(cudaEventRecord(b->in, s), "event");
   OIT_TRY_CUDA(cudaStreamWaitEvent(b->stream, b->in, 0), "wait");

@@ -11,6 +11,7 @@
 // and scan scratch, the A-buffer, the colour and depth targets) is carved out
 // of one file-scope device array, reserved when the library is loaded. The
 // caller passes only the inputs (state, scene, mesh) and the output image.
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 
@@ -27,22 +28,25 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratch
 
 // Device address of the arena per device. In host code g_noalloc_scratch only
 // names a host-side stand-in, so the address is looked up with
-// cudaGetSymbolAddress, once per device, with that device current.
+// cudaGetSymbolAddress, once per device, with that device current. Concurrent
+// first calls may both look it up; they store the same value (atomically).
 constexpr int kMaxDevices = 64;
-unsigned char* g_scratch_addr[kMaxDevices] = {};
+std::atomic<unsigned char*> g_scratch_addr[kMaxDevices] = {};
 
 cudaError_t scratch_base(unsigned char** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  if (!g_scratch_addr[dev]) {
+  unsigned char* a = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!a) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+    a = static_cast<unsigned char*>(p);
+    g_scratch_addr[dev].store(a, std::memory_order_release);
   }
-  *out = g_scratch_addr[dev];
+  *out = a;
   return cudaSuccess;
 }
 
@@ -94,6 +98,10 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
     default: return OIT_ERR_INVALID_ARGUMENT;
   }
   if (st->record_format != OIT_RECORD_RGBA8) return OIT_ERR_UNSUPPORTED;
+  // no linear output image is passed in; OIT_FLAG_CUDA_GRAPH does not apply
+  // (the call is synchronous); OIT_FLAG_HALF_COLOR is honoured
+  if (st->flags & OIT_FLAG_LINEAR_OUTPUT) return OIT_ERR_UNSUPPORTED;
+  const bool half_color = (st->flags & OIT_FLAG_HALF_COLOR) != 0;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const Alg alg = static_cast<Alg>(st->algorithm);
   const int W = (int)st->width, H = (int)st->height, S = msaa, L = (int)st->oit_layers;
@@ -116,9 +124,10 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   NOALLOC_TRY(scratch_base(&base));
   Arena a{base, 0, kNoallocScratchBytes};
   uint32_t* words = a.take<uint32_t>(64);  // [0] error bits, [1] pair count, [2] node counter, [4..5] fragments
+  float* scene_dev = a.take<float>(32 * sizeof(float));  // proj_view, view (read by the setup kernel)
   uint32_t* depth = opaque ? a.take<uint32_t>((size_t)S * P * 4) : nullptr;
   float4* opaque_color = opaque ? a.take<float4>((size_t)S * P * 16) : nullptr;
-  float4* color = a.take<float4>((size_t)P * 16);
+  float4* color = a.take<float4>((size_t)P * (half_color ? 8 : 16));
   size_t abuf_bytes = 0;
   switch (alg) {
     case Alg::Simple: case Alg::Spinlock: case Alg::Interlock: abuf_bytes = (size_t)P * L * (coverage ? 16 : 8); break;
@@ -138,8 +147,8 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   uint32_t* pair_offset = a.take<uint32_t>(((size_t)N + 1) * 4);
   uint32_t* tile_begin = a.take<uint32_t>((size_t)2 * num_tiles * 4);
   uint32_t* tile_end = a.take<uint32_t>((size_t)2 * num_tiles * 4);
-  if (!words || (opaque && (!depth || !opaque_color)) || !color || (abuf_bytes && !abuf) || !aux || !auxdepth ||
-      (weighted && (!accum || !reveal || !persp)) || !setup || !bbox || !pair_count || !pair_offset ||
+  if (!words || !scene_dev || (opaque && (!depth || !opaque_color)) || !color || (abuf_bytes && !abuf) || !aux ||
+      !auxdepth || (weighted && (!accum || !reveal || !persp)) || !setup || !bbox || !pair_count || !pair_offset ||
       !tile_begin || !tile_end)
     return OIT_ERR_TOO_LARGE;
   // The rest holds the pairs: 16 bytes per pair (keys, triangles, ping-pong),
@@ -167,6 +176,10 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   // Calls share the arena and find the previous call's contents: clear what
   // must start at zero (error bits, pair count, node counter, fragment count).
   NOALLOC_TRY(cudaMemsetAsync(words, 0, 64, s));
+  float scene_words[32];
+  std::memcpy(scene_words, scene->proj_view_matrix, 16 * sizeof(float));
+  std::memcpy(scene_words + 16, scene->view_matrix, 16 * sizeof(float));
+  NOALLOC_TRY(cudaMemcpyAsync(scene_dev, scene_words, sizeof(scene_words), cudaMemcpyHostToDevice, s));
   const float4 bg = make_float4(0.2f, 0.2f, 0.2f, 0.2f);  // oitRender.cpp:90
   if (opaque) {
     NOALLOC_TRY(launch_fill_u32(depth, 0x3F800000u, (size_t)S * P, s));
@@ -177,8 +190,7 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   sp.indices = mesh->indices_device;
   sp.first_triangle = 0;
   sp.num_triangles = N;
-  std::memcpy(sp.proj_view.m, scene->proj_view_matrix, sizeof(sp.proj_view.m));
-  std::memcpy(sp.view.m, scene->view_matrix, sizeof(sp.view.m));
+  sp.scene = scene_dev;
   sp.RW = W;
   sp.RH = H;
   sp.alpha_min = st->alpha_min;
@@ -197,6 +209,10 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   NOALLOC_TRY(cudaMemcpyAsync(&pairs, b.total, 4, cudaMemcpyDeviceToHost, s));
   NOALLOC_TRY(cudaStreamSynchronize(s));
   if (pairs > pair_cap) return OIT_ERR_TOO_LARGE;  // more (tile, triangle) pairs than the arena holds
+  // the sort's grids and histogram scans follow the capacity: size it to this
+  // frame's pairs (the regions carved for pair_cap cover the smaller one)
+  b.capacity = ((size_t)pairs + 4095) & ~(size_t)4095;
+  if (b.capacity < 4096) b.capacity = 4096;
   NOALLOC_TRY(bin_sort(sp, b, key_bits, num_tiles, words, s, &launches));
 
   RasterParams p{};
@@ -222,6 +238,7 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   p.has_opaque = opaque ? 1 : 0;
   p.background = bg;
   p.color = color;
+  p.color_half = half_color ? 1 : 0;
   p.abuf = abuf;
   p.aux = aux;
   p.auxdepth = auxdepth;
@@ -261,6 +278,7 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   c.abuf = abuf;
   c.aux = aux;
   c.color = color;
+  c.color_half = half_color ? 1 : 0;
   c.opaque_color = opaque_color;
   c.has_opaque = p.has_opaque;
   c.background = bg;

@@ -27,8 +27,10 @@ struct SetupParams {
   uint32_t template_triangles;  // triangles per instance
   uint32_t first_triangle;
   uint32_t num_triangles;
-  Mat4 proj_view;
-  Mat4 view;
+  // device memory: proj_view (16 floats, column-major) then view (16 floats),
+  // 16-byte aligned. Read by the kernel, so a captured CUDA graph replays with
+  // whatever the scene buffer holds when it runs (SceneData, shaders/common.h:77-92).
+  const float* scene;
   int RW, RH;
   float alpha_min, alpha_width;
   uint32_t opaque_from;     // triangles t >= opaque_from (relative) are opaque: back faces culled, kind 0

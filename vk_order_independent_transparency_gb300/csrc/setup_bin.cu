@@ -57,8 +57,22 @@ __global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
   const uint32_t i2 = __ldg(&p.indices[3 * (size_t)tri + 2]);
   const uint32_t vid[3] = {i0, i1, i2};
   float cx[3], cy[3], cz[3], cw[3], vz[3], nx[3], ny[3], nz[3];
-  const float* m = p.proj_view.m;
-  const float* v = p.view.m;
+  // scene constants from device memory (every thread reads the same 80 bytes)
+  float m[16], v[16];
+  {
+    const float4* sc = reinterpret_cast<const float4*>(p.scene);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float4 c = __ldg(sc + k);
+      m[4 * k + 0] = c.x;
+      m[4 * k + 1] = c.y;
+      m[4 * k + 2] = c.z;
+      m[4 * k + 3] = c.w;
+    }
+    // of the view matrix only row 2 (view-space z) is used: columns' z entries
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[4 * k + 2] = __ldg(p.scene + 16 + 4 * k + 2);
+  }
   float4 ic = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
   if (inst) ic = __ldg(reinterpret_cast<const float4*>(inst));
 #pragma unroll
