@@ -50,8 +50,8 @@ DEFAULT_WORKLOAD = BATCH_WORKLOAD
 def batch_views(seed=SEED, n=64):
     """The batched workload's views: square resolutions log-uniform in
     [256, 2048], sphere counts log-uniform in [64, 8192], radii 0.01-0.05,
-    Linked List and Loop64 alternating, OIT_LAYERS cycling 4, 8, 16, 32
-    (Loop64 views use 4, 8, 16: its float-record variant keeps 16 at most)."""
+    Linked List and Loop64 alternating, OIT_LAYERS cycling 4, 8, 16, 32 for
+    each algorithm."""
     import numpy as np
     rng = np.random.default_rng(seed)
     views = []
@@ -59,7 +59,7 @@ def batch_views(seed=SEED, n=64):
         side = int(round(256 * 8 ** rng.uniform()))
         spheres = int(round(64 * 128 ** rng.uniform()))
         alg = 'linkedlist' if k % 2 == 0 else 'loop64'
-        L = [4, 8, 16, 32][(k // 2) % 4] if alg == 'linkedlist' else [4, 8, 16][(k // 2) % 3]
+        L = [4, 8, 16, 32][(k // 2) % 4]
         views.append(dict(algorithm=alg, width=side, height=side, oit_layers=L, nodes_per_pixel=8, aa_type=0,
                           spheres=spheres, radius_min=0.01, radius_max=0.05, percent_transparent=100,
                           alpha_min=0.2, alpha_width=0.6, seed=seed * 1000 + k))
@@ -158,6 +158,19 @@ def cpu_baseline_views(views, budget_s=15.0):
     return frags, busy, n, images
 
 
+def oracle_images_all(views, procs=None):
+    """The FP64 oracle's image of every view (a spawn pool, largest views
+    first): the accuracy reference for the whole batch. Not timed."""
+    import oracle  # noqa: F401  (builds the oracle library if needed)
+    ctx = mp.get_context('spawn')
+    procs = procs or max(1, min(len(views), os.cpu_count() or 1))
+    order = sorted(range(len(views)), key=lambda k: -(views[k]['width'] * views[k]['height'] +
+                                                       1000 * views[k]['spheres']))
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_oracle_frame, [(views[k], 'image') for k in order], chunksize=1)
+    return {k: r[2] for k, r in zip(order, res)}
+
+
 def cpu_baseline_omp(works, budget_s=10.0):
     """The oracle's FP32 + OpenMP build (every host core, draws split over
     screen tiles) on whole frames of `works` in order until about budget_s;
@@ -176,11 +189,13 @@ def cpu_baseline_omp(works, budget_s=10.0):
     return frags, busy, n, int(os.environ.get('OMP_NUM_THREADS', os.cpu_count() or 1))
 
 
-def weighted_precision(wd, width=960, height=540):
-    """The WBOIT precision study: the workload's scene at width x height with
-    FP16 and FP32 accumulators on the GPU against the FP64 oracle; per-pixel
-    relative error of the accumulation (RGBA, where the oracle's magnitude is
-    above 1e-3) and of the revealage."""
+def weighted_precision(wd, width=None, height=None):
+    """The WBOIT precision study: the workload's scene (at its own size unless
+    given) with FP16 and FP32 accumulators on the GPU against the FP64 oracle;
+    per-pixel relative error of the accumulation (RGBA, where the oracle's
+    magnitude is above 1e-3) and of the revealage. Not timed."""
+    width = width or wd['width']
+    height = height or wd['height']
     import importlib.util
     import numpy as np
     import vk_order_independent_transparency_gb300 as oit
@@ -210,7 +225,7 @@ def weighted_precision(wd, width=960, height=540):
     return out
 
 
-def image_error(gpu_images, oracle_images):
+def image_error(gpu_images, oracle_images, reference='FP64 oracle, same scenes'):
     """Max and mean absolute RGBA8 difference (LSB) over the views both have."""
     import numpy as np
     mx, tot, cnt, over = 0, 0.0, 0, 0
@@ -221,19 +236,14 @@ def image_error(gpu_images, oracle_images):
         cnt += d.size
         over += int((d > 1).sum())
     return {'views_compared': len(oracle_images), 'max_lsb': mx, 'mean_lsb': round(tot / max(cnt, 1), 6),
-            'channels_over_1_lsb': over, 'reference': 'FP64 oracle, same scenes'}
+            'channels_over_1_lsb': over, 'reference': reference}
 
 
-REFERENCE_SAMPLE_VIEWS = 48
-
-
-def reference_views(step, cores):
+def reference_views():
     """The views the reference arm renders in one step of the batch workload:
-    one per core, cycling through the 48 cheapest of the 64 (a bounded sample:
-    the largest views take the oracle several seconds each)."""
-    vs = sorted(batch_views(SEED), key=lambda vd: vd['width'] * vd['height'] + 1000 * vd['spheres'])
-    vs = vs[:REFERENCE_SAMPLE_VIEWS]
-    return [vs[(step * cores + j) % len(vs)] for j in range(cores)]
+    all 64 of the GPU arm's batch, largest first (so the pool's cores finish
+    together)."""
+    return sorted(batch_views(SEED), key=lambda vd: -(vd['width'] * vd['height'] + 1000 * vd['spheres']))
 
 
 # ---------------------------------------------------------------------------
@@ -742,10 +752,13 @@ def run_batch(a, rank):
     res_bytes = resolve_bytes(vs, mixed)
     batch.render(stream)
     images = [r.output() for r in mixed]
+    # the FP64 verification resolve of every view's frame (not timed)
+    fp64_images = {k: r.verify_composite_fp64(stream)[1] for k, r in enumerate(mixed)}
     return dict(frags=frags, t_mixed=t_mixed, t_plain=t_plain, launches=launches, clocks=clk, sections=sections,
                 e2e_s=e2e_s, h2d=h2d, d2h=d2h, views=vs, t_res_mixed=t_res_mixed, t_res_plain=t_res_plain,
                 res_cfg=res_cfg, res_bytes=res_bytes, e2e_flat_s=e2e_flat_s, h2d_flat=h2d_flat, e2e_same=e2e_same,
-                raster_bytes=raster_bytes, raster_intermediate=raster_intermediate, images=images)
+                raster_bytes=raster_bytes, raster_intermediate=raster_intermediate, images=images,
+                fp64_images=fp64_images)
 
 
 def _copy_d2h(host_tensor, dev_ptr, nbytes, stream):
@@ -775,11 +788,14 @@ def main_batch(a, rank, world):
     cpu_omp_line = None
     accuracy = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        f, busy, n, oracle_images = cpu_baseline_views(res['views'])
+        f, busy, n, _ = cpu_baseline_views(res['views'])
         cpu_line = {'value': round(f / busy / 1e6, 4), 'unit': 'Mfragments/s', 'cores': 1, 'kind': 'port',
                     'sample': '%d of the %d views (the smallest), whole frames, single-threaded FP64 oracle' % (
                         n, len(res['views']))}
-        accuracy = image_error(res['images'], oracle_images)
+        accuracy = image_error(res['images'], oracle_images_all(res['views']))
+        accuracy['vs_fp64_gpu_resolve'] = image_error(
+            res['images'], res['fp64_images'],
+            'oit_verify_composite_fp64: the same frames resolved in FP64 on the GPU')
         order = sorted(range(len(res['views'])), key=lambda k: res['views'][k]['width'] * res['views'][k]['height'] +
                        1000 * res['views'][k]['spheres'])
         try:
@@ -891,9 +907,10 @@ def main():
         pool = mp.get_context('spawn').Pool(cores)
 
         def ref_step(k):
-            # one step = every core renders one whole frame of the workload
-            # (batch: one view of the batch per core)
-            args = [(vd, 1) for vd in reference_views(k, cores)] if batch else [(wd, 1)] * cores
+            # one step = the workload: the batch's 64 views spread over the
+            # cores (one whole frame per task), or one frame per core of a
+            # single-view workload
+            args = [(vd, 1) for vd in reference_views()] if batch else [(wd, 1)] * cores
             t0 = time.perf_counter()
             res = pool.map(_oracle_frame, args, chunksize=1)
             return sum(r[0] for r in res), time.perf_counter() - t0
@@ -915,8 +932,8 @@ def main():
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64 blend',
             'data': 'synthetic: seeded UV-sphere scene', 'config': wd,
             'cpu_baseline': {'value': round(value, 4), 'unit': 'Mfragments/s', 'cores': cores, 'kind': 'port',
-                             'sample': '%d whole frames per step, one per core%s' % (
-                                 cores, ' (the 48 cheapest batch views in turn)' if batch else '')},
+                             'sample': ('the whole 64-view batch per step, one view per task on %d processes' % cores)
+                             if batch else '%d whole frames per step, one per core' % cores},
             'e2e': {'value': round(value, 4), 'unit': 'Mfragments/s', 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0},
             'note': 'reference Vulkan build unavailable on this box (no graphics stack); CPU restatement of the '

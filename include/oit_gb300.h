@@ -124,6 +124,11 @@ typedef struct oit_context oit_context;
 #define OIT_BUF_REVEAL 8         /* WBOIT revealage, half or float per sample */
 #define OIT_BUF_OUTPUT 9         /* resolved RGBA8 output image (width*height*4) */
 #define OIT_BUF_OUTPUT_LINEAR 10 /* resolved premultiplied linear float4 output */
+#define OIT_BUF_MICROTILE_LENGTHS 11 /* u8 per 8x4 micro-tile: most fragments any of its pixels received
+                                        (batched-resolve views: linked list or Loop64, 1x, RGBA8) */
+#define OIT_BUF_NODE_RANGES 12   /* linked list, batched-resolve views: per 8x4 micro-tile, the node ranges
+                                    its raster warp allocated: u32 {first0, first1, first2,
+                                    count0 | count1 << 8 | count2 << 16 | ranges << 24} */
 
 /* ---- lifetime ---------------------------------------------------------- */
 
@@ -176,6 +181,18 @@ int oit_draw_transparent_color(oit_context* ctx, const oit_mesh* mesh, uint32_t 
  * Replaces the full-screen composite draws (oitRender.cpp:191-198, 232-239,
  * 293-300, 327-334, 373-381, 416-424). */
 int oit_composite(oit_context* ctx, uint8_t* out_rgba8_device, void* stream);
+
+/* FP64 verification resolve: the COMPOSITE pass of the context's current
+ * frame (after oit_draw_transparent_color, oit_render_frame* or a batch)
+ * recomputed in double precision from the same A-buffer, aux words and
+ * tail-blended colour target -- the reference's sorts with doBlend /
+ * doBlendPacked (shaders/shaderCommon.glsl:108-124) and the blend onto the
+ * colour target (main.cpp:548-558) in FP64, then the MSAA / supersample
+ * resolve. Writes width*height premultiplied linear double4 colours to
+ * out_linear_device and/or RGBA8 sRGB pixels to out_rgba8_device (either may
+ * be NULL, not both). A checker of the FP32 resolve, not part of a frame: no
+ * counterpart in the reference, whose composite runs in FP32 shaders. */
+int oit_verify_composite_fp64(oit_context* ctx, double* out_linear_device, uint8_t* out_rgba8_device, void* stream);
 
 /* drawTransparent*(cmd, numObjects) (oit.h:379-425): COLOR + COMPOSITE over the
  * first num_triangles triangles of the mesh. */
@@ -312,6 +329,9 @@ typedef struct oit_resolve_shape {
   int32_t register_slots;   /* micro-tiles whose lists hold at most this many nodes (0, 4 or 8) are staged
                                in shared memory and sorted by a network in registers */
   int32_t dense;            /* 1: at most 32 registers per thread (eight 256-thread blocks per SM) */
+  int32_t node_ranges;      /* linked lists, 1: the node ranges the raster allocated for each micro-tile
+                               (at most three) staged in shared memory with coalesced loads and the lists
+                               walked there */
 } oit_resolve_shape;
 
 /* Part 0: linked-list views, 1: Loop64 views. A part without views reports
@@ -321,11 +341,11 @@ int oit_batch_resolve_config(oit_batch* batch, uint32_t part, oit_resolve_shape*
 /* Pins the shape of one part of the batched resolve (a shape reported by
  * oit_batch_resolve_config, e.g. tuned once offline): the autotuner then
  * skips that part. blocks 0: every block that fits on the GPU. Shapes the
- * engine has no kernel for (for Loop64: shared or register slots; for linked
- * lists: more than one of shared slots, register slots and two items per
- * step, or dense with shared slots, register slots 4 or two items per step)
- * return OIT_ERR_INVALID_ARGUMENT. NULL unpins. The next render or resolve
- * of the batch uses it. */
+ * engine has no kernel for (for Loop64: shared or register slots or node
+ * ranges; for linked lists: more than one of shared slots, register slots,
+ * two items per step and node ranges, or dense with shared slots, register
+ * slots 4 or two items per step) return OIT_ERR_INVALID_ARGUMENT. NULL
+ * unpins. The next render or resolve of the batch uses it. */
 int oit_batch_set_resolve_config(oit_batch* batch, uint32_t part, const oit_resolve_shape* shape);
 
 /* ---- inspection -------------------------------------------------------- */

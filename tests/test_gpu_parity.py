@@ -252,7 +252,7 @@ def test_batched_views_match_single_frames(engine):
 
 
 @pytest.mark.parametrize('aa', [0, 1, 5])
-@pytest.mark.parametrize('L', [4, 16])
+@pytest.mark.parametrize('L', [4, 16, 32])
 @pytest.mark.parametrize('alg', [1, 3])
 def test_rgba32f_records(engine, alg, L, aa):
     """Plain FP32 records: float colours stored bit-exactly (nodes / payloads),
@@ -265,7 +265,7 @@ def test_rgba32f_records(engine, alg, L, aa):
 
 def test_rgba32f_unsupported_combinations(engine):
     import ctypes
-    for alg, L in ((0, 8), (2, 8), (3, 32), (6, 8)):
+    for alg, L in ((0, 8), (2, 8), (4, 8), (5, 8), (6, 8)):
         st = engine.make_state(alg, 64, 64, oit_layers=L, record_format=engine.OIT_RECORD_RGBA32F)
         ctx = ctypes.c_void_p()
         assert engine.library().oit_create(ctypes.byref(st), ctypes.byref(ctx)) == engine.OIT_ERR_UNSUPPORTED

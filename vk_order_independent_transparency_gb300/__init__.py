@@ -38,7 +38,8 @@ OIT_ERR_STATE = -6
 OIT_ERR_TOO_LARGE = -7
 
 OIT_BUF_ABUFFER, OIT_BUF_AUX, OIT_BUF_AUXDEPTH, OIT_BUF_COUNTER, OIT_BUF_DEPTH, OIT_BUF_OPAQUE_COLOR, \
-    OIT_BUF_COLOR, OIT_BUF_ACCUM, OIT_BUF_REVEAL, OIT_BUF_OUTPUT, OIT_BUF_OUTPUT_LINEAR = range(11)
+    OIT_BUF_COLOR, OIT_BUF_ACCUM, OIT_BUF_REVEAL, OIT_BUF_OUTPUT, OIT_BUF_OUTPUT_LINEAR, \
+    OIT_BUF_MICROTILE_LENGTHS, OIT_BUF_NODE_RANGES = range(13)
 
 # The C ABI's exported symbols (include/oit_gb300.h).
 EXPORTS = [
@@ -51,6 +52,7 @@ EXPORTS = [
     'oit_batch_create', 'oit_batch_destroy', 'oit_batch_render', 'oit_batch_launch_count',
     'oit_render_frame_instanced', 'oit_render_frame_instanced_host', 'oit_scene_generate_instanced',
     'oit_batch_resolve', 'oit_batch_resolve_config', 'oit_batch_set_resolve_config', 'oit_debug_fail_allocations',
+    'oit_verify_composite_fp64',
 ]
 PROF_SECTIONS = ['opaque_bin', 'opaque_raster', 'transparent_bin', 'transparent_raster', 'composite']
 
@@ -85,7 +87,7 @@ class OitInstancedMesh(ctypes.Structure):
 class OitResolveShape(ctypes.Structure):
     _fields_ = [('threads_per_block', ctypes.c_uint32), ('blocks', ctypes.c_uint32), ('binned', ctypes.c_int32),
                 ('tile_order', ctypes.c_int32), ('shared_slots', ctypes.c_int32), ('items_per_step', ctypes.c_int32),
-                ('register_slots', ctypes.c_int32), ('dense', ctypes.c_int32)]
+                ('register_slots', ctypes.c_int32), ('dense', ctypes.c_int32), ('node_ranges', ctypes.c_int32)]
 
 
 class OitSceneDesc(ctypes.Structure):
@@ -162,6 +164,7 @@ def library():
         'oit_batch_resolve_config': (I, [P, U, ctypes.POINTER(OitResolveShape)]),
         'oit_batch_set_resolve_config': (I, [P, U, ctypes.POINTER(OitResolveShape)]),
         'oit_debug_fail_allocations': (I, [ctypes.c_int32]),
+        'oit_verify_composite_fp64': (I, [P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -416,6 +419,19 @@ class Renderer:
         """Resolved RGBA8 image as (height, width, 4) uint8."""
         return self.read_buffer(OIT_BUF_OUTPUT, np.uint8).reshape(self.state.height, self.state.width, 4)
 
+    def verify_composite_fp64(self, stream=None):
+        """FP64 verification resolve of the current frame: (linear float64
+        (height, width, 4) premultiplied, RGBA8 (height, width, 4))."""
+        import torch
+        H, W = self.state.height, self.state.width
+        lin = torch.empty((H, W, 4), dtype=torch.float64, device='cuda')
+        img = torch.empty((H, W, 4), dtype=torch.uint8, device='cuda')
+        _check(self.lib.oit_verify_composite_fp64(self._ctx, ctypes.c_void_p(lin.data_ptr()),
+                                                  ctypes.c_void_p(img.data_ptr()), stream),
+               'oit_verify_composite_fp64')
+        torch.cuda.synchronize()
+        return lin.cpu().numpy(), img.cpu().numpy()
+
     def get_error(self):
         bits = ctypes.c_uint32()
         _check(self.lib.oit_get_error(self._ctx, ctypes.byref(bits)), 'oit_get_error')
@@ -502,7 +518,8 @@ class Batch:
         for part, name in ((0, 'linkedlist'), (1, 'loop64')):
             sh = OitResolveShape()
             _check(self.lib.oit_batch_resolve_config(self._b, part, ctypes.byref(sh)), 'oit_batch_resolve_config')
-            out[name] = {f: (bool(getattr(sh, f)) if f in ('binned', 'tile_order', 'dense') else getattr(sh, f))
+            out[name] = {f: (bool(getattr(sh, f)) if f in ('binned', 'tile_order', 'dense', 'node_ranges')
+                             else getattr(sh, f))
                          for f, _ in OitResolveShape._fields_}
         return out
 

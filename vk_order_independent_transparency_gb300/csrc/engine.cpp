@@ -108,6 +108,7 @@ struct oit_context {
   DevBuf mesh_v, mesh_i;
   DevBuf scene_dev;  // proj_view then view, read by k_setup
   DevBuf lens;  // per 8x4 micro-tile fragment counts for the batched resolve
+  DevBuf node_ranges;  // linked list: per 8x4 micro-tile, the node ranges its raster warp allocated
   size_t tri_cap = 0, pair_cap = 0;
   bool opaque_valid = false;
   bool color_valid = false;
@@ -182,7 +183,7 @@ struct oit_context {
     DevBuf* all[] = {&depth, &opaque_color, &color, &abuf, &aux, &auxdepth, &counter, &accum, &reveal, &out,
                      &out_linear, &err, &frag, &bbox, &setup, &persp, &pair_count, &pair_offset, &scan_tmp, &total,
                      &keys, &tris, &keys_alt, &tris_alt, &hist, &tile_begin, &tile_end, &mesh_v, &mesh_i,
-                     &scene_dev, &lens};
+                     &scene_dev, &lens, &node_ranges};
     for (DevBuf* b : all) b->release();
   }
 
@@ -250,6 +251,10 @@ struct oit_context {
     if (batch_resolvable()) {
       OIT_TRY_CUDA(lens.ensure(lens_count()), "alloc lens");
       OIT_TRY_CUDA(cudaMemset(lens.p, 0, lens_count()), "memset");
+      if (alg() == oit::Alg::LinkedList) {
+        OIT_TRY_CUDA(node_ranges.ensure(lens_count() * 16), "alloc node ranges");
+        OIT_TRY_CUDA(cudaMemset(node_ranges.p, 0, lens_count() * 16), "memset");
+      }
     }
     return OIT_OK;
   }
@@ -468,6 +473,7 @@ struct oit_context {
     if (tile_offset != 0 && batch_resolvable()) {
       p.lens = lens.as<uint8_t>();
       p.lens_stride = lens_stride();
+      if (alg() == oit::Alg::LinkedList) p.node_ranges = node_ranges.as<uint4>();
     }
     return p;
   }
@@ -482,6 +488,7 @@ struct oit_context {
     v.out = out_dev ? out_dev : out.as<uint8_t>();
     v.out_linear = nullptr;
     v.lens = lens.as<uint8_t>();
+    v.node_ranges = node_ranges.as<uint4>();
     v.P = P;
     v.capacity = capacity;
     v.W = RW;
@@ -582,9 +589,7 @@ struct oit_context {
     return raster_transparent(s);
   }
 
-  int composite(uint8_t* out_dev, cudaStream_t s) {
-    last_stream = s;
-    if (!color_valid) return OIT_ERR_STATE;
+  oit::CompositeParams composite_params(uint8_t* out_dev) {
     oit::CompositeParams c{};
     c.W = W;
     c.H = H;
@@ -609,8 +614,15 @@ struct oit_context {
     c.background = background;
     c.accum = accum.p;
     c.reveal = reveal.p;
-    c.out_rgba8 = out_dev ? out_dev : out.as<uint8_t>();
+    c.out_rgba8 = out_dev;
     c.out_linear = nullptr;
+    return c;
+  }
+
+  int composite(uint8_t* out_dev, cudaStream_t s) {
+    last_stream = s;
+    if (!color_valid) return OIT_ERR_STATE;
+    oit::CompositeParams c = composite_params(out_dev ? out_dev : out.as<uint8_t>());
     if (st.flags & OIT_FLAG_LINEAR_OUTPUT) {
       OIT_TRY_CUDA(out_linear.ensure((size_t)W * H * 16), "alloc linear");
       c.out_linear = out_linear.as<float4>();
@@ -620,6 +632,15 @@ struct oit_context {
     const int r = cuda_status(oit::launch_composite(alg(), c, s), "composite");
     prof_end(OIT_PROF_COMPOSITE, t0, s);
     return r;
+  }
+
+  // FP64 verification resolve of the current frame (not part of a frame).
+  int verify_composite_fp64(double* out_linear_dev, uint8_t* out_rgba8_dev, cudaStream_t s) {
+    if (!color_valid) return OIT_ERR_STATE;
+    last_stream = s;
+    const oit::CompositeParams c = composite_params(out_rgba8_dev);
+    ++launches;
+    return cuda_status(oit::launch_composite_fp64(alg(), c, out_linear_dev, s), "composite fp64");
   }
 
   // Sample::onRender, oitRender.cpp:43-153. The transparent objects are the
@@ -854,10 +875,10 @@ int validate(const oit_state* s, int* msaa, int* ss, int* sup) {
     return OIT_ERR_INVALID_ARGUMENT;
   if (!std::isfinite(s->alpha_min) || !std::isfinite(s->alpha_width)) return OIT_ERR_INVALID_ARGUMENT;
   if (s->record_format == OIT_RECORD_RGBA32F) {
-    // float records exist for the linked list and Loop64; Loop64's float
-    // payloads need 24 bytes of shared memory per layer and lane (L <= 16)
+    // float records exist for the linked list and Loop64 (whose float payloads
+    // take 24 bytes of shared memory per layer and lane: 24 KB per warp at 32
+    // layers)
     if (s->algorithm != OIT_LINKEDLIST && s->algorithm != OIT_LOOP64) return OIT_ERR_UNSUPPORTED;
-    if (s->algorithm == OIT_LOOP64 && s->oit_layers > 16) return OIT_ERR_UNSUPPORTED;
   }
   return OIT_OK;
 }
@@ -993,7 +1014,8 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
     if (part == 0)
       variants = {oit::kResolveVariantList, oit::kResolveVariantListShared, oit::kResolveVariantListx2,
                   oit::kResolveVariantListShort4, oit::kResolveVariantListShort8, oit::kResolveVariantListDense,
-                  oit::kResolveVariantListShort8Dense};
+                  oit::kResolveVariantListShort8Dense, oit::kResolveVariantListRanges,
+                  oit::kResolveVariantListRangesDense};
     else variants = {oit::kResolveVariantLoop64, oit::kResolveVariantLoop64x2, oit::kResolveVariantLoop64Dense};
     for (int variant : variants) {
       for (int threads : {64, 128, 256}) {
@@ -1198,6 +1220,11 @@ int oit_draw_transparent_color(oit_context* ctx, const oit_mesh* mesh, uint32_t 
 int oit_composite(oit_context* ctx, uint8_t* out, void* stream) {
   if (!ctx) return OIT_ERR_INVALID_ARGUMENT;
   return ctx->composite(out, static_cast<cudaStream_t>(stream));
+}
+
+int oit_verify_composite_fp64(oit_context* ctx, double* out_linear, uint8_t* out_rgba8, void* stream) {
+  if (!ctx || (!out_linear && !out_rgba8)) return OIT_ERR_INVALID_ARGUMENT;
+  return ctx->verify_composite_fp64(out_linear, out_rgba8, static_cast<cudaStream_t>(stream));
 }
 
 int oit_draw_transparent(oit_context* ctx, const oit_mesh* mesh, uint32_t num_triangles, uint8_t* out, void* stream) {
@@ -1450,6 +1477,9 @@ int oit_batch_set_resolve_config(oit_batch* b, uint32_t part, const oit_resolve_
         (sh.dense != 0 && sh.dense != 1) || (sh.items_per_step != 0 && sh.items_per_step != 1 && sh.items_per_step != 2))
       return OIT_ERR_INVALID_ARGUMENT;
     const bool x2 = sh.items_per_step == 2;
+    if (sh.node_ranges != 0 && sh.node_ranges != 1) return OIT_ERR_INVALID_ARGUMENT;
+    if (sh.node_ranges && (part == 1 || sh.shared_slots != 0 || sh.register_slots != 0 || x2))
+      return OIT_ERR_INVALID_ARGUMENT;
     if (part == 1) {
       if (sh.shared_slots != 0 || sh.register_slots != 0 || (x2 && sh.dense)) return OIT_ERR_INVALID_ARGUMENT;
       pn.variant = x2 ? oit::kResolveVariantLoop64x2
@@ -1460,7 +1490,8 @@ int oit_batch_set_resolve_config(oit_batch* b, uint32_t part, const oit_resolve_
         return OIT_ERR_INVALID_ARGUMENT;
       if ((sh.shared_slots != 0) + (sh.register_slots != 0) + (int)x2 > 1) return OIT_ERR_INVALID_ARGUMENT;
       if (sh.dense && (sh.shared_slots != 0 || sh.register_slots == 4 || x2)) return OIT_ERR_INVALID_ARGUMENT;
-      if (sh.shared_slots) pn.variant = oit::kResolveVariantListShared;
+      if (sh.node_ranges) pn.variant = sh.dense ? oit::kResolveVariantListRangesDense : oit::kResolveVariantListRanges;
+      else if (sh.shared_slots) pn.variant = oit::kResolveVariantListShared;
       else if (x2) pn.variant = oit::kResolveVariantListx2;
       else if (sh.register_slots == 4) pn.variant = oit::kResolveVariantListShort4;
       else if (sh.register_slots == 8)
@@ -1504,9 +1535,11 @@ int oit_batch_resolve_config(oit_batch* b, uint32_t part, oit_resolve_shape* out
                             ? 8
                             : 0;
   out->dense = (rp.variant == oit::kResolveVariantListDense || rp.variant == oit::kResolveVariantListShort8Dense ||
-                rp.variant == oit::kResolveVariantLoop64Dense)
+                rp.variant == oit::kResolveVariantLoop64Dense || rp.variant == oit::kResolveVariantListRangesDense)
                    ? 1
                    : 0;
+  out->node_ranges =
+      (rp.variant == oit::kResolveVariantListRanges || rp.variant == oit::kResolveVariantListRangesDense) ? 1 : 0;
   return OIT_OK;
 }
 
@@ -1540,6 +1573,8 @@ int oit_get_buffer(oit_context* ctx, int which, void** ptr, size_t* bytes) {
     case OIT_BUF_REVEAL: b = &ctx->reveal; n = b->bytes; break;
     case OIT_BUF_OUTPUT: b = &ctx->out; n = (size_t)ctx->W * ctx->H * 4; break;
     case OIT_BUF_OUTPUT_LINEAR: b = &ctx->out_linear; n = b->p ? (size_t)ctx->W * ctx->H * 16 : 0; break;
+    case OIT_BUF_MICROTILE_LENGTHS: b = &ctx->lens; n = b->p ? ctx->lens_count() : 0; break;
+    case OIT_BUF_NODE_RANGES: b = &ctx->node_ranges; n = b->p ? ctx->lens_count() * 16 : 0; break;
     default: return OIT_ERR_INVALID_ARGUMENT;
   }
   *ptr = b->p;

@@ -41,6 +41,13 @@ __device__ __forceinline__ WalkNode load_node(const uint4* __restrict__ pool, ui
   return WalkNode{n.x, n.y, n.z, n.w};
 }
 
+// Node loads straight from the pool.
+template <bool F32>
+struct PoolFetch {
+  const uint4* __restrict__ pool;
+  __device__ __forceinline__ WalkNode operator()(uint32_t off) const { return load_node<F32>(pool, off); }
+};
+
 template <bool F32>
 __device__ __forceinline__ float4 node_colour(const uint4* __restrict__ pool, uint32_t c) {
   if (F32) {
@@ -87,13 +94,13 @@ struct ListWalk {
 
 // bubbleSort exactly (swap on >=) over the first k nodes in list order, read
 // again from the pool.
-template <bool F32, class A>
-__device__ __noinline__ void walk_bubble(const uint4* __restrict__ pool, uint32_t head, uint32_t cap, int k, A& a) {
+template <bool F32, class A, class Fetch>
+__device__ __noinline__ void walk_bubble(const Fetch& fetch, uint32_t head, uint32_t cap, int k, A& a) {
   constexpr bool Mask = A::kMask;
   uint32_t o = head;
 #pragma unroll 1
   for (int i = 0; i < k; ++i) {
-    const WalkNode n = load_node<F32>(pool, o);
+    const WalkNode n = fetch(o);
     a.C(i) = n.c;
     a.D(i) = n.d;
     if (Mask) a.M(i) = n.m;
@@ -123,9 +130,9 @@ __device__ __noinline__ void walk_bubble(const uint4* __restrict__ pool, uint32_
 // insertion, each placed before equal depths; equal depths are flagged, and on
 // reaching OIT_LAYERS nodes (or the end of a shorter list) a flagged array is
 // rebuilt by bubbleSort itself. Later nodes go through insertionSortTail.
-template <bool F32, class A>
-__device__ __forceinline__ void walk_step(ListWalk& w, A& a, const WalkNode& n, const uint4* __restrict__ pool,
-                                          uint32_t cap, int L, int tail) {
+template <bool F32, class A, class Fetch>
+__device__ __forceinline__ void walk_step(ListWalk& w, A& a, const WalkNode& n, const Fetch& fetch,
+                                          const uint4* __restrict__ pool, uint32_t cap, int L, int tail) {
   constexpr bool Mask = A::kMask;
   const uint32_t next = n.next < cap ? n.next : 0u;
   if (w.k < L) {
@@ -146,7 +153,7 @@ __device__ __forceinline__ void walk_step(ListWalk& w, A& a, const WalkNode& n, 
     ++w.k;
     w.off = next;
     if (w.tie && (w.k == L || next == 0)) {
-      walk_bubble<F32>(pool, w.head, cap, w.k, a);
+      walk_bubble<F32>(fetch, w.head, cap, w.k, a);
       w.tie = false;
     }
     return;
@@ -179,9 +186,9 @@ __device__ __forceinline__ void walk_step(ListWalk& w, A& a, const WalkNode& n, 
 // Walks the list from `head` and returns the composited colour: kept entries
 // front to back (with coverage: per MSAA sample, the entries covering it,
 // averaged over the S samples, oitSimple.frag.glsl:142-159), then the tail.
-template <bool F32, class A>
-__device__ __forceinline__ float4 walk_list(const uint4* __restrict__ pool, uint32_t head, uint32_t cap, int L,
-                                            int tail, int S, A& a) {
+template <bool F32, class A, class Fetch>
+__device__ __forceinline__ float4 walk_list_with(const Fetch& fetch, const uint4* __restrict__ pool, uint32_t head,
+                                                 uint32_t cap, int L, int tail, int S, A& a) {
   constexpr bool Mask = A::kMask;
   ListWalk w;
   w.head = head < cap ? head : 0u;
@@ -191,7 +198,7 @@ __device__ __forceinline__ float4 walk_list(const uint4* __restrict__ pool, uint
   w.tie = false;
   w.tail = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
-  while (w.off != 0) walk_step<F32>(w, a, load_node<F32>(pool, w.off), pool, cap, L, tail);
+  while (w.off != 0) walk_step<F32>(w, a, fetch(w.off), fetch, pool, cap, L, tail);
   float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
   if (!Mask) {
 #pragma unroll 1
@@ -213,6 +220,12 @@ __device__ __forceinline__ float4 walk_list(const uint4* __restrict__ pool, uint
   }
   blend_under(sum, w.tail);
   return sum;
+}
+
+template <bool F32, class A>
+__device__ __forceinline__ float4 walk_list(const uint4* __restrict__ pool, uint32_t head, uint32_t cap, int L,
+                                            int tail, int S, A& a) {
+  return walk_list_with<F32>(PoolFetch<F32>{pool}, pool, head, cap, L, tail, S, a);
 }
 
 // Sorting networks on (depth, colour) pairs, ascending depth: the 5- and

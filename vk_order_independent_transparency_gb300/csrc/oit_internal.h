@@ -127,6 +127,12 @@ struct RasterParams {
   // work binning; null = not wanted (1x only)
   uint8_t* lens;
   int lens_stride;               // micro-tiles per row, (RW + 7) / 8
+  // linked list, per 8x4 micro-tile (indexed as lens): the node ranges the
+  // micro-tile's warp allocated, {first0, first1, first2, count0 | count1 << 8 |
+  // count2 << 16 | ranges << 24} (ranges = all ranges it allocated, capped at
+  // 255; only the first three are listed; counts exclude nodes beyond the
+  // pool); null = not wanted
+  uint4* node_ranges;
 };
 
 struct CompositeParams {
@@ -164,6 +170,7 @@ struct ResolveView {
   uint8_t* out;                  // [P] RGBA8
   float4* out_linear;            // optional [P]
   const uint8_t* lens;           // [mty][mtx] per 8x4 micro-tile fragment counts
+  const uint4* node_ranges;      // [mty][mtx] linked list: the micro-tile's node ranges (RasterParams)
   uint32_t P, capacity;
   int W, H, L, kind, tail, mtx, mty;
   int color_half;
@@ -198,6 +205,10 @@ cudaError_t launch_raster_a(Alg alg, const RasterParams& p, cudaStream_t s);  //
 cudaError_t launch_raster_b(Alg alg, const RasterParams& p, cudaStream_t s);  // Loop, Loop64
 cudaError_t launch_raster_c(Alg alg, const RasterParams& p, cudaStream_t s);  // Spinlock, Interlock, Weighted
 cudaError_t launch_composite(Alg alg, const CompositeParams& p, cudaStream_t s);
+// FP64 verification resolve (verify.cu): the composite recomputed in double;
+// writes double4 linear colours to out_linear (may be null) and RGBA8 to
+// p.out_rgba8 (may be null).
+cudaError_t launch_composite_fp64(Alg alg, const CompositeParams& p, double* out_linear, cudaStream_t s);
 // Batched resolve: bin the micro-tiles of every view by cost (costliest
 // first), then one persistent launch resolves them all.
 // Kernel variants: Loop64 views; linked-list views with their sort arrays in
@@ -214,6 +225,8 @@ enum ResolveVariant : int {
   kResolveVariantListDense = 7,   // local arrays, at most 32 registers (eight 256-thread blocks per SM)
   kResolveVariantListShort8Dense = 8,  // Short8 at most 32 registers
   kResolveVariantLoop64Dense = 9,      // Loop64 at most 32 registers
+  kResolveVariantListRanges = 10,      // the micro-tile's node ranges staged in shared memory, <= 40 registers
+  kResolveVariantListRangesDense = 11, // the same at most 32 registers
 };
 cudaError_t resolve_bin(const ResolveBatch& b, cudaStream_t s, uint64_t* launches);
 cudaError_t resolve_run(const ResolveBatch& b, int variant, int threads, int blocks, cudaStream_t s);

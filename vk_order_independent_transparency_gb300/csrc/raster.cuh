@@ -551,9 +551,13 @@ __device__ __forceinline__ bool lane_in_bbox(uint2 bb, const WarpTile& w) {
 }
 
 // Per-warp fragment queue: coverage appends (stage slot, lane, coverage,
-// depth) in primitive-then-lane order; shading then runs one queued fragment
-// per lane; finally each lane feeds its own pixel's fragments, in queue order,
-// to the algorithm.
+// depth) in primitive-then-lane order; shading runs one queued fragment per
+// lane once a staged chunk is covered (the setup records it reads are then
+// replaced); when the queue is full, and at the end, each lane feeds its own
+// pixel's fragments, in queue order, to the algorithm. Feeding a full queue
+// rather than each chunk's fragments gives the linked list node ranges of up
+// to kQueue nodes per allocation. vz holds the view-space z (WBOIT, which
+// feeds per chunk) or, for every other algorithm, the fragment's alpha.
 constexpr int kQueue = 64;
 struct FragQueue {
   uint32_t depth[kQueue];
@@ -568,6 +572,8 @@ struct HitRanges {
   // of bbox ∩ micro-tile relative to the micro-tile (bits 11-13, 14-15), its
   // width (bits 16-19) and ceil(256 / width) (bits 20-28)
   uint32_t packed[32];
+  // linked list: the node ranges the warp allocated (RasterParams::node_ranges)
+  uint32_t ranges[4];
 };
 constexpr size_t kWarpStageBytes = kStageSlots * (sizeof(TriSetup) + sizeof(uint32_t) + sizeof(uint2)) +
                                    sizeof(FragQueue) + sizeof(HitRanges);
@@ -629,39 +635,65 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
   const uint32_t lt = (1u << w.lane) - 1u;
   uint32_t nfrag = 0;  // warp-uniform
   uint32_t mine = 0;   // fragments delivered to this lane's pixel
-  int qn = 0;          // warp-uniform
+  int qn = 0;          // warp-uniform: queued fragments
+  int qs = 0;          // warp-uniform: queued fragments already shaded
+  if (Pol::kNodes && w.lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) hr->ranges[k] = 0u;
+  }
   const uint32_t lane_bytes = (uint32_t)w.lane * 0x01010101u;
 
   for (int pass = 0; pass < Pol::kPasses; ++pass) {
     const bool shading = Pol::kPasses == 1 || pass == Pol::kPasses - 1;
 
+    // Shades queue entries [qs, qn): their setup records are still staged.
+    auto shade_pending = [&]() {
+      if (!shading || qs == qn) {
+        qs = qn;
+        return;
+      }
+      __syncwarp();
+      for (int j = qs + w.lane; j < qn; j += 32) {
+        const TriSetup& T = stage[q->tri[j]];
+        const int l = q->lane[j];
+        // shading point: the pixel centre, or the lane's sample with sample shading
+        const int pl = M::pix(l);
+        const int2 sp = SSN > 1 ? sample_pos<SSN>(M::sample(l)) : make_int2(128, 128);
+        const int sx = (w.rx0 + pl % M::kW) * 256 + sp.x, sy = (w.ry0 + pl / M::kW) * 256 + sp.y;
+        const TriPersp* P = Pol::kViewZ ? persp + stage_t[q->tri[j]] : nullptr;
+        const int4 a = T.xy01, b = T.xy2f;
+        Shade sh;
+        if (b.z & kFlagSmall) sh = shade(T, edges_at<int>(a, b, sx, sy), P);
+        else sh = shade(T, edges_at<long long>(a, b, sx, sy), P);
+        q->packed[j] = pack_rgba8(sh, (uint32_t)(b.z >> 8) & 255u);
+        q->r[j] = sh.r;
+        q->g[j] = sh.g;
+        q->b[j] = sh.b;
+        q->vz[j] = Pol::kViewZ ? sh.view_z : __int_as_float(b.w);  // view z, or alpha
+      }
+      qs = qn;
+      __syncwarp();
+    };
+
+    // Feeds the queue to the algorithm (after shading what is left).
     auto flush = [&]() {
       if (qn == 0) return;
-      __syncwarp();
-      if (shading) {
-        for (int j = w.lane; j < qn; j += 32) {
-          const TriSetup& T = stage[q->tri[j]];
-          const int l = q->lane[j];
-          // shading point: the pixel centre, or the lane's sample with sample shading
-          const int pl = M::pix(l);
-          const int2 sp = SSN > 1 ? sample_pos<SSN>(M::sample(l)) : make_int2(128, 128);
-          const int sx = (w.rx0 + pl % M::kW) * 256 + sp.x, sy = (w.ry0 + pl / M::kW) * 256 + sp.y;
-          const TriPersp* P = Pol::kViewZ ? persp + stage_t[q->tri[j]] : nullptr;
-          const int4 a = T.xy01, b = T.xy2f;
-          Shade sh;
-          if (b.z & kFlagSmall) sh = shade(T, edges_at<int>(a, b, sx, sy), P);
-          else sh = shade(T, edges_at<long long>(a, b, sx, sy), P);
-          q->packed[j] = pack_rgba8(sh, (uint32_t)(b.z >> 8) & 255u);
-          q->r[j] = sh.r;
-          q->g[j] = sh.g;
-          q->b[j] = sh.b;
-          q->vz[j] = sh.view_z;
-        }
-        __syncwarp();
-      }
+      shade_pending();
       uint32_t node0 = 0;
       if (Pol::kNodes && shading) {
-        if (w.lane == 0) node0 = atomicAdd(p.counter, (uint32_t)qn);
+        if (w.lane == 0) {
+          node0 = atomicAdd(p.counter, (uint32_t)qn);
+          // this allocation's nodes node0 + 1 .. node0 + qn, those in the pool
+          const uint32_t first = node0 + 1u;
+          const uint32_t last = min(node0 + (uint32_t)qn, p.capacity > 0 ? p.capacity - 1u : 0u);
+          const uint32_t cnt = (first <= last && first < p.capacity) ? last - first + 1u : 0u;
+          const uint32_t k = hr->ranges[3] >> 24;
+          if (cnt > 0 && k < 3u) {
+            hr->ranges[k] = first;
+            hr->ranges[3] |= cnt << (8 * k);
+          }
+          if (cnt > 0 && k < 255u) hr->ranges[3] += 1u << 24;
+        }
         node0 = __shfl_sync(kFull, node0, 0);
       }
       // this lane's entries: scan the owner byte of every queued fragment
@@ -685,13 +717,14 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
           f.r = q->r[j];
           f.g = q->g[j];
           f.b = q->b[j];
-          f.a = __int_as_float(stage[q->tri[j]].xy2f.w);
+          f.a = Pol::kViewZ ? __int_as_float(stage[q->tri[j]].xy2f.w) : q->vz[j];
           f.view_z = q->vz[j];
         }
         pol.fragment(p, pass, f, node0 + (uint32_t)j + 1u, tg);
       }
       if (shading) nfrag += (uint32_t)qn;
       qn = 0;
+      qs = 0;
       __syncwarp();
     };
 
@@ -838,8 +871,11 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
       } else {
         for (int k = 0; k < nh; ++k) cover_one(k);  // one lane per sample
       }
-      flush();
+      // the next chunk replaces the staged records: shade now; WBOIT's
+      // fragments also need their record's alpha, so it feeds every chunk
+      if (Pol::kViewZ) flush(); else shade_pending();
     });
+    flush();
   }
 
   pol.flush(p, w.valid);
@@ -859,8 +895,12 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
   if (SSN == 1 && p.lens) {
     const uint32_t mx = __reduce_max_sync(kFull, w.valid ? mine : 0u);
     // micro-tiles of edge tiles may lie wholly outside the image
-    if (w.lane == 0 && w.rx0 < p.RW && w.ry0 < p.RH)
-      p.lens[(size_t)(w.ry0 >> 2) * p.lens_stride + (w.rx0 >> 3)] = (uint8_t)min(mx, 255u);
+    if (w.lane == 0 && w.rx0 < p.RW && w.ry0 < p.RH) {
+      const size_t mt = (size_t)(w.ry0 >> 2) * p.lens_stride + (w.rx0 >> 3);
+      p.lens[mt] = (uint8_t)min(mx, 255u);
+      if (Pol::kNodes && p.node_ranges)
+        p.node_ranges[mt] = make_uint4(hr->ranges[0], hr->ranges[1], hr->ranges[2], hr->ranges[3]);
+    }
   }
 }
 
