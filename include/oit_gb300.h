@@ -72,7 +72,10 @@ extern "C" {
 #define OIT_ERR_TOO_LARGE (-7)   /* the frame does not fit oit_render_frame_noalloc's scratch arena */
 
 /* Device error bits reported by oit_get_error. */
-#define OIT_DEVERR_BIN_OVERFLOW 0x1u  /* triangle/tile pairs exceeded the bin capacity */
+#define OIT_DEVERR_BIN_OVERFLOW 0x1u  /* a draw's triangle/tile pairs exceeded the bin capacity sized on earlier
+                                         frames: its image is still complete (the triangles that did not fit
+                                         were tested by bbox, a slower walk) and the next frame call re-sizes
+                                         the bins */
 #define OIT_DEVERR_TIMEOUT 0x2u       /* a bounded wait gave up */
 
 /* Renderer settings: State (oit.h:64-116) plus the SceneData scalars
@@ -126,9 +129,6 @@ typedef struct oit_context oit_context;
 #define OIT_BUF_OUTPUT_LINEAR 10 /* resolved premultiplied linear float4 output */
 #define OIT_BUF_MICROTILE_LENGTHS 11 /* u8 per 8x4 micro-tile: most fragments any of its pixels received
                                         (batched-resolve views: linked list or Loop64, 1x, RGBA8) */
-#define OIT_BUF_NODE_RANGES 12   /* linked list, batched-resolve views: per 8x4 micro-tile, the node ranges
-                                    its raster warp allocated: u32 {first0, first1, first2,
-                                    count0 | count1 << 8 | count2 << 16 | ranges << 24} */
 
 /* ---- lifetime ---------------------------------------------------------- */
 
@@ -329,9 +329,6 @@ typedef struct oit_resolve_shape {
   int32_t register_slots;   /* micro-tiles whose lists hold at most this many nodes (0, 4 or 8) are staged
                                in shared memory and sorted by a network in registers */
   int32_t dense;            /* 1: at most 32 registers per thread (eight 256-thread blocks per SM) */
-  int32_t node_ranges;      /* linked lists, 1: the node ranges the raster allocated for each micro-tile
-                               (at most three) staged in shared memory with coalesced loads and the lists
-                               walked there */
 } oit_resolve_shape;
 
 /* Part 0: linked-list views, 1: Loop64 views. A part without views reports
@@ -341,11 +338,11 @@ int oit_batch_resolve_config(oit_batch* batch, uint32_t part, oit_resolve_shape*
 /* Pins the shape of one part of the batched resolve (a shape reported by
  * oit_batch_resolve_config, e.g. tuned once offline): the autotuner then
  * skips that part. blocks 0: every block that fits on the GPU. Shapes the
- * engine has no kernel for (for Loop64: shared or register slots or node
- * ranges; for linked lists: more than one of shared slots, register slots,
- * two items per step and node ranges, or dense with shared slots, register
- * slots 4 or two items per step) return OIT_ERR_INVALID_ARGUMENT. NULL
- * unpins. The next render or resolve of the batch uses it. */
+ * engine has no kernel for (for Loop64: shared or register slots; for linked
+ * lists: more than one of shared slots, register slots and two items per
+ * step, or dense with shared slots, register slots 4 or two items per step)
+ * return OIT_ERR_INVALID_ARGUMENT. NULL unpins. The next render or resolve
+ * of the batch uses it. */
 int oit_batch_set_resolve_config(oit_batch* batch, uint32_t part, const oit_resolve_shape* shape);
 
 /* ---- inspection -------------------------------------------------------- */

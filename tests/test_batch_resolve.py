@@ -65,7 +65,6 @@ def test_batch_render_and_resolve_match_single_frames():
     assert cfg['linkedlist']['register_slots'] in (0, 4, 8) and cfg['loop64']['register_slots'] == 0
     assert cfg['loop64']['items_per_step'] in (1, 2) and cfg['loop64']['dense'] in (0, 1)
     assert cfg['loop64']['items_per_step'] == 1 or not cfg['loop64']['dense']
-    assert not cfg['loop64']['node_ranges']
     # resolve alone, after clearing the outputs
     import torch
     for r, _, _, _ in views:
@@ -118,8 +117,6 @@ PINNED = [
     ('linkedlist', dict(threads_per_block=64, register_slots=4)),
     ('linkedlist', dict(threads_per_block=128, register_slots=8)),
     ('linkedlist', dict(threads_per_block=256, register_slots=8, dense=1)),
-    ('linkedlist', dict(threads_per_block=256, node_ranges=1)),
-    ('linkedlist', dict(threads_per_block=128, node_ranges=1, dense=1)),
     ('loop64', dict(threads_per_block=256)),
     ('loop64', dict(threads_per_block=128, items_per_step=2)),
     ('loop64', dict(threads_per_block=256, dense=1)),
@@ -169,11 +166,7 @@ def test_pinned_shape_validation():
            ('linkedlist', dict(threads_per_block=128, register_slots=4, dense=1)),
            ('linkedlist', dict(threads_per_block=128, items_per_step=3)),
            ('linkedlist', dict(threads_per_block=48)), ('linkedlist', dict(threads_per_block=512)),
-           ('linkedlist', dict(threads_per_block=128, shared_slots=4)),
-           ('loop64', dict(threads_per_block=128, node_ranges=1)),
-           ('linkedlist', dict(threads_per_block=128, node_ranges=1, register_slots=8)),
-           ('linkedlist', dict(threads_per_block=128, node_ranges=1, items_per_step=2)),
-           ('linkedlist', dict(threads_per_block=128, node_ranges=2))]
+           ('linkedlist', dict(threads_per_block=128, shared_slots=4))]
     for part, shape in bad:
         with pytest.raises(oit.OitError) as e:
             batch.set_resolve_config(part, shape)
@@ -181,47 +174,3 @@ def test_pinned_shape_validation():
     batch.set_resolve_config('linkedlist', dict(threads_per_block=128))
     batch.set_resolve_config('linkedlist', None)
 
-
-def test_node_ranges_cover_the_lists():
-    """The transparent raster records, per 8x4 micro-tile, the node ranges its
-    warp allocated (at most three listed, all counted): every node of every
-    list of the micro-tile's pixels lies in its listed ranges when it
-    allocated at most three; the listed counts never pass the pool's end."""
-    W, H, L = 150, 100, 8
-    v, i, tpo, sd = pu.scene(120, W, H, seed=77, radius_min=0.08, radius_max=0.3)
-    for npp in (12, 2):  # the second pool overflows
-        g = pu.render_gpu(oit.OIT_LINKEDLIST, W, H, v, i, tpo, sd, 100, oit_layers=L, nodes_per_pixel=npp)
-        r = g['renderer']
-        batch = oit.Batch(parallel_streams=1)
-        batch.set_views([(r, g['mesh'], tpo, 100)])
-        batch.render()  # the batched path records the ranges
-        ranges = _node_ranges(r, W, H)
-        pool = r.read_buffer(oit.OIT_BUF_ABUFFER).reshape(-1, 4)
-        heads = r.read_buffer(oit.OIT_BUF_AUX)[:W * H]
-        cap = npp * W * H
-        mtx, mty = (W + 7) // 8, (H + 3) // 4
-        many = 0
-        for my in range(mty):
-            for mx in range(mtx):
-                f0, f1, f2, w = (int(x) for x in ranges[my * mtx + mx])
-                n = w >> 24
-                cnt = [w & 255, (w >> 8) & 255, (w >> 16) & 255]
-                spans = [(f, c) for f, c in zip((f0, f1, f2), cnt) if c]
-                assert len(spans) == min(n, 3)
-                for f, c in spans:
-                    assert 1 <= f and f + c <= cap and c <= 64
-                if n > 3:
-                    many += 1
-                    continue
-                for y in range(my * 4, min(my * 4 + 4, H)):
-                    for x in range(mx * 8, min(mx * 8 + 8, W)):
-                        off = int(heads[y * W + x])
-                        while off:
-                            assert any(f <= off < f + c for f, c in spans), (mx, my, off, spans)
-                            off = int(pool[off][3])
-        print('npp %d: micro-tiles with more than three ranges: %d of %d' % (npp, many, mtx * mty))
-
-
-def _node_ranges(r, W, H):
-    """The context's per-micro-tile node ranges (uint32 [micro-tiles, 4])."""
-    return r.read_buffer(oit.OIT_BUF_NODE_RANGES).reshape(-1, 4)[:((W + 7) // 8) * ((H + 3) // 4)]

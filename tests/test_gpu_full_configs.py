@@ -101,7 +101,9 @@ def test_weighted_3840x2160_against_oracle(engine):
     """The WBOIT precision study at full size: FP16 (RGBA16F/R16F emulation)
     and FP32 accumulators against the FP64 oracle, per-pixel relative error of
     the accumulation (where the oracle's magnitude is above 1e-3) and of the
-    revealage. Bounds: about twice the measured maxima."""
+    revealage. Bounds: about twice the measured values (GB300: FP16 accumulation
+    relative max 4.5e-3, mean 4.2e-4, revealage max 8.4e-3, mean 2.2e-4; FP32
+    accumulation max 6.1e-7, revealage max 5.7e-7; images within 1 LSB)."""
     W, H = 3840, 2160
     v, i, tpo = oit.make_scene(16384, seed=2, radius_min=0.01, radius_max=0.05)
     sd = oit.make_camera(W, H)
@@ -121,5 +123,5 @@ def test_weighted_3840x2160_against_oracle(engine):
         print('wboit 3840x2160 %s vs FP64 oracle: accum rel max %.3g mean %.3g, reveal rel max %.3g mean %.3g, '
               'image max %d LSB' % ((name,) + stats[name]))
     h, f = stats['fp16'], stats['fp32']
-    assert f[0] < 2e-6 and f[2] < 2e-6 and f[4] <= 1, f
-    assert h[0] < 1e-2 and h[1] < 1e-3 and h[2] < 5e-3 and h[4] <= 2, h
+    assert f[0] < 1.3e-6 and f[2] < 1.2e-6 and f[4] <= 1, f
+    assert h[0] < 9e-3 and h[1] < 8.5e-4 and h[2] < 1.7e-2 and h[3] < 4.5e-4 and h[4] <= 1, h

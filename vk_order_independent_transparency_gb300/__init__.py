@@ -37,9 +37,12 @@ OIT_ERR_DEVICE = -5
 OIT_ERR_STATE = -6
 OIT_ERR_TOO_LARGE = -7
 
+OIT_DEVERR_BIN_OVERFLOW = 0x1
+OIT_DEVERR_TIMEOUT = 0x2
+
 OIT_BUF_ABUFFER, OIT_BUF_AUX, OIT_BUF_AUXDEPTH, OIT_BUF_COUNTER, OIT_BUF_DEPTH, OIT_BUF_OPAQUE_COLOR, \
     OIT_BUF_COLOR, OIT_BUF_ACCUM, OIT_BUF_REVEAL, OIT_BUF_OUTPUT, OIT_BUF_OUTPUT_LINEAR, \
-    OIT_BUF_MICROTILE_LENGTHS, OIT_BUF_NODE_RANGES = range(13)
+    OIT_BUF_MICROTILE_LENGTHS = range(12)
 
 # The C ABI's exported symbols (include/oit_gb300.h).
 EXPORTS = [
@@ -87,7 +90,7 @@ class OitInstancedMesh(ctypes.Structure):
 class OitResolveShape(ctypes.Structure):
     _fields_ = [('threads_per_block', ctypes.c_uint32), ('blocks', ctypes.c_uint32), ('binned', ctypes.c_int32),
                 ('tile_order', ctypes.c_int32), ('shared_slots', ctypes.c_int32), ('items_per_step', ctypes.c_int32),
-                ('register_slots', ctypes.c_int32), ('dense', ctypes.c_int32), ('node_ranges', ctypes.c_int32)]
+                ('register_slots', ctypes.c_int32), ('dense', ctypes.c_int32)]
 
 
 class OitSceneDesc(ctypes.Structure):
@@ -518,8 +521,7 @@ class Batch:
         for part, name in ((0, 'linkedlist'), (1, 'loop64')):
             sh = OitResolveShape()
             _check(self.lib.oit_batch_resolve_config(self._b, part, ctypes.byref(sh)), 'oit_batch_resolve_config')
-            out[name] = {f: (bool(getattr(sh, f)) if f in ('binned', 'tile_order', 'dense', 'node_ranges')
-                             else getattr(sh, f))
+            out[name] = {f: (bool(getattr(sh, f)) if f in ('binned', 'tile_order', 'dense') else getattr(sh, f))
                          for f, _ in OitResolveShape._fields_}
         return out
 

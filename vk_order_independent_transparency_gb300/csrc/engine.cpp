@@ -108,8 +108,8 @@ struct oit_context {
   DevBuf mesh_v, mesh_i;
   DevBuf scene_dev;  // proj_view then view, read by k_setup
   DevBuf lens;  // per 8x4 micro-tile fragment counts for the batched resolve
-  DevBuf node_ranges;  // linked list: per 8x4 micro-tile, the node ranges its raster warp allocated
   size_t tri_cap = 0, pair_cap = 0;
+  uint32_t bin_tris = 0, bin_opaque_from = 0;  // the last binned draw: triangles, first opaque one
   bool opaque_valid = false;
   bool color_valid = false;
   cudaStream_t last_stream = nullptr;
@@ -183,7 +183,7 @@ struct oit_context {
     DevBuf* all[] = {&depth, &opaque_color, &color, &abuf, &aux, &auxdepth, &counter, &accum, &reveal, &out,
                      &out_linear, &err, &frag, &bbox, &setup, &persp, &pair_count, &pair_offset, &scan_tmp, &total,
                      &keys, &tris, &keys_alt, &tris_alt, &hist, &tile_begin, &tile_end, &mesh_v, &mesh_i,
-                     &scene_dev, &lens, &node_ranges};
+                     &scene_dev, &lens};
     for (DevBuf* b : all) b->release();
   }
 
@@ -251,10 +251,6 @@ struct oit_context {
     if (batch_resolvable()) {
       OIT_TRY_CUDA(lens.ensure(lens_count()), "alloc lens");
       OIT_TRY_CUDA(cudaMemset(lens.p, 0, lens_count()), "memset");
-      if (alg() == oit::Alg::LinkedList) {
-        OIT_TRY_CUDA(node_ranges.ensure(lens_count() * 16), "alloc node ranges");
-        OIT_TRY_CUDA(cudaMemset(node_ranges.p, 0, lens_count() * 16), "memset");
-      }
     }
     return OIT_OK;
   }
@@ -398,6 +394,8 @@ struct oit_context {
     r = ensure_pairs(ps ? ps->known : 0);
     if (r != OIT_OK) return r;
     oit::SetupParams sp = setup_params(mesh, first, count, opaque_from);
+    bin_tris = count;
+    bin_opaque_from = opaque_from;
     oit::Bins b = bins();
     OIT_TRY_CUDA(oit::bin_setup_scan(sp, b, s, &launches), "bin_setup_scan");
     if (!ps) {
@@ -448,6 +446,13 @@ struct oit_context {
     p.tile_begin = tile_begin.as<uint32_t>();
     p.tile_end = tile_end.as<uint32_t>();
     p.tile_offset = tile_offset;
+    p.pair_total = total.as<uint32_t>();
+    p.pair_offset = pair_offset.as<uint32_t>();
+    p.pair_count = pair_count.as<uint32_t>();
+    p.pair_capacity = (uint32_t)std::min<size_t>(pair_cap, 0xFFFFFFFFu);
+    p.num_tris = bin_tris;
+    p.pass_first = tile_offset != 0 ? 0u : bin_opaque_from;
+    p.pass_end = tile_offset != 0 ? bin_opaque_from : bin_tris;
     p.tile_tris = tris.as<uint32_t>();
     p.tile_keys = keys.as<uint32_t>();
     p.bbox = bbox.as<uint2>();
@@ -473,7 +478,6 @@ struct oit_context {
     if (tile_offset != 0 && batch_resolvable()) {
       p.lens = lens.as<uint8_t>();
       p.lens_stride = lens_stride();
-      if (alg() == oit::Alg::LinkedList) p.node_ranges = node_ranges.as<uint4>();
     }
     return p;
   }
@@ -488,7 +492,6 @@ struct oit_context {
     v.out = out_dev ? out_dev : out.as<uint8_t>();
     v.out_linear = nullptr;
     v.lens = lens.as<uint8_t>();
-    v.node_ranges = node_ranges.as<uint4>();
     v.P = P;
     v.capacity = capacity;
     v.W = RW;
@@ -1014,8 +1017,7 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
     if (part == 0)
       variants = {oit::kResolveVariantList, oit::kResolveVariantListShared, oit::kResolveVariantListx2,
                   oit::kResolveVariantListShort4, oit::kResolveVariantListShort8, oit::kResolveVariantListDense,
-                  oit::kResolveVariantListShort8Dense, oit::kResolveVariantListRanges,
-                  oit::kResolveVariantListRangesDense};
+                  oit::kResolveVariantListShort8Dense};
     else variants = {oit::kResolveVariantLoop64, oit::kResolveVariantLoop64x2, oit::kResolveVariantLoop64Dense};
     for (int variant : variants) {
       for (int threads : {64, 128, 256}) {
@@ -1477,9 +1479,6 @@ int oit_batch_set_resolve_config(oit_batch* b, uint32_t part, const oit_resolve_
         (sh.dense != 0 && sh.dense != 1) || (sh.items_per_step != 0 && sh.items_per_step != 1 && sh.items_per_step != 2))
       return OIT_ERR_INVALID_ARGUMENT;
     const bool x2 = sh.items_per_step == 2;
-    if (sh.node_ranges != 0 && sh.node_ranges != 1) return OIT_ERR_INVALID_ARGUMENT;
-    if (sh.node_ranges && (part == 1 || sh.shared_slots != 0 || sh.register_slots != 0 || x2))
-      return OIT_ERR_INVALID_ARGUMENT;
     if (part == 1) {
       if (sh.shared_slots != 0 || sh.register_slots != 0 || (x2 && sh.dense)) return OIT_ERR_INVALID_ARGUMENT;
       pn.variant = x2 ? oit::kResolveVariantLoop64x2
@@ -1490,8 +1489,7 @@ int oit_batch_set_resolve_config(oit_batch* b, uint32_t part, const oit_resolve_
         return OIT_ERR_INVALID_ARGUMENT;
       if ((sh.shared_slots != 0) + (sh.register_slots != 0) + (int)x2 > 1) return OIT_ERR_INVALID_ARGUMENT;
       if (sh.dense && (sh.shared_slots != 0 || sh.register_slots == 4 || x2)) return OIT_ERR_INVALID_ARGUMENT;
-      if (sh.node_ranges) pn.variant = sh.dense ? oit::kResolveVariantListRangesDense : oit::kResolveVariantListRanges;
-      else if (sh.shared_slots) pn.variant = oit::kResolveVariantListShared;
+      if (sh.shared_slots) pn.variant = oit::kResolveVariantListShared;
       else if (x2) pn.variant = oit::kResolveVariantListx2;
       else if (sh.register_slots == 4) pn.variant = oit::kResolveVariantListShort4;
       else if (sh.register_slots == 8)
@@ -1535,11 +1533,9 @@ int oit_batch_resolve_config(oit_batch* b, uint32_t part, oit_resolve_shape* out
                             ? 8
                             : 0;
   out->dense = (rp.variant == oit::kResolveVariantListDense || rp.variant == oit::kResolveVariantListShort8Dense ||
-                rp.variant == oit::kResolveVariantLoop64Dense || rp.variant == oit::kResolveVariantListRangesDense)
+                rp.variant == oit::kResolveVariantLoop64Dense)
                    ? 1
                    : 0;
-  out->node_ranges =
-      (rp.variant == oit::kResolveVariantListRanges || rp.variant == oit::kResolveVariantListRangesDense) ? 1 : 0;
   return OIT_OK;
 }
 
@@ -1574,7 +1570,6 @@ int oit_get_buffer(oit_context* ctx, int which, void** ptr, size_t* bytes) {
     case OIT_BUF_OUTPUT: b = &ctx->out; n = (size_t)ctx->W * ctx->H * 4; break;
     case OIT_BUF_OUTPUT_LINEAR: b = &ctx->out_linear; n = b->p ? (size_t)ctx->W * ctx->H * 16 : 0; break;
     case OIT_BUF_MICROTILE_LENGTHS: b = &ctx->lens; n = b->p ? ctx->lens_count() : 0; break;
-    case OIT_BUF_NODE_RANGES: b = &ctx->node_ranges; n = b->p ? ctx->lens_count() * 16 : 0; break;
     default: return OIT_ERR_INVALID_ARGUMENT;
   }
   *ptr = b->p;

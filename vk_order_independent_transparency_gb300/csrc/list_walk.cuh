@@ -41,13 +41,6 @@ __device__ __forceinline__ WalkNode load_node(const uint4* __restrict__ pool, ui
   return WalkNode{n.x, n.y, n.z, n.w};
 }
 
-// Node loads straight from the pool.
-template <bool F32>
-struct PoolFetch {
-  const uint4* __restrict__ pool;
-  __device__ __forceinline__ WalkNode operator()(uint32_t off) const { return load_node<F32>(pool, off); }
-};
-
 template <bool F32>
 __device__ __forceinline__ float4 node_colour(const uint4* __restrict__ pool, uint32_t c) {
   if (F32) {
@@ -57,6 +50,15 @@ __device__ __forceinline__ float4 node_colour(const uint4* __restrict__ pool, ui
   }
   return decode_premult(c);
 }
+
+// Node loads straight from the pool; colours decoded with the global tables.
+template <bool F32>
+struct PoolFetch {
+  const uint4* __restrict__ pool;
+  __device__ __forceinline__ WalkNode operator()(uint32_t off) const { return load_node<F32>(pool, off); }
+  __device__ __forceinline__ float4 colour(uint32_t c) const { return node_colour<F32>(pool, c); }
+};
+
 
 // Sort arrays in local memory.
 template <bool Mask>
@@ -179,7 +181,7 @@ __device__ __forceinline__ void walk_step(ListWalk& w, A& a, const WalkNode& n, 
     if (Mask) a.M(pos) = n.m;
   }
   // the linked list's tail ignores coverage (oitLinkedList.frag.glsl:137-138)
-  if (tail) blend_under(w.tail, node_colour<F32>(pool, ev));
+  if (tail) blend_under(w.tail, fetch.colour(ev));
   w.off = next;
 }
 
@@ -202,14 +204,14 @@ __device__ __forceinline__ float4 walk_list_with(const Fetch& fetch, const uint4
   float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
   if (!Mask) {
 #pragma unroll 1
-    for (int i = 0; i < w.k; ++i) blend_under(sum, node_colour<F32>(pool, a.C(i)));
+    for (int i = 0; i < w.k; ++i) blend_under(sum, fetch.colour(a.C(i)));
   } else {
 #pragma unroll 1
     for (int s = 0; s < S; ++s) {
       float4 sc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
       for (int i = 0; i < w.k; ++i)
-        if ((a.M(i) >> s) & 1u) blend_under(sc, node_colour<F32>(pool, a.C(i)));
+        if ((a.M(i) >> s) & 1u) blend_under(sc, fetch.colour(a.C(i)));
       sum.x += sc.x;
       sum.y += sc.y;
       sum.z += sc.z;

@@ -230,6 +230,11 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   p.tile_end = b.tile_end;
   p.tile_tris = b.tris;
   p.tile_keys = b.keys;
+  p.pair_total = b.total;
+  p.pair_offset = pair_offset;
+  p.pair_count = pair_count;
+  p.pair_capacity = (uint32_t)b.capacity;
+  p.num_tris = N;
   p.bbox = bbox;
   p.setup = setup;
   p.persp = persp;
@@ -252,9 +257,13 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   p.frag_count = reinterpret_cast<unsigned long long*>(words + 4);
   if (opaque) {
     p.tile_offset = 0;
+    p.pass_first = nt;
+    p.pass_end = N;
     NOALLOC_TRY(launch_raster_a(Alg::Opaque, p, s));
   }
   p.tile_offset = num_tiles;
+  p.pass_first = 0;
+  p.pass_end = nt;
   switch (alg) {
     case Alg::Simple: case Alg::LinkedList: NOALLOC_TRY(launch_raster_a(alg, p, s)); break;
     case Alg::Loop: case Alg::Loop64: NOALLOC_TRY(launch_raster_b(alg, p, s)); break;

@@ -103,6 +103,17 @@ struct RasterParams {
   const uint2* bbox;
   const void* setup;
   const void* persp;
+  // Bin overflow: when the draw's (tile, triangle) pairs exceed the bin
+  // capacity, the pairs of the first triangles (triangle order) fill the bins
+  // and the rest are dropped; the raster then walks its tile list for the
+  // triangles that were binned whole and tests every later triangle of the
+  // pass's range [pass_first, pass_end) by bbox. Null pair_total: no check.
+  const uint32_t* pair_total;    // [1] the draw's pair count (device)
+  const uint32_t* pair_offset;   // [num_tris] exclusive scan of pair_count
+  const uint32_t* pair_count;    // [num_tris]
+  uint32_t pair_capacity;
+  uint32_t num_tris;             // triangles of the draw (bin-relative ids 0 .. num_tris - 1)
+  uint32_t pass_first, pass_end; // this pass's triangles: transparent [0, opaque_from), opaque the rest
   // frame targets
   uint32_t* depth;               // [S][P] opaque depth (read by transparent passes)
   float4* opaque_color;          // [S][P]
@@ -127,12 +138,6 @@ struct RasterParams {
   // work binning; null = not wanted (1x only)
   uint8_t* lens;
   int lens_stride;               // micro-tiles per row, (RW + 7) / 8
-  // linked list, per 8x4 micro-tile (indexed as lens): the node ranges the
-  // micro-tile's warp allocated, {first0, first1, first2, count0 | count1 << 8 |
-  // count2 << 16 | ranges << 24} (ranges = all ranges it allocated, capped at
-  // 255; only the first three are listed; counts exclude nodes beyond the
-  // pool); null = not wanted
-  uint4* node_ranges;
 };
 
 struct CompositeParams {
@@ -170,7 +175,6 @@ struct ResolveView {
   uint8_t* out;                  // [P] RGBA8
   float4* out_linear;            // optional [P]
   const uint8_t* lens;           // [mty][mtx] per 8x4 micro-tile fragment counts
-  const uint4* node_ranges;      // [mty][mtx] linked list: the micro-tile's node ranges (RasterParams)
   uint32_t P, capacity;
   int W, H, L, kind, tail, mtx, mty;
   int color_half;
@@ -225,8 +229,6 @@ enum ResolveVariant : int {
   kResolveVariantListDense = 7,   // local arrays, at most 32 registers (eight 256-thread blocks per SM)
   kResolveVariantListShort8Dense = 8,  // Short8 at most 32 registers
   kResolveVariantLoop64Dense = 9,      // Loop64 at most 32 registers
-  kResolveVariantListRanges = 10,      // the micro-tile's node ranges staged in shared memory, <= 40 registers
-  kResolveVariantListRangesDense = 11, // the same at most 32 registers
 };
 cudaError_t resolve_bin(const ResolveBatch& b, cudaStream_t s, uint64_t* launches);
 cudaError_t resolve_run(const ResolveBatch& b, int variant, int threads, int blocks, cudaStream_t s);

@@ -499,33 +499,35 @@ constexpr int kStageSlots = 32;
 // Mask (8x4 micro-tiles, one lane per pixel): the test is the micro-tile's bit
 // in the pair's sorted key (the binning wrote the bbox's micro-tile overlap
 // there), so only hits gather their bbox; else the bbox itself is tested.
+// List entries of triangles >= limit are skipped. With `ident` (an overflowed
+// draw's unbinned triangles) [beg, end) are triangle ids, each tested by bbox.
 template <bool Mask, class Chunk>
 __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile& w, TriSetup* stage,
                                           uint32_t* stage_t, uint2* stage_bb, uint32_t beg, uint32_t end,
-                                          Chunk&& chunk) {
+                                          bool ident, uint32_t limit, Chunk&& chunk) {
   const TriSetup* __restrict__ setup = reinterpret_cast<const TriSetup*>(p.setup);
   const uint32_t lt = (1u << w.lane) - 1u;
   const uint32_t mbit = 1u << (oit::kMaskShift + (Mask ? w.mt : 0));
+  const bool use_mask = Mask && !ident;
   uint32_t t_next = 0;
   bool h_next = false;
   uint2 bb_next = make_uint2(0xFFFFFFFFu, 0u);  // empty bbox
+  auto fetch = [&](uint32_t i) {
+    t_next = ident ? i : __ldg(&p.tile_tris[i]);
+    if (use_mask) h_next = (__ldg(&p.tile_keys[i]) & mbit) != 0u && t_next < limit;
+  };
   if (beg + w.lane < end) {
-    t_next = __ldg(&p.tile_tris[beg + w.lane]);
-    if (Mask) h_next = (__ldg(&p.tile_keys[beg + w.lane]) & mbit) != 0u;
-    if (!Mask || h_next) bb_next = __ldg(&p.bbox[t_next]);
+    fetch(beg + w.lane);
+    if (!use_mask || h_next) bb_next = __ldg(&p.bbox[t_next]);
   }
   for (uint32_t base = beg; base < end; base += 32) {
     const uint32_t t = t_next;
     const uint2 bb = bb_next;
-    const bool hit = (base + w.lane < end) && (Mask ? h_next : bbox_hits(bb, w));
+    const bool hit = (base + w.lane < end) && (use_mask ? h_next : (bbox_hits(bb, w) && t < limit));
     const uint32_t nb = base + 32;
     const bool more = nb + w.lane < end;
-    if (more) {
-      t_next = __ldg(&p.tile_tris[nb + w.lane]);
-      if (Mask) h_next = (__ldg(&p.tile_keys[nb + w.lane]) & mbit) != 0u;
-    } else {
-      h_next = false;
-    }
+    if (more) fetch(nb + w.lane);
+    else h_next = false;
     const uint32_t m = __ballot_sync(kFull, hit);
     const int rank = __popc(m & lt);
     auto stage_hit = [&](int slot) {
@@ -537,11 +539,42 @@ __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile&
       stage_bb[slot] = bb;
     };
     if (hit) stage_hit(rank);
-    bb_next = more && (!Mask || h_next) ? __ldg(&p.bbox[t_next]) : make_uint2(0xFFFFFFFFu, 0u);
+    bb_next = more && (!use_mask || h_next) ? __ldg(&p.bbox[t_next]) : make_uint2(0xFFFFFFFFu, 0u);
     cp_async_wait_all();
     __syncwarp();
     if (m) chunk(__popc(m));
     __syncwarp();
+  }
+}
+
+// Triangles of the draw binned whole: all of them, or after a bin overflow
+// those before the first triangle whose pairs reach past the capacity (pairs
+// are emitted in triangle order). Warp-uniform.
+__device__ __forceinline__ uint32_t binned_triangles(const RasterParams& p) {
+  if (!p.pair_total || *p.pair_total <= p.pair_capacity) return 0xFFFFFFFFu;
+  uint32_t lo = 0, hi = p.num_tris;  // first t with pair_offset[t] + pair_count[t] > capacity
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&p.pair_offset[mid]) + __ldg(&p.pair_count[mid]) > p.pair_capacity) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
+
+// The pass's walk: the tile list (triangles binned whole), then, after a bin
+// overflow, the unbinned triangles of the pass by bbox; primitive order is
+// kept because every binned triangle precedes every unbinned one.
+template <bool Mask, class Chunk>
+__device__ __forceinline__ void walk_pass(const RasterParams& p, const WarpTile& w, TriSetup* stage,
+                                          uint32_t* stage_t, uint2* stage_bb, uint32_t beg, uint32_t end,
+                                          Chunk&& chunk) {
+  const uint32_t cut = binned_triangles(p);
+  const bool rest = cut < p.pass_end;
+  const uint32_t nph = rest ? 2u : 1u;
+#pragma unroll 1
+  for (uint32_t ph = 0; ph < nph; ++ph) {
+    const bool ident = ph == 1;
+    walk_tile<Mask>(p, w, stage, stage_t, stage_bb, ident ? max(cut, p.pass_first) : beg, ident ? p.pass_end : end,
+                    ident, ident ? 0xFFFFFFFFu : cut, chunk);
   }
 }
 
@@ -554,10 +587,11 @@ __device__ __forceinline__ bool lane_in_bbox(uint2 bb, const WarpTile& w) {
 // depth) in primitive-then-lane order; shading runs one queued fragment per
 // lane once a staged chunk is covered (the setup records it reads are then
 // replaced); when the queue is full, and at the end, each lane feeds its own
-// pixel's fragments, in queue order, to the algorithm. Feeding a full queue
-// rather than each chunk's fragments gives the linked list node ranges of up
-// to kQueue nodes per allocation. vz holds the view-space z (WBOIT, which
-// feeds per chunk) or, for every other algorithm, the fragment's alpha.
+// pixel's fragments, in queue order, to the algorithm (feeding a full queue
+// rather than each chunk's fragments: fewer passes over the owner bytes and
+// linked-list node allocations of up to kQueue nodes). vz holds the
+// view-space z (WBOIT, which feeds per chunk) or, for every other algorithm,
+// the fragment's alpha.
 constexpr int kQueue = 64;
 struct FragQueue {
   uint32_t depth[kQueue];
@@ -572,8 +606,6 @@ struct HitRanges {
   // of bbox ∩ micro-tile relative to the micro-tile (bits 11-13, 14-15), its
   // width (bits 16-19) and ceil(256 / width) (bits 20-28)
   uint32_t packed[32];
-  // linked list: the node ranges the warp allocated (RasterParams::node_ranges)
-  uint32_t ranges[4];
 };
 constexpr size_t kWarpStageBytes = kStageSlots * (sizeof(TriSetup) + sizeof(uint32_t) + sizeof(uint2)) +
                                    sizeof(FragQueue) + sizeof(HitRanges);
@@ -637,10 +669,6 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
   uint32_t mine = 0;   // fragments delivered to this lane's pixel
   int qn = 0;          // warp-uniform: queued fragments
   int qs = 0;          // warp-uniform: queued fragments already shaded
-  if (Pol::kNodes && w.lane == 0) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) hr->ranges[k] = 0u;
-  }
   const uint32_t lane_bytes = (uint32_t)w.lane * 0x01010101u;
 
   for (int pass = 0; pass < Pol::kPasses; ++pass) {
@@ -681,19 +709,7 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
       shade_pending();
       uint32_t node0 = 0;
       if (Pol::kNodes && shading) {
-        if (w.lane == 0) {
-          node0 = atomicAdd(p.counter, (uint32_t)qn);
-          // this allocation's nodes node0 + 1 .. node0 + qn, those in the pool
-          const uint32_t first = node0 + 1u;
-          const uint32_t last = min(node0 + (uint32_t)qn, p.capacity > 0 ? p.capacity - 1u : 0u);
-          const uint32_t cnt = (first <= last && first < p.capacity) ? last - first + 1u : 0u;
-          const uint32_t k = hr->ranges[3] >> 24;
-          if (cnt > 0 && k < 3u) {
-            hr->ranges[k] = first;
-            hr->ranges[3] |= cnt << (8 * k);
-          }
-          if (cnt > 0 && k < 255u) hr->ranges[3] += 1u << 24;
-        }
+        if (w.lane == 0) node0 = atomicAdd(p.counter, (uint32_t)qn);
         node0 = __shfl_sync(kFull, node0, 0);
       }
       // this lane's entries: scan the owner byte of every queued fragment
@@ -865,7 +881,7 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
       __syncwarp();
     };
 
-    walk_tile<SSN == 1>(p, w, stage, stage_t, stage_bb, beg, end, [&](int nh) {
+    walk_pass<SSN == 1>(p, w, stage, stage_t, stage_bb, beg, end, [&](int nh) {
       if (SSN == 1) {
         cover_pairs(nh);
       } else {
@@ -895,12 +911,8 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
   if (SSN == 1 && p.lens) {
     const uint32_t mx = __reduce_max_sync(kFull, w.valid ? mine : 0u);
     // micro-tiles of edge tiles may lie wholly outside the image
-    if (w.lane == 0 && w.rx0 < p.RW && w.ry0 < p.RH) {
-      const size_t mt = (size_t)(w.ry0 >> 2) * p.lens_stride + (w.rx0 >> 3);
-      p.lens[mt] = (uint8_t)min(mx, 255u);
-      if (Pol::kNodes && p.node_ranges)
-        p.node_ranges[mt] = make_uint4(hr->ranges[0], hr->ranges[1], hr->ranges[2], hr->ranges[3]);
-    }
+    if (w.lane == 0 && w.rx0 < p.RW && w.ry0 < p.RH)
+      p.lens[(size_t)(w.ry0 >> 2) * p.lens_stride + (w.rx0 >> 3)] = (uint8_t)min(mx, 255u);
   }
 }
 
@@ -924,7 +936,8 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock) k_raster_opaque(Ras
     col[s] = w.valid ? p.opaque_color[(size_t)s * p.P + w.pixel] : p.background;
   }
   const int tile = (int)((blockIdx.x * kRasterWarpsPerBlock + warp) / oit::kWarpsPerTile) + p.tile_offset;
-  walk_tile<true>(p, w, stage, stage_t_all + warp * kStageSlots, stage_bb, p.tile_begin[tile], p.tile_end[tile], [&](int nh) {
+  walk_pass<true>(p, w, stage, stage_t_all + warp * kStageSlots, stage_bb, p.tile_begin[tile], p.tile_end[tile],
+                  [&](int nh) {
     for (int k = 0; k < nh; ++k) {
       if (!lane_in_bbox(stage_bb[k], w)) continue;  // no warp-collective operation follows
       const TriSetup& T = stage[k];

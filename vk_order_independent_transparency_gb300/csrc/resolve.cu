@@ -134,7 +134,8 @@ __global__ void __launch_bounds__(kBinThreads) k_rbin_scatter(ResolveBatch b) {
 // sectors).
 constexpr int kLoop64Batch = 4;
 
-__device__ __forceinline__ float4 resolve_loop64(const ResolveView& v, uint32_t pixel, uint2 key0, int nmax) {
+__device__ __forceinline__ float4 resolve_loop64(const ResolveView& v, uint32_t pixel,
+                                                 uint2 key0, int nmax) {
   const uint2* __restrict__ ab = reinterpret_cast<const uint2*>(v.abuf) + pixel;
   float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
   if (key0.y == kEmptyKey) return sum;
@@ -161,7 +162,6 @@ __device__ __forceinline__ float4 resolve_loop64(const ResolveView& v, uint32_t 
 struct ItemPixel {
   const ResolveView* v;
   uint32_t tile, pixel;
-  bool in_view;  // the work item is one of the view's micro-tiles (warp-uniform)
 };
 
 __device__ __forceinline__ bool item_pixel(const ResolveBatch& b, const uint32_t* tb, uint32_t it, int lane, int& vi,
@@ -176,45 +176,13 @@ __device__ __forceinline__ bool item_pixel(const ResolveBatch& b, const uint32_t
   const ResolveView& v = b.views[vi];
   o.v = &v;
   uint32_t mx, my;
-  o.in_view = item_microtile(v, g - tb[vi], b.order, mx, my);
-  if (!o.in_view) return false;
+  if (!item_microtile(v, g - tb[vi], b.order, mx, my)) return false;
   o.tile = my * (uint32_t)v.mtx + mx;  // the micro-tile's index in the view's lengths
   const int x = (int)mx * 8 + (lane & 7), y = (int)my * 4 + (lane >> 3);
   if (x >= v.W || y >= v.H) return false;
   o.pixel = (uint32_t)y * (uint32_t)v.W + (uint32_t)x;
   return true;
 }
-
-// Linked-list nodes staged in shared memory: the node ranges the raster
-// allocated for the micro-tile (RasterParams::node_ranges, at most three of up
-// to kQueue = 64 nodes each) are copied with coalesced 16-byte loads, and
-// every node's `next` (and every lane's head) is rewritten at that point as
-// 1 + its slot in the stage, so each lane then walks its list in shared
-// memory. Every node of a micro-tile's lists lies in the ranges its warp
-// allocated (nodes beyond the pool are never linked); micro-tiles that
-// allocated more than three ranges walk the pool instead.
-constexpr int kRangeSlots = 192;
-
-struct StagedRanges {
-  uint32_t f0, f1, f2;  // first node of each range
-  uint32_t c0, c1, c2;  // nodes in each range
-  // slot + 1 of node x of one of the ranges, 0 for the list end
-  __device__ __forceinline__ uint32_t slot(uint32_t x) const {
-    uint32_t d;
-    if ((d = x - f0) < c0) return 1u + d;
-    if ((d = x - f1) < c1) return 1u + c0 + d;
-    if ((d = x - f2) < c2) return 1u + c0 + c1 + d;
-    return 0u;
-  }
-};
-
-struct StageFetch {
-  const uint4* stage;  // slot s at stage[s - 1]
-  __device__ __forceinline__ WalkNode operator()(uint32_t off) const {
-    const uint4 v = stage[off - 1u];
-    return WalkNode{v.x, v.y, v.z, v.w};
-  }
-};
 
 // Persistent: every warp resolves micro-tiles (one lane per pixel) from the
 // work list in static cyclic order. One kernel per view kind, so each gets the
@@ -225,9 +193,8 @@ constexpr int kSplitSlots = 8;
 
 // U micro-tiles per step: the independent first loads of all U (colour
 // target, list head) are issued before any list is walked.
-template <bool Split, int U, int Short = 0, int MinBlocks = 1, bool Ranges = false>
+template <bool Split, int U, int Short = 0, int MinBlocks = 1>
 __global__ void __launch_bounds__(256, MinBlocks) k_resolve_list(ResolveBatch b) {
-  static_assert(!Ranges || (!Split && U == 1 && Short == 0), "staged node ranges: one micro-tile per step");
   extern __shared__ __align__(16) uint32_t rsm[];
   load_bases(b, rsm);
   const int lane = threadIdx.x & 31;
@@ -245,8 +212,6 @@ __global__ void __launch_bounds__(256, MinBlocks) k_resolve_list(ResolveBatch b)
   constexpr int kStage = Short > 0 ? Short : 1;
   uint32_t* stc = col + (threadIdx.x >> 5) * (2 * kStage * 32) + lane;
   uint32_t* std_ = stc + kStage * 32;
-  // Ranges: the warp's staged nodes (col is 16-byte aligned)
-  uint4* rstage = reinterpret_cast<uint4*>(col) + (threadIdx.x >> 5) * kRangeSlots;
   int vi = 0;
   for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < b.total_tiles; it += U * warps) {
     ItemPixel ip[U];
@@ -256,34 +221,11 @@ __global__ void __launch_bounds__(256, MinBlocks) k_resolve_list(ResolveBatch b)
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const uint32_t iu = it + u * warps;
-      ip[u].in_view = false;
       ok[u] = iu < b.total_tiles && item_pixel(b, rsm, iu, lane, vi, ip[u]);
       if (ok[u]) {
         c[u] = load_color(ip[u].v->color, ip[u].v->color_half != 0, ip[u].pixel);
         head[u] = __ldg(ip[u].v->aux + ip[u].pixel);
       }
-    }
-    bool staged = false;  // warp-uniform
-    if constexpr (Ranges) {
-      if (ip[0].in_view) {  // warp-uniform: the whole warp stages the micro-tile's nodes
-        const ResolveView& v = *ip[0].v;
-        const uint4 rg = __ldg(v.node_ranges + ip[0].tile);
-        staged = (rg.w >> 24) <= 3u;
-        if (staged) {
-          const uint4* pool = reinterpret_cast<const uint4*>(v.abuf);
-          const StagedRanges sr{rg.x, rg.y, rg.z, rg.w & 255u, (rg.w >> 8) & 255u, (rg.w >> 16) & 255u};
-          const uint32_t total = sr.c0 + sr.c1 + sr.c2;  // <= 3 * 64 = kRangeSlots
-          for (uint32_t k = lane; k < total; k += 32) {
-            const uint32_t node =
-                k < sr.c0 ? sr.f0 + k : (k < sr.c0 + sr.c1 ? sr.f1 + (k - sr.c0) : sr.f2 + (k - sr.c0 - sr.c1));
-            uint4 nd = __ldg(pool + node);
-            nd.w = sr.slot(nd.w);
-            rstage[k] = nd;
-          }
-          if (ok[0]) head[0] = sr.slot(head[0]);
-        }
-      }
-      __syncwarp();
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
@@ -303,16 +245,10 @@ __global__ void __launch_bounds__(256, MinBlocks) k_resolve_list(ResolveBatch b)
         else if (Short > 4 && len <= min(Short, v.L))
           done = walk_list_staged<Short>(pool, head[u], v.capacity, stc, std_, sum);
       }
-      if (!done) {
-        if (Ranges && staged)
-          sum = walk_list_with<false>(StageFetch{rstage}, pool, head[u], kRangeSlots + 1, v.L, v.tail, 1, a);
-        else
-          sum = walk_list<false>(pool, head[u], v.capacity, v.L, v.tail, 1, a);
-      }
+      if (!done) sum = walk_list<false>(pool, head[u], v.capacity, v.L, v.tail, 1, a);
       rop_over(c[u], sum);
       write_rgba8(v.out, v.out_linear, ip[u].pixel, c[u]);
     }
-    if constexpr (Ranges) __syncwarp();  // the next micro-tile's staging overwrites rstage
   }
 }
 
@@ -353,8 +289,6 @@ __global__ void __launch_bounds__(256, MinBlocks) k_resolve_loop64(ResolveBatch 
 
 size_t resolve_smem(const ResolveBatch& b, int variant, int threads) {
   const size_t bases = (size_t)((b.num_views + 3) & ~3) * 4;
-  if (variant == kResolveVariantListRanges || variant == kResolveVariantListRangesDense)
-    return bases + (size_t)(threads / 32) * kRangeSlots * 16;
   const int slots = variant == kResolveVariantListShared || variant == kResolveVariantListShort8 ||
                             variant == kResolveVariantListShort8Dense
                         ? 8
@@ -376,8 +310,6 @@ cudaError_t with_kernel(int variant, F f) {
     case kResolveVariantListDense: return f(k_resolve_list<false, 1, 0, 8>);
     case kResolveVariantListShort8Dense: return f(k_resolve_list<false, 1, 8, 8>);
     case kResolveVariantLoop64Dense: return f(k_resolve_loop64<1, 8>);
-    case kResolveVariantListRanges: return f(k_resolve_list<false, 1, 0, 6, true>);
-    case kResolveVariantListRangesDense: return f(k_resolve_list<false, 1, 0, 8, true>);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -195,6 +195,10 @@ __global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
     p.bbox[t] = make_uint2((uint32_t)bx0 | ((uint32_t)by0 << 16), (uint32_t)bx1 | ((uint32_t)by1 << 16));
     const int tx0 = bx0 / kTile, tx1 = bx1 / kTile, ty0 = by0 / kTile, ty1 = by1 / kTile;
     pairs = (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
+  } else {
+    // an empty bbox (x0 > x1): the unbinned walk of an overflowed frame
+    // tests every triangle's bbox
+    p.bbox[t] = make_uint2(0xFFFFFFFFu, 0u);
   }
   p.pair_count[t] = pairs;
 }
