@@ -749,6 +749,7 @@ def run_batch(a, rank):
     t_res_plain = timed(step_resolve_plain)
     torch.cuda.nvtx.range_pop()
     res_cfg = batch.resolve_config()
+    raster_mode = batch.raster_mode()
     res_bytes = resolve_bytes(vs, mixed)
     batch.render(stream)
     images = [r.output() for r in mixed]
@@ -758,7 +759,7 @@ def run_batch(a, rank):
                 e2e_s=e2e_s, h2d=h2d, d2h=d2h, views=vs, t_res_mixed=t_res_mixed, t_res_plain=t_res_plain,
                 res_cfg=res_cfg, res_bytes=res_bytes, e2e_flat_s=e2e_flat_s, h2d_flat=h2d_flat, e2e_same=e2e_same,
                 raster_bytes=raster_bytes, raster_intermediate=raster_intermediate, images=images,
-                fp64_images=fp64_images)
+                fp64_images=fp64_images, raster_mode=raster_mode)
 
 
 def _copy_d2h(host_tensor, dev_ptr, nbytes, stream):
@@ -822,7 +823,7 @@ def main_batch(a, rank, world):
         'data': 'synthetic: 64 seeded UV-sphere scenes, inputs resident in HBM',
         'config': dict(workload_dict(BATCH_WORKLOAD), views=len(res['views']), fragments_per_batch=res['frags'],
                        parallelism='replicas' if world > 1 else 'single',
-                       frame='all 64 views in one CUDA graph, 8 parallel streams',
+                       frame='all 64 views in one CUDA graph (binning on 8 parallel streams)',
                        l2='working set larger than L2, no flush'),
         'plain_fp32': {'value': round(plain, 3), 'unit': 'Mfragments/s', 'ms_per_step': round(t_plain / a.steps, 4),
                        'path': 'one oit_render_frame per view, RGBA32F records, no graph'},
@@ -840,6 +841,8 @@ def main_batch(a, rank, world):
         'roofline': resolve['roofline'],
         'raster_roofline': raster_roofline(res, sec, peak, peak_kind),
         'kernels': {k: {'ms_sum_over_views': round(v, 4)} for k, v in sec.items()},
+        'autotuned_raster': {'mode': 'multi-view launches' if res['raster_mode'] == 1 else 'one launch per view',
+                             'picked_by': 'oit_batch_render timing both graphs on the batch\'s frames'},
         'resolve': resolve,
         'cpu_baseline': cpu_line,
         'cpu_baseline_fp32_omp': cpu_omp_line,

@@ -318,6 +318,18 @@ int oit_batch_launch_count(oit_batch* batch, uint64_t* launches);
  * oit_batch_resolve_config) and keeps the fastest. */
 int oit_batch_resolve(oit_batch* batch, const oit_view_frame* views, uint32_t num_views, void* stream);
 
+/* Tile rasters of a batch's graph: 0 one raster launch per view and pass
+ * (views on the forked streams), 1 multi-view launches (after every view's
+ * binning, one launch per pass, algorithm and sample layout runs the CTAs of
+ * all its views, largest views first), -1 (default) the autotuner captures
+ * both when the graph is built, times them on the batch's own frames and
+ * keeps the faster. Setting it makes the next oit_batch_render capture again. */
+int oit_batch_set_raster_mode(oit_batch* batch, int32_t mode);
+
+/* The raster mode of the batch's current graph (0 or 1); OIT_ERR_STATE before
+ * the first capture. */
+int oit_batch_raster_mode(oit_batch* batch, int32_t* mode);
+
 /* The shape the autotuner picked for one part of the batched resolve. */
 typedef struct oit_resolve_shape {
   uint32_t threads_per_block;

@@ -49,9 +49,11 @@ def _views(specs, seed0, dup=False):
     return views, refs, scenes
 
 
-def test_batch_render_and_resolve_match_single_frames():
+@pytest.mark.parametrize('raster_mode', [0, 1])
+def test_batch_render_and_resolve_match_single_frames(raster_mode):
     views, refs, _ = _views(SPECS, 300)
     batch = oit.Batch(parallel_streams=4)
+    batch.set_raster_mode(raster_mode)
     batch.set_views(views)
     for _ in range(3):  # plain frames + autotune + capture, then replays
         batch.render()

@@ -64,7 +64,8 @@ def test_grown_scene_is_complete_on_the_first_replay(engine, alg):
         same(alg, got, ref_big, L)
 
 
-def test_grown_scene_in_a_batch(engine):
+@pytest.mark.parametrize('raster_mode', [0, 1])
+def test_grown_scene_in_a_batch(engine, raster_mode):
     import torch
     (vs, i, tpo), (vb, _, _) = scenes(engine)
     specs = [(1, 8), (3, 16), (0, 4)]
@@ -76,6 +77,7 @@ def test_grown_scene_in_a_batch(engine):
         r.update_scene(sd)
         views.append((r, engine.DeviceMesh(vs, i), tpo, 100))
     batch = engine.Batch(parallel_streams=2)
+    batch.set_raster_mode(raster_mode)
     batch.set_views(views)
     for _ in range(2):
         batch.render()

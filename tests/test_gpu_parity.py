@@ -228,9 +228,11 @@ def test_cuda_graph_replay(engine, alg):
     assert r.get_error() == 0
 
 
-def test_batched_views_match_single_frames(engine):
+@pytest.mark.parametrize('raster_mode', [0, 1, -1])
+def test_batched_views_match_single_frames(engine, raster_mode):
     """oit_batch_render (one CUDA graph, views on forked streams) gives every
-    view the image its own oit_render_frame gives."""
+    view the image its own oit_render_frame gives, with one raster launch per
+    view and pass (0), multi-view raster launches (1) or the autotuner's pick."""
     specs = [(1, 96, 80, 4, 12), (3, 160, 120, 16, 40), (1, 64, 64, 8, 8), (3, 128, 128, 32, 30),
              (0, 80, 60, 8, 20), (6, 96, 96, 8, 24)]
     views, refs, keep = [], [], []
@@ -242,13 +244,15 @@ def test_batched_views_match_single_frames(engine):
         mesh = engine.DeviceMesh(v, i)
         views.append((r, mesh, tpo, 80))
     batch = engine.Batch(parallel_streams=4)
+    batch.set_raster_mode(raster_mode)
     batch.set_views(views)
     for _ in range(3):
         batch.render()
         for (r, _, _, _), ref in zip(views, refs):
             np.testing.assert_array_equal(r.output(), ref)
             assert r.get_error() == 0
-    assert batch.launch_count() >= len(specs) * 10
+    assert batch.raster_mode() in ((0, 1) if raster_mode < 0 else (raster_mode,))
+    assert batch.launch_count() >= len(specs) * 6
 
 
 @pytest.mark.parametrize('aa', [0, 1, 5])

@@ -89,7 +89,8 @@ def test_queued_frames_keep_their_camera(engine):
             np.testing.assert_array_equal(dst.cpu().numpy(), ref)
 
 
-def test_batch_replay_follows_camera(engine):
+@pytest.mark.parametrize('raster_mode', [0, 1])
+def test_batch_replay_follows_camera(engine, raster_mode):
     specs = [(1, 96, 80, 4, 12), (3, 160, 120, 16, 40), (5, 128, 96, 8, 30), (6, 96, 96, 8, 24)]
     views, rigs = [], []
     for k, (alg, w, h, L, n) in enumerate(specs):
@@ -102,6 +103,7 @@ def test_batch_replay_follows_camera(engine):
         views.append((r, mesh, tpo, 80))
         rigs.append((alg, w, h, L, v, i, tpo, ca, cb))
     batch = engine.Batch(parallel_streams=4)
+    batch.set_raster_mode(raster_mode)
     batch.set_views(views)
     for _ in range(2):  # plain frames + capture, then a replay
         batch.render()

@@ -55,7 +55,7 @@ EXPORTS = [
     'oit_batch_create', 'oit_batch_destroy', 'oit_batch_render', 'oit_batch_launch_count',
     'oit_render_frame_instanced', 'oit_render_frame_instanced_host', 'oit_scene_generate_instanced',
     'oit_batch_resolve', 'oit_batch_resolve_config', 'oit_batch_set_resolve_config', 'oit_debug_fail_allocations',
-    'oit_verify_composite_fp64',
+    'oit_verify_composite_fp64', 'oit_batch_set_raster_mode', 'oit_batch_raster_mode',
 ]
 PROF_SECTIONS = ['opaque_bin', 'opaque_raster', 'transparent_bin', 'transparent_raster', 'composite']
 
@@ -168,6 +168,8 @@ def library():
         'oit_batch_set_resolve_config': (I, [P, U, ctypes.POINTER(OitResolveShape)]),
         'oit_debug_fail_allocations': (I, [ctypes.c_int32]),
         'oit_verify_composite_fp64': (I, [P, P, P, P]),
+        'oit_batch_set_raster_mode': (I, [P, ctypes.c_int32]),
+        'oit_batch_raster_mode': (I, [P, ctypes.POINTER(ctypes.c_int32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -513,6 +515,17 @@ class Batch:
         """COMPOSITE of every view's current frame: one persistent launch for the
         linked-list and Loop64 views, a composite launch per other view."""
         _check(self.lib.oit_batch_resolve(self._b, self._frames, len(self._frames), stream), 'oit_batch_resolve')
+
+    def set_raster_mode(self, mode):
+        """Tile rasters of the batch graph: 0 one launch per view and pass, 1
+        multi-view launches, -1 autotuned (default)."""
+        _check(self.lib.oit_batch_set_raster_mode(self._b, int(mode)), 'oit_batch_set_raster_mode')
+
+    def raster_mode(self):
+        """The raster mode of the current graph (0 per view, 1 multi-view)."""
+        m = ctypes.c_int32()
+        _check(self.lib.oit_batch_raster_mode(self._b, ctypes.byref(m)), 'oit_batch_raster_mode')
+        return m.value
 
     def resolve_config(self):
         """{'linkedlist': {...}, 'loop64': {...}}: per part of the batched

@@ -12,11 +12,18 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <vector>
 
 #include "../../include/oit_gb300.h"
 #include "oit_internal.h"
+
+// defined with the C entry points below
+extern "C" {
+static oit::MeshRef view_mesh(const oit_view_frame& v);
+static uint32_t view_tpo(const oit_view_frame& v);
+}
 
 namespace {
 
@@ -564,10 +571,15 @@ struct oit_context {
     return OIT_OK;
   }
 
-  int raster_opaque(cudaStream_t s) {
+  oit::RasterParams opaque_pass_params() {
     oit::RasterParams p = raster_params(0);
     p.S = S;    // the opaque pass always tests every sample of a pixel
     p.ssn = 1;
+    return p;
+  }
+
+  int raster_opaque(cudaStream_t s) {
+    oit::RasterParams p = opaque_pass_params();
     cudaEvent_t t1 = prof_begin(s);
     const int r = raster(oit::Alg::Opaque, p, s);
     prof_end(OIT_PROF_OPAQUE_RASTER, t1, s);
@@ -649,8 +661,11 @@ struct oit_context {
   // Sample::onRender, oitRender.cpp:43-153. The transparent objects are the
   // first percent_transparent% of the mesh and the opaque ones the rest, so one
   // binning pass serves both the opaque and the transparent raster.
+  // raster = false (a batch whose rasters run as multi-view launches): the
+  // frame stops after binning; frame_has_opaque tells whether it has an opaque pass.
+  bool frame_has_opaque = false;
   int render_frame_body(const oit::MeshRef& mesh, uint32_t tpo, int32_t percent, uint8_t* out_dev, cudaStream_t s,
-                        bool resolve = true) {
+                        bool resolve = true, bool raster = true) {
     const uint32_t num_objects = mesh.num_triangles / tpo;
     uint32_t num_transparent = (uint32_t)(((uint64_t)num_objects * (uint32_t)percent) / 100u);
     if (num_transparent > num_objects) num_transparent = num_objects;
@@ -664,6 +679,11 @@ struct oit_context {
     r = bin(mesh, 0, total_tris, nt, s);
     if (r != OIT_OK) return r;
     prof_end(OIT_PROF_TRANSPARENT_BIN, t0, s);
+    frame_has_opaque = num_opaque > 0;
+    if (!raster) {
+      color_valid = true;  // the batch's multi-view rasters follow in the same graph
+      return OIT_OK;
+    }
     if (num_opaque > 0) r = raster_opaque(s);
     if (r == OIT_OK) r = raster_transparent(s);
     if (r == OIT_OK && resolve) r = composite(out_dev, s);
@@ -820,6 +840,10 @@ struct oit_batch {
   float r_share = 1.0f;
   uint64_t rsig = 0;
   bool r_tuned = false;
+  // tile rasters: 0 one launch per view and pass, 1 multi-view launches;
+  // raster_pin -1 lets the autotuner time both when a graph is captured
+  int raster_pin = -1;
+  int raster_mode = -1;
   int num_sms = 0;
   cudaEvent_t rfork = nullptr, rjoin[2] = {nullptr, nullptr};
 
@@ -1085,6 +1109,140 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
   b->r_tuned = true;
   // leave the outputs written by the chosen shapes
   return batch_resolve_launch(b, s, &scratch);
+}
+
+// The tile rasters of a batch as multi-view launches, after every view's
+// binning: one launch per (pass, algorithm, sample layout) group and at most
+// kMvMaxViews views, the largest views' CTAs first; opaque passes before the
+// transparent ones that read their depth.
+int batch_mv_rasters(const oit_view_frame* views, uint32_t n, cudaStream_t s, uint64_t* launches) {
+  struct Item {
+    bool opaque;
+    int alg, S, ssn;
+    uint64_t size;
+    oit_context* c;
+  };
+  std::vector<Item> items;
+  for (uint32_t i = 0; i < n; ++i) {
+    oit_context* c = views[i].ctx;
+    if (c->frame_has_opaque) items.push_back({true, (int)oit::Alg::Opaque, c->S, 1, (uint64_t)c->P * c->S, c});
+    items.push_back({false, (int)c->alg(), c->ssn > 1 ? 1 : c->S, c->ssn, (uint64_t)c->P * c->ssn, c});
+  }
+  std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) {
+    if (a.opaque != b.opaque) return a.opaque;
+    if (a.alg != b.alg) return a.alg < b.alg;
+    if (a.S != b.S) return a.S < b.S;
+    if (a.ssn != b.ssn) return a.ssn < b.ssn;
+    return a.size > b.size;
+  });
+  std::unique_ptr<oit::MvRaster> mv(new (std::nothrow) oit::MvRaster());
+  if (!mv) return OIT_ERR_OUT_OF_MEMORY;
+  size_t k = 0;
+  while (k < items.size()) {
+    const Item& g = items[k];
+    mv->n = 0;
+    uint32_t ctas = 0;
+    while (k < items.size() && mv->n < oit::kMvMaxViews && items[k].opaque == g.opaque && items[k].alg == g.alg &&
+           items[k].S == g.S && items[k].ssn == g.ssn) {
+      oit_context* c = items[k].c;
+      mv->v[mv->n] = g.opaque ? c->opaque_pass_params() : c->raster_params(c->num_tiles);
+      ctas += (uint32_t)(c->tiles_x * c->tiles_y * (g.opaque ? 1 : c->ssn) *
+                         (oit::kWarpsPerTile / oit::kRasterWarpsPerBlock));
+      mv->cta_end[mv->n++] = ctas;
+      ++k;
+    }
+    cudaError_t e;
+    const oit::Alg a = static_cast<oit::Alg>(g.alg);
+    switch (a) {
+      case oit::Alg::Simple:
+      case oit::Alg::LinkedList:
+      case oit::Alg::Opaque: e = oit::launch_raster_mv_a(a, *mv, s); break;
+      case oit::Alg::Loop:
+      case oit::Alg::Loop64: e = oit::launch_raster_mv_b(a, *mv, s); break;
+      default: e = oit::launch_raster_mv_c(a, *mv, s); break;
+    }
+    ++*launches;
+    if (e != cudaSuccess) return cuda_status(e, "multi-view raster");
+  }
+  return OIT_OK;
+}
+
+// Captures the batch's graph: every view's frame on the forked streams (with
+// multi_view, only up to its binning; the rasters then run as multi-view
+// launches), then the batched resolve. The caller has rendered plain frames
+// (buffers sized) and tuned the resolve.
+int batch_capture(oit_batch* b, const oit_view_frame* views, uint32_t n, cudaStream_t s, bool multi_view,
+                  cudaGraphExec_t* exec, uint64_t* launches) {
+  *exec = nullptr;
+  OIT_TRY_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed), "capture");
+  int r = OIT_OK;
+  cudaError_t e = cudaEventRecord(b->fork, b->stream);
+  const size_t K = b->lanes.size();
+  for (size_t k = 0; k < K && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b->lanes[k], b->fork, 0);
+  uint64_t nodes = 0;
+  b->ctxs.assign(n, nullptr);
+  b->opaque_valid.assign(n, false);
+  for (uint32_t i = 0; i < n && e == cudaSuccess && r == OIT_OK; ++i) {
+    const oit_view_frame& v = views[i];
+    oit_context* c = v.ctx;
+    const uint64_t l0 = c->launches;
+    c->graph_stats.clear();
+    c->capturing = true;
+    r = c->render_frame_body(view_mesh(v), view_tpo(v), v.percent_transparent, v.out_rgba8_device,
+                             b->lanes[i % K], !multi_view && !c->batch_resolvable(), !multi_view);
+    c->capturing = false;
+    nodes += c->launches - l0;
+    c->launches = l0;
+    c->last_stream = s;
+    b->ctxs[i] = c;
+    b->opaque_valid[i] = c->opaque_valid;
+  }
+  for (size_t k = 0; k < K && e == cudaSuccess; ++k) {
+    e = cudaEventRecord(b->joins[k], b->lanes[k]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->joins[k], 0);
+  }
+  if (e == cudaSuccess && r == OIT_OK && multi_view) {
+    r = batch_mv_rasters(views, n, b->stream, &nodes);
+    for (uint32_t i = 0; i < n && r == OIT_OK; ++i) {
+      oit_context* c = views[i].ctx;
+      if (c->batch_resolvable()) continue;
+      const uint64_t l0 = c->launches;
+      r = c->composite(views[i].out_rgba8_device, b->stream);
+      nodes += c->launches - l0;
+      c->launches = l0;
+      c->last_stream = s;
+    }
+  }
+  if (e == cudaSuccess && r == OIT_OK) r = batch_resolve_launch(b, b->stream, &nodes);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+  if (r != OIT_OK || e != cudaSuccess || ce != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (r != OIT_OK) return r;
+    return cuda_status(e != cudaSuccess ? e : ce, "batch capture");
+  }
+  const cudaError_t ie = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  OIT_TRY_CUDA(ie, "batch instantiate");
+  *launches = nodes;
+  return OIT_OK;
+}
+
+// Mean time of `reps` replays of a batch graph (after one warm-up).
+int time_graph(cudaGraphExec_t exec, cudaStream_t s, int reps, float* ms) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  OIT_TRY_CUDA(cudaEventCreate(&e0), "event");
+  cudaError_t e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
+  if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+  for (int k = 0; k < reps && e == cudaSuccess; ++k) e = cudaGraphLaunch(exec, s);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+  cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  *ms /= (float)reps;
+  return cuda_status(e, "time graph");
 }
 
 }  // namespace
@@ -1382,46 +1540,42 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
     pr = b->r_tuned ? batch_resolve_launch(b, s, &scratch) : batch_autotune(b, s);
     if (pr != OIT_OK) return pr;
     OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
-    OIT_TRY_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed), "capture");
-    int r = OIT_OK;
-    cudaError_t e = cudaEventRecord(b->fork, b->stream);
-    const size_t K = b->lanes.size();
-    for (size_t k = 0; k < K && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b->lanes[k], b->fork, 0);
-    uint64_t nodes = 0;
-    b->ctxs.assign(n, nullptr);
-    b->opaque_valid.assign(n, false);
-    for (uint32_t i = 0; i < n && e == cudaSuccess && r == OIT_OK; ++i) {
-      const oit_view_frame& v = views[i];
-      oit_context* c = v.ctx;
-      const uint64_t l0 = c->launches;
-      c->graph_stats.clear();
-      c->capturing = true;
-      r = c->render_frame_body(view_mesh(v), view_tpo(v), v.percent_transparent, v.out_rgba8_device,
-                               b->lanes[i % K], !c->batch_resolvable());
-      c->capturing = false;
-      nodes += c->launches - l0;
-      c->launches = l0;
-      c->last_stream = s;
-      b->ctxs[i] = c;
-      b->opaque_valid[i] = c->opaque_valid;
+    // the graph: per-view raster launches or multi-view ones, as pinned, or
+    // both captured and timed on these frames, the faster kept
+    const int modes[2] = {0, 1};
+    cudaGraphExec_t best = nullptr;
+    uint64_t best_launches = 0;
+    float best_ms = 1e30f;
+    int best_mode = 0;
+    for (int mode : modes) {
+      if (b->raster_pin >= 0 && mode != b->raster_pin) continue;
+      cudaGraphExec_t ex = nullptr;
+      uint64_t nodes = 0;
+      int r = batch_capture(b, views, n, s, mode == 1, &ex, &nodes);
+      if (r == OIT_OK && b->raster_pin < 0) {
+        float ms = 0.f;
+        r = time_graph(ex, b->stream, 3, &ms);
+        if (r == OIT_OK && ms >= best_ms) {
+          cudaGraphExecDestroy(ex);
+          continue;
+        }
+        best_ms = ms;
+      }
+      if (r != OIT_OK) {
+        if (ex) cudaGraphExecDestroy(ex);
+        if (best) cudaGraphExecDestroy(best);
+        return r;
+      }
+      if (best) cudaGraphExecDestroy(best);
+      best = ex;
+      best_launches = nodes;
+      best_mode = mode;
     }
-    for (size_t k = 0; k < K && e == cudaSuccess; ++k) {
-      e = cudaEventRecord(b->joins[k], b->lanes[k]);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->joins[k], 0);
-    }
-    if (e == cudaSuccess && r == OIT_OK) r = batch_resolve_launch(b, b->stream, &nodes);
-    cudaGraph_t g = nullptr;
-    const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
-    if (r != OIT_OK || e != cudaSuccess || ce != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      if (r != OIT_OK) return r;
-      return cuda_status(e != cudaSuccess ? e : ce, "batch capture");
-    }
-    const cudaError_t ie = cudaGraphInstantiate(&b->exec, g, 0);
-    cudaGraphDestroy(g);
-    OIT_TRY_CUDA(ie, "batch instantiate");
+    OIT_TRY_CUDA(cudaStreamSynchronize(b->stream), "sync");
+    b->exec = best;
     b->sig = sig;
-    b->graph_launches = nodes;
+    b->graph_launches = best_launches;
+    b->raster_mode = best_mode;
     return OIT_OK;  // the plain frames produced this call's images
   }
   for (uint32_t i = 0; i < n; ++i) {  // each view's newest scene constants, before the replay
@@ -1508,6 +1662,21 @@ int oit_batch_set_resolve_config(oit_batch* b, uint32_t part, const oit_resolve_
   if (b->stream) OIT_TRY_CUDA(cudaStreamSynchronize(b->stream), "sync");
   b->r_tuned = false;
   b->drop();
+  return OIT_OK;
+}
+
+int oit_batch_set_raster_mode(oit_batch* b, int32_t mode) {
+  if (!b || mode < -1 || mode > 1) return OIT_ERR_INVALID_ARGUMENT;
+  if (b->stream) OIT_TRY_CUDA(cudaStreamSynchronize(b->stream), "sync");
+  b->raster_pin = mode;
+  b->drop();  // captured again on the next render
+  return OIT_OK;
+}
+
+int oit_batch_raster_mode(oit_batch* b, int32_t* mode) {
+  if (!b || !mode) return OIT_ERR_INVALID_ARGUMENT;
+  if (b->raster_mode < 0) return OIT_ERR_STATE;
+  *mode = b->raster_mode;
   return OIT_OK;
 }
 

@@ -10,6 +10,7 @@ namespace oit {
 
 constexpr int kTile = 16;            // binning tile edge in pixels
 constexpr int kWarpsPerTile = 8;     // one warp per 8x4 micro-tile
+constexpr int kRasterWarpsPerBlock = 2;  // micro-tile warps per tile-raster CTA
 // pair keys: tile id in the low 24 bits (sorted), the micro-tile mask above
 constexpr int kMaskShift = 24;
 constexpr uint32_t kTileKeyMask = (1u << kMaskShift) - 1u;
@@ -140,6 +141,16 @@ struct RasterParams {
   int lens_stride;               // micro-tiles per row, (RW + 7) / 8
 };
 
+// Several views' raster passes in one launch (the tile rasters of a batch):
+// CTAs [cta_end[i-1], cta_end[i]) run view i's pass with v[i]. Passed as a
+// kernel parameter (kMvMaxViews x RasterParams fits the parameter space).
+constexpr int kMvMaxViews = 48;
+struct MvRaster {
+  int n;
+  uint32_t cta_end[kMvMaxViews];
+  RasterParams v[kMvMaxViews];
+};
+
 struct CompositeParams {
   int W, H;                      // output size
   int RW, RH;                    // render size
@@ -208,6 +219,11 @@ size_t radix_hist_words(size_t pairs);
 cudaError_t launch_raster_a(Alg alg, const RasterParams& p, cudaStream_t s);  // Simple, LinkedList, Opaque
 cudaError_t launch_raster_b(Alg alg, const RasterParams& p, cudaStream_t s);  // Loop, Loop64
 cudaError_t launch_raster_c(Alg alg, const RasterParams& p, cudaStream_t s);  // Spinlock, Interlock, Weighted
+// Multi-view launches (every view of mv runs algorithm alg with one S / SSN);
+// Alg::Opaque runs the views' opaque passes.
+cudaError_t launch_raster_mv_a(Alg alg, const MvRaster& mv, cudaStream_t s);  // Simple, LinkedList, Opaque
+cudaError_t launch_raster_mv_b(Alg alg, const MvRaster& mv, cudaStream_t s);  // Loop, Loop64
+cudaError_t launch_raster_mv_c(Alg alg, const MvRaster& mv, cudaStream_t s);  // Spinlock, Interlock, Weighted
 cudaError_t launch_composite(Alg alg, const CompositeParams& p, cudaStream_t s);
 // FP64 verification resolve (verify.cu): the composite recomputed in double;
 // writes double4 linear colours to out_linear (may be null) and RGBA8 to

@@ -15,6 +15,8 @@
 
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "oit_device.cuh"
 
 namespace oitd {
@@ -445,13 +447,14 @@ struct LaneMap {
   __device__ static int sample(int lane) { return lane / kPix; }
 };
 
+// cta: the CTA's index within its view's grid.
 template <int SSN>
-__device__ __forceinline__ WarpTile warp_tile(const RasterParams& p) {
+__device__ __forceinline__ WarpTile warp_tile(const RasterParams& p, int cta) {
   using M = LaneMap<SSN>;
   WarpTile w;
   const int warp = threadIdx.x >> 5;
   w.lane = threadIdx.x & 31;
-  const int gw = blockIdx.x * (int)(blockDim.x >> 5) + warp;   // warp within the pass
+  const int gw = cta * (int)(blockDim.x >> 5) + warp;   // warp within the pass
   const int tile = gw / (oit::kWarpsPerTile * SSN);
   const int mt = gw % (oit::kWarpsPerTile * SSN);           // micro-tile within the tile
   w.mt = mt;
@@ -620,20 +623,18 @@ constexpr size_t kWarpStageBytes = kStageSlots * (sizeof(TriSetup) + sizeof(uint
 // resources are released when its slowest warp is done, and micro-tiles of
 // one tile differ in work (2 warps per CTA: the 64-view batch 5.6% faster
 // than 8; Loop64 k-buffers at large OIT_LAYERS pack shared memory better).
-constexpr int kRasterWarpsPerBlock = 2;
+using oit::kRasterWarpsPerBlock;
 // Policy::kWarpsPerSM resident warps per SM for one coverage sample per lane
 // (36 at 56 registers: the 64-view batch 19.28 -> 18.96 ms against 32 at 64;
 // shared memory still limits Loop64 and Loop32 at large OIT_LAYERS), 24 for
 // MSAA lanes, whose per-sample state needs more.
 template <template <int> class Policy, int S, int SSN>
-__global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
-                                  (S == 1 ? Policy<S>::kWarpsPerSM : 24) / kRasterWarpsPerBlock)
-    k_raster_transparent(RasterParams p) {
+__device__ __forceinline__ void raster_transparent_body(const RasterParams& p, int cta) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using Pol = Policy<S>;
   using M = LaneMap<SSN>;
   const int warp = threadIdx.x >> 5;
-  const WarpTile w = warp_tile<SSN>(p);
+  const WarpTile w = warp_tile<SSN>(p, cta);
   const uint32_t elem = (uint32_t)w.sample * p.P + w.pixel;  // this lane's sample of the pixel
   unsigned char* wbase = smem_raw + (size_t)warp * kWarpStageBytes;
   TriSetup* stage = reinterpret_cast<TriSetup*>(wbase);
@@ -661,7 +662,7 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
   Pol pol;
   pol.init(p, pol_smem, w.lane, w.sample, w.pixel);
 
-  const int tile = (int)((blockIdx.x * (blockDim.x >> 5) + warp) / (oit::kWarpsPerTile * SSN)) + p.tile_offset;
+  const int tile = (int)((cta * (blockDim.x >> 5) + warp) / (oit::kWarpsPerTile * SSN)) + p.tile_offset;
   const uint32_t beg = p.tile_begin[tile], end = p.tile_end[tile];
   const TriPersp* __restrict__ persp = reinterpret_cast<const TriPersp*>(p.persp);
   const uint32_t lt = (1u << w.lane) - 1u;
@@ -916,16 +917,68 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
   }
 }
 
+// The view of a multi-view launch that CTA `block` belongs to, and the CTA's
+// index within that view's grid (block-uniform).
+__device__ __forceinline__ int mv_view(const oit::MvRaster& mv, uint32_t block, int& cta) {
+  int lo = 0, hi = mv.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (mv.cta_end[mid] > block) hi = mid; else lo = mid + 1;
+  }
+  cta = (int)(block - (lo ? mv.cta_end[lo - 1] : 0u));
+  return lo;
+}
+
+#ifndef OIT_MV_PARAMS_IN_SMEM
+#define OIT_MV_PARAMS_IN_SMEM 0
+#endif
+// Copies the CTA's view parameters into shared memory: the pass reads them at
+// fixed shared addresses (as the single-view kernel reads its parameters at
+// fixed constant-bank addresses) instead of through a register-held index.
+__device__ __forceinline__ void mv_params(const oit::MvRaster& mv, int v, RasterParams& dst) {
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(&mv.v[v]);
+  uint32_t* d = reinterpret_cast<uint32_t*>(&dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(RasterParams) / 4); i += blockDim.x) d[i] = src[i];
+  __syncthreads();
+}
+
+// One view's pass: one CTA per kRasterWarpsPerBlock micro-tile warps.
+template <template <int> class Policy, int S, int SSN>
+__global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
+                                  (S == 1 ? Policy<S>::kWarpsPerSM : 24) / kRasterWarpsPerBlock)
+    k_raster_transparent(RasterParams p) {
+  raster_transparent_body<Policy, S, SSN>(p, (int)blockIdx.x);
+}
+
+// Several views' passes in one grid: the CTAs of view 0, then view 1, ...
+// (the hardware hands out CTAs as earlier ones retire, so the views share the
+// machine and small views fill what large ones leave).
+template <template <int> class Policy, int S, int SSN>
+__global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
+                                  (S == 1 ? Policy<S>::kWarpsPerSM : 24) / kRasterWarpsPerBlock)
+    k_raster_transparent_mv(const __grid_constant__ oit::MvRaster mv) {
+#if OIT_MV_PARAMS_IN_SMEM
+  __shared__ __align__(16) RasterParams vp;
+  int cta;
+  mv_params(mv, mv_view(mv, blockIdx.x, cta), vp);
+  raster_transparent_body<Policy, S, SSN>(vp, cta);
+#else
+  int cta;
+  const int v = mv_view(mv, blockIdx.x, cta);
+  raster_transparent_body<Policy, S, SSN>(mv.v[v], cta);
+#endif
+}
+
 // ---------------------------------------------------------------------------
 // Opaque pass: opaque.frag.glsl:30-35, depth LESS with write (main.cpp:542-547).
 // ---------------------------------------------------------------------------
 template <int S>
-__global__ void __launch_bounds__(32 * kRasterWarpsPerBlock) k_raster_opaque(RasterParams p) {
+__device__ __forceinline__ void raster_opaque_body(const RasterParams& p, int cta) {
   __shared__ TriSetup stage_all[kRasterWarpsPerBlock * kStageSlots];
   __shared__ uint32_t stage_t_all[kRasterWarpsPerBlock * kStageSlots];
   __shared__ uint2 stage_bb_all[kRasterWarpsPerBlock * kStageSlots];
   const int warp = threadIdx.x >> 5;
-  const WarpTile w = warp_tile<1>(p);
+  const WarpTile w = warp_tile<1>(p, cta);
   TriSetup* stage = stage_all + warp * kStageSlots;
   uint2* stage_bb = stage_bb_all + warp * kStageSlots;
   uint32_t dep[S];
@@ -935,7 +988,7 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock) k_raster_opaque(Ras
     dep[s] = w.valid ? p.depth[(size_t)s * p.P + w.pixel] : 0x3F800000u;
     col[s] = w.valid ? p.opaque_color[(size_t)s * p.P + w.pixel] : p.background;
   }
-  const int tile = (int)((blockIdx.x * kRasterWarpsPerBlock + warp) / oit::kWarpsPerTile) + p.tile_offset;
+  const int tile = (int)((cta * kRasterWarpsPerBlock + warp) / oit::kWarpsPerTile) + p.tile_offset;
   walk_pass<true>(p, w, stage, stage_t_all + warp * kStageSlots, stage_bb, p.tile_begin[tile], p.tile_end[tile],
                   [&](int nh) {
     for (int k = 0; k < nh; ++k) {
@@ -982,6 +1035,19 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock) k_raster_opaque(Ras
   }
 }
 
+template <int S>
+__global__ void __launch_bounds__(32 * kRasterWarpsPerBlock) k_raster_opaque(RasterParams p) {
+  raster_opaque_body<S>(p, (int)blockIdx.x);
+}
+
+template <int S>
+__global__ void __launch_bounds__(32 * kRasterWarpsPerBlock) k_raster_opaque_mv(const __grid_constant__ oit::MvRaster mv) {
+  __shared__ __align__(16) RasterParams vp;
+  int cta;
+  mv_params(mv, mv_view(mv, blockIdx.x, cta), vp);
+  raster_opaque_body<S>(vp, cta);
+}
+
 }  // namespace oitd
 
 namespace oitd {
@@ -1006,6 +1072,64 @@ cudaError_t launch_transparent_s(const RasterParams& p, cudaStream_t s) {
   k_raster_transparent<Pol, S, SSN><<<(unsigned)(p.tiles_x * p.tiles_y * SSN * (oit::kWarpsPerTile /
                                                                                kRasterWarpsPerBlock)),
                                       32 * kRasterWarpsPerBlock, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+// Multi-view launch of one policy: mv.v[0..n) share S / SSN; the dynamic
+// shared memory covers the largest per-warp policy state among them.
+template <template <int> class Pol, int S, int SSN>
+cudaError_t launch_transparent_mv_s(const oit::MvRaster& mv, cudaStream_t s) {
+  size_t per_warp = 0;
+  for (int i = 0; i < mv.n; ++i)
+    per_warp = std::max(per_warp, Pol<S>::smem_bytes_per_warp(mv.v[i].L, mv.v[i].coverage, mv.v[i].record_fp32));
+  const size_t smem = (size_t)kRasterWarpsPerBlock * (kWarpStageBytes + per_warp);
+  if (smem > 48 * 1024) {
+    static int cap_set[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || cap_set[dev] < (int)smem) {
+      cudaError_t e = cudaFuncSetAttribute(k_raster_transparent_mv<Pol, S, SSN>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      if (dev >= 0 && dev < 64) cap_set[dev] = (int)smem;
+    }
+  }
+  const uint32_t ctas = mv.n > 0 ? mv.cta_end[mv.n - 1] : 0u;
+  if (!ctas) return cudaSuccess;
+  k_raster_transparent_mv<Pol, S, SSN><<<ctas, 32 * kRasterWarpsPerBlock, smem, s>>>(mv);
+  return cudaGetLastError();
+}
+
+template <template <int> class Pol>
+cudaError_t launch_transparent_mv(const oit::MvRaster& mv, cudaStream_t s) {
+  if (mv.n <= 0) return cudaSuccess;
+  const RasterParams& p = mv.v[0];
+  if (p.ssn > 1) {
+    switch (p.ssn) {
+      case 4: return launch_transparent_mv_s<Pol, 1, 4>(mv, s);
+      case 8: return launch_transparent_mv_s<Pol, 1, 8>(mv, s);
+      default: return cudaErrorInvalidValue;
+    }
+  }
+  switch (p.S) {
+    case 1: return launch_transparent_mv_s<Pol, 1, 1>(mv, s);
+    case 4: return launch_transparent_mv_s<Pol, 4, 1>(mv, s);
+    case 8: return launch_transparent_mv_s<Pol, 8, 1>(mv, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+inline cudaError_t launch_opaque_mv(const oit::MvRaster& mv, cudaStream_t s) {
+  if (mv.n <= 0) return cudaSuccess;
+  const uint32_t ctas = mv.cta_end[mv.n - 1];
+  if (!ctas) return cudaSuccess;
+  constexpr int kThreads = 32 * kRasterWarpsPerBlock;
+  switch (mv.v[0].S) {
+    case 1: k_raster_opaque_mv<1><<<ctas, kThreads, 0, s>>>(mv); break;
+    case 4: k_raster_opaque_mv<4><<<ctas, kThreads, 0, s>>>(mv); break;
+    case 8: k_raster_opaque_mv<8><<<ctas, kThreads, 0, s>>>(mv); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

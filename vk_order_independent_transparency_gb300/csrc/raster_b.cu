@@ -9,4 +9,11 @@ cudaError_t launch_raster_b(Alg alg, const RasterParams& p, cudaStream_t s) {
     default: return cudaErrorInvalidValue;
   }
 }
+cudaError_t launch_raster_mv_b(Alg alg, const MvRaster& mv, cudaStream_t s) {
+  switch (alg) {
+    case Alg::Loop: return oitd::launch_transparent_mv<oitd::LoopPolicy>(mv, s);
+    case Alg::Loop64: return oitd::launch_transparent_mv<oitd::Loop64Policy>(mv, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
 }  // namespace oit

@@ -10,4 +10,12 @@ cudaError_t launch_raster_c(Alg alg, const RasterParams& p, cudaStream_t s) {
     default: return cudaErrorInvalidValue;
   }
 }
+cudaError_t launch_raster_mv_c(Alg alg, const MvRaster& mv, cudaStream_t s) {
+  switch (alg) {
+    case Alg::Spinlock:
+    case Alg::Interlock: return oitd::launch_transparent_mv<oitd::LockPolicy>(mv, s);
+    case Alg::Weighted: return oitd::launch_transparent_mv<oitd::WeightedPolicy>(mv, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
 }  // namespace oit
