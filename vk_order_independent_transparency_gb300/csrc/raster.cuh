@@ -929,18 +929,6 @@ __device__ __forceinline__ int mv_view(const oit::MvRaster& mv, uint32_t block, 
   return lo;
 }
 
-#ifndef OIT_MV_PARAMS_IN_SMEM
-#define OIT_MV_PARAMS_IN_SMEM 0
-#endif
-// Copies the CTA's view parameters into shared memory: the pass reads them at
-// fixed shared addresses (as the single-view kernel reads its parameters at
-// fixed constant-bank addresses) instead of through a register-held index.
-__device__ __forceinline__ void mv_params(const oit::MvRaster& mv, int v, RasterParams& dst) {
-  const uint32_t* src = reinterpret_cast<const uint32_t*>(&mv.v[v]);
-  uint32_t* d = reinterpret_cast<uint32_t*>(&dst);
-  for (int i = threadIdx.x; i < (int)(sizeof(RasterParams) / 4); i += blockDim.x) d[i] = src[i];
-  __syncthreads();
-}
 
 // One view's pass: one CTA per kRasterWarpsPerBlock micro-tile warps.
 template <template <int> class Policy, int S, int SSN>
@@ -957,16 +945,9 @@ template <template <int> class Policy, int S, int SSN>
 __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
                                   (S == 1 ? Policy<S>::kWarpsPerSM : 24) / kRasterWarpsPerBlock)
     k_raster_transparent_mv(const __grid_constant__ oit::MvRaster mv) {
-#if OIT_MV_PARAMS_IN_SMEM
-  __shared__ __align__(16) RasterParams vp;
-  int cta;
-  mv_params(mv, mv_view(mv, blockIdx.x, cta), vp);
-  raster_transparent_body<Policy, S, SSN>(vp, cta);
-#else
   int cta;
   const int v = mv_view(mv, blockIdx.x, cta);
   raster_transparent_body<Policy, S, SSN>(mv.v[v], cta);
-#endif
 }
 
 // ---------------------------------------------------------------------------
@@ -1042,10 +1023,9 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock) k_raster_opaque(Ras
 
 template <int S>
 __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock) k_raster_opaque_mv(const __grid_constant__ oit::MvRaster mv) {
-  __shared__ __align__(16) RasterParams vp;
   int cta;
-  mv_params(mv, mv_view(mv, blockIdx.x, cta), vp);
-  raster_opaque_body<S>(vp, cta);
+  const int v = mv_view(mv, blockIdx.x, cta);
+  raster_opaque_body<S>(mv.v[v], cta);
 }
 
 }  // namespace oitd
