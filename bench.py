@@ -749,7 +749,7 @@ def run_batch(a, rank):
     t_res_plain = timed(step_resolve_plain)
     torch.cuda.nvtx.range_pop()
     res_cfg = batch.resolve_config()
-    raster_mode = batch.raster_mode()
+    raster_cfg = batch.raster_config()
     res_bytes = resolve_bytes(vs, mixed)
     batch.render(stream)
     images = [r.output() for r in mixed]
@@ -759,7 +759,7 @@ def run_batch(a, rank):
                 e2e_s=e2e_s, h2d=h2d, d2h=d2h, views=vs, t_res_mixed=t_res_mixed, t_res_plain=t_res_plain,
                 res_cfg=res_cfg, res_bytes=res_bytes, e2e_flat_s=e2e_flat_s, h2d_flat=h2d_flat, e2e_same=e2e_same,
                 raster_bytes=raster_bytes, raster_intermediate=raster_intermediate, images=images,
-                fp64_images=fp64_images, raster_mode=raster_mode)
+                fp64_images=fp64_images, raster_cfg=raster_cfg)
 
 
 def _copy_d2h(host_tensor, dev_ptr, nbytes, stream):
@@ -841,8 +841,8 @@ def main_batch(a, rank, world):
         'roofline': resolve['roofline'],
         'raster_roofline': raster_roofline(res, sec, peak, peak_kind),
         'kernels': {k: {'ms_sum_over_views': round(v, 4)} for k, v in sec.items()},
-        'autotuned_raster': {'mode': 'multi-view launches' if res['raster_mode'] == 1 else 'one launch per view',
-                             'picked_by': 'oit_batch_render timing both graphs on the batch\'s frames'},
+        'autotuned_raster': dict(res['raster_cfg'], picked_by='oit_batch_render timing the candidate graphs on the '
+                                 'batch\'s frames (per-view launches at 36 and 32 warps per SM, multi-view launches)'),
         'resolve': resolve,
         'cpu_baseline': cpu_line,
         'cpu_baseline_fp32_omp': cpu_omp_line,

@@ -318,17 +318,26 @@ int oit_batch_launch_count(oit_batch* batch, uint64_t* launches);
  * oit_batch_resolve_config) and keeps the fastest. */
 int oit_batch_resolve(oit_batch* batch, const oit_view_frame* views, uint32_t num_views, void* stream);
 
-/* Tile rasters of a batch's graph: 0 one raster launch per view and pass
- * (views on the forked streams), 1 multi-view launches (after every view's
- * binning, one launch per pass, algorithm and sample layout runs the CTAs of
- * all its views, largest views first), -1 (default) the autotuner captures
- * both when the graph is built, times them on the batch's own frames and
- * keeps the faster. Setting it makes the next oit_batch_render capture again. */
-int oit_batch_set_raster_mode(oit_batch* batch, int32_t mode);
+/* Tile rasters of a batch's graph. */
+typedef struct oit_raster_config {
+  int32_t multi_view;     /* 0: one raster launch per view and pass (views on the forked streams);
+                             1: after every view's binning, one launch per pass, algorithm and sample
+                             layout runs the CTAs of all its views, largest views first */
+  uint32_t warps_per_sm;  /* register budget of the 1x linked-list, Simple, Loop64 and lock rasters:
+                             36 resident warps per SM (56 registers, the default) or 32 (64 registers;
+                             per-view launches only) */
+} oit_raster_config;
 
-/* The raster mode of the batch's current graph (0 or 1); OIT_ERR_STATE before
- * the first capture. */
-int oit_batch_raster_mode(oit_batch* batch, int32_t* mode);
+/* Pins the batch's raster configuration; NULL (the default) lets the
+ * autotuner capture the candidates (per-view launches at 36 and 32 warps per
+ * SM, multi-view launches) when the graph is built, time them on the batch's
+ * own frames and keep the fastest. The next oit_batch_render captures again.
+ * Unknown values return OIT_ERR_INVALID_ARGUMENT. */
+int oit_batch_set_raster_config(oit_batch* batch, const oit_raster_config* config);
+
+/* The raster configuration of the batch's current graph; OIT_ERR_STATE
+ * before the first capture. */
+int oit_batch_raster_config(oit_batch* batch, oit_raster_config* config);
 
 /* The shape the autotuner picked for one part of the batched resolve. */
 typedef struct oit_resolve_shape {
@@ -341,6 +350,8 @@ typedef struct oit_resolve_shape {
   int32_t register_slots;   /* micro-tiles whose lists hold at most this many nodes (0, 4 or 8) are staged
                                in shared memory and sorted by a network in registers */
   int32_t dense;            /* 1: at most 32 registers per thread (eight 256-thread blocks per SM) */
+  int32_t bin_edges;        /* binned work lists: 0 cost buckets 1, 2-3, 4-7, ... (log2); 1 one bucket per
+                               cost 1, 2, ..., 6 and 7 or more */
 } oit_resolve_shape;
 
 /* Part 0: linked-list views, 1: Loop64 views. A part without views reports

@@ -119,7 +119,9 @@ PINNED = [
     ('linkedlist', dict(threads_per_block=64, register_slots=4)),
     ('linkedlist', dict(threads_per_block=128, register_slots=8)),
     ('linkedlist', dict(threads_per_block=256, register_slots=8, dense=1)),
+    ('linkedlist', dict(threads_per_block=256, dense=1, bin_edges=1)),
     ('loop64', dict(threads_per_block=256)),
+    ('loop64', dict(threads_per_block=128, bin_edges=1)),
     ('loop64', dict(threads_per_block=128, items_per_step=2)),
     ('loop64', dict(threads_per_block=256, dense=1)),
 ]
@@ -145,8 +147,10 @@ def test_every_pinned_resolve_shape(binned, order):
         batch.resolve()
         got = batch.resolve_config()[part]
         for f, v in shape.items():
-            assert got[f] == v, (part, shape, got)
+            if f != 'bin_edges':  # reported for binned work lists only (checked below)
+                assert got[f] == v, (part, shape, got)
         assert got['binned'] == bool(binned) and got['tile_order'] == bool(order)
+        assert got['bin_edges'] == (shape.get('bin_edges', 0) if binned else 0)
         for k, ((r, _, _, _), ref) in enumerate(zip(views, refs)):
             np.testing.assert_array_equal(r.output(), ref, err_msg='%s %s view %d' % (part, shape, k))
         batch.set_resolve_config(part, None)
@@ -168,7 +172,8 @@ def test_pinned_shape_validation():
            ('linkedlist', dict(threads_per_block=128, register_slots=4, dense=1)),
            ('linkedlist', dict(threads_per_block=128, items_per_step=3)),
            ('linkedlist', dict(threads_per_block=48)), ('linkedlist', dict(threads_per_block=512)),
-           ('linkedlist', dict(threads_per_block=128, shared_slots=4))]
+           ('linkedlist', dict(threads_per_block=128, shared_slots=4)),
+           ('linkedlist', dict(threads_per_block=128, bin_edges=2))]
     for part, shape in bad:
         with pytest.raises(oit.OitError) as e:
             batch.set_resolve_config(part, shape)
@@ -176,3 +181,16 @@ def test_pinned_shape_validation():
     batch.set_resolve_config('linkedlist', dict(threads_per_block=128))
     batch.set_resolve_config('linkedlist', None)
 
+
+
+def test_raster_config_validation():
+    batch = oit.Batch()
+    for cfg in ({'multi_view': 2}, {'warps_per_sm': 40}, {'multi_view': 1, 'warps_per_sm': 32}):
+        with pytest.raises(oit.OitError) as e:
+            batch.set_raster_config(cfg)
+        assert e.value.status == oit.OIT_ERR_INVALID_ARGUMENT
+    with pytest.raises(oit.OitError) as e:
+        batch.raster_config()  # nothing captured yet
+    assert e.value.status == oit.OIT_ERR_STATE
+    batch.set_raster_config({'multi_view': 0, 'warps_per_sm': 32})
+    batch.set_raster_config(None)

@@ -228,11 +228,15 @@ def test_cuda_graph_replay(engine, alg):
     assert r.get_error() == 0
 
 
-@pytest.mark.parametrize('raster_mode', [0, 1, -1])
-def test_batched_views_match_single_frames(engine, raster_mode):
+RASTER_CONFIGS = [{'multi_view': 0}, {'multi_view': 0, 'warps_per_sm': 32}, {'multi_view': 1}, None]
+
+
+@pytest.mark.parametrize('raster_cfg', RASTER_CONFIGS)
+def test_batched_views_match_single_frames(engine, raster_cfg):
     """oit_batch_render (one CUDA graph, views on forked streams) gives every
     view the image its own oit_render_frame gives, with one raster launch per
-    view and pass (0), multi-view raster launches (1) or the autotuner's pick."""
+    view and pass (at either register budget), multi-view raster launches, or
+    the autotuner's pick of those."""
     specs = [(1, 96, 80, 4, 12), (3, 160, 120, 16, 40), (1, 64, 64, 8, 8), (3, 128, 128, 32, 30),
              (0, 80, 60, 8, 20), (6, 96, 96, 8, 24)]
     views, refs, keep = [], [], []
@@ -244,14 +248,18 @@ def test_batched_views_match_single_frames(engine, raster_mode):
         mesh = engine.DeviceMesh(v, i)
         views.append((r, mesh, tpo, 80))
     batch = engine.Batch(parallel_streams=4)
-    batch.set_raster_mode(raster_mode)
+    batch.set_raster_config(raster_cfg)
     batch.set_views(views)
     for _ in range(3):
         batch.render()
         for (r, _, _, _), ref in zip(views, refs):
             np.testing.assert_array_equal(r.output(), ref)
             assert r.get_error() == 0
-    assert batch.raster_mode() in ((0, 1) if raster_mode < 0 else (raster_mode,))
+    got = batch.raster_config()
+    if raster_cfg is None:
+        assert (got['multi_view'], got['warps_per_sm']) in ((0, 36), (0, 32), (1, 36))
+    else:
+        assert got == dict({'warps_per_sm': 36}, **raster_cfg)
     assert batch.launch_count() >= len(specs) * 6
 
 

@@ -55,7 +55,7 @@ EXPORTS = [
     'oit_batch_create', 'oit_batch_destroy', 'oit_batch_render', 'oit_batch_launch_count',
     'oit_render_frame_instanced', 'oit_render_frame_instanced_host', 'oit_scene_generate_instanced',
     'oit_batch_resolve', 'oit_batch_resolve_config', 'oit_batch_set_resolve_config', 'oit_debug_fail_allocations',
-    'oit_verify_composite_fp64', 'oit_batch_set_raster_mode', 'oit_batch_raster_mode',
+    'oit_verify_composite_fp64', 'oit_batch_set_raster_config', 'oit_batch_raster_config',
 ]
 PROF_SECTIONS = ['opaque_bin', 'opaque_raster', 'transparent_bin', 'transparent_raster', 'composite']
 
@@ -90,7 +90,11 @@ class OitInstancedMesh(ctypes.Structure):
 class OitResolveShape(ctypes.Structure):
     _fields_ = [('threads_per_block', ctypes.c_uint32), ('blocks', ctypes.c_uint32), ('binned', ctypes.c_int32),
                 ('tile_order', ctypes.c_int32), ('shared_slots', ctypes.c_int32), ('items_per_step', ctypes.c_int32),
-                ('register_slots', ctypes.c_int32), ('dense', ctypes.c_int32)]
+                ('register_slots', ctypes.c_int32), ('dense', ctypes.c_int32), ('bin_edges', ctypes.c_int32)]
+
+
+class OitRasterConfig(ctypes.Structure):
+    _fields_ = [('multi_view', ctypes.c_int32), ('warps_per_sm', ctypes.c_uint32)]
 
 
 class OitSceneDesc(ctypes.Structure):
@@ -168,8 +172,8 @@ def library():
         'oit_batch_set_resolve_config': (I, [P, U, ctypes.POINTER(OitResolveShape)]),
         'oit_debug_fail_allocations': (I, [ctypes.c_int32]),
         'oit_verify_composite_fp64': (I, [P, P, P, P]),
-        'oit_batch_set_raster_mode': (I, [P, ctypes.c_int32]),
-        'oit_batch_raster_mode': (I, [P, ctypes.POINTER(ctypes.c_int32)]),
+        'oit_batch_set_raster_config': (I, [P, ctypes.POINTER(OitRasterConfig)]),
+        'oit_batch_raster_config': (I, [P, ctypes.POINTER(OitRasterConfig)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -516,16 +520,29 @@ class Batch:
         linked-list and Loop64 views, a composite launch per other view."""
         _check(self.lib.oit_batch_resolve(self._b, self._frames, len(self._frames), stream), 'oit_batch_resolve')
 
+    def set_raster_config(self, config):
+        """Pins the tile-raster configuration ({'multi_view': 0|1,
+        'warps_per_sm': 36|32}) or, with None, lets the autotuner pick it."""
+        if config is None:
+            _check(self.lib.oit_batch_set_raster_config(self._b, None), 'oit_batch_set_raster_config')
+            return
+        c = OitRasterConfig(int(config.get('multi_view', 0)), int(config.get('warps_per_sm', 36)))
+        _check(self.lib.oit_batch_set_raster_config(self._b, ctypes.byref(c)), 'oit_batch_set_raster_config')
+
+    def raster_config(self):
+        """The current graph's tile-raster configuration as a dict."""
+        c = OitRasterConfig()
+        _check(self.lib.oit_batch_raster_config(self._b, ctypes.byref(c)), 'oit_batch_raster_config')
+        return {'multi_view': c.multi_view, 'warps_per_sm': c.warps_per_sm}
+
     def set_raster_mode(self, mode):
-        """Tile rasters of the batch graph: 0 one launch per view and pass, 1
-        multi-view launches, -1 autotuned (default)."""
-        _check(self.lib.oit_batch_set_raster_mode(self._b, int(mode)), 'oit_batch_set_raster_mode')
+        """0 one raster launch per view and pass, 1 multi-view launches (both at
+        the default register budget), -1 autotuned."""
+        self.set_raster_config(None if mode < 0 else {'multi_view': int(mode)})
 
     def raster_mode(self):
-        """The raster mode of the current graph (0 per view, 1 multi-view)."""
-        m = ctypes.c_int32()
-        _check(self.lib.oit_batch_raster_mode(self._b, ctypes.byref(m)), 'oit_batch_raster_mode')
-        return m.value
+        """The current graph's raster launches: 0 per view, 1 multi-view."""
+        return self.raster_config()['multi_view']
 
     def resolve_config(self):
         """{'linkedlist': {...}, 'loop64': {...}}: per part of the batched

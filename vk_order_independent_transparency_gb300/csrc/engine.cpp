@@ -119,6 +119,7 @@ struct oit_context {
   uint32_t bin_tris = 0, bin_opaque_from = 0;  // the last binned draw: triangles, first opaque one
   bool opaque_valid = false;
   bool color_valid = false;
+  int raster_wpsm = 0;  // RasterParams::warps_per_sm of this context's transparent rasters
   cudaStream_t last_stream = nullptr;
   uint64_t launches = 0;
 
@@ -482,6 +483,7 @@ struct oit_context {
     p.weighted_fp32 = st.weighted_precision == OIT_WEIGHTED_FP32;
     p.error = err.as<uint32_t>();
     p.frag_count = frag.as<unsigned long long>();
+    p.warps_per_sm = raster_wpsm;
     if (tile_offset != 0 && batch_resolvable()) {
       p.lens = lens.as<uint8_t>();
       p.lens_stride = lens_stride();
@@ -824,14 +826,14 @@ struct oit_batch {
   struct ResolvePart {
     DevBuf views, base, hist, items;
     oit::ResolveBatch rb{};
-    int variant = 0, threads = 128, blocks = 0, order = 0;
+    int variant = 0, threads = 128, blocks = 0, order = 0, edges = 0;
     bool binned = false;
   };
   ResolvePart rparts[2];
   // shapes pinned by oit_batch_set_resolve_config (blocks 0: all that fit)
   struct Pin {
     bool set = false;
-    int variant = 0, threads = 128, blocks = 0, order = 0;
+    int variant = 0, threads = 128, blocks = 0, order = 0, edges = 0;
     bool binned = false;
   };
   Pin pin[2];
@@ -840,10 +842,13 @@ struct oit_batch {
   float r_share = 1.0f;
   uint64_t rsig = 0;
   bool r_tuned = false;
-  // tile rasters: 0 one launch per view and pass, 1 multi-view launches;
-  // raster_pin -1 lets the autotuner time both when a graph is captured
-  int raster_pin = -1;
-  int raster_mode = -1;
+  // tile rasters: multi-view launches or one per view and pass, and the 1x
+  // register budget (warps per SM, 0 = default); pinned, or picked by timing
+  // the candidates when a graph is captured
+  bool raster_pinned = false;
+  oit_raster_config raster_pin{};
+  oit_raster_config raster_cfg{};
+  bool raster_known = false;
   int num_sms = 0;
   cudaEvent_t rfork = nullptr, rjoin[2] = {nullptr, nullptr};
 
@@ -968,11 +973,12 @@ int batch_prepare_resolve(oit_batch* b, const oit_view_frame* views, uint32_t n)
 }
 
 int part_launch(const oit_batch::ResolvePart& rp, cudaStream_t s, int variant, bool binned, int threads, int blocks,
-                int order, uint64_t* launches) {
+                int order, int edges, uint64_t* launches) {
   oit::ResolveBatch rb = rp.rb;
   if (rb.num_views == 0) return OIT_OK;
   if (!binned) rb.items = nullptr;
   rb.order = order;
+  rb.edges = edges;
   OIT_TRY_CUDA(oit::resolve_bin(rb, s, launches), "resolve bin");
   OIT_TRY_CUDA(oit::resolve_run(rb, variant, threads, blocks, s), "resolve");
   ++*launches;
@@ -985,7 +991,7 @@ int batch_resolve_launch(oit_batch* b, cudaStream_t s, uint64_t* launches) {
   const bool two = b->rparts[0].rb.num_views > 0 && b->rparts[1].rb.num_views > 0 && b->lanes.size() >= 2;
   if (!two) {
     for (const oit_batch::ResolvePart& rp : b->rparts) {
-      const int r = part_launch(rp, s, rp.variant, rp.binned, rp.threads, rp.blocks, rp.order, launches);
+      const int r = part_launch(rp, s, rp.variant, rp.binned, rp.threads, rp.blocks, rp.order, rp.edges, launches);
       if (r != OIT_OK) return r;
     }
     return OIT_OK;
@@ -996,7 +1002,8 @@ int batch_resolve_launch(oit_batch* b, cudaStream_t s, uint64_t* launches) {
     OIT_TRY_CUDA(cudaStreamWaitEvent(b->lanes[k], b->rfork, 0), "wait");
     const float share = b->r_share >= 1.0f ? 1.0f : (k == 0 ? b->r_share : 1.0f - b->r_share);
     const int blocks = std::max(1, (int)((float)rp.blocks * share));
-    const int r = part_launch(rp, b->lanes[k], rp.variant, rp.binned, rp.threads, blocks, rp.order, launches);
+    const int r =
+        part_launch(rp, b->lanes[k], rp.variant, rp.binned, rp.threads, blocks, rp.order, rp.edges, launches);
     if (r != OIT_OK) return r;
     OIT_TRY_CUDA(cudaEventRecord(b->rjoin[k], b->lanes[k]), "event");
     OIT_TRY_CUDA(cudaStreamWaitEvent(s, b->rjoin[k], 0), "wait");
@@ -1034,6 +1041,7 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
       rp.blocks = pn.blocks > 0 ? pn.blocks : bps * b->num_sms;
       rp.binned = pn.binned;
       rp.order = pn.order;
+      rp.edges = pn.edges;
       continue;
     }
     float best = 1e30f;
@@ -1049,12 +1057,14 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
         if (bps <= 0) continue;
         const int blocks = bps * b->num_sms;
         for (int order : {0, 1})
-          for (bool binned : {true, false}) {
-            r = part_launch(rp, s, variant, binned, threads, blocks, order, &scratch);  // warm-up
+          for (int bin_mode : {1, 2, 0}) {  // binned by log2 cost, binned by cost, view order
+            const bool binned = bin_mode > 0;
+            const int edges = bin_mode == 2 ? 1 : 0;
+            r = part_launch(rp, s, variant, binned, threads, blocks, order, edges, &scratch);  // warm-up
             if (r != OIT_OK) break;
             cudaEventRecord(e0, s);
             for (int k = 0; k < 3 && r == OIT_OK; ++k)
-              r = part_launch(rp, s, variant, binned, threads, blocks, order, &scratch);
+              r = part_launch(rp, s, variant, binned, threads, blocks, order, edges, &scratch);
             cudaEventRecord(e1, s);
             if (r != OIT_OK) break;
             if (cudaEventSynchronize(e1) != cudaSuccess) {
@@ -1070,6 +1080,7 @@ int batch_autotune(oit_batch* b, cudaStream_t s) {
               rp.blocks = blocks;
               rp.binned = binned;
               rp.order = order;
+              rp.edges = edges;
             }
           }
         if (r != OIT_OK) break;
@@ -1540,19 +1551,27 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
     pr = b->r_tuned ? batch_resolve_launch(b, s, &scratch) : batch_autotune(b, s);
     if (pr != OIT_OK) return pr;
     OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
-    // the graph: per-view raster launches or multi-view ones, as pinned, or
-    // both captured and timed on these frames, the faster kept
-    const int modes[2] = {0, 1};
+    // the graph: as pinned, or each raster configuration (per-view launches at
+    // the default and at the 32-warp register budget, multi-view launches)
+    // captured and timed on these frames, the fastest kept
+    std::vector<oit_raster_config> cands;
+    if (b->raster_pinned) cands.push_back(b->raster_pin);
+    else cands = {oit_raster_config{0, 0}, oit_raster_config{0, 32}, oit_raster_config{1, 0}};
     cudaGraphExec_t best = nullptr;
     uint64_t best_launches = 0;
     float best_ms = 1e30f;
-    int best_mode = 0;
-    for (int mode : modes) {
-      if (b->raster_pin >= 0 && mode != b->raster_pin) continue;
+    oit_raster_config best_cfg{};
+    for (const oit_raster_config& cfg : cands) {
       cudaGraphExec_t ex = nullptr;
       uint64_t nodes = 0;
-      int r = batch_capture(b, views, n, s, mode == 1, &ex, &nodes);
-      if (r == OIT_OK && b->raster_pin < 0) {
+      std::vector<int> saved(n);
+      for (uint32_t i = 0; i < n; ++i) {  // the budget is baked into the captured launches
+        saved[i] = views[i].ctx->raster_wpsm;
+        views[i].ctx->raster_wpsm = (int)cfg.warps_per_sm;
+      }
+      int r = batch_capture(b, views, n, s, cfg.multi_view == 1, &ex, &nodes);
+      for (uint32_t i = 0; i < n; ++i) views[i].ctx->raster_wpsm = saved[i];
+      if (r == OIT_OK && !b->raster_pinned) {
         float ms = 0.f;
         r = time_graph(ex, b->stream, 3, &ms);
         if (r == OIT_OK && ms >= best_ms) {
@@ -1569,13 +1588,14 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
       if (best) cudaGraphExecDestroy(best);
       best = ex;
       best_launches = nodes;
-      best_mode = mode;
+      best_cfg = cfg;
     }
     OIT_TRY_CUDA(cudaStreamSynchronize(b->stream), "sync");
     b->exec = best;
     b->sig = sig;
     b->graph_launches = best_launches;
-    b->raster_mode = best_mode;
+    b->raster_cfg = best_cfg;
+    b->raster_known = true;
     return OIT_OK;  // the plain frames produced this call's images
   }
   for (uint32_t i = 0; i < n; ++i) {  // each view's newest scene constants, before the replay
@@ -1630,6 +1650,7 @@ int oit_batch_set_resolve_config(oit_batch* b, uint32_t part, const oit_resolve_
     if (sh.threads_per_block < 32 || sh.threads_per_block > 256 || sh.threads_per_block % 32 != 0)
       return OIT_ERR_INVALID_ARGUMENT;
     if ((sh.binned != 0 && sh.binned != 1) || (sh.tile_order != 0 && sh.tile_order != 1) ||
+        (sh.bin_edges != 0 && sh.bin_edges != 1) ||
         (sh.dense != 0 && sh.dense != 1) || (sh.items_per_step != 0 && sh.items_per_step != 1 && sh.items_per_step != 2))
       return OIT_ERR_INVALID_ARGUMENT;
     const bool x2 = sh.items_per_step == 2;
@@ -1655,6 +1676,7 @@ int oit_batch_set_resolve_config(oit_batch* b, uint32_t part, const oit_resolve_
     pn.blocks = (int)std::min<uint32_t>(sh.blocks, 1u << 20);
     pn.binned = sh.binned != 0;
     pn.order = sh.tile_order;
+    pn.edges = sh.bin_edges;
   }
   b->pin[part] = pn;
   // tune (or apply the pins) again on the next render or resolve, and capture
@@ -1665,18 +1687,25 @@ int oit_batch_set_resolve_config(oit_batch* b, uint32_t part, const oit_resolve_
   return OIT_OK;
 }
 
-int oit_batch_set_raster_mode(oit_batch* b, int32_t mode) {
-  if (!b || mode < -1 || mode > 1) return OIT_ERR_INVALID_ARGUMENT;
+int oit_batch_set_raster_config(oit_batch* b, const oit_raster_config* cfg) {
+  if (!b) return OIT_ERR_INVALID_ARGUMENT;
+  if (cfg) {
+    if (cfg->multi_view != 0 && cfg->multi_view != 1) return OIT_ERR_INVALID_ARGUMENT;
+    if (cfg->warps_per_sm != 0 && cfg->warps_per_sm != 32 && cfg->warps_per_sm != 36) return OIT_ERR_INVALID_ARGUMENT;
+    if (cfg->multi_view && cfg->warps_per_sm == 32) return OIT_ERR_INVALID_ARGUMENT;
+  }
   if (b->stream) OIT_TRY_CUDA(cudaStreamSynchronize(b->stream), "sync");
-  b->raster_pin = mode;
+  b->raster_pinned = cfg != nullptr;
+  if (cfg) b->raster_pin = oit_raster_config{cfg->multi_view, cfg->warps_per_sm == 36 ? 0u : cfg->warps_per_sm};
   b->drop();  // captured again on the next render
   return OIT_OK;
 }
 
-int oit_batch_raster_mode(oit_batch* b, int32_t* mode) {
-  if (!b || !mode) return OIT_ERR_INVALID_ARGUMENT;
-  if (b->raster_mode < 0) return OIT_ERR_STATE;
-  *mode = b->raster_mode;
+int oit_batch_raster_config(oit_batch* b, oit_raster_config* cfg) {
+  if (!b || !cfg) return OIT_ERR_INVALID_ARGUMENT;
+  if (!b->raster_known) return OIT_ERR_STATE;
+  *cfg = b->raster_cfg;
+  if (cfg->warps_per_sm == 0) cfg->warps_per_sm = 36;
   return OIT_OK;
 }
 
@@ -1694,6 +1723,7 @@ int oit_batch_resolve_config(oit_batch* b, uint32_t part, oit_resolve_shape* out
     out->blocks = (uint32_t)std::max(1, (int)((float)rp.blocks * (part == 0 ? b->r_share : 1.0f - b->r_share)));
   out->binned = rp.binned ? 1 : 0;
   out->tile_order = rp.order;
+  out->bin_edges = rp.binned ? rp.edges : 0;
   out->shared_slots = rp.variant == oit::kResolveVariantListShared ? 8 : 0;
   out->items_per_step = (rp.variant == oit::kResolveVariantListx2 || rp.variant == oit::kResolveVariantLoop64x2) ? 2 : 1;
   out->register_slots = rp.variant == oit::kResolveVariantListShort4 ? 4

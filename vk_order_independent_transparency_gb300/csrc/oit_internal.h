@@ -139,6 +139,9 @@ struct RasterParams {
   // work binning; null = not wanted (1x only)
   uint8_t* lens;
   int lens_stride;               // micro-tiles per row, (RW + 7) / 8
+  // 1x transparent raster register budget: 32 runs the passes compiled for 36
+  // resident warps per SM (56 registers) at 32 (64 registers); 0 = default
+  int warps_per_sm;
 };
 
 // Several views' raster passes in one launch (the tile rasters of a batch):
@@ -206,6 +209,7 @@ struct ResolveBatch {
   int num_views;
   uint32_t total_tiles;          // work items (micro-tiles, padded to whole tiles) over all views
   int order;                     // 0: micro-tiles row by row; 1: tile by tile (8 micro-tiles of a tile in a row)
+  int edges;                     // cost buckets: 0 log2 (1, 2-3, 4-7, ...), 1 one per cost (1, 2, ..., 6, 7+)
   uint32_t* hist;                // [kResolveBuckets] (device)
   uint32_t* fill;                // [kResolveBuckets] (device)
   uint32_t* items;               // [total_tiles] work list, costliest bucket first; null = view order

@@ -930,10 +930,11 @@ __device__ __forceinline__ int mv_view(const oit::MvRaster& mv, uint32_t block, 
 }
 
 
-// One view's pass: one CTA per kRasterWarpsPerBlock micro-tile warps.
-template <template <int> class Policy, int S, int SSN>
-__global__ void __launch_bounds__(32 * kRasterWarpsPerBlock,
-                                  (S == 1 ? Policy<S>::kWarpsPerSM : 24) / kRasterWarpsPerBlock)
+// One view's pass: one CTA per kRasterWarpsPerBlock micro-tile warps, compiled
+// for WPSM resident warps per SM with one coverage sample per lane (the
+// register budget: 36 -> 56 registers, 32 -> 64).
+template <template <int> class Policy, int S, int SSN, int WPSM = Policy<S>::kWarpsPerSM>
+__global__ void __launch_bounds__(32 * kRasterWarpsPerBlock, (S == 1 ? WPSM : 24) / kRasterWarpsPerBlock)
     k_raster_transparent(RasterParams p) {
   raster_transparent_body<Policy, S, SSN>(p, (int)blockIdx.x);
 }
@@ -1032,8 +1033,8 @@ __global__ void __launch_bounds__(32 * kRasterWarpsPerBlock) k_raster_opaque_mv(
 
 namespace oitd {
 
-template <template <int> class Pol, int S, int SSN>
-cudaError_t launch_transparent_s(const RasterParams& p, cudaStream_t s) {
+template <template <int> class Pol, int S, int SSN, int WPSM>
+cudaError_t launch_transparent_w(const RasterParams& p, cudaStream_t s) {
   const size_t smem = (size_t)kRasterWarpsPerBlock *
                       (kWarpStageBytes + Pol<S>::smem_bytes_per_warp(p.L, p.coverage, p.record_fp32));
   if (smem > 48 * 1024) {
@@ -1043,16 +1044,27 @@ cudaError_t launch_transparent_s(const RasterParams& p, cudaStream_t s) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || cap_set[dev] < (int)smem) {
-      cudaError_t e = cudaFuncSetAttribute(k_raster_transparent<Pol, S, SSN>,
+      cudaError_t e = cudaFuncSetAttribute(k_raster_transparent<Pol, S, SSN, WPSM>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
       if (dev >= 0 && dev < 64) cap_set[dev] = (int)smem;
     }
   }
-  k_raster_transparent<Pol, S, SSN><<<(unsigned)(p.tiles_x * p.tiles_y * SSN * (oit::kWarpsPerTile /
-                                                                               kRasterWarpsPerBlock)),
-                                      32 * kRasterWarpsPerBlock, smem, s>>>(p);
+  k_raster_transparent<Pol, S, SSN, WPSM><<<(unsigned)(p.tiles_x * p.tiles_y * SSN *
+                                                       (oit::kWarpsPerTile / kRasterWarpsPerBlock)),
+                                            32 * kRasterWarpsPerBlock, smem, s>>>(p);
   return cudaGetLastError();
+}
+
+// p.warps_per_sm 32 runs the 1x rasters whose default budget is 36 resident
+// warps per SM at 32 (64 registers instead of 56); other values, the default.
+template <template <int> class Pol, int S, int SSN>
+cudaError_t launch_transparent_s(const RasterParams& p, cudaStream_t s) {
+  constexpr int kDefault = Pol<S>::kWarpsPerSM;
+  if constexpr (S == 1 && SSN == 1 && kDefault != 32) {
+    if (p.warps_per_sm == 32) return launch_transparent_w<Pol, S, SSN, 32>(p, s);
+  }
+  return launch_transparent_w<Pol, S, SSN, kDefault>(p, s);
 }
 
 // Multi-view launch of one policy: mv.v[0..n) share S / SSN; the dynamic

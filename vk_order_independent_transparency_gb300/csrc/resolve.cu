@@ -56,11 +56,12 @@ __device__ __forceinline__ bool item_microtile(const ResolveView& v, uint32_t t,
   return mx < (uint32_t)v.mtx && my < (uint32_t)v.mty;
 }
 
-// Cost bucket of a micro-tile: 0 for no node reads, else 1 + floor(log2(cost)),
-// at most kResolveBuckets - 1. A list pixel reads one node per fragment; a
-// Loop64 pixel reads its kept keys plus the terminating empty key.
+// Cost bucket of a micro-tile: 0 for no node reads, else 1 + floor(log2(cost))
+// (edges 0) or the cost itself (edges 1), at most kResolveBuckets - 1. A list
+// pixel reads one node per fragment; a Loop64 pixel reads its kept keys plus
+// the terminating empty key.
 __device__ __forceinline__ int tile_bucket(const ResolveView* __restrict__ views, const uint32_t* tb, int nv,
-                                           uint32_t g, int order) {
+                                           uint32_t g, int order, int edges) {
   const int v = find_view(tb, nv, g);
   uint32_t mx, my;
   if (!item_microtile(views[v], g - tb[v], order, mx, my)) return 0;
@@ -68,7 +69,7 @@ __device__ __forceinline__ int tile_bucket(const ResolveView* __restrict__ views
   const int L = views[v].L;
   const uint32_t cost = views[v].kind == kResolveList ? len : min(len, (uint32_t)L) + (len < (uint32_t)L ? 1u : 0u);
   if (cost == 0) return 0;
-  return min(32 - __clz(cost), kResolveBuckets - 1);
+  return edges ? (int)min(cost, (uint32_t)kResolveBuckets - 1u) : min(32 - __clz(cost), kResolveBuckets - 1);
 }
 
 __device__ __forceinline__ void load_bases(const ResolveBatch& b, uint32_t* tb) {
@@ -84,7 +85,7 @@ __global__ void __launch_bounds__(kBinThreads) k_rbin_count(ResolveBatch b) {
   const uint32_t lane = threadIdx.x & 31;
   for (int i = 0; i < kBinPerThread; ++i) {
     const uint32_t g = blockIdx.x * kBinChunk + i * kBinThreads + threadIdx.x;
-    const int bk = g < b.total_tiles ? tile_bucket(b.views, tb, b.num_views, g, b.order) : -1;
+    const int bk = g < b.total_tiles ? tile_bucket(b.views, tb, b.num_views, g, b.order, b.edges) : -1;
     const uint32_t peers = __match_any_sync(0xffffffffu, bk);
     if (bk >= 0 && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&cnt[bk], (uint32_t)__popc(peers));
   }
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(kBinThreads) k_rbin_scatter(ResolveBatch b) {
 #pragma unroll
   for (int i = 0; i < kBinPerThread; ++i) {
     const uint32_t g = blockIdx.x * kBinChunk + i * kBinThreads + threadIdx.x;
-    bk[i] = g < b.total_tiles ? tile_bucket(b.views, tb, b.num_views, g, b.order) : -1;
+    bk[i] = g < b.total_tiles ? tile_bucket(b.views, tb, b.num_views, g, b.order, b.edges) : -1;
     const uint32_t peers = __match_any_sync(0xffffffffu, bk[i]);
     const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
     uint32_t r = 0;
