@@ -609,6 +609,28 @@ def run_batch(a, rank):
     torch.cuda.nvtx.range_pop()
     launches = batch.launch_count() * a.steps
 
+    # A/B: the linked-list views' COLOR pass in arrival order (fragment-parallel,
+    # HBM atomics, no tile binning) beside the same Loop64 views
+    arrival = []
+    for r, vd in zip(mixed, vs):
+        if vd['algorithm'] != 'linkedlist':
+            arrival.append(r)
+            continue
+        ra = oit.Renderer(oit.make_state(oit.OIT_LINKEDLIST, vd['width'], vd['height'], oit_layers=vd['oit_layers'],
+                                         nodes_per_pixel=vd['nodes_per_pixel'], alpha_min=vd['alpha_min'],
+                                         alpha_width=vd['alpha_width'],
+                                         flags=oit.OIT_FLAG_HALF_COLOR | oit.OIT_FLAG_ARRIVAL_ORDER))
+        ra.update_scene(oit.make_camera(vd['width'], vd['height']))
+        arrival.append(ra)
+    batch_arr = oit.Batch(parallel_streams=8)
+    batch_arr.set_views([(r, m, h[2], 100) for r, m, h in zip(arrival, meshes, host)])
+    for _ in range(max(3, a.warmup)):
+        batch_arr.render(stream)
+    t_arrival = timed(lambda: batch_arr.render(stream))
+    frags_arr = sum(r.fragment_count() for r in arrival)
+    arr_err = max(r.get_error() for r in arrival)
+    batch_arr.close()
+
     # per-pass times: every view rendered alone with section timing, and the
     # transparent raster's algorithmic bytes summed over the views
     sections = {}
@@ -759,7 +781,8 @@ def run_batch(a, rank):
                 e2e_s=e2e_s, h2d=h2d, d2h=d2h, views=vs, t_res_mixed=t_res_mixed, t_res_plain=t_res_plain,
                 res_cfg=res_cfg, res_bytes=res_bytes, e2e_flat_s=e2e_flat_s, h2d_flat=h2d_flat, e2e_same=e2e_same,
                 raster_bytes=raster_bytes, raster_intermediate=raster_intermediate, images=images,
-                fp64_images=fp64_images, raster_cfg=raster_cfg)
+                fp64_images=fp64_images, raster_cfg=raster_cfg, t_arrival=t_arrival, frags_arr=frags_arr,
+                arr_err=arr_err)
 
 
 def _copy_d2h(host_tensor, dev_ptr, nbytes, stream):
@@ -841,6 +864,13 @@ def main_batch(a, rank, world):
         'roofline': resolve['roofline'],
         'raster_roofline': raster_roofline(res, sec, peak, peak_kind),
         'kernels': {k: {'ms_sum_over_views': round(v, 4)} for k, v in sec.items()},
+        'arrival_order_ll': {'ms_per_step': round(res['t_arrival'] / a.steps, 4),
+                             'value': round(res['frags_arr'] * a.steps / (res['t_arrival'] * 1e-3) / 1e6, 3),
+                             'unit': 'Mfragments/s', 'fragments_equal': res['frags_arr'] == res['frags'],
+                             'device_error_bits': int(res['arr_err']),
+                             'path': 'the same batch with the linked-list views in OIT_FLAG_ARRIVAL_ORDER: '
+                                     'fragment-parallel COLOR pass, warp-aggregated node counter, atomicExch '
+                                     'heads in HBM, no tile binning; list order not deterministic'},
         'autotuned_raster': dict(res['raster_cfg'], picked_by='oit_batch_render timing the candidate graphs on the '
                                  'batch\'s frames (per-view launches at 36 and 32 warps per SM, multi-view launches)'),
         'resolve': resolve,

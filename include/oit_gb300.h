@@ -60,6 +60,15 @@ extern "C" {
 #define OIT_FLAG_CUDA_GRAPH 0x2u     /* oit_render_frame replays a captured CUDA graph of the whole frame */
 #define OIT_FLAG_HALF_COLOR 0x4u     /* colour target after tail blending stored as FP16 (blended in FP32
                                         within a tile, rounded once); the reference's is RGBA8 sRGB */
+#define OIT_FLAG_ARRIVAL_ORDER 0x8u  /* linked list, 1x (and 2x2 supersampling), RGBA8 records: the COLOR pass
+                                        as the reference's GPU runs it -- fragments of all triangles in
+                                        parallel, nodes from the global counter linked by atomic exchanges
+                                        of the head image in HBM (oitLinkedList.frag.glsl:51-85), pool
+                                        overflow tail-blended under per-pixel spinlocks; list order is
+                                        arrival order (not deterministic), the stored set per pixel is the
+                                        same as in primitive order when the pool does not overflow. A frame
+                                        without opaque objects needs no tile binning. Other states with it
+                                        return OIT_ERR_UNSUPPORTED */
 
 /* Status codes. */
 #define OIT_OK 0
@@ -76,7 +85,7 @@ extern "C" {
                                          frames: its image is still complete (the triangles that did not fit
                                          were tested by bbox, a slower walk) and the next frame call re-sizes
                                          the bins */
-#define OIT_DEVERR_TIMEOUT 0x2u       /* a bounded wait gave up */
+#define OIT_DEVERR_TIMEOUT 0x2u       /* a bounded wait gave up (an arrival-order tail blend's spinlock) */
 
 /* Renderer settings: State (oit.h:64-116) plus the SceneData scalars
  * (shaders/common.h:77-92). */

@@ -1109,6 +1109,15 @@ void or_load_state(or_frame* f, const uint32_t* abuffer, const uint32_t* aux, co
   if (counter) f->counter = *counter;
 }
 
+void or_load_color(or_frame* f, const double* rgba) {
+  for (size_t i = 0; i < (size_t)f->S * f->P; ++i) {
+    f->color[i].r = (or_real)rgba[4 * i + 0];
+    f->color[i].g = (or_real)rgba[4 * i + 1];
+    f->color[i].b = (or_real)rgba[4 * i + 2];
+    f->color[i].a = (or_real)rgba[4 * i + 3];
+  }
+}
+
 void or_set_ll_store_limit(or_frame* f, const uint32_t* limit) { f->ll_limit = limit; }
 
 const void* or_buffer(const or_frame* f, int which, size_t* bytes) {

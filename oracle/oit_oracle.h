@@ -96,6 +96,11 @@ void or_composite(or_frame* f, uint8_t* out_rgba8, double* out_linear);
 void or_load_state(or_frame* f, const uint32_t* abuffer, const uint32_t* aux,
                    const uint32_t* counter);
 
+/* Replay: the colour target after tail blending (S*P premultiplied linear
+ * RGBA doubles) supplied by the caller, e.g. a GPU frame whose tail blends ran
+ * in arrival order. */
+void or_load_color(or_frame* f, const double* rgba);
+
 /* Per-pixel cap on stored linked-list nodes (replays the GPU's allocation
  * order on pool overflow); NULL disables. Array of render-size elements. */
 void or_set_ll_store_limit(or_frame* f, const uint32_t* limit);

@@ -58,6 +58,7 @@ def lib(variant='fp64'):
         L.or_inject_fragments.argtypes = [P, ctypes.c_int, P, P, P, P, P, P]
         L.or_composite.argtypes = [P, P, P]
         L.or_load_state.argtypes = [P, P, P, P]
+        L.or_load_color.argtypes = [P, P]
         L.or_set_ll_store_limit.argtypes = [P, P]
         L.or_buffer.restype = P
         L.or_buffer.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
@@ -165,6 +166,12 @@ class Frame:
         self._keep += [a, x, c]
         self.lib.or_load_state(self.f, None if a is None else a.ctypes.data, None if x is None else x.ctypes.data,
                                None if c is None else c.ctypes.data)
+
+    def load_color(self, color):
+        """The colour target after tail blending ((S*P, 4) premultiplied linear)."""
+        c = np.ascontiguousarray(color, np.float64)
+        self._keep.append(c)
+        self.lib.or_load_color(self.f, c.ctypes.data)
 
     def set_ll_store_limit(self, limit):
         lim = None if limit is None else np.ascontiguousarray(limit, np.uint32)

@@ -27,6 +27,7 @@ OIT_WEIGHTED_FP16, OIT_WEIGHTED_FP32 = 0, 1
 OIT_FLAG_LINEAR_OUTPUT = 0x1
 OIT_FLAG_CUDA_GRAPH = 0x2
 OIT_FLAG_HALF_COLOR = 0x4
+OIT_FLAG_ARRIVAL_ORDER = 0x8
 
 OIT_OK = 0
 OIT_ERR_INVALID_ARGUMENT = -1

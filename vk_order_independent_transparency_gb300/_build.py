@@ -16,7 +16,7 @@ LIB = os.path.join(PKG, 'liboit_gb300.so')
 BUILD = os.path.join(PKG, '_objs')
 
 CU_SOURCES = ['setup_bin.cu', 'raster_a.cu', 'raster_b.cu', 'raster_c.cu', 'composite.cu', 'resolve.cu',
-              'verify.cu', 'noalloc.cu']
+              'verify.cu', 'arrival.cu', 'noalloc.cu']
 CPP_SOURCES = ['engine.cpp', 'scene.cpp']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 

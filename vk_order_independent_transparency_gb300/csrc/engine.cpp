@@ -197,6 +197,7 @@ struct oit_context {
 
   oit::Alg alg() const { return static_cast<oit::Alg>(st.algorithm); }
   bool color_half() const { return (st.flags & OIT_FLAG_HALF_COLOR) != 0; }
+  bool arrival() const { return (st.flags & OIT_FLAG_ARRIVAL_ORDER) != 0; }
   size_t color_bytes() const { return color_half() ? 8 : 16; }
 
   // Views the batched resolve handles: linked list or Loop64, 1x, RGBA8 records.
@@ -392,6 +393,15 @@ struct oit_context {
     if (r != OIT_OK) return r;
     r = ensure_triangles(count);
     if (r != OIT_OK) return r;
+    if (arrival() && opaque_from == count) {
+      // an arrival-order draw without opaque triangles reads only the setup
+      // records and bboxes: no tile bins
+      oit::SetupParams sp = setup_params(mesh, first, count, opaque_from);
+      bin_tris = count;
+      bin_opaque_from = opaque_from;
+      OIT_TRY_CUDA(oit::bin_setup_only(sp, s, &launches), "setup");
+      return OIT_OK;
+    }
     const uint64_t key = ((uint64_t)first << 32) ^ ((uint64_t)count << 1) ^ ((uint64_t)opaque_from * 0x9E3779B1ull) ^
                          ((uint64_t)(uintptr_t)mesh.indices << 7) ^ ((uint64_t)(uintptr_t)mesh.instances << 3);
     PairStat* ps = pair_stat(key);
@@ -588,7 +598,41 @@ struct oit_context {
     return r;
   }
 
+  // The arrival-order linked-list COLOR pass (OIT_FLAG_ARRIVAL_ORDER).
+  int raster_arrival(cudaStream_t s) {
+    oit::ArrivalParams a{};
+    a.RW = RW;
+    a.RH = RH;
+    a.P = P;
+    a.num_tris = bin_opaque_from;  // the draw's transparent triangles
+    a.bbox = bbox.as<uint2>();
+    a.setup = setup.p;
+    a.depth = depth.as<uint32_t>();
+    a.opaque_color = opaque_color.as<float4>();
+    a.has_opaque = opaque_valid ? 1 : 0;
+    a.background = background;
+    a.color = color.as<float4>();
+    a.color_half = color_half() ? 1 : 0;
+    a.pool = abuf.as<uint32_t>();
+    a.heads = aux.as<uint32_t>();
+    a.counter = counter.as<uint32_t>();
+    a.capacity = capacity;
+    a.locks = auxdepth.as<uint32_t>();
+    a.tail = st.tail_blend ? 1 : 0;
+    a.error = err.as<uint32_t>();
+    a.frag_count = frag.as<unsigned long long>();
+    // the batched resolve's per-micro-tile list lengths are not counted: the
+    // most any list may hold
+    if (batch_resolvable()) OIT_TRY_CUDA(cudaMemsetAsync(lens.p, 0xFF, lens_count(), s), "lens");
+    cudaEvent_t t1 = prof_begin(s);
+    const cudaError_t e = oit::launch_arrival_ll(a, s, &launches);
+    prof_end(OIT_PROF_TRANSPARENT_RASTER, t1, s);
+    if (e == cudaSuccess) color_valid = true;
+    return cuda_status(e, "arrival raster");
+  }
+
   int raster_transparent(cudaStream_t s) {
+    if (arrival()) return raster_arrival(s);
     oit::RasterParams p = raster_params(num_tiles);
     cudaEvent_t t1 = prof_begin(s);
     const int r = raster(alg(), p, s);
@@ -906,6 +950,11 @@ int validate(const oit_state* s, int* msaa, int* ss, int* sup) {
   if (s->record_format > OIT_RECORD_RGBA32F || s->weighted_precision > OIT_WEIGHTED_FP32)
     return OIT_ERR_INVALID_ARGUMENT;
   if (!std::isfinite(s->alpha_min) || !std::isfinite(s->alpha_width)) return OIT_ERR_INVALID_ARGUMENT;
+  if (s->flags & OIT_FLAG_ARRIVAL_ORDER) {
+    // the arrival-order pass: linked list, one sample per pixel, RGBA8 nodes
+    if (s->algorithm != OIT_LINKEDLIST || *msaa != 1 || *ss || s->record_format != OIT_RECORD_RGBA8)
+      return OIT_ERR_UNSUPPORTED;
+  }
   if (s->record_format == OIT_RECORD_RGBA32F) {
     // float records exist for the linked list and Loop64 (whose float payloads
     // take 24 bytes of shared memory per layer and lane: 24 KB per warp at 32
@@ -1137,7 +1186,7 @@ int batch_mv_rasters(const oit_view_frame* views, uint32_t n, cudaStream_t s, ui
   for (uint32_t i = 0; i < n; ++i) {
     oit_context* c = views[i].ctx;
     if (c->frame_has_opaque) items.push_back({true, (int)oit::Alg::Opaque, c->S, 1, (uint64_t)c->P * c->S, c});
-    items.push_back({false, (int)c->alg(), c->ssn > 1 ? 1 : c->S, c->ssn, (uint64_t)c->P * c->ssn, c});
+    if (!c->arrival()) items.push_back({false, (int)c->alg(), c->ssn > 1 ? 1 : c->S, c->ssn, (uint64_t)c->P * c->ssn, c});
   }
   std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) {
     if (a.opaque != b.opaque) return a.opaque;
@@ -1174,6 +1223,15 @@ int batch_mv_rasters(const oit_view_frame* views, uint32_t n, cudaStream_t s, ui
     }
     ++*launches;
     if (e != cudaSuccess) return cuda_status(e, "multi-view raster");
+  }
+  for (uint32_t i = 0; i < n; ++i) {  // arrival-order passes are launched per view
+    oit_context* c = views[i].ctx;
+    if (!c->arrival()) continue;
+    const uint64_t l0 = c->launches;
+    const int r = c->raster_arrival(s);
+    *launches += c->launches - l0;
+    c->launches = l0;
+    if (r != OIT_OK) return r;
   }
   return OIT_OK;
 }

@@ -154,6 +154,31 @@ struct MvRaster {
   RasterParams v[kMvMaxViews];
 };
 
+// The arrival-order linked-list COLOR pass (1x): triangles [0, num_tris) of
+// the draw straight from their setup records, nodes linked by atomic head
+// exchanges, pool overflow tail-blended under per-pixel locks.
+struct ArrivalParams {
+  int RW, RH;
+  uint32_t P;
+  uint32_t num_tris;
+  const uint2* bbox;
+  const void* setup;
+  const uint32_t* depth;         // [P] opaque depth
+  const float4* opaque_color;    // [P]
+  int has_opaque;
+  float4 background;
+  float4* color;                 // [P] colour target (initialised by the pass)
+  int color_half;
+  uint32_t* pool;                // uint4 nodes
+  uint32_t* heads;               // [P]
+  uint32_t* counter;
+  uint32_t capacity;
+  uint32_t* locks;               // [P] spin words (zeroed by the pass)
+  int tail;
+  uint32_t* error;
+  unsigned long long* frag_count;
+};
+
 struct CompositeParams {
   int W, H;                      // output size
   int RW, RH;                    // render size
@@ -229,6 +254,9 @@ cudaError_t launch_raster_mv_a(Alg alg, const MvRaster& mv, cudaStream_t s);  //
 cudaError_t launch_raster_mv_b(Alg alg, const MvRaster& mv, cudaStream_t s);  // Loop, Loop64
 cudaError_t launch_raster_mv_c(Alg alg, const MvRaster& mv, cudaStream_t s);  // Spinlock, Interlock, Weighted
 cudaError_t launch_composite(Alg alg, const CompositeParams& p, cudaStream_t s);
+cudaError_t launch_arrival_ll(const ArrivalParams& p, cudaStream_t s, uint64_t* launches);  // arrival.cu
+// Setup only (a draw whose rasters need no tile bins).
+cudaError_t bin_setup_only(const SetupParams& sp, cudaStream_t s, uint64_t* launches);
 // FP64 verification resolve (verify.cu): the composite recomputed in double;
 // writes double4 linear colours to out_linear (may be null) and RGBA8 to
 // p.out_rgba8 (may be null).

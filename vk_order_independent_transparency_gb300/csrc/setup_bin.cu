@@ -502,6 +502,14 @@ cudaError_t launch_fill_f4(float4* dst, float4 value, size_t count, cudaStream_t
   return cudaGetLastError();
 }
 
+cudaError_t bin_setup_only(const SetupParams& sp, cudaStream_t s, uint64_t* launches) {
+  const uint32_t n = sp.num_triangles;
+  if (n == 0) return cudaSuccess;
+  k_setup<<<(n + 255) / 256, 256, 0, s>>>(sp, sp.samples > 1 ? sp.samples : 1);
+  ++*launches;
+  return cudaGetLastError();
+}
+
 // Binning, step 1: setup + pair counts + exclusive scan; the number of
 // (tile, triangle) pairs lands in b.total (device).
 cudaError_t bin_setup_scan(const SetupParams& sp, Bins& b, cudaStream_t s, uint64_t* launches) {
