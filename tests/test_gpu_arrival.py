@@ -33,15 +33,15 @@ def list_sets(g, o, P):
     return gl, ol
 
 
-def replay_image(g, W, H, L, npp, aa=0, tail=True, with_color=False):
-    """The oracle's composite of the GPU's pool, heads and counter (and its
-    colour target): the reference's composite on the GPU's arrival order."""
+def replay_image(g, W, H, L, npp, aa=0, tail=True):
+    """The oracle's composite of the GPU's pool, heads, counter and colour
+    target (opaque colour or background, plus any tail blends): the
+    reference's composite on the GPU's arrival order."""
     fr = orc.Frame(orc.LINKEDLIST, W, H, oit_layers=L, nodes_per_pixel=npp, aa_type=aa, tail_blend=tail)
     fr.begin()
     fr.clear_transparent()
     fr.load_state(g['abuf'], g['aux'], g['counter'])
-    if with_color:
-        fr.load_color(g['color'].astype(np.float64))
+    fr.load_color(g['color'].astype(np.float64))
     img, _ = fr.composite()
     return img
 
@@ -90,7 +90,7 @@ def test_arrival_pool_overflow(engine):
             rest.remove(e)  # each stored node is one of the pixel's fragments
         stored += len(a)
     assert stored == P - 1  # nodes 1 .. P-1
-    d = np.abs(g['image'].astype(np.int32) - replay_image(g, W, H, L, npp, with_color=True).astype(np.int32))
+    d = np.abs(g['image'].astype(np.int32) - replay_image(g, W, H, L, npp).astype(np.int32))
     assert d.max() <= 1
 
 
