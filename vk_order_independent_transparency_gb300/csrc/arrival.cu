@@ -7,8 +7,9 @@
 // fragments) and links itself in front of its pixel's list by an atomic
 // exchange of the head in HBM (imageAtomicExchange, :60-67). A fragment that
 // finds the pool full is blended into the colour target (:71-83) under a
-// per-pixel spinlock, in arrival order; the spin is bounded and a spin that
-// gives up raises OIT_DEVERR_TIMEOUT instead of blending.
+// per-pixel spinlock, in arrival order (lanes of one warp with the same pixel
+// in lane order); the spin is bounded and a spin that gives up raises
+// OIT_DEVERR_TIMEOUT instead of blending.
 //
 // Work: a warp takes 32 consecutive triangles of the pass and numbers the
 // pixels of their bboxes (a prefix sum over the bbox areas); lane g of each
@@ -59,7 +60,7 @@ __device__ __forceinline__ bool locked_tail_blend(const ArrivalParams& p, uint32
   return false;
 }
 
-__global__ void __launch_bounds__(32 * kArrivalWarps) k_arrival_ll(ArrivalParams p) {
+__global__ void __launch_bounds__(32 * kArrivalWarps, 4) k_arrival_ll(ArrivalParams p) {
   __shared__ unsigned long long pre_s[kArrivalWarps][32];  // exclusive prefix of the bbox areas
   __shared__ uint4 geo_s[kArrivalWarps][32];               // bbox x0, y0, width; triangle
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -138,6 +139,8 @@ __global__ void __launch_bounds__(32 * kArrivalWarps) k_arrival_ll(ArrivalParams
       uint32_t node0 = 0;
       if (lane == __ffs(m) - 1) node0 = atomicAdd(p.counter, (uint32_t)__popc(m));
       node0 = __shfl_sync(kFullMask, node0, __ffs(m) - 1);
+      bool pending = false;  // a tail blend to make
+      float4 src = make_float4(0.f, 0.f, 0.f, 0.f);
       if (frag) {
         const TriSetup& T = setup[tri];
         const int4 a = T.xy01, b = T.xy2f;
@@ -152,8 +155,18 @@ __global__ void __launch_bounds__(32 * kArrivalWarps) k_arrival_ll(ArrivalParams
           reinterpret_cast<uint4*>(p.pool)[node] = make_uint4(packed, zbits, 0u, old);
         } else if (p.tail) {
           const float al = __int_as_float(b.w);
-          if (!locked_tail_blend(p, pixel, make_float4(sh.r * al, sh.g * al, sh.b * al, al)))
-            atomicOr(p.error, OIT_DEVERR_TIMEOUT);
+          src = make_float4(sh.r * al, sh.g * al, sh.b * al, al);
+          pending = true;
+        }
+      }
+      // Tail blends: lanes of one warp that share a pixel take its lock one at
+      // a time, lowest lane (earliest node) first, so a lock is only ever
+      // contended by other warps, which run independently.
+      while (__any_sync(kFullMask, pending)) {
+        const uint32_t peers = __match_any_sync(kFullMask, pending ? pixel : 0xFFFFFFFFu);
+        if (pending && lane == __ffs(peers) - 1) {
+          if (!locked_tail_blend(p, pixel, src)) atomicOr(p.error, OIT_DEVERR_TIMEOUT);
+          pending = false;
         }
       }
       nfrag += (uint32_t)__popc(m);
