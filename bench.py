@@ -40,7 +40,12 @@ WORKLOADS = {
     'interlock_2560x1440_msaa8_L8_4096spheres': ('interlock', 2560, 1440, 8, 8, 4, 4096, 0.02, 0.08, 100, 0.2, 0.6),
     'simple_2560x1440_msaa8_L8_4096spheres': ('simple', 2560, 1440, 8, 8, 4, 4096, 0.02, 0.08, 100, 0.2, 0.6),
     'weighted_3840x2160_16384spheres': ('weighted', 3840, 2160, 8, 8, 0, 16384, 0.01, 0.05, 100, 0.05, 0.9),
+    'linkedlist_1920x1080_L16_1024spheres': ('linkedlist', 1920, 1080, 16, 8, 0, 1024, 0.03, 0.10, 100, 0.2, 0.6),
+    # the same frame with the COLOR pass in arrival order (OIT_FLAG_ARRIVAL_ORDER)
+    'linkedlist_arrival_1920x1080_L16_1024spheres': ('linkedlist', 1920, 1080, 16, 8, 0, 1024, 0.03, 0.10, 100, 0.2,
+                                                     0.6),
 }
+ARRIVAL_WORKLOADS = {'linkedlist_arrival_1920x1080_L16_1024spheres'}
 ALGS = ['simple', 'linkedlist', 'loop', 'loop64', 'spinlock', 'interlock', 'weighted']
 SEED = 2
 BATCH_WORKLOAD = 'batch_64views_ll_loop64_mixed_vs_fp32'
@@ -460,9 +465,10 @@ def run_gpu(a, wd, rank, world):
     v, i, tpo = oit.make_scene(wd['spheres'], seed=wd['seed'] + rank, radius_min=wd['radius_min'],
                                radius_max=wd['radius_max'])
     sd = oit.make_camera(W, H)
+    flags = oit.OIT_FLAG_CUDA_GRAPH | (oit.OIT_FLAG_ARRIVAL_ORDER if wd['workload'] in ARRIVAL_WORKLOADS else 0)
     st = oit.make_state(alg, W, H, oit_layers=wd['oit_layers'], nodes_per_pixel=wd['nodes_per_pixel'],
                         aa_type=wd['aa_type'], alpha_min=wd['alpha_min'], alpha_width=wd['alpha_width'],
-                        flags=oit.OIT_FLAG_CUDA_GRAPH)
+                        flags=flags)
     r = oit.Renderer(st)
     mesh = oit.DeviceMesh(v, i)
     r.update_scene(sd)
