@@ -258,24 +258,74 @@ typedef struct {
   int bx0, by0, bx1, by1;
 } tri_setup;
 
-/* Vertex layout: utilities_vk.h:48-88 (pos.xyz, normal.xyz, color.rgba; 40 B). */
+/* A clip-space vertex and the attributes the raster interpolates. */
+typedef struct { float x, y, z, w, vz, n[3]; } clip_vert;
+
+/* The vertex where edge a -> b crosses the near plane z = 0: attributes
+ * interpolated linearly at t = za / (za - zb), z exactly 0. */
+static clip_vert near_cut(const clip_vert* a, const clip_vert* b) {
+  float t = a->z / (a->z - b->z);
+  clip_vert r;
+  r.x = fmaf(t, b->x - a->x, a->x);
+  r.y = fmaf(t, b->y - a->y, a->y);
+  r.z = 0.0f;
+  r.w = fmaf(t, b->w - a->w, a->w);
+  r.vz = fmaf(t, b->vz - a->vz, a->vz);
+  for (int i = 0; i < 3; ++i) r.n[i] = fmaf(t, b->n[i] - a->n[i], a->n[i]);
+  return r;
+}
+
+static int setup_half(const or_frame* f, const clip_vert* cv, const float* v0, int cull_back, tri_setup* T);
+
+/* Vertex layout: utilities_vk.h:48-88 (pos.xyz, normal.xyz, color.rgba; 40 B).
+ * Returns a bit mask of the triangle's halves that reach the raster: a
+ * triangle wholly in front of the near plane has one (T[0]); one the plane
+ * crosses is clipped (Sutherland-Hodgman against z = 0 in clip space, over
+ * the edges 0->1, 1->2, 2->0) into a triangle (T[0]) or a quad split into the
+ * fan (0, 1, 2) = T[0] and (0, 2, 3) = T[1]. */
 static int setup_triangle(const or_frame* f, const float* pv, const float* view,
                           const float* vertices, const uint32_t* indices, uint32_t t,
-                          int cull_back, tri_setup* T) {
-  float cx[3], cy[3], cz[3], cw[3], vz[3], n[3][3];
+                          int cull_back, tri_setup T[2]) {
+  clip_vert cv[3];
   const float* v0 = vertices + 10 * (size_t)indices[3 * (size_t)t];
   for (int k = 0; k < 3; ++k) {
     const float* v = vertices + 10 * (size_t)indices[3 * (size_t)t + k];
     float x = v[0], y = v[1], z = v[2];
     /* object.vert.glsl:34-35: gl_Position = projView * pos; depth = (view * pos).z */
-    cx[k] = fmaf(pv[0], x, fmaf(pv[4], y, fmaf(pv[8], z, pv[12])));
-    cy[k] = fmaf(pv[1], x, fmaf(pv[5], y, fmaf(pv[9], z, pv[13])));
-    cz[k] = fmaf(pv[2], x, fmaf(pv[6], y, fmaf(pv[10], z, pv[14])));
-    cw[k] = fmaf(pv[3], x, fmaf(pv[7], y, fmaf(pv[11], z, pv[15])));
-    vz[k] = fmaf(view[2], x, fmaf(view[6], y, fmaf(view[10], z, view[14])));
-    n[k][0] = v[3]; n[k][1] = v[4]; n[k][2] = v[5];
+    cv[k].x = fmaf(pv[0], x, fmaf(pv[4], y, fmaf(pv[8], z, pv[12])));
+    cv[k].y = fmaf(pv[1], x, fmaf(pv[5], y, fmaf(pv[9], z, pv[13])));
+    cv[k].z = fmaf(pv[2], x, fmaf(pv[6], y, fmaf(pv[10], z, pv[14])));
+    cv[k].w = fmaf(pv[3], x, fmaf(pv[7], y, fmaf(pv[11], z, pv[15])));
+    cv[k].vz = fmaf(view[2], x, fmaf(view[6], y, fmaf(view[10], z, view[14])));
+    cv[k].n[0] = v[3]; cv[k].n[1] = v[4]; cv[k].n[2] = v[5];
   }
-  /* Triangles not wholly inside 0 <= z <= w, w > 0 are dropped (no clipping). */
+  int nin = (cv[0].z >= 0.0f) + (cv[1].z >= 0.0f) + (cv[2].z >= 0.0f);
+  if (nin == 3 || nin == 0) return setup_half(f, cv, v0, cull_back, &T[0]);
+  clip_vert poly[4];
+  int n = 0;
+  for (int k = 0; k < 3; ++k) {
+    const clip_vert* a = &cv[k];
+    const clip_vert* b = &cv[(k + 1) % 3];
+    int ina = a->z >= 0.0f, inb = b->z >= 0.0f;
+    if (ina) poly[n++] = *a;
+    if (ina != inb) poly[n++] = near_cut(a, b);
+  }
+  int mask = setup_half(f, poly, v0, cull_back, &T[0]);
+  if (n == 4) {
+    clip_vert second[3] = {poly[0], poly[2], poly[3]};
+    mask |= setup_half(f, second, v0, cull_back, &T[1]) << 1;
+  }
+  return mask;
+}
+
+/* One triangle of clip-space vertices: the 0 <= z <= w, w > 0 test (far
+ * plane and w <= 0: dropped), projection, snap, orientation, bbox, record. */
+static int setup_half(const or_frame* f, const clip_vert* cv, const float* v0, int cull_back, tri_setup* T) {
+  float cx[3], cy[3], cz[3], cw[3], vz[3], n[3][3];
+  for (int k = 0; k < 3; ++k) {
+    cx[k] = cv[k].x; cy[k] = cv[k].y; cz[k] = cv[k].z; cw[k] = cv[k].w; vz[k] = cv[k].vz;
+    n[k][0] = cv[k].n[0]; n[k][1] = cv[k].n[1]; n[k][2] = cv[k].n[2];
+  }
   for (int k = 0; k < 3; ++k)
     if (!(cw[k] > 0.0f) || !(cz[k] >= 0.0f) || !(cz[k] <= cw[k])) return 0;
   const float halfW = 0.5f * (float)f->RW, halfH = 0.5f * (float)f->RH;
@@ -754,8 +804,8 @@ static uint64_t raster_transparent(or_frame* f, const tri_setup* T, int loop_pas
  * kOrTile x kOrTile pixel tiles in primitive order (CSR lists). */
 enum { kOrTile = 32 };
 typedef struct {
-  tri_setup* T;
-  unsigned char* ok;
+  tri_setup* T;      /* two slots per triangle: its halves */
+  unsigned char* ok; /* bit mask of the triangle's halves */
   uint32_t* start; /* [tiles + 1] */
   uint32_t* list;  /* triangle slots, primitive order per tile */
   int tx, ty;
@@ -770,17 +820,17 @@ static void bins_free(or_bins* b) {
 
 static void bins_build(const or_frame* f, const float* pv, const float* view, const float* vertices,
                        const uint32_t* indices, uint32_t first, uint32_t count, int opaque, or_bins* b) {
-  b->T = (tri_setup*)xcalloc(count ? count : 1, sizeof(tri_setup));
+  b->T = (tri_setup*)xcalloc(2 * (size_t)(count ? count : 1), sizeof(tri_setup));
   b->ok = (unsigned char*)xcalloc(count ? count : 1, 1);
   OR_OMP("omp parallel for schedule(static)")
   for (int64_t i = 0; i < (int64_t)count; ++i)
-    b->ok[i] = (unsigned char)setup_triangle(f, pv, view, vertices, indices, first + (uint32_t)i, opaque, &b->T[i]);
+    b->ok[i] = (unsigned char)setup_triangle(f, pv, view, vertices, indices, first + (uint32_t)i, opaque, &b->T[2 * i]);
   b->tx = (f->RW + kOrTile - 1) / kOrTile;
   b->ty = (f->RH + kOrTile - 1) / kOrTile;
   const size_t nt = (size_t)b->tx * b->ty;
   b->start = (uint32_t*)xcalloc(nt + 1, sizeof(uint32_t));
-  for (uint32_t i = 0; i < count; ++i) {
-    if (!b->ok[i]) continue;
+  for (uint32_t i = 0; i < 2 * count; ++i) {
+    if (!((b->ok[i >> 1] >> (i & 1)) & 1)) continue;
     const tri_setup* T = &b->T[i];
     for (int y = T->by0 / kOrTile; y <= T->by1 / kOrTile; ++y)
       for (int x = T->bx0 / kOrTile; x <= T->bx1 / kOrTile; ++x) b->start[(size_t)y * b->tx + x + 1]++;
@@ -789,8 +839,8 @@ static void bins_build(const or_frame* f, const float* pv, const float* view, co
   b->list = (uint32_t*)xcalloc(b->start[nt] ? b->start[nt] : 1, sizeof(uint32_t));
   uint32_t* cur = (uint32_t*)xcalloc(nt ? nt : 1, sizeof(uint32_t));
   memcpy(cur, b->start, nt * sizeof(uint32_t));
-  for (uint32_t i = 0; i < count; ++i) {
-    if (!b->ok[i]) continue;
+  for (uint32_t i = 0; i < 2 * count; ++i) {
+    if (!((b->ok[i >> 1] >> (i & 1)) & 1)) continue;
     const tri_setup* T = &b->T[i];
     for (int y = T->by0 / kOrTile; y <= T->by1 / kOrTile; ++y)
       for (int x = T->bx0 / kOrTile; x <= T->bx1 / kOrTile; ++x) b->list[cur[(size_t)y * b->tx + x]++] = i;
@@ -821,9 +871,10 @@ void or_draw_transparent(or_frame* f, const float* pv, const float* view, const 
   for (int pass = 0; pass < passes; ++pass) {
     int loop_pass = (f->p.algorithm == OR_LOOP) ? pass : 1;
     for (uint32_t t = first; t < first + count; ++t) {
-      tri_setup T;
-      if (!setup_triangle(f, pv, view, vertices, indices, t, 0, &T)) continue;
-      f->fragments += raster_transparent(f, &T, loop_pass, 0, 0, f->RW - 1, f->RH - 1);
+      tri_setup T[2];
+      const int halves = setup_triangle(f, pv, view, vertices, indices, t, 0, T);
+      for (int h = 0; h < 2; ++h)
+        if ((halves >> h) & 1) f->fragments += raster_transparent(f, &T[h], loop_pass, 0, 0, f->RW - 1, f->RH - 1);
     }
   }
 #endif
@@ -877,9 +928,10 @@ void or_draw_opaque(or_frame* f, const float* pv, const float* view, const float
   bins_free(&b);
 #else
   for (uint32_t t = first; t < first + count; ++t) {
-    tri_setup T;
-    if (!setup_triangle(f, pv, view, vertices, indices, t, 1, &T)) continue;
-    raster_opaque(f, &T, 0, 0, f->RW - 1, f->RH - 1);
+    tri_setup T[2];
+    const int halves = setup_triangle(f, pv, view, vertices, indices, t, 1, T);
+    for (int h = 0; h < 2; ++h)
+      if ((halves >> h) & 1) raster_opaque(f, &T[h], 0, 0, f->RW - 1, f->RH - 1);
   }
 #endif
 }

@@ -223,3 +223,31 @@ def test_srgb_encode_is_exact(oracle_lib):
         assert L.or_srgb_encode(float(below)) == k
     assert L.or_srgb_encode(0.0) == 0 and L.or_srgb_encode(1.0) == 255
     assert L.or_srgb_encode(float('nan')) == 0
+
+
+def test_oracle_clips_at_the_near_plane(oracle_lib):
+    """A triangle with one vertex behind the near plane is drawn in part (the
+    part in front of the plane; fragments with window depth down to 0), one
+    wholly behind it is not drawn."""
+    import numpy as np
+    import vk_order_independent_transparency_gb300 as oit
+    W, H = 64, 48
+    sd = oit.make_camera(W, H, eye=(0.0, 0.0, 0.0), target=(0.0, 0.0, -1.0), z_near=0.5, z_far=10.0)
+    # a large triangle in the y = 0 plane reaching from 2 units in front to 0.2 (closer than near)
+    def tri(zs):
+        v = np.zeros((3, 10), np.float32)
+        v[:, 0] = [-1.0, 1.0, 0.0]
+        v[:, 1] = [-0.3, -0.3, 0.3]
+        v[:, 2] = zs
+        v[:, 4] = 1.0
+        v[:, 6:10] = [0.8, 0.4, 0.2, 1.0]
+        return v
+    idx = np.array([[0, 1, 2]], np.uint32)
+    fr = oracle_lib.render(oracle_lib.LINKEDLIST, W, H, sd, tri([-2.0, -2.0, -0.2]), idx, 1, 100, oit_layers=4)
+    n_cut = fr.fragment_count()
+    assert n_cut > 0
+    ab = fr.buffer(oracle_lib.BUF_ABUFFER).reshape(-1, 4)
+    depths = ab[1:n_cut + 1, 1].view(np.float32)
+    assert depths.min() < 0.05  # fragments reach the near plane
+    fr2 = oracle_lib.render(oracle_lib.LINKEDLIST, W, H, sd, tri([-0.3, -0.2, -0.1]), idx, 1, 100, oit_layers=4)
+    assert fr2.fragment_count() == 0

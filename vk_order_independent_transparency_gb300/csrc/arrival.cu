@@ -70,13 +70,17 @@ __global__ void __launch_bounds__(32 * kArrivalWarps, 4) k_arrival_ll(ArrivalPar
   const TriSetup* __restrict__ setup = reinterpret_cast<const TriSetup*>(p.setup);
   const uint32_t stride = gridDim.x * kArrivalWarps * 32u;
   uint32_t nfrag = 0;  // warp-uniform
-  for (uint32_t base = (blockIdx.x * kArrivalWarps + warp) * 32u; base < p.num_tris; base += stride) {
-    const uint32_t t = base + lane;
+  // entries [0, n): records 0 .. n-1; entries [n, 2n): the second halves of
+  // near-clipped triangles, records second_base + 0 .. n-1
+  for (uint32_t base = (blockIdx.x * kArrivalWarps + warp) * 32u; base < 2u * p.num_tris; base += stride) {
+    const uint32_t v = base + lane;
+    const bool second = v >= p.num_tris;
+    const uint32_t t = second ? p.second_base + (v - p.num_tris) : v;
     uint32_t x0 = 0, y0 = 0, wd = 1;
     unsigned long long area = 0;
-    if (t < p.num_tris) {
+    if (v < 2u * p.num_tris && (!second || (__ldg(&p.bbox[v - p.num_tris]).y >> 31))) {
       const uint2 bb = __ldg(&p.bbox[t]);
-      const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = bb.y >> 16;
+      const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = (bb.y >> 16) & 0x7FFF;
       if (bx0 <= bx1 && by0 <= by1) {  // culled triangles carry an empty bbox
         x0 = (uint32_t)bx0;
         y0 = (uint32_t)by0;
@@ -197,7 +201,7 @@ cudaError_t launch_arrival_ll(const ArrivalParams& p, cudaStream_t s, uint64_t* 
     if (e != cudaSuccess) return e;
   }
   if (p.num_tris) {
-    const size_t warps = ((size_t)p.num_tris + 31) / 32;
+    const size_t warps = (2 * (size_t)p.num_tris + 31) / 32;
     const unsigned blocks = (unsigned)std::min<size_t>((warps + kArrivalWarps - 1) / kArrivalWarps, 152 * 16);
     k_arrival_ll<<<blocks, 32 * kArrivalWarps, 0, s>>>(p);
     ++*launches;

@@ -273,9 +273,11 @@ struct oit_context {
   int ensure_triangles(size_t n) {
     if (n <= tri_cap) return OIT_OK;
     const size_t cap = std::max<size_t>(n, 1024);
-    OIT_TRY_CUDA(bbox.ensure(cap * 8), "alloc bbox");
-    OIT_TRY_CUDA(setup.ensure(cap * 96), "alloc setup");
-    if (alg() == oit::Alg::Weighted) OIT_TRY_CUDA(persp.ensure(cap * 32), "alloc persp");
+    // two records per triangle: the second half of a triangle the near plane
+    // splits lives at record count + t
+    OIT_TRY_CUDA(bbox.ensure(2 * cap * 8), "alloc bbox");
+    OIT_TRY_CUDA(setup.ensure(2 * cap * 96), "alloc setup");
+    if (alg() == oit::Alg::Weighted) OIT_TRY_CUDA(persp.ensure(2 * cap * 32), "alloc persp");
     OIT_TRY_CUDA(pair_count.ensure(cap * 4), "alloc pair_count");
     OIT_TRY_CUDA(pair_offset.ensure((cap + 1) * 4), "alloc pair_offset");
     tri_cap = cap;
@@ -605,6 +607,7 @@ struct oit_context {
     a.RH = RH;
     a.P = P;
     a.num_tris = bin_opaque_from;  // the draw's transparent triangles
+    a.second_base = bin_tris;
     a.bbox = bbox.as<uint2>();
     a.setup = setup.p;
     a.depth = depth.as<uint32_t>();

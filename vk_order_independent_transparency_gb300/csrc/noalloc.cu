@@ -140,9 +140,10 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   uint32_t* auxdepth = a.take<uint32_t>((size_t)P * 4);
   void* accum = weighted ? a.take<void>((size_t)S * P * (wf32 ? 16 : 8)) : nullptr;
   void* reveal = weighted ? a.take<void>((size_t)S * P * (wf32 ? 4 : 2)) : nullptr;
-  void* setup = a.take<void>((size_t)N * 96);
-  void* persp = weighted ? a.take<void>((size_t)N * 32) : nullptr;
-  uint2* bbox = a.take<uint2>((size_t)N * 8);
+  // two records per triangle (the second half of a near-clipped one at N + t)
+  void* setup = a.take<void>((size_t)N * 2 * 96);
+  void* persp = weighted ? a.take<void>((size_t)N * 2 * 32) : nullptr;
+  uint2* bbox = a.take<uint2>((size_t)N * 2 * 8);
   uint32_t* pair_count = a.take<uint32_t>((size_t)N * 4);
   uint32_t* pair_offset = a.take<uint32_t>(((size_t)N + 1) * 4);
   uint32_t* tile_begin = a.take<uint32_t>((size_t)2 * num_tiles * 4);

@@ -39,10 +39,13 @@ struct SetupParams {
   int tiles_x;
   int num_tiles;           // key = tile + (transparent ? num_tiles : 0)
   // outputs
-  uint2* bbox;            // [num_triangles] pixel bbox (x0 | y0 << 16, x1 | y1 << 16)
-  void* setup;            // [num_triangles] TriSetup records (96 B)
-  void* persp;            // [num_triangles] TriPersp records (32 B, WBOIT only) or null
-  uint32_t* pair_count;   // [num_triangles] tiles overlapped (0 = culled)
+  // Per record, 2 * num_triangles of them: record t is triangle t, or the
+  // first half of a triangle the near plane splits into two; its second half
+  // is record num_triangles + t.
+  uint2* bbox;            // pixel bbox (x0 | y0 << 16, x1 | y1 << 16); bit 31 of .y: a second half follows
+  void* setup;            // TriSetup records (96 B)
+  void* persp;            // TriPersp records (32 B, WBOIT only) or null
+  uint32_t* pair_count;   // [num_triangles] tiles overlapped by both halves (0 = culled)
 };
 
 // The engine's view of a frame's geometry: a flattened triangle mesh
@@ -161,6 +164,7 @@ struct ArrivalParams {
   int RW, RH;
   uint32_t P;
   uint32_t num_tris;
+  uint32_t second_base;          // the draw's triangle count: record of the second half of a near-clipped t
   const uint2* bbox;
   const void* setup;
   const uint32_t* depth;         // [P] opaque depth

@@ -483,7 +483,7 @@ __device__ __forceinline__ void cp_async_wait_all() {
 }
 
 __device__ __forceinline__ bool bbox_hits(uint2 bb, const WarpTile& w) {
-  const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = bb.y >> 16;
+  const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = (bb.y >> 16) & 0x7FFF;
   return !(bx1 < w.rx0 || bx0 > w.rx1 || by1 < w.ry0 || by0 > w.ry1);
 }
 
@@ -502,8 +502,11 @@ constexpr int kStageSlots = 32;
 // Mask (8x4 micro-tiles, one lane per pixel): the test is the micro-tile's bit
 // in the pair's sorted key (the binning wrote the bbox's micro-tile overlap
 // there), so only hits gather their bbox; else the bbox itself is tested.
-// List entries of triangles >= limit are skipped. With `ident` (an overflowed
-// draw's unbinned triangles) [beg, end) are triangle ids, each tested by bbox.
+// List entries of triangles >= limit are skipped (the second half of a
+// near-clipped triangle t, record num_tris + t, counts as triangle t). With
+// `ident` (an overflowed draw's unbinned triangles) entry i of [beg, end) is
+// half i & 1 of triangle i >> 1, tested by its bbox (a second half only when
+// the first's bbox says it exists).
 template <bool Mask, class Chunk>
 __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile& w, TriSetup* stage,
                                           uint32_t* stage_t, uint2* stage_bb, uint32_t beg, uint32_t end,
@@ -515,18 +518,24 @@ __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile&
   uint32_t t_next = 0;
   bool h_next = false;
   uint2 bb_next = make_uint2(0xFFFFFFFFu, 0u);  // empty bbox
+  auto orig = [&](uint32_t t) { return t >= p.num_tris ? t - p.num_tris : t; };
   auto fetch = [&](uint32_t i) {
-    t_next = ident ? i : __ldg(&p.tile_tris[i]);
-    if (use_mask) h_next = (__ldg(&p.tile_keys[i]) & mbit) != 0u && t_next < limit;
+    t_next = ident ? ((i & 1u) ? p.num_tris + (i >> 1) : (i >> 1)) : __ldg(&p.tile_tris[i]);
+    if (use_mask) h_next = (__ldg(&p.tile_keys[i]) & mbit) != 0u && orig(t_next) < limit;
+  };
+  // a second half exists when its first half's bbox says so
+  auto fetch_bb = [&](uint32_t i) {
+    if (ident && (i & 1u) && !(__ldg(&p.bbox[i >> 1]).y >> 31)) return make_uint2(0xFFFFFFFFu, 0u);
+    return __ldg(&p.bbox[t_next]);
   };
   if (beg + w.lane < end) {
     fetch(beg + w.lane);
-    if (!use_mask || h_next) bb_next = __ldg(&p.bbox[t_next]);
+    if (!use_mask || h_next) bb_next = fetch_bb(beg + w.lane);
   }
   for (uint32_t base = beg; base < end; base += 32) {
     const uint32_t t = t_next;
     const uint2 bb = bb_next;
-    const bool hit = (base + w.lane < end) && (use_mask ? h_next : (bbox_hits(bb, w) && t < limit));
+    const bool hit = (base + w.lane < end) && (use_mask ? h_next : (bbox_hits(bb, w) && orig(t) < limit));
     const uint32_t nb = base + 32;
     const bool more = nb + w.lane < end;
     if (more) fetch(nb + w.lane);
@@ -542,7 +551,7 @@ __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile&
       stage_bb[slot] = bb;
     };
     if (hit) stage_hit(rank);
-    bb_next = more && (!use_mask || h_next) ? __ldg(&p.bbox[t_next]) : make_uint2(0xFFFFFFFFu, 0u);
+    bb_next = more && (!use_mask || h_next) ? fetch_bb(nb + w.lane) : make_uint2(0xFFFFFFFFu, 0u);
     cp_async_wait_all();
     __syncwarp();
     if (m) chunk(__popc(m));
@@ -576,14 +585,14 @@ __device__ __forceinline__ void walk_pass(const RasterParams& p, const WarpTile&
 #pragma unroll 1
   for (uint32_t ph = 0; ph < nph; ++ph) {
     const bool ident = ph == 1;
-    walk_tile<Mask>(p, w, stage, stage_t, stage_bb, ident ? max(cut, p.pass_first) : beg, ident ? p.pass_end : end,
-                    ident, ident ? 0xFFFFFFFFu : cut, chunk);
+    walk_tile<Mask>(p, w, stage, stage_t, stage_bb, ident ? 2u * max(cut, p.pass_first) : beg,
+                    ident ? 2u * p.pass_end : end, ident, ident ? 0xFFFFFFFFu : cut, chunk);
   }
 }
 
 __device__ __forceinline__ bool lane_in_bbox(uint2 bb, const WarpTile& w) {
   return w.valid && w.px >= (int)(bb.x & 0xFFFF) && w.px <= (int)(bb.y & 0xFFFF) && w.py >= (int)(bb.x >> 16) &&
-         w.py <= (int)(bb.y >> 16);
+         w.py <= (int)((bb.y >> 16) & 0x7FFF);
 }
 
 // Per-warp fragment queue: coverage appends (stage slot, lane, coverage,
@@ -799,7 +808,7 @@ __device__ __forceinline__ void raster_transparent_body(const RasterParams& p, i
         ox = max((int)(bb.x & 0xFFFF), w.rx0);
         oy = max((int)(bb.x >> 16), w.ry0);
         const int x1 = min(min((int)(bb.y & 0xFFFF), w.rx1), p.RW - 1);
-        const int y1 = min(min((int)(bb.y >> 16), w.ry1), p.RH - 1);
+        const int y1 = min(min((int)((bb.y >> 16) & 0x7FFF), w.ry1), p.RH - 1);
         wd = x1 - ox + 1;
         const int ht = y1 - oy + 1;
         n = (wd > 0 && ht > 0) ? wd * ht : 0;

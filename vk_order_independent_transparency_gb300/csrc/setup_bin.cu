@@ -34,79 +34,51 @@ constexpr int kRadixBits = 8;
 constexpr int kRadixBins = 1 << kRadixBits;
 
 // ---------------------------------------------------------------------------
-// Setup (object.vert.glsl:32-39 + viewport transform + triangle setup)
+// Setup (object.vert.glsl:32-39 + near-plane clip + viewport transform +
+// triangle setup)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.num_triangles) return;
-  const uint32_t tg = p.first_triangle + t;
-  const float* __restrict__ vtx = p.vertices;
-  // Flattened mesh: 10 floats per vertex, colour of the first vertex. Instanced:
-  // template vertex (6 floats) scaled by the instance's radius and moved to its
-  // centre, one multiply and one add each rounded (as a flattened copy of the
-  // template is built on the host), colour of the instance.
-  const float* inst = nullptr;
-  uint32_t tri = tg;
-  if (p.instances) {
-    const uint32_t o = tg / p.template_triangles;
-    tri = tg - o * p.template_triangles;
-    inst = p.instances + 8 * (size_t)o;
-  }
-  const uint32_t i0 = __ldg(&p.indices[3 * (size_t)tri + 0]);
-  const uint32_t i1 = __ldg(&p.indices[3 * (size_t)tri + 1]);
-  const uint32_t i2 = __ldg(&p.indices[3 * (size_t)tri + 2]);
-  const uint32_t vid[3] = {i0, i1, i2};
-  float cx[3], cy[3], cz[3], cw[3], vz[3], nx[3], ny[3], nz[3];
-  // scene constants from device memory (every thread reads the same 80 bytes)
-  float m[16], v[16];
-  {
-    const float4* sc = reinterpret_cast<const float4*>(p.scene);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const float4 c = __ldg(sc + k);
-      m[4 * k + 0] = c.x;
-      m[4 * k + 1] = c.y;
-      m[4 * k + 2] = c.z;
-      m[4 * k + 3] = c.w;
-    }
-    // of the view matrix only row 2 (view-space z) is used: columns' z entries
-#pragma unroll
-    for (int k = 0; k < 4; ++k) v[4 * k + 2] = __ldg(p.scene + 16 + 4 * k + 2);
-  }
-  float4 ic = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
-  if (inst) ic = __ldg(reinterpret_cast<const float4*>(inst));
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float* pv = inst ? vtx + 6 * (size_t)vid[k] : vtx + 10 * (size_t)vid[k];
-    float x = __ldg(pv + 0), y = __ldg(pv + 1), z = __ldg(pv + 2);
-    if (inst) {
-      x = __fadd_rn(__fmul_rn(x, ic.w), ic.x);
-      y = __fadd_rn(__fmul_rn(y, ic.w), ic.y);
-      z = __fadd_rn(__fmul_rn(z, ic.w), ic.z);
-    }
-    cx[k] = __fmaf_rn(m[0], x, __fmaf_rn(m[4], y, __fmaf_rn(m[8], z, m[12])));
-    cy[k] = __fmaf_rn(m[1], x, __fmaf_rn(m[5], y, __fmaf_rn(m[9], z, m[13])));
-    cz[k] = __fmaf_rn(m[2], x, __fmaf_rn(m[6], y, __fmaf_rn(m[10], z, m[14])));
-    cw[k] = __fmaf_rn(m[3], x, __fmaf_rn(m[7], y, __fmaf_rn(m[11], z, m[15])));
-    vz[k] = __fmaf_rn(v[2], x, __fmaf_rn(v[6], y, __fmaf_rn(v[10], z, v[14])));
-    nx[k] = __ldg(pv + 3);
-    ny[k] = __ldg(pv + 4);
-    nz[k] = __ldg(pv + 5);
-  }
-  uint32_t pairs = 0;
+// One clip-space vertex with the attributes the raster interpolates.
+struct ClipVert {
+  float x, y, z, w, vz, nx, ny, nz;
+};
+
+// The vertex where edge a -> b crosses the near plane z = 0 (Vulkan clip
+// space): attributes interpolated linearly at t = za / (za - zb), z exactly 0.
+__device__ __forceinline__ ClipVert near_cut(const ClipVert& a, const ClipVert& b) {
+  const float t = __fdiv_rn(a.z, __fsub_rn(a.z, b.z));
+  ClipVert r;
+  r.x = __fmaf_rn(t, __fsub_rn(b.x, a.x), a.x);
+  r.y = __fmaf_rn(t, __fsub_rn(b.y, a.y), a.y);
+  r.z = 0.0f;
+  r.w = __fmaf_rn(t, __fsub_rn(b.w, a.w), a.w);
+  r.vz = __fmaf_rn(t, __fsub_rn(b.vz, a.vz), a.vz);
+  r.nx = __fmaf_rn(t, __fsub_rn(b.nx, a.nx), a.nx);
+  r.ny = __fmaf_rn(t, __fsub_rn(b.ny, a.ny), a.ny);
+  r.nz = __fmaf_rn(t, __fsub_rn(b.nz, a.nz), a.nz);
+  return r;
+}
+
+// Setup of one triangle of clip-space vertices into record `slot`: the
+// 0 <= z <= w, w > 0 test, projection, snap, orientation (back faces culled
+// for opaque triangles), bbox, the small-triangle sample test and the record.
+// Writes bbox[slot] (empty when dropped, bit 31 of .y = has_second) and
+// returns the number of tiles the bbox overlaps (0 when dropped).
+__device__ __forceinline__ uint32_t setup_half(const SetupParams& p, int S, uint32_t slot, bool opaque,
+                                               const ClipVert (&cv)[3], const float* c0, bool has_second) {
+  const uint32_t second_bit = has_second ? 0x80000000u : 0u;
   bool ok = true;
 #pragma unroll
   for (int k = 0; k < 3; ++k)
-    if (!(cw[k] > 0.0f) || !(cz[k] >= 0.0f) || !(cz[k] <= cw[k])) ok = false;
+    if (!(cv[k].w > 0.0f) || !(cv[k].z >= 0.0f) || !(cv[k].z <= cv[k].w)) ok = false;
   int X[3], Y[3];
   float zz[3], q[3];
   if (ok) {
     const float halfW = 0.5f * (float)p.RW, halfH = 0.5f * (float)p.RH;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      q[k] = __fdiv_rn(1.0f, cw[k]);
-      const float ndx = __fmul_rn(cx[k], q[k]), ndy = __fmul_rn(cy[k], q[k]);
-      zz[k] = __fmul_rn(cz[k], q[k]);
+      q[k] = __fdiv_rn(1.0f, cv[k].w);
+      const float ndx = __fmul_rn(cv[k].x, q[k]), ndy = __fmul_rn(cv[k].y, q[k]);
+      zz[k] = __fmul_rn(cv[k].z, q[k]);
       const float sx = __fmaf_rn(ndx, halfW, halfW), sy = __fmaf_rn(ndy, halfH, halfH);
       if (!(fabsf(sx) < 16384.0f) || !(fabsf(sy) < 16384.0f)) ok = false;
       X[k] = __float2int_rn(__fmul_rn(sx, 256.0f));
@@ -120,7 +92,7 @@ __global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
     // area > 0: clockwise on the y-down framebuffer = back face for
     // VK_FRONT_FACE_COUNTER_CLOCKWISE (main.cpp:520-525); only opaque
     // triangles cull back faces (transparent ones are double-sided, oit.cpp:703).
-    if (area > 0 && t >= p.opaque_from) ok = false;
+    if (area > 0 && opaque) ok = false;
   }
   int o1 = 1, o2 = 2;
   if (ok && area < 0) {
@@ -165,40 +137,129 @@ __global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
         }
     if (!any) ok = false;
   }
-  if (ok) {
-    const int order[3] = {0, o1, o2};
-    TriSetup T;
-    T.xy01 = make_int4(PX[0], PY[0], PX[1], PY[1]);
-    const float* c0 = inst ? inst + 4 : vtx + 10 * (size_t)i0 + 6;  // color.rgba
-    float alpha = __fmaf_rn(__ldg(c0 + 3), p.alpha_width, p.alpha_min);
-    alpha = (alpha > 0.0f) ? alpha : 0.0f;
-    alpha = (alpha < 1.0f) ? alpha : 1.0f;
-    const int acode = __float2int_rn(__fmul_rn(alpha, 255.0f));
-    const int minX = min(PX[0], min(PX[1], PX[2])), maxX = max(PX[0], max(PX[1], PX[2]));
-    const int minY = min(PY[0], min(PY[1], PY[2])), maxY = max(PY[0], max(PY[1], PY[2]));
-    const int small = (maxX - minX < kSmallExtent && maxY - minY < kSmallExtent) ? kFlagSmall : 0;
-    T.xy2f = make_int4(PX[2], PY[2], tl | small | (acode << 8), __float_as_int(alpha));
-    const float z0 = zz[0], z1 = zz[order[1]], z2 = zz[order[2]];
-    T.zc = make_float4(z0, __fsub_rn(z1, z0), __fsub_rn(z2, z0), __fdiv_rn(1.0f, __ll2float_rn(area)));
-    const float q0 = q[0], q1 = q[order[1]], q2 = q[order[2]];
-    const int j1 = order[1], j2 = order[2];
-    T.n0 = make_float4(__fmul_rn(nx[0], q0), __fmul_rn(ny[0], q0), __fmul_rn(nz[0], q0), __ldg(c0 + 0));
-    T.n1 = make_float4(__fmul_rn(nx[j1], q1), __fmul_rn(ny[j1], q1), __fmul_rn(nz[j1], q1), __ldg(c0 + 1));
-    T.n2 = make_float4(__fmul_rn(nx[j2], q2), __fmul_rn(ny[j2], q2), __fmul_rn(nz[j2], q2), __ldg(c0 + 2));
-    reinterpret_cast<TriSetup*>(p.setup)[t] = T;
-    if (p.persp) {
-      TriPersp Q;
-      Q.q = make_float4(q0, q1, q2, 0.0f);
-      Q.vzq = make_float4(__fmul_rn(vz[0], q0), __fmul_rn(vz[j1], q1), __fmul_rn(vz[j2], q2), 0.0f);
-      reinterpret_cast<TriPersp*>(p.persp)[t] = Q;
-    }
-    p.bbox[t] = make_uint2((uint32_t)bx0 | ((uint32_t)by0 << 16), (uint32_t)bx1 | ((uint32_t)by1 << 16));
-    const int tx0 = bx0 / kTile, tx1 = bx1 / kTile, ty0 = by0 / kTile, ty1 = by1 / kTile;
-    pairs = (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
-  } else {
+  if (!ok) {
     // an empty bbox (x0 > x1): the unbinned walk of an overflowed frame
     // tests every triangle's bbox
-    p.bbox[t] = make_uint2(0xFFFFFFFFu, 0u);
+    p.bbox[slot] = make_uint2(0xFFFFFFFFu, second_bit);
+    return 0;
+  }
+  const int order[3] = {0, o1, o2};
+  TriSetup T;
+  T.xy01 = make_int4(PX[0], PY[0], PX[1], PY[1]);
+  float alpha = __fmaf_rn(__ldg(c0 + 3), p.alpha_width, p.alpha_min);
+  alpha = (alpha > 0.0f) ? alpha : 0.0f;
+  alpha = (alpha < 1.0f) ? alpha : 1.0f;
+  const int acode = __float2int_rn(__fmul_rn(alpha, 255.0f));
+  const int minX = min(PX[0], min(PX[1], PX[2])), maxX = max(PX[0], max(PX[1], PX[2]));
+  const int minY = min(PY[0], min(PY[1], PY[2])), maxY = max(PY[0], max(PY[1], PY[2]));
+  const int small = (maxX - minX < kSmallExtent && maxY - minY < kSmallExtent) ? kFlagSmall : 0;
+  T.xy2f = make_int4(PX[2], PY[2], tl | small | (acode << 8), __float_as_int(alpha));
+  const float z0 = zz[0], z1 = zz[order[1]], z2 = zz[order[2]];
+  T.zc = make_float4(z0, __fsub_rn(z1, z0), __fsub_rn(z2, z0), __fdiv_rn(1.0f, __ll2float_rn(area)));
+  const float q0 = q[0], q1 = q[order[1]], q2 = q[order[2]];
+  const ClipVert& v1 = cv[order[1]];
+  const ClipVert& v2 = cv[order[2]];
+  T.n0 = make_float4(__fmul_rn(cv[0].nx, q0), __fmul_rn(cv[0].ny, q0), __fmul_rn(cv[0].nz, q0), __ldg(c0 + 0));
+  T.n1 = make_float4(__fmul_rn(v1.nx, q1), __fmul_rn(v1.ny, q1), __fmul_rn(v1.nz, q1), __ldg(c0 + 1));
+  T.n2 = make_float4(__fmul_rn(v2.nx, q2), __fmul_rn(v2.ny, q2), __fmul_rn(v2.nz, q2), __ldg(c0 + 2));
+  reinterpret_cast<TriSetup*>(p.setup)[slot] = T;
+  if (p.persp) {
+    TriPersp Q;
+    Q.q = make_float4(q0, q1, q2, 0.0f);
+    Q.vzq = make_float4(__fmul_rn(cv[0].vz, q0), __fmul_rn(v1.vz, q1), __fmul_rn(v2.vz, q2), 0.0f);
+    reinterpret_cast<TriPersp*>(p.persp)[slot] = Q;
+  }
+  p.bbox[slot] =
+      make_uint2((uint32_t)bx0 | ((uint32_t)by0 << 16), ((uint32_t)bx1 | ((uint32_t)by1 << 16)) | second_bit);
+  const int tx0 = bx0 / kTile, tx1 = bx1 / kTile, ty0 = by0 / kTile, ty1 = by1 / kTile;
+  return (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
+}
+
+__global__ void __launch_bounds__(256) k_setup(SetupParams p, int S) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.num_triangles) return;
+  const uint32_t tg = p.first_triangle + t;
+  const float* __restrict__ vtx = p.vertices;
+  // Flattened mesh: 10 floats per vertex, colour of the first vertex. Instanced:
+  // template vertex (6 floats) scaled by the instance's radius and moved to its
+  // centre, one multiply and one add each rounded (as a flattened copy of the
+  // template is built on the host), colour of the instance.
+  const float* inst = nullptr;
+  uint32_t tri = tg;
+  if (p.instances) {
+    const uint32_t o = tg / p.template_triangles;
+    tri = tg - o * p.template_triangles;
+    inst = p.instances + 8 * (size_t)o;
+  }
+  const uint32_t i0 = __ldg(&p.indices[3 * (size_t)tri + 0]);
+  const uint32_t i1 = __ldg(&p.indices[3 * (size_t)tri + 1]);
+  const uint32_t i2 = __ldg(&p.indices[3 * (size_t)tri + 2]);
+  const uint32_t vid[3] = {i0, i1, i2};
+  ClipVert cv[3];
+  // scene constants from device memory (every thread reads the same 80 bytes)
+  float m[16], v[16];
+  {
+    const float4* sc = reinterpret_cast<const float4*>(p.scene);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float4 c = __ldg(sc + k);
+      m[4 * k + 0] = c.x;
+      m[4 * k + 1] = c.y;
+      m[4 * k + 2] = c.z;
+      m[4 * k + 3] = c.w;
+    }
+    // of the view matrix only row 2 (view-space z) is used: columns' z entries
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[4 * k + 2] = __ldg(p.scene + 16 + 4 * k + 2);
+  }
+  float4 ic = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+  if (inst) ic = __ldg(reinterpret_cast<const float4*>(inst));
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float* pv = inst ? vtx + 6 * (size_t)vid[k] : vtx + 10 * (size_t)vid[k];
+    float x = __ldg(pv + 0), y = __ldg(pv + 1), z = __ldg(pv + 2);
+    if (inst) {
+      x = __fadd_rn(__fmul_rn(x, ic.w), ic.x);
+      y = __fadd_rn(__fmul_rn(y, ic.w), ic.y);
+      z = __fadd_rn(__fmul_rn(z, ic.w), ic.z);
+    }
+    cv[k].x = __fmaf_rn(m[0], x, __fmaf_rn(m[4], y, __fmaf_rn(m[8], z, m[12])));
+    cv[k].y = __fmaf_rn(m[1], x, __fmaf_rn(m[5], y, __fmaf_rn(m[9], z, m[13])));
+    cv[k].z = __fmaf_rn(m[2], x, __fmaf_rn(m[6], y, __fmaf_rn(m[10], z, m[14])));
+    cv[k].w = __fmaf_rn(m[3], x, __fmaf_rn(m[7], y, __fmaf_rn(m[11], z, m[15])));
+    cv[k].vz = __fmaf_rn(v[2], x, __fmaf_rn(v[6], y, __fmaf_rn(v[10], z, v[14])));
+    cv[k].nx = __ldg(pv + 3);
+    cv[k].ny = __ldg(pv + 4);
+    cv[k].nz = __ldg(pv + 5);
+  }
+  const float* c0 = inst ? inst + 4 : vtx + 10 * (size_t)i0 + 6;  // color.rgba
+  const bool opaque = t >= p.opaque_from;
+  const int nin = (cv[0].z >= 0.0f) + (cv[1].z >= 0.0f) + (cv[2].z >= 0.0f);
+  uint32_t pairs;
+  if (nin == 3 || nin == 0) {
+    // wholly in front of the near plane, or wholly behind it (dropped by the
+    // clip-volume test)
+    pairs = setup_half(p, S, t, opaque, cv, c0, false);
+  } else {
+    // Sutherland-Hodgman against z = 0 over the edges 0->1, 1->2, 2->0: the
+    // polygon keeps the triangle's winding; 3 vertices, or 4 split into the
+    // fan (0, 1, 2) + (0, 2, 3), the second half at record num_triangles + t
+    ClipVert poly[4];
+    int n = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const ClipVert& a = cv[k];
+      const ClipVert& b = cv[(k + 1) % 3];
+      const bool ina = a.z >= 0.0f, inb = b.z >= 0.0f;
+      if (ina) poly[n++] = a;
+      if (ina != inb) poly[n++] = near_cut(a, b);
+    }
+    const ClipVert first[3] = {poly[0], poly[1], poly[2]};
+    pairs = setup_half(p, S, t, opaque, first, c0, n == 4);
+    if (n == 4) {
+      const ClipVert second[3] = {poly[0], poly[2], poly[3]};
+      pairs += setup_half(p, S, p.num_triangles + t, opaque, second, c0, false);
+    }
   }
   p.pair_count[t] = pairs;
 }
@@ -332,6 +393,31 @@ cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, size_t n, uint32_t
 // ---------------------------------------------------------------------------
 // Pair emission: pair j of triangle t lands at pair_offset[t] + j.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t emit_bbox(uint2 bb, uint32_t t, uint32_t tile_base, int tiles_x, uint32_t off,
+                                              uint32_t j, uint32_t* __restrict__ keys, uint32_t* __restrict__ tris,
+                                              size_t capacity) {
+  const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = (bb.y >> 16) & 0x7FFF;
+  if (bx0 > bx1 || by0 > by1) return j;
+  const int tx0 = bx0 / kTile, ty0 = by0 / kTile, tx1 = bx1 / kTile, ty1 = by1 / kTile;
+  for (int ty = ty0; ty <= ty1; ++ty) {
+    // rows of 8x4 micro-tiles the bbox overlaps in this tile row
+    const int ly0 = max(by0 - ty * kTile, 0), ly1 = min(by1 - ty * kTile, kTile - 1);
+    uint32_t rows = 0;
+    for (int r = ly0 >> 2; r <= (ly1 >> 2); ++r) rows |= 3u << (2 * r);
+    for (int tx = tx0; tx <= tx1; ++tx, ++j) {
+      const size_t pos = (size_t)off + j;
+      if (pos >= capacity) return j;
+      const int lx0 = max(bx0 - tx * kTile, 0), lx1 = min(bx1 - tx * kTile, kTile - 1);
+      const uint32_t cols = (lx0 <= 7 ? 0x55u : 0u) | (lx1 >= 8 ? 0xAAu : 0u);
+      keys[pos] = (tile_base + (uint32_t)(ty * tiles_x + tx)) | ((rows & cols) << kMaskShift);
+      tris[pos] = t;
+    }
+  }
+  return j;
+}
+
+// The pairs of triangle t: its first (or only) half's tiles, then the second
+// half's (record n + t) when the near-plane clip split it.
 __global__ void __launch_bounds__(256) k_emit(const uint32_t* __restrict__ pair_count,
                                               const uint32_t* __restrict__ pair_offset, const uint2* __restrict__ bbox,
                                               uint32_t n, int tiles_x, uint32_t opaque_from, uint32_t num_tiles,
@@ -344,25 +430,9 @@ __global__ void __launch_bounds__(256) k_emit(const uint32_t* __restrict__ pair_
   if (!c) return;
   const uint32_t off = pair_offset[t];
   const uint2 bb = bbox[t];
-  const int tx0 = (bb.x & 0xFFFF) / kTile, ty0 = (bb.x >> 16) / kTile;
-  const int tx1 = (bb.y & 0xFFFF) / kTile, ty1 = (bb.y >> 16) / kTile;
   const uint32_t tile_base = t < opaque_from ? num_tiles : 0u;
-  const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = bb.y >> 16;
-  uint32_t j = 0;
-  for (int ty = ty0; ty <= ty1; ++ty) {
-    // rows of 8x4 micro-tiles the bbox overlaps in this tile row
-    const int ly0 = max(by0 - ty * kTile, 0), ly1 = min(by1 - ty * kTile, kTile - 1);
-    uint32_t rows = 0;
-    for (int r = ly0 >> 2; r <= (ly1 >> 2); ++r) rows |= 3u << (2 * r);
-    for (int tx = tx0; tx <= tx1; ++tx, ++j) {
-      const size_t pos = (size_t)off + j;
-      if (pos >= capacity) return;
-      const int lx0 = max(bx0 - tx * kTile, 0), lx1 = min(bx1 - tx * kTile, kTile - 1);
-      const uint32_t cols = (lx0 <= 7 ? 0x55u : 0u) | (lx1 >= 8 ? 0xAAu : 0u);
-      keys[pos] = (tile_base + (uint32_t)(ty * tiles_x + tx)) | ((rows & cols) << kMaskShift);
-      tris[pos] = t;
-    }
-  }
+  const uint32_t j = emit_bbox(bb, t, tile_base, tiles_x, off, 0u, keys, tris, capacity);
+  if (bb.y >> 31) emit_bbox(bbox[n + t], n + t, tile_base, tiles_x, off, j, keys, tris, capacity);
 }
 
 // ---------------------------------------------------------------------------
