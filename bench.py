@@ -81,6 +81,9 @@ def parse():
                     help='batch workload: the first N of its 64 views (smaller cases for profiling)')
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--raster-config', default='auto', choices=['auto', 'per-view', 'per-view-32', 'multi-view'],
+                    help='batch workload: pin the tile-raster configuration instead of letting the graph capture '
+                         'time the candidates (profilers distort those timings)')
     return ap.parse_args()
 
 
@@ -570,7 +573,10 @@ def run_batch(a, rank):
                                             record_format=fmt, flags=flags))
             r.update_scene(sd)
             recs.append(r)
+    raster_pin = {'auto': None, 'per-view': {'multi_view': 0}, 'per-view-32': {'multi_view': 0, 'warps_per_sm': 32},
+                  'multi-view': {'multi_view': 1}}[a.raster_config]
     batch = oit.Batch(parallel_streams=8)
+    batch.set_raster_config(raster_pin)
     batch.set_views([(r, m, h[2], 100) for r, m, h in zip(mixed, meshes, host)])
 
     def step_mixed():
@@ -629,6 +635,7 @@ def run_batch(a, rank):
         ra.update_scene(oit.make_camera(vd['width'], vd['height']))
         arrival.append(ra)
     batch_arr = oit.Batch(parallel_streams=8)
+    batch_arr.set_raster_config(raster_pin)
     batch_arr.set_views([(r, m, h[2], 100) for r, m, h in zip(arrival, meshes, host)])
     for _ in range(max(3, a.warmup)):
         batch_arr.render(stream)
@@ -691,6 +698,7 @@ def run_batch(a, rank):
         out_dev = torch.empty(int(out_at[-1]), dtype=torch.uint8, device='cuda')
         out_host = torch.empty(int(out_at[-1]), dtype=torch.uint8).pin_memory()
         bt = oit.Batch(parallel_streams=8)
+        bt.set_raster_config(raster_pin)
         bt.set_views([(r, m, 0, 100, out_dev.data_ptr() + int(o)) for r, m, o in zip(mixed, inst_views, out_at)])
         pipe.append(dict(scene=scene_dev, out=out_dev, host=out_host, batch=bt, meshes=inst_views,
                          uploaded=torch.cuda.Event(), rendered=torch.cuda.Event(), read=torch.cuda.Event()))

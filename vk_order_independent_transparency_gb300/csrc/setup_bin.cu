@@ -175,41 +175,14 @@ __device__ __forceinline__ uint32_t setup_half(const SetupParams& p, int S, uint
   return (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
 }
 
-// A triangle the near plane crosses: Sutherland-Hodgman against z = 0 over
-// the edges 0->1, 1->2, 2->0 keeps the triangle's winding; 3 vertices give one
-// triangle (record t), 4 the fan (0, 1, 2) in record t and (0, 2, 3) in record
-// num_triangles + t. Out of line: rare, and it keeps the common path's
-// registers down.
-__device__ __noinline__ uint32_t setup_clipped(const SetupParams& p, int S, uint32_t t, bool opaque,
-                                               const ClipVert (&cv)[3], const float* c0) {
-  ClipVert poly[4];
-  int n = 0;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const ClipVert& a = cv[k];
-    const ClipVert& b = cv[(k + 1) % 3];
-    const bool ina = a.z >= 0.0f, inb = b.z >= 0.0f;
-    if (ina) poly[n++] = a;
-    if (ina != inb) poly[n++] = near_cut(a, b);
-  }
-  const ClipVert first[3] = {poly[0], poly[1], poly[2]};
-  uint32_t pairs = setup_half(p, S, t, opaque, first, c0, n == 4);
-  if (n == 4) {
-    const ClipVert second[3] = {poly[0], poly[2], poly[3]};
-    pairs += setup_half(p, S, p.num_triangles + t, opaque, second, c0, false);
-  }
-  return pairs;
-}
-
-__global__ void __launch_bounds__(256, 4) k_setup(SetupParams p, int S) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.num_triangles) return;
+// Triangle t's clip-space vertices (object.vert.glsl:32-39) and colour.
+// Flattened mesh: 10 floats per vertex, colour of the first vertex.
+// Instanced: template vertex (6 floats) scaled by the instance's radius and
+// moved to its centre, one multiply and one add each rounded (as a flattened
+// copy of the template is built on the host), colour of the instance.
+__device__ __forceinline__ const float* clip_vertices(const SetupParams& p, uint32_t t, ClipVert (&cv)[3]) {
   const uint32_t tg = p.first_triangle + t;
   const float* __restrict__ vtx = p.vertices;
-  // Flattened mesh: 10 floats per vertex, colour of the first vertex. Instanced:
-  // template vertex (6 floats) scaled by the instance's radius and moved to its
-  // centre, one multiply and one add each rounded (as a flattened copy of the
-  // template is built on the host), colour of the instance.
   const float* inst = nullptr;
   uint32_t tri = tg;
   if (p.instances) {
@@ -221,7 +194,6 @@ __global__ void __launch_bounds__(256, 4) k_setup(SetupParams p, int S) {
   const uint32_t i1 = __ldg(&p.indices[3 * (size_t)tri + 1]);
   const uint32_t i2 = __ldg(&p.indices[3 * (size_t)tri + 2]);
   const uint32_t vid[3] = {i0, i1, i2};
-  ClipVert cv[3];
   // scene constants from device memory (every thread reads the same 80 bytes)
   float m[16], v[16];
   {
@@ -258,13 +230,47 @@ __global__ void __launch_bounds__(256, 4) k_setup(SetupParams p, int S) {
     cv[k].ny = __ldg(pv + 4);
     cv[k].nz = __ldg(pv + 5);
   }
-  const float* c0 = inst ? inst + 4 : vtx + 10 * (size_t)i0 + 6;  // color.rgba
+  return inst ? inst + 4 : vtx + 10 * (size_t)i0 + 6;  // color.rgba
+}
+
+// A triangle the near plane crosses: Sutherland-Hodgman against z = 0 over
+// the edges 0->1, 1->2, 2->0 keeps the triangle's winding; 3 vertices give one
+// triangle (record t), 4 the fan (0, 1, 2) in record t and (0, 2, 3) in record
+// num_triangles + t. Out of line and from the mesh again: rare, and the common
+// path keeps its vertices in registers.
+__device__ __noinline__ uint32_t setup_clipped(const SetupParams& p, int S, uint32_t t) {
+  ClipVert cv[3];
+  const float* c0 = clip_vertices(p, t, cv);
   const bool opaque = t >= p.opaque_from;
+  ClipVert poly[4];
+  int n = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const ClipVert& a = cv[k];
+    const ClipVert& b = cv[(k + 1) % 3];
+    const bool ina = a.z >= 0.0f, inb = b.z >= 0.0f;
+    if (ina) poly[n++] = a;
+    if (ina != inb) poly[n++] = near_cut(a, b);
+  }
+  const ClipVert first[3] = {poly[0], poly[1], poly[2]};
+  uint32_t pairs = setup_half(p, S, t, opaque, first, c0, n == 4);
+  if (n == 4) {
+    const ClipVert second[3] = {poly[0], poly[2], poly[3]};
+    pairs += setup_half(p, S, p.num_triangles + t, opaque, second, c0, false);
+  }
+  return pairs;
+}
+
+__global__ void __launch_bounds__(256, 4) k_setup(SetupParams p, int S) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.num_triangles) return;
+  ClipVert cv[3];
+  const float* c0 = clip_vertices(p, t, cv);
   const int nin = (cv[0].z >= 0.0f) + (cv[1].z >= 0.0f) + (cv[2].z >= 0.0f);
   // wholly in front of the near plane, or wholly behind it (dropped by the
   // clip-volume test); a crossing triangle takes the out-of-line clip
-  p.pair_count[t] = (nin == 3 || nin == 0) ? setup_half(p, S, t, opaque, cv, c0, false)
-                                           : setup_clipped(p, S, t, opaque, cv, c0);
+  p.pair_count[t] = (nin == 3 || nin == 0) ? setup_half(p, S, t, t >= p.opaque_from, cv, c0, false)
+                                           : setup_clipped(p, S, t);
 }
 
 // ---------------------------------------------------------------------------
