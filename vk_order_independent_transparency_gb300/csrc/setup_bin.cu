@@ -6,6 +6,8 @@
 // blending. Here the same work is split into:
 //   k_setup       one thread per triangle: transform, cull, snap to 1/256 px,
 //                 bbox, interpolation constants (the raster specification);
+//   k_setup_clip  the same for the triangles that cross the near plane,
+//                 clipped into one or two;
 //   scan + emit   one (tile, triangle) pair per 16x16 tile the bbox touches,
 //                 written in triangle order; the key holds the tile id (bits
 //                 0-23) and the 8x4 micro-tiles the bbox overlaps (bits 24-31);
@@ -94,18 +96,16 @@ __device__ __forceinline__ uint32_t setup_half(const SetupParams& p, int S, uint
     // triangles cull back faces (transparent ones are double-sided, oit.cpp:703).
     if (area > 0 && opaque) ok = false;
   }
-  int o1 = 1, o2 = 2;
-  if (ok && area < 0) {
-    area = -area;
-    o1 = 2;
-    o2 = 1;
-  }
+  // counter-clockwise (area < 0) triangles swap vertices 1 and 2 so that
+  // every record winds one way; selects, not an index, keep it in registers
+  const bool sw = ok && area < 0;
+  if (sw) area = -area;
   int bx0 = 0, by0 = 0, bx1 = -1, by1 = -1;
   int PX[3], PY[3];
   if (ok) {
     PX[0] = X[0]; PY[0] = Y[0];
-    PX[1] = X[o1]; PY[1] = Y[o1];
-    PX[2] = X[o2]; PY[2] = Y[o2];
+    PX[1] = sw ? X[2] : X[1]; PY[1] = sw ? Y[2] : Y[1];
+    PX[2] = sw ? X[1] : X[2]; PY[2] = sw ? Y[1] : Y[2];
     const int minX = min(PX[0], min(PX[1], PX[2])), maxX = max(PX[0], max(PX[1], PX[2]));
     const int minY = min(PY[0], min(PY[1], PY[2])), maxY = max(PY[0], max(PY[1], PY[2]));
     bx0 = max(minX >> 8, 0);
@@ -143,7 +143,6 @@ __device__ __forceinline__ uint32_t setup_half(const SetupParams& p, int S, uint
     p.bbox[slot] = make_uint2(0xFFFFFFFFu, second_bit);
     return 0;
   }
-  const int order[3] = {0, o1, o2};
   TriSetup T;
   T.xy01 = make_int4(PX[0], PY[0], PX[1], PY[1]);
   float alpha = __fmaf_rn(__ldg(c0 + 3), p.alpha_width, p.alpha_min);
@@ -154,11 +153,11 @@ __device__ __forceinline__ uint32_t setup_half(const SetupParams& p, int S, uint
   const int minY = min(PY[0], min(PY[1], PY[2])), maxY = max(PY[0], max(PY[1], PY[2]));
   const int small = (maxX - minX < kSmallExtent && maxY - minY < kSmallExtent) ? kFlagSmall : 0;
   T.xy2f = make_int4(PX[2], PY[2], tl | small | (acode << 8), __float_as_int(alpha));
-  const float z0 = zz[0], z1 = zz[order[1]], z2 = zz[order[2]];
+  const float z0 = zz[0], z1 = sw ? zz[2] : zz[1], z2 = sw ? zz[1] : zz[2];
   T.zc = make_float4(z0, __fsub_rn(z1, z0), __fsub_rn(z2, z0), __fdiv_rn(1.0f, __ll2float_rn(area)));
-  const float q0 = q[0], q1 = q[order[1]], q2 = q[order[2]];
-  const ClipVert& v1 = cv[order[1]];
-  const ClipVert& v2 = cv[order[2]];
+  const float q0 = q[0], q1 = sw ? q[2] : q[1], q2 = sw ? q[1] : q[2];
+  const ClipVert& v1 = sw ? cv[2] : cv[1];
+  const ClipVert& v2 = sw ? cv[1] : cv[2];
   T.n0 = make_float4(__fmul_rn(cv[0].nx, q0), __fmul_rn(cv[0].ny, q0), __fmul_rn(cv[0].nz, q0), __ldg(c0 + 0));
   T.n1 = make_float4(__fmul_rn(v1.nx, q1), __fmul_rn(v1.ny, q1), __fmul_rn(v1.nz, q1), __ldg(c0 + 1));
   T.n2 = make_float4(__fmul_rn(v2.nx, q2), __fmul_rn(v2.ny, q2), __fmul_rn(v2.nz, q2), __ldg(c0 + 2));
@@ -233,44 +232,60 @@ __device__ __forceinline__ const float* clip_vertices(const SetupParams& p, uint
   return inst ? inst + 4 : vtx + 10 * (size_t)i0 + 6;  // color.rgba
 }
 
-// A triangle the near plane crosses: Sutherland-Hodgman against z = 0 over
-// the edges 0->1, 1->2, 2->0 keeps the triangle's winding; 3 vertices give one
-// triangle (record t), 4 the fan (0, 1, 2) in record t and (0, 2, 3) in record
-// num_triangles + t. Out of line and from the mesh again: rare, and the common
-// path keeps its vertices in registers.
-__device__ __noinline__ uint32_t setup_clipped(const SetupParams& p, int S, uint32_t t) {
-  ClipVert cv[3];
-  const float* c0 = clip_vertices(p, t, cv);
-  const bool opaque = t >= p.opaque_from;
-  ClipVert poly[4];
-  int n = 0;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const ClipVert& a = cv[k];
-    const ClipVert& b = cv[(k + 1) % 3];
-    const bool ina = a.z >= 0.0f, inb = b.z >= 0.0f;
-    if (ina) poly[n++] = a;
-    if (ina != inb) poly[n++] = near_cut(a, b);
-  }
-  const ClipVert first[3] = {poly[0], poly[1], poly[2]};
-  uint32_t pairs = setup_half(p, S, t, opaque, first, c0, n == 4);
-  if (n == 4) {
-    const ClipVert second[3] = {poly[0], poly[2], poly[3]};
-    pairs += setup_half(p, S, p.num_triangles + t, opaque, second, c0, false);
-  }
-  return pairs;
-}
+// pair_count of a triangle the near plane crosses, between k_setup and
+// k_setup_clip (no triangle overlaps 2^32 - 1 tiles)
+constexpr uint32_t kClipPending = 0xFFFFFFFFu;
 
+// One thread per triangle. Triangles wholly in front of the near plane, or
+// wholly behind it (dropped by the clip-volume test), are set up here; a
+// crossing triangle is marked for k_setup_clip, which keeps this kernel's
+// vertices in registers and free of the clip's extra state.
 __global__ void __launch_bounds__(256, 4) k_setup(SetupParams p, int S) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.num_triangles) return;
   ClipVert cv[3];
   const float* c0 = clip_vertices(p, t, cv);
   const int nin = (cv[0].z >= 0.0f) + (cv[1].z >= 0.0f) + (cv[2].z >= 0.0f);
-  // wholly in front of the near plane, or wholly behind it (dropped by the
-  // clip-volume test); a crossing triangle takes the out-of-line clip
-  p.pair_count[t] = (nin == 3 || nin == 0) ? setup_half(p, S, t, t >= p.opaque_from, cv, c0, false)
-                                           : setup_clipped(p, S, t);
+  if (nin == 1 || nin == 2) {
+    p.pair_count[t] = kClipPending;
+    return;
+  }
+  p.pair_count[t] = setup_half(p, S, t, t >= p.opaque_from, cv, c0, false);
+}
+
+// The triangles k_setup marked: Sutherland-Hodgman against z = 0 over the
+// edges 0->1, 1->2, 2->0 keeps the triangle's winding; 3 vertices give one
+// triangle (record t), 4 the fan (0, 1, 2) in record t and (0, 2, 3) in record
+// num_triangles + t. The vertices are derived from the mesh again, with the
+// same rounded operations as in k_setup.
+__global__ void __launch_bounds__(128) k_setup_clip(SetupParams p, int S) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.num_triangles || p.pair_count[t] != kClipPending) return;
+  ClipVert cv[3];
+  const float* c0 = clip_vertices(p, t, cv);
+  const bool opaque = t >= p.opaque_from;
+  const bool in[3] = {cv[0].z >= 0.0f, cv[1].z >= 0.0f, cv[2].z >= 0.0f};
+  // the polygon: in-front vertices and edge cuts in edge order (3 or 4 of them)
+  ClipVert poly[4];
+  int n = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int k1 = k == 2 ? 0 : k + 1;
+    if (in[k] && n < 4) poly[n++] = cv[k];
+    if (in[k] != in[k1] && n < 4) poly[n++] = near_cut(cv[k], cv[k1]);
+  }
+  uint32_t pairs = 0;
+  if (n >= 3) {
+    const ClipVert first[3] = {poly[0], poly[1], poly[2]};
+    pairs = setup_half(p, S, t, opaque, first, c0, n == 4);
+    if (n == 4) {
+      const ClipVert second[3] = {poly[0], poly[2], poly[3]};
+      pairs += setup_half(p, S, p.num_triangles + t, opaque, second, c0, false);
+    }
+  } else {
+    p.bbox[t] = make_uint2(0xFFFFFFFFu, 0u);  // not reached: a crossing triangle gives 3 or 4
+  }
+  p.pair_count[t] = pairs;
 }
 
 // ---------------------------------------------------------------------------
@@ -581,12 +596,25 @@ cudaError_t launch_fill_f4(float4* dst, float4 value, size_t count, cudaStream_t
   return cudaGetLastError();
 }
 
+namespace {
+// k_setup, then k_setup_clip over the triangles it marked
+cudaError_t launch_setup(const SetupParams& sp, cudaStream_t s, uint64_t* launches) {
+  const uint32_t n = sp.num_triangles;
+  const int S = sp.samples > 1 ? sp.samples : 1;
+  k_setup<<<(n + 255) / 256, 256, 0, s>>>(sp, S);
+  ++*launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_setup_clip<<<(n + 127) / 128, 128, 0, s>>>(sp, S);
+  ++*launches;
+  return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t bin_setup_only(const SetupParams& sp, cudaStream_t s, uint64_t* launches) {
   const uint32_t n = sp.num_triangles;
   if (n == 0) return cudaSuccess;
-  k_setup<<<(n + 255) / 256, 256, 0, s>>>(sp, sp.samples > 1 ? sp.samples : 1);
-  ++*launches;
-  return cudaGetLastError();
+  return launch_setup(sp, s, launches);
 }
 
 // Binning, step 1: setup + pair counts + exclusive scan; the number of
@@ -595,9 +623,7 @@ cudaError_t bin_setup_scan(const SetupParams& sp, Bins& b, cudaStream_t s, uint6
   cudaError_t e;
   const uint32_t n = sp.num_triangles;
   if (n == 0) return cudaMemsetAsync(b.total, 0, 4, s);
-  k_setup<<<(n + 255) / 256, 256, 0, s>>>(sp, sp.samples > 1 ? sp.samples : 1);
-  ++*launches;
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = launch_setup(sp, s, launches)) != cudaSuccess) return e;
   return scan_exclusive(sp.pair_count, b.pair_offset, n, b.scan_tmp, b.total, s, launches);
 }
 
