@@ -253,14 +253,12 @@ __global__ void __launch_bounds__(256, 4) k_setup(SetupParams p, int S) {
   p.pair_count[t] = setup_half(p, S, t, t >= p.opaque_from, cv, c0, false);
 }
 
-// The triangles k_setup marked: Sutherland-Hodgman against z = 0 over the
-// edges 0->1, 1->2, 2->0 keeps the triangle's winding; 3 vertices give one
-// triangle (record t), 4 the fan (0, 1, 2) in record t and (0, 2, 3) in record
+// A triangle k_setup marked: Sutherland-Hodgman against z = 0 over the edges
+// 0->1, 1->2, 2->0 keeps the triangle's winding; 3 vertices give one triangle
+// (record t), 4 the fan (0, 1, 2) in record t and (0, 2, 3) in record
 // num_triangles + t. The vertices are derived from the mesh again, with the
 // same rounded operations as in k_setup.
-__global__ void __launch_bounds__(128) k_setup_clip(SetupParams p, int S) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= p.num_triangles || p.pair_count[t] != kClipPending) return;
+__device__ __forceinline__ void setup_clipped(const SetupParams& p, int S, uint32_t t) {
   ClipVert cv[3];
   const float* c0 = clip_vertices(p, t, cv);
   const bool opaque = t >= p.opaque_from;
@@ -286,6 +284,29 @@ __global__ void __launch_bounds__(128) k_setup_clip(SetupParams p, int S) {
     p.bbox[t] = make_uint2(0xFFFFFFFFu, 0u);  // not reached: a crossing triangle gives 3 or 4
   }
   p.pair_count[t] = pairs;
+}
+
+// Grid-stride over pair_count four words (one 16-byte load) at a time; the
+// rare marked triangles are set up one by one. pair_count is 16-byte aligned.
+constexpr int kClipThreads = 256;
+__global__ void __launch_bounds__(kClipThreads) k_setup_clip(SetupParams p, int S) {
+  const uint32_t n = p.num_triangles, groups = (n + 3) / 4;
+  for (uint32_t g = blockIdx.x * kClipThreads + threadIdx.x; g < groups; g += gridDim.x * kClipThreads) {
+    const uint32_t t0 = 4 * g;
+    uint4 c;
+    if (t0 + 3 < n) {
+      c = __ldcg(reinterpret_cast<const uint4*>(p.pair_count) + g);
+    } else {
+      c.x = p.pair_count[t0];
+      c.y = t0 + 1 < n ? p.pair_count[t0 + 1] : 0u;
+      c.z = t0 + 2 < n ? p.pair_count[t0 + 2] : 0u;
+      c.w = 0u;
+    }
+    const uint32_t cw[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k)
+      if (cw[k] == kClipPending) setup_clipped(p, S, t0 + (uint32_t)k);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -605,7 +626,9 @@ cudaError_t launch_setup(const SetupParams& sp, cudaStream_t s, uint64_t* launch
   ++*launches;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_setup_clip<<<(n + 127) / 128, 128, 0, s>>>(sp, S);
+  const unsigned clip_blocks = (unsigned)std::min<size_t>(((size_t)n + 4 * kClipThreads - 1) / (4 * kClipThreads),
+                                                          152 * 8);
+  k_setup_clip<<<clip_blocks, kClipThreads, 0, s>>>(sp, S);
   ++*launches;
   return cudaGetLastError();
 }
