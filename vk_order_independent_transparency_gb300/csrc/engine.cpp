@@ -296,7 +296,7 @@ struct oit_context {
     }
     const size_t hist_words = std::max<size_t>(oit::radix_hist_words(pair_cap), 256);
     OIT_TRY_CUDA(hist.ensure(hist_words * 4), "alloc hist");
-    const size_t scan_words = std::max(oit::scan_scratch_words(tri_cap), oit::scan_scratch_words(hist_words));
+    const size_t scan_words = oit::bin_scan_words(tri_cap);
     OIT_TRY_CUDA(scan_tmp.ensure(scan_words * 4), "alloc scan");
     return OIT_OK;
   }

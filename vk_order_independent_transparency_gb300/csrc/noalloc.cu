@@ -152,13 +152,13 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
       !auxdepth || (weighted && (!accum || !reveal || !persp)) || !setup || !bbox || !pair_count || !pair_offset ||
       !tile_begin || !tile_end)
     return OIT_ERR_TOO_LARGE;
-  // The rest holds the pairs: 16 bytes per pair (keys, triangles, ping-pong),
-  // radix histograms and the scan scratch.
+  // The rest holds the pairs (16 bytes each: keys, triangles, ping-pong), the
+  // radix sort's digit counts and the pair-offset scan's words.
   const size_t left = a.cap - ((a.off + 255) & ~(size_t)255);
-  size_t pair_cap = (left / 18) & ~(size_t)4095;
-  size_t hist_words = radix_hist_words(pair_cap) > 256 ? radix_hist_words(pair_cap) : 256;
-  const size_t scan_n = scan_scratch_words(N) > scan_scratch_words(hist_words) ? scan_scratch_words(N)
-                                                                               : scan_scratch_words(hist_words);
+  const size_t reserve = (radix_hist_words(0) + bin_scan_words(N)) * 4 + 6 * 256;  // + alignment of 6 regions
+  size_t pair_cap = left > reserve ? ((left - reserve) / 16) & ~(size_t)4095 : 0;
+  const size_t hist_words = radix_hist_words(pair_cap);
+  const size_t scan_n = bin_scan_words(N);
   Bins b{};
   b.keys = a.take<uint32_t>(pair_cap * 4);
   b.tris = a.take<uint32_t>(pair_cap * 4);

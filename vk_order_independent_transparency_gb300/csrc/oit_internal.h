@@ -249,6 +249,10 @@ cudaError_t bin_setup_scan(const SetupParams& sp, Bins& b, cudaStream_t s, uint6
 cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles, uint32_t* error, cudaStream_t s,
                      uint64_t* launches);
 size_t radix_hist_words(size_t pairs);
+// Triangle blocks of the clip and emit kernels, and the words of b.scan_tmp
+// (their pair counts, scanned in place, and the scan's scratch).
+size_t emit_blocks(size_t tris);
+size_t bin_scan_words(size_t tris);
 cudaError_t launch_raster_a(Alg alg, const RasterParams& p, cudaStream_t s);  // Simple, LinkedList, Opaque
 cudaError_t launch_raster_b(Alg alg, const RasterParams& p, cudaStream_t s);  // Loop, Loop64
 cudaError_t launch_raster_c(Alg alg, const RasterParams& p, cudaStream_t s);  // Spinlock, Interlock, Weighted

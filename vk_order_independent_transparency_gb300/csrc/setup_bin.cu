@@ -31,7 +31,6 @@ constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;  // 4096 elements per block
 constexpr int kRadixThreads = 256;
 constexpr int kRadixRounds = 16;
-constexpr int kRadixTile = kRadixThreads * kRadixRounds;  // 4096 pairs per block
 constexpr int kRadixBits = 8;
 constexpr int kRadixBins = 1 << kRadixBits;
 
@@ -257,8 +256,8 @@ __global__ void __launch_bounds__(256, 4) k_setup(SetupParams p, int S) {
 // 0->1, 1->2, 2->0 keeps the triangle's winding; 3 vertices give one triangle
 // (record t), 4 the fan (0, 1, 2) in record t and (0, 2, 3) in record
 // num_triangles + t. The vertices are derived from the mesh again, with the
-// same rounded operations as in k_setup.
-__device__ __forceinline__ void setup_clipped(const SetupParams& p, int S, uint32_t t) {
+// same rounded operations as in k_setup. Returns the pair count.
+__device__ __forceinline__ uint32_t setup_clipped(const SetupParams& p, int S, uint32_t t) {
   ClipVert cv[3];
   const float* c0 = clip_vertices(p, t, cv);
   const bool opaque = t >= p.opaque_from;
@@ -284,28 +283,45 @@ __device__ __forceinline__ void setup_clipped(const SetupParams& p, int S, uint3
     p.bbox[t] = make_uint2(0xFFFFFFFFu, 0u);  // not reached: a crossing triangle gives 3 or 4
   }
   p.pair_count[t] = pairs;
+  return pairs;
 }
 
-// Grid-stride over pair_count four words (one 16-byte load) at a time; the
-// rare marked triangles are set up one by one. pair_count is 16-byte aligned.
-constexpr int kClipThreads = 256;
-__global__ void __launch_bounds__(kClipThreads) k_setup_clip(SetupParams p, int S) {
-  const uint32_t n = p.num_triangles, groups = (n + 3) / 4;
-  for (uint32_t g = blockIdx.x * kClipThreads + threadIdx.x; g < groups; g += gridDim.x * kClipThreads) {
-    const uint32_t t0 = 4 * g;
-    uint4 c;
-    if (t0 + 3 < n) {
-      c = __ldcg(reinterpret_cast<const uint4*>(p.pair_count) + g);
-    } else {
-      c.x = p.pair_count[t0];
-      c.y = t0 + 1 < n ? p.pair_count[t0 + 1] : 0u;
-      c.z = t0 + 2 < n ? p.pair_count[t0 + 2] : 0u;
-      c.w = 0u;
-    }
-    const uint32_t cw[4] = {c.x, c.y, c.z, c.w};
+// Triangles per block of the clip and emit kernels (4 per thread).
+constexpr int kEmitThreads = 256;
+constexpr int kEmitItems = 4;
+constexpr int kEmitTile = kEmitThreads * kEmitItems;
+
+// The marked triangles of each 1024-triangle block are clipped one by one;
+// with block_sums, the block's pair count (after clipping) is written there,
+// the first level of the pair-offset scan. pair_count is 16-byte aligned.
+__global__ void __launch_bounds__(kEmitThreads) k_setup_clip(SetupParams p, int S, uint32_t* __restrict__ block_sums) {
+  __shared__ uint32_t warp_sums[kEmitThreads / 32];
+  const uint32_t n = p.num_triangles;
+  const uint32_t t0 = blockIdx.x * kEmitTile + threadIdx.x * kEmitItems;
+  uint32_t c[kEmitItems] = {0u, 0u, 0u, 0u};
+  if (t0 + 3 < n) {
+    const uint4 v = __ldcg(reinterpret_cast<const uint4*>(p.pair_count + t0));
+    c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < kEmitItems; ++k) c[k] = t0 + k < n ? p.pair_count[t0 + k] : 0u;
+  }
+  uint32_t sum = 0;
 #pragma unroll 1
-    for (int k = 0; k < 4; ++k)
-      if (cw[k] == kClipPending) setup_clipped(p, S, t0 + (uint32_t)k);
+  for (int k = 0; k < kEmitItems; ++k) {
+    const uint32_t ck = c[k] == kClipPending ? setup_clipped(p, S, t0 + (uint32_t)k) : c[k];
+    sum += ck;
+  }
+  if (!block_sums) return;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t b = 0;
+#pragma unroll
+    for (int w = 0; w < kEmitThreads / 32; ++w) b += warp_sums[w];
+    block_sums[blockIdx.x] = b;
   }
 }
 
@@ -461,55 +477,94 @@ __device__ __forceinline__ uint32_t emit_bbox(uint2 bb, uint32_t t, uint32_t til
   return j;
 }
 
-// The pairs of triangle t: its first (or only) half's tiles, then the second
-// half's (record n + t) when the near-plane clip split it.
-__global__ void __launch_bounds__(256) k_emit(const uint32_t* __restrict__ pair_count,
-                                              const uint32_t* __restrict__ pair_offset, const uint2* __restrict__ bbox,
-                                              uint32_t n, int tiles_x, uint32_t opaque_from, uint32_t num_tiles,
-                                              uint32_t* __restrict__ keys, uint32_t* __restrict__ tris,
-                                              size_t capacity, const uint32_t* __restrict__ total, uint32_t* err) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t == 0 && *total > capacity) atomicOr(err, 1u);  // OIT_DEVERR_BIN_OVERFLOW
-  if (t >= n) return;
-  const uint32_t c = pair_count[t];
-  if (!c) return;
-  const uint32_t off = pair_offset[t];
-  const uint2 bb = bbox[t];
-  const uint32_t tile_base = t < opaque_from ? num_tiles : 0u;
-  const uint32_t j = emit_bbox(bb, t, tile_base, tiles_x, off, 0u, keys, tris, capacity);
-  if (bb.y >> 31) emit_bbox(bbox[n + t], n + t, tile_base, tiles_x, off, j, keys, tris, capacity);
+// The pairs of the block's 1024 triangles: each triangle's offset is the
+// scanned block sum plus the exclusive prefix of the counts before it in the
+// block (written to pair_offset, which the bin-overflow walk reads); a
+// triangle emits its first (or only) half's tiles, then the second half's
+// (record n + t) when the near-plane clip split it.
+__global__ void __launch_bounds__(kEmitThreads) k_emit(const uint32_t* __restrict__ pair_count,
+                                                       uint32_t* __restrict__ pair_offset,
+                                                       const uint32_t* __restrict__ block_offsets,
+                                                       const uint2* __restrict__ bbox, uint32_t n, int tiles_x,
+                                                       uint32_t opaque_from, uint32_t num_tiles,
+                                                       uint32_t* __restrict__ keys, uint32_t* __restrict__ tris,
+                                                       size_t capacity, const uint32_t* __restrict__ total,
+                                                       uint32_t* err) {
+  __shared__ uint32_t smem[64];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && *total > capacity) atomicOr(err, 1u);  // OIT_DEVERR_BIN_OVERFLOW
+  const uint32_t t0 = blockIdx.x * kEmitTile + threadIdx.x * kEmitItems;
+  uint32_t c[kEmitItems];
+  if (t0 + 3 < n) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(pair_count + t0));
+    c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < kEmitItems; ++k) c[k] = t0 + k < n ? pair_count[t0 + k] : 0u;
+  }
+  uint32_t block_total;
+  uint32_t off = block_exclusive_scan(c[0] + c[1] + c[2] + c[3], &block_total, smem) + block_offsets[blockIdx.x];
+#pragma unroll 1
+  for (int k = 0; k < kEmitItems; ++k) {
+    const uint32_t t = t0 + (uint32_t)k;
+    if (t >= n) break;
+    pair_offset[t] = off;
+    if (c[k]) {
+      const uint2 bb = bbox[t];
+      const uint32_t tile_base = t < opaque_from ? num_tiles : 0u;
+      const uint32_t j = emit_bbox(bb, t, tile_base, tiles_x, off, 0u, keys, tris, capacity);
+      if (bb.y >> 31) emit_bbox(bbox[n + t], n + t, tile_base, tiles_x, off, j, keys, tris, capacity);
+    }
+    off += c[k];
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Stable LSD radix sort of (key, value) pairs, 8-bit digits.
+//
+// The pairs are cut into at most kSortBlocks chunks (multiples of 4096
+// pairs). k_radix_hist counts each chunk's digits; k_radix_scatter derives
+// its chunk's output offset for every digit from those counts itself (the
+// digit's start over all chunks plus the counts of the chunks before it) and
+// moves the chunk 4096 pairs at a time: each warp ranks its 512 consecutive
+// pairs with its own shared-memory counters, so a sub-tile costs three block
+// barriers. Pairs keep their order within a digit: the sort is stable.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ size_t pair_count_of(const uint32_t* total, size_t capacity) {
   const size_t t = *total;
   return t < capacity ? t : capacity;
 }
 
-// Per-block digit histogram; one shared-memory atomic per distinct digit per
+constexpr int kSortSubTile = kRadixThreads * kRadixRounds;  // 4096 pairs: 8 warps x 16 rounds of 32
+constexpr int kSortWarps = kRadixThreads / 32;
+
+// Digit counts of chunk blockIdx.x, written digit-major per chunk:
+// counts[chunk * 256 + digit]. One shared-memory atomic per distinct digit per
 // warp (tile ids of neighbouring pairs are mostly equal).
 __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t* __restrict__ keys,
                                                               const uint32_t* __restrict__ total, size_t capacity,
-                                                              int shift, uint32_t* __restrict__ hist, uint32_t nblk) {
+                                                              int shift, size_t chunk, uint32_t* __restrict__ counts) {
   __shared__ uint32_t h[kRadixBins];
   h[threadIdx.x] = 0;
   __syncthreads();
   const size_t n = pair_count_of(total, capacity);
-  const size_t base = (size_t)blockIdx.x * kRadixTile;
+  const size_t beg = (size_t)blockIdx.x * chunk;
+  const size_t end = beg + chunk < n ? beg + chunk : n;
   const uint32_t lane = threadIdx.x & 31;
-  if (base < n) {
-#pragma unroll 4
-    for (int r = 0; r < kRadixRounds; ++r) {
-      const size_t i = base + (size_t)r * kRadixThreads + threadIdx.x;
-      const uint32_t d = (i < n) ? ((keys[i] >> shift) & (kRadixBins - 1)) : kRadixBins;
-      const uint32_t peers = __match_any_sync(0xffffffffu, d);
-      if (d < kRadixBins && (__ffs(peers) - 1) == (int)lane) atomicAdd(&h[d], (uint32_t)__popc(peers));
+  for (size_t base = beg; base < end; base += kRadixThreads * 4) {
+    uint32_t d[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const size_t i = base + (size_t)k * kRadixThreads + threadIdx.x;
+      d[k] = i < end ? (__ldg(&keys[i]) >> shift) & (kRadixBins - 1) : kRadixBins;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t peers = __match_any_sync(0xffffffffu, d[k]);
+      if (d[k] < kRadixBins && (__ffs(peers) - 1) == (int)lane) atomicAdd(&h[d[k]], (uint32_t)__popc(peers));
     }
   }
   __syncthreads();
-  hist[(size_t)threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];
+  counts[(size_t)blockIdx.x * kRadixBins + threadIdx.x] = h[threadIdx.x];
 }
 
 __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t* __restrict__ keys_in,
@@ -517,53 +572,82 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t*
                                                                  uint32_t* __restrict__ keys_out,
                                                                  uint32_t* __restrict__ vals_out,
                                                                  const uint32_t* __restrict__ total, size_t capacity,
-                                                                 int shift, const uint32_t* __restrict__ offsets,
-                                                                 uint32_t nblk) {
-  constexpr int kWarps = kRadixThreads / 32;
-  __shared__ uint32_t base[kRadixBins];
-  __shared__ uint32_t running[kRadixBins];
-  __shared__ uint32_t wh[kWarps][kRadixBins];
+                                                                 int shift, size_t chunk, uint32_t nchunks,
+                                                                 const uint32_t* __restrict__ counts) {
+  __shared__ uint32_t base[kRadixBins];             // output position of the chunk's next pair of each digit
+  __shared__ uint32_t wcount[kSortWarps][kRadixBins];  // per warp: counts, then exclusive offsets in the sub-tile
+  __shared__ uint32_t sub_total[kRadixBins];
+  __shared__ uint32_t scan_s[64];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  base[threadIdx.x] = offsets[(size_t)threadIdx.x * nblk + blockIdx.x];
-  running[threadIdx.x] = 0;
-  const size_t blk = (size_t)blockIdx.x * kRadixTile;
-  const size_t n = pair_count_of(total, capacity);
-  if (blk >= n) return;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  for (int r = 0; r < kRadixRounds; ++r) {
-#pragma unroll
-    for (int k = 0; k < kRadixBins / 32; ++k) wh[warp][lane + 32 * k] = 0;
-    __syncthreads();
-    const size_t i = blk + (size_t)r * kRadixThreads + threadIdx.x;
-    const bool valid = i < n;
-    uint32_t key = 0, val = 0, d = kRadixBins;
-    if (valid) {
-      key = keys_in[i];
-      val = vals_in[i];
-      d = (key >> shift) & (kRadixBins - 1);
+  const size_t n = pair_count_of(total, capacity);
+  const size_t beg = (size_t)blockIdx.x * chunk;
+  // this digit's pairs in all chunks, and in the chunks before this one
+  {
+    const uint32_t d = threadIdx.x;
+    uint32_t all = 0, before = 0;
+#pragma unroll 8
+    for (uint32_t c = 0; c < nchunks; ++c) {
+      const uint32_t v = __ldg(&counts[(size_t)c * kRadixBins + d]);
+      all += v;
+      before += c < blockIdx.x ? v : 0u;
     }
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t rank = __popc(peers & lt_mask);
-    if (valid && rank == 0) wh[warp][d] = __popc(peers);
+    uint32_t sum_all;
+    base[d] = block_exclusive_scan(all, &sum_all, scan_s) + before;
+  }
+  if (beg >= n) return;
+  const size_t end = beg + chunk < n ? beg + chunk : n;
+  for (size_t sub = beg; sub < end; sub += kSortSubTile) {
+#pragma unroll
+    for (int k = 0; k < kRadixBins / 32; ++k) wcount[warp][lane + 32 * k] = 0;
+    __syncwarp();
+    // this warp's 512 consecutive pairs of the sub-tile, 32 per round
+    const size_t wbase = sub + (size_t)warp * (32 * kRadixRounds);
+    uint32_t key[kRadixRounds], val[kRadixRounds], dr[kRadixRounds];
+#pragma unroll
+    for (int r = 0; r < kRadixRounds; ++r) {
+      const size_t i = wbase + (size_t)r * 32 + lane;
+      key[r] = i < end ? __ldg(&keys_in[i]) : 0u;
+      val[r] = i < end ? __ldg(&vals_in[i]) : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < kRadixRounds; ++r) {
+      const size_t i = wbase + (size_t)r * 32 + lane;
+      const uint32_t d = i < end ? (key[r] >> shift) & (kRadixBins - 1) : kRadixBins;
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      const int leader = __ffs(peers) - 1;
+      uint32_t old = 0;
+      if (lane == leader && d < kRadixBins) {
+        old = wcount[warp][d];
+        wcount[warp][d] = old + (uint32_t)__popc(peers);
+      }
+      old = __shfl_sync(0xffffffffu, old, leader);
+      dr[r] = (d << 16) | (old + (uint32_t)__popc(peers & lt_mask));  // digit (256 = none), rank in the warp
+    }
     __syncthreads();
     {
-      const int dd = threadIdx.x;
-      uint32_t acc = running[dd];
+      const int d = threadIdx.x;
+      uint32_t acc = 0;
 #pragma unroll
-      for (int w = 0; w < kWarps; ++w) {
-        const uint32_t c = wh[w][dd];
-        wh[w][dd] = acc;
+      for (int w = 0; w < kSortWarps; ++w) {
+        const uint32_t c = wcount[w][d];
+        wcount[w][d] = acc;
         acc += c;
       }
-      running[dd] = acc;
+      sub_total[d] = acc;
     }
     __syncthreads();
-    if (valid) {
-      const uint32_t pos = base[d] + wh[warp][d] + rank;
-      keys_out[pos] = key;
-      vals_out[pos] = val;
+#pragma unroll
+    for (int r = 0; r < kRadixRounds; ++r) {
+      const uint32_t d = dr[r] >> 16;
+      if (d < kRadixBins) {
+        const uint32_t pos = base[d] + wcount[warp][d] + (dr[r] & 0xFFFFu);
+        keys_out[pos] = key[r];
+        vals_out[pos] = val[r];
+      }
     }
     __syncthreads();
+    base[threadIdx.x] += sub_total[threadIdx.x];
   }
 }
 
@@ -618,36 +702,53 @@ cudaError_t launch_fill_f4(float4* dst, float4 value, size_t count, cudaStream_t
 }
 
 namespace {
-// k_setup, then k_setup_clip over the triangles it marked
-cudaError_t launch_setup(const SetupParams& sp, cudaStream_t s, uint64_t* launches) {
+// k_setup, then k_setup_clip over the triangles it marked (and, with
+// block_sums, the pair count of every 1024-triangle block)
+cudaError_t launch_setup(const SetupParams& sp, uint32_t* block_sums, cudaStream_t s, uint64_t* launches) {
   const uint32_t n = sp.num_triangles;
   const int S = sp.samples > 1 ? sp.samples : 1;
   k_setup<<<(n + 255) / 256, 256, 0, s>>>(sp, S);
   ++*launches;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const unsigned clip_blocks = (unsigned)std::min<size_t>(((size_t)n + 4 * kClipThreads - 1) / (4 * kClipThreads),
-                                                          152 * 8);
-  k_setup_clip<<<clip_blocks, kClipThreads, 0, s>>>(sp, S);
+  k_setup_clip<<<(unsigned)emit_blocks(n), kEmitThreads, 0, s>>>(sp, S, block_sums);
   ++*launches;
   return cudaGetLastError();
 }
+
+// Pairs per chunk of the radix sort: whole 4096-pair sub-tiles, at most
+// kSortBlocks chunks.
+constexpr size_t kSortBlocks = 256;
+size_t sort_chunk(size_t capacity) {
+  const size_t per = (capacity + kSortBlocks - 1) / kSortBlocks;
+  const size_t sub = (per + kSortSubTile - 1) / kSortSubTile * kSortSubTile;
+  return sub > (size_t)kSortSubTile ? sub : (size_t)kSortSubTile;
+}
 }  // namespace
+
+size_t emit_blocks(size_t tris) { return (tris + kEmitTile - 1) / kEmitTile; }
+
+size_t bin_scan_words(size_t tris) {
+  const size_t nb = emit_blocks(tris > 0 ? tris : 1);
+  return nb + scan_scratch_words(nb);
+}
 
 cudaError_t bin_setup_only(const SetupParams& sp, cudaStream_t s, uint64_t* launches) {
   const uint32_t n = sp.num_triangles;
   if (n == 0) return cudaSuccess;
-  return launch_setup(sp, s, launches);
+  return launch_setup(sp, nullptr, s, launches);
 }
 
-// Binning, step 1: setup + pair counts + exclusive scan; the number of
-// (tile, triangle) pairs lands in b.total (device).
+// Binning, step 1: setup, clip, pair counts per 1024-triangle block and their
+// exclusive scan (in b.scan_tmp, read by k_emit); the number of (tile,
+// triangle) pairs lands in b.total (device).
 cudaError_t bin_setup_scan(const SetupParams& sp, Bins& b, cudaStream_t s, uint64_t* launches) {
   cudaError_t e;
   const uint32_t n = sp.num_triangles;
   if (n == 0) return cudaMemsetAsync(b.total, 0, 4, s);
-  if ((e = launch_setup(sp, s, launches)) != cudaSuccess) return e;
-  return scan_exclusive(sp.pair_count, b.pair_offset, n, b.scan_tmp, b.total, s, launches);
+  if ((e = launch_setup(sp, b.scan_tmp, s, launches)) != cudaSuccess) return e;
+  const size_t nb = emit_blocks(n);
+  return scan_exclusive(b.scan_tmp, b.scan_tmp, nb, b.scan_tmp + nb, b.total, s, launches);
 }
 
 // Binning, step 2: emit pairs in triangle order, stable radix sort by tile id,
@@ -659,19 +760,20 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles
   cudaError_t e;
   const uint32_t n = sp.num_triangles;
   if (n > 0) {
-    k_emit<<<(n + 255) / 256, 256, 0, s>>>(sp.pair_count, b.pair_offset, sp.bbox, n, sp.tiles_x, sp.opaque_from,
-                                           (uint32_t)sp.num_tiles, b.keys, b.tris, b.capacity, b.total, error);
+    k_emit<<<(unsigned)emit_blocks(n), kEmitThreads, 0, s>>>(sp.pair_count, b.pair_offset, b.scan_tmp, sp.bbox, n,
+                                                             sp.tiles_x, sp.opaque_from, (uint32_t)sp.num_tiles,
+                                                             b.keys, b.tris, b.capacity, b.total, error);
     ++*launches;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
-  const uint32_t nblk = (uint32_t)((b.capacity + kRadixTile - 1) / kRadixTile);
+  const size_t chunk = sort_chunk(b.capacity);
+  const uint32_t nchunks = (uint32_t)std::max<size_t>((b.capacity + chunk - 1) / chunk, 1);
   uint32_t *kin = b.keys, *vin = b.tris, *kout = b.keys_alt, *vout = b.tris_alt;
   for (int shift = 0; shift < key_bits; shift += kRadixBits) {
-    k_radix_hist<<<nblk, kRadixThreads, 0, s>>>(kin, b.total, b.capacity, shift, b.hist, nblk);
+    k_radix_hist<<<nchunks, kRadixThreads, 0, s>>>(kin, b.total, b.capacity, shift, chunk, b.hist);
     ++*launches;
-    if ((e = scan_exclusive(b.hist, b.hist, (size_t)nblk * kRadixBins, b.scan_tmp, nullptr, s, launches)) != cudaSuccess)
-      return e;
-    k_radix_scatter<<<nblk, kRadixThreads, 0, s>>>(kin, vin, kout, vout, b.total, b.capacity, shift, b.hist, nblk);
+    k_radix_scatter<<<nchunks, kRadixThreads, 0, s>>>(kin, vin, kout, vout, b.total, b.capacity, shift, chunk,
+                                                      nchunks, b.hist);
     ++*launches;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     std::swap(kin, kout);
@@ -693,7 +795,8 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles
   return cudaGetLastError();
 }
 
-size_t radix_hist_words(size_t pairs) { return ((pairs + kRadixTile - 1) / kRadixTile) * kRadixBins; }
+// Digit counts of at most kSortBlocks chunks.
+size_t radix_hist_words(size_t) { return kSortBlocks * kRadixBins; }
 
 void srgb_host_tables(float* thr256, float* dec256) {
   static const float thr[256] = OIT_SRGB_THR_INIT;
