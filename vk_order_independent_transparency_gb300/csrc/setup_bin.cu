@@ -286,16 +286,17 @@ __device__ __forceinline__ uint32_t setup_clipped(const SetupParams& p, int S, u
   return pairs;
 }
 
-// Triangles per block of the clip and emit kernels (4 per thread).
-constexpr int kEmitThreads = 256;
+// Triangles per block of the clip kernel (4 per thread) and of the emit
+// kernel (one per thread): the pair-count sums are per 1024 triangles.
+constexpr int kClipThreads = 256;
 constexpr int kEmitItems = 4;
-constexpr int kEmitTile = kEmitThreads * kEmitItems;
+constexpr int kEmitTile = kClipThreads * kEmitItems;
 
 // The marked triangles of each 1024-triangle block are clipped one by one;
 // with block_sums, the block's pair count (after clipping) is written there,
 // the first level of the pair-offset scan. pair_count is 16-byte aligned.
-__global__ void __launch_bounds__(kEmitThreads) k_setup_clip(SetupParams p, int S, uint32_t* __restrict__ block_sums) {
-  __shared__ uint32_t warp_sums[kEmitThreads / 32];
+__global__ void __launch_bounds__(kClipThreads) k_setup_clip(SetupParams p, int S, uint32_t* __restrict__ block_sums) {
+  __shared__ uint32_t warp_sums[kClipThreads / 32];
   const uint32_t n = p.num_triangles;
   const uint32_t t0 = blockIdx.x * kEmitTile + threadIdx.x * kEmitItems;
   uint32_t c[kEmitItems] = {0u, 0u, 0u, 0u};
@@ -320,7 +321,7 @@ __global__ void __launch_bounds__(kEmitThreads) k_setup_clip(SetupParams p, int 
   if (threadIdx.x == 0) {
     uint32_t b = 0;
 #pragma unroll
-    for (int w = 0; w < kEmitThreads / 32; ++w) b += warp_sums[w];
+    for (int w = 0; w < kClipThreads / 32; ++w) b += warp_sums[w];
     block_sums[blockIdx.x] = b;
   }
 }
@@ -477,45 +478,32 @@ __device__ __forceinline__ uint32_t emit_bbox(uint2 bb, uint32_t t, uint32_t til
   return j;
 }
 
-// The pairs of the block's 1024 triangles: each triangle's offset is the
-// scanned block sum plus the exclusive prefix of the counts before it in the
-// block (written to pair_offset, which the bin-overflow walk reads); a
-// triangle emits its first (or only) half's tiles, then the second half's
+// The pairs of the block's 1024 triangles, one per thread: a triangle's
+// offset is the scanned block sum plus the exclusive prefix of the counts
+// before it in the block (written to pair_offset, which the bin-overflow walk
+// reads); it emits its first (or only) half's tiles, then the second half's
 // (record n + t) when the near-plane clip split it.
-__global__ void __launch_bounds__(kEmitThreads) k_emit(const uint32_t* __restrict__ pair_count,
-                                                       uint32_t* __restrict__ pair_offset,
-                                                       const uint32_t* __restrict__ block_offsets,
-                                                       const uint2* __restrict__ bbox, uint32_t n, int tiles_x,
-                                                       uint32_t opaque_from, uint32_t num_tiles,
-                                                       uint32_t* __restrict__ keys, uint32_t* __restrict__ tris,
-                                                       size_t capacity, const uint32_t* __restrict__ total,
-                                                       uint32_t* err) {
+__global__ void __launch_bounds__(kEmitTile) k_emit(const uint32_t* __restrict__ pair_count,
+                                                    uint32_t* __restrict__ pair_offset,
+                                                    const uint32_t* __restrict__ block_offsets,
+                                                    const uint2* __restrict__ bbox, uint32_t n, int tiles_x,
+                                                    uint32_t opaque_from, uint32_t num_tiles,
+                                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ tris,
+                                                    size_t capacity, const uint32_t* __restrict__ total,
+                                                    uint32_t* err) {
   __shared__ uint32_t smem[64];
   if (blockIdx.x == 0 && threadIdx.x == 0 && *total > capacity) atomicOr(err, 1u);  // OIT_DEVERR_BIN_OVERFLOW
-  const uint32_t t0 = blockIdx.x * kEmitTile + threadIdx.x * kEmitItems;
-  uint32_t c[kEmitItems];
-  if (t0 + 3 < n) {
-    const uint4 v = __ldg(reinterpret_cast<const uint4*>(pair_count + t0));
-    c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
-  } else {
-#pragma unroll
-    for (int k = 0; k < kEmitItems; ++k) c[k] = t0 + k < n ? pair_count[t0 + k] : 0u;
-  }
+  const uint32_t t = blockIdx.x * kEmitTile + threadIdx.x;
+  const uint32_t c = t < n ? __ldg(&pair_count[t]) : 0u;
   uint32_t block_total;
-  uint32_t off = block_exclusive_scan(c[0] + c[1] + c[2] + c[3], &block_total, smem) + block_offsets[blockIdx.x];
-#pragma unroll 1
-  for (int k = 0; k < kEmitItems; ++k) {
-    const uint32_t t = t0 + (uint32_t)k;
-    if (t >= n) break;
-    pair_offset[t] = off;
-    if (c[k]) {
-      const uint2 bb = bbox[t];
-      const uint32_t tile_base = t < opaque_from ? num_tiles : 0u;
-      const uint32_t j = emit_bbox(bb, t, tile_base, tiles_x, off, 0u, keys, tris, capacity);
-      if (bb.y >> 31) emit_bbox(bbox[n + t], n + t, tile_base, tiles_x, off, j, keys, tris, capacity);
-    }
-    off += c[k];
-  }
+  const uint32_t off = block_exclusive_scan(c, &block_total, smem) + block_offsets[blockIdx.x];
+  if (t >= n) return;
+  pair_offset[t] = off;
+  if (!c) return;
+  const uint2 bb = bbox[t];
+  const uint32_t tile_base = t < opaque_from ? num_tiles : 0u;
+  const uint32_t j = emit_bbox(bb, t, tile_base, tiles_x, off, 0u, keys, tris, capacity);
+  if (bb.y >> 31) emit_bbox(bbox[n + t], n + t, tile_base, tiles_x, off, j, keys, tris, capacity);
 }
 
 // ---------------------------------------------------------------------------
@@ -584,13 +572,19 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t*
   const size_t beg = (size_t)blockIdx.x * chunk;
   // this digit's pairs in all chunks, and in the chunks before this one
   {
+    // 32 independent loads in flight per thread: the chunks' counts are read
+    // by every block, so their latency, not their bytes, is the cost
     const uint32_t d = threadIdx.x;
     uint32_t all = 0, before = 0;
-#pragma unroll 8
-    for (uint32_t c = 0; c < nchunks; ++c) {
-      const uint32_t v = __ldg(&counts[(size_t)c * kRadixBins + d]);
-      all += v;
-      before += c < blockIdx.x ? v : 0u;
+    for (uint32_t c0 = 0; c0 < nchunks; c0 += 32) {
+      uint32_t v[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) v[k] = c0 + k < nchunks ? __ldg(&counts[(size_t)(c0 + k) * kRadixBins + d]) : 0u;
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        all += v[k];
+        before += c0 + k < blockIdx.x ? v[k] : 0u;
+      }
     }
     uint32_t sum_all;
     base[d] = block_exclusive_scan(all, &sum_all, scan_s) + before;
@@ -711,14 +705,14 @@ cudaError_t launch_setup(const SetupParams& sp, uint32_t* block_sums, cudaStream
   ++*launches;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_setup_clip<<<(unsigned)emit_blocks(n), kEmitThreads, 0, s>>>(sp, S, block_sums);
+  k_setup_clip<<<(unsigned)emit_blocks(n), kClipThreads, 0, s>>>(sp, S, block_sums);
   ++*launches;
   return cudaGetLastError();
 }
 
 // Pairs per chunk of the radix sort: whole 4096-pair sub-tiles, at most
 // kSortBlocks chunks.
-constexpr size_t kSortBlocks = 256;
+constexpr size_t kSortBlocks = 128;
 size_t sort_chunk(size_t capacity) {
   const size_t per = (capacity + kSortBlocks - 1) / kSortBlocks;
   const size_t sub = (per + kSortSubTile - 1) / kSortSubTile * kSortSubTile;
@@ -760,9 +754,9 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles
   cudaError_t e;
   const uint32_t n = sp.num_triangles;
   if (n > 0) {
-    k_emit<<<(unsigned)emit_blocks(n), kEmitThreads, 0, s>>>(sp.pair_count, b.pair_offset, b.scan_tmp, sp.bbox, n,
-                                                             sp.tiles_x, sp.opaque_from, (uint32_t)sp.num_tiles,
-                                                             b.keys, b.tris, b.capacity, b.total, error);
+    k_emit<<<(unsigned)emit_blocks(n), kEmitTile, 0, s>>>(sp.pair_count, b.pair_offset, b.scan_tmp, sp.bbox, n,
+                                                          sp.tiles_x, sp.opaque_from, (uint32_t)sp.num_tiles, b.keys,
+                                                          b.tris, b.capacity, b.total, error);
     ++*launches;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
