@@ -497,9 +497,8 @@ constexpr int kStageSlots = 32;
 // Walks [beg, end) of the tile list in primitive order, 32 entries at a time:
 // the lanes test their triangle against the warp's micro-tile, the hits copy
 // their setup records into the warp's shared-memory stage in parallel
-// (cp.async) with their triangle ids and bboxes, and when the stage is full
-// (or the list ends) chunk(nh) processes stage slots 0..nh-1, which are in
-// list order. chunk is warp-uniform.
+// (cp.async) with their triangle ids and bboxes, then chunk(nh) processes
+// stage slots 0..nh-1, which are in list order. chunk is warp-uniform.
 // Mask (8x4 micro-tiles, one lane per pixel): the test is the micro-tile's bit
 // in the pair's sorted key (the binning wrote the bbox's micro-tile overlap
 // there), so only hits gather their bbox; else the bbox itself is tested.
@@ -533,18 +532,6 @@ __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile&
     fetch(beg + w.lane);
     if (!use_mask || h_next) bb_next = fetch_bb(beg + w.lane);
   }
-  // Hits of successive 32-entry chunks are appended to the stage until the
-  // next chunk's would not fit; only then does the warp wait for the copies
-  // and process the stage, so one wait serves up to kStageSlots records and
-  // the coverage and shading rounds run on fuller groups.
-  int ns = 0;  // warp-uniform: records staged
-  auto process = [&]() {
-    cp_async_wait_all();
-    __syncwarp();
-    chunk(ns);
-    __syncwarp();
-    ns = 0;
-  };
   for (uint32_t base = beg; base < end; base += 32) {
     const uint32_t t = t_next;
     const uint2 bb = bb_next;
@@ -554,21 +541,22 @@ __device__ __forceinline__ void walk_tile(const RasterParams& p, const WarpTile&
     if (more) fetch(nb + w.lane);
     else h_next = false;
     const uint32_t m = __ballot_sync(kFull, hit);
-    const int nh = __popc(m);
-    if (ns + nh > kStageSlots) process();
-    if (hit) {
-      const int slot = ns + __popc(m & lt);
+    const int rank = __popc(m & lt);
+    auto stage_hit = [&](int slot) {
       const int4* src = reinterpret_cast<const int4*>(setup + t);
       int4* dst = reinterpret_cast<int4*>(stage + slot);
 #pragma unroll
       for (int k = 0; k < 6; ++k) cp_async16(dst + k, src + k);
       stage_t[slot] = t;
       stage_bb[slot] = bb;
-    }
-    ns += nh;
+    };
+    if (hit) stage_hit(rank);
     bb_next = more && (!use_mask || h_next) ? fetch_bb(nb + w.lane) : make_uint2(0xFFFFFFFFu, 0u);
+    cp_async_wait_all();
+    __syncwarp();
+    if (m) chunk(__popc(m));
+    __syncwarp();
   }
-  if (ns) process();
 }
 
 // Triangles of the draw binned whole: all of them, or after a bin overflow
