@@ -117,11 +117,12 @@ def _oracle_frame(args):
     variant = args[2] if len(args) > 2 else 'fp64'
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
     import oracle as orc
-    import vk_order_independent_transparency_gb300 as oit
     W, H = wd['width'], wd['height']
-    v, i, tpo = oit.make_scene(wd['spheres'], seed=wd['seed'], radius_min=wd['radius_min'],
+    # the oracle library's copy of the engine's scene generator (pinned to it
+    # bit for bit by tests/test_oracle_workload.py): no product code here
+    v, i, tpo = orc.make_scene(wd['spheres'], seed=wd['seed'], radius_min=wd['radius_min'],
                                radius_max=wd['radius_max'])
-    sd = oit.make_camera(W, H)
+    sd = orc.make_camera(W, H)
     t = time.perf_counter()
     fr = orc.render(ALGS.index(wd['algorithm']), W, H, sd, v, i, tpo, wd['percent_transparent'],
                     oit_layers=wd['oit_layers'], nodes_per_pixel=wd['nodes_per_pixel'], aa_type=wd['aa_type'],

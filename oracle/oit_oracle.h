@@ -119,6 +119,16 @@ enum {
 const void* or_buffer(const or_frame* f, int which, size_t* bytes);
 uint64_t or_fragment_count(const or_frame* f);
 
+/* The CPU legs' workload (oit_workload.c): the engine's seeded sphere scene
+ * generator and camera, restated. Return 0, or -1 on invalid arguments.
+ * Vertices: 10 floats each (pos.xyz, normal.xyz, color.rgba). */
+int or_scene_size(uint32_t num_objects, uint32_t stacks, uint32_t slices, uint32_t* num_vertices,
+                  uint32_t* num_triangles, uint32_t* triangles_per_object);
+int or_scene_generate(uint64_t seed, uint32_t num_objects, uint32_t stacks, uint32_t slices, float half_extent,
+                      float radius_min, float radius_max, float* vertices, uint32_t* indices);
+int or_camera(uint32_t width, uint32_t height, const float eye[3], const float target[3], float fov_y_degrees,
+              float z_near, float z_far, float* proj_view16, float* view16);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,6 +68,12 @@ def lib(variant='fp64'):
         L.or_srgb_threshold.argtypes = [ctypes.c_int]
         L.or_srgb_decode.restype = ctypes.c_double
         L.or_srgb_decode.argtypes = [ctypes.c_int]
+        U32P = ctypes.POINTER(ctypes.c_uint32)
+        L.or_scene_size.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, U32P, U32P, U32P]
+        L.or_scene_generate.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                        ctypes.c_float, ctypes.c_float, ctypes.c_float, P, P]
+        L.or_camera.argtypes = [ctypes.c_uint32, ctypes.c_uint32, P, P, ctypes.c_float, ctypes.c_float,
+                                ctypes.c_float, P, P]
         L.or_srgb_encode.restype = ctypes.c_uint32
         L.or_srgb_encode.argtypes = [ctypes.c_float]
         _libs[variant] = L
@@ -203,3 +209,39 @@ def render(algorithm, width, height, scene, vertices, indices, triangles_per_obj
                        (num_objects - num_transparent) * triangles_per_object)
     fr.draw_transparent(scene, vertices, indices, 0, num_transparent * triangles_per_object)
     return fr
+
+
+class Camera:
+    """SceneData matrices of the oracle's camera, with the attribute names of
+    the engine's scene-data structure (column-major 4x4 float32 each)."""
+
+    def __init__(self, proj_view, view):
+        self.proj_view_matrix = (ctypes.c_float * 16)(*proj_view)
+        self.view_matrix = (ctypes.c_float * 16)(*view)
+
+
+def make_scene(num_objects, seed=1, radius_min=0.05, radius_max=0.15, half_extent=1.0, stacks=16, slices=32):
+    """The engine's seeded sphere scene (vertices float32 [nv,10], indices
+    uint32 [nt,3], triangles_per_object), generated by the oracle library."""
+    L = lib()
+    nv, nt, tpo = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+    if L.or_scene_size(num_objects, stacks, slices, ctypes.byref(nv), ctypes.byref(nt), ctypes.byref(tpo)) != 0:
+        raise ValueError('invalid scene description')
+    v = np.empty((nv.value, 10), np.float32)
+    i = np.empty((nt.value, 3), np.uint32)
+    if L.or_scene_generate(seed, num_objects, stacks, slices, half_extent, radius_min, radius_max, v.ctypes.data,
+                           i.ctypes.data) != 0:
+        raise ValueError('invalid scene description')
+    return v, i, tpo.value
+
+
+def make_camera(width, height, eye=(0.0, 0.0, 3.0), target=(0.0, 0.0, 0.0), fov_y=45.0, z_near=0.1, z_far=10.0):
+    """The engine's camera (lookAt + Vulkan perspective), from the oracle library."""
+    e = np.asarray(eye, np.float32)
+    t = np.asarray(target, np.float32)
+    pv = np.empty(16, np.float32)
+    vw = np.empty(16, np.float32)
+    if lib().or_camera(width, height, e.ctypes.data, t.ctypes.data, fov_y, z_near, z_far, pv.ctypes.data,
+                       vw.ctypes.data) != 0:
+        raise ValueError('invalid camera')
+    return Camera(pv, vw)
