@@ -81,7 +81,8 @@ def parse():
                     help='batch workload: the first N of its 64 views (smaller cases for profiling)')
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
-    ap.add_argument('--raster-config', default='auto', choices=['auto', 'per-view', 'per-view-32', 'multi-view'],
+    ap.add_argument('--raster-config', default='auto',
+                    choices=['auto', 'per-view', 'per-view-longest-first', 'per-view-32', 'multi-view'],
                     help='batch workload: pin the tile-raster configuration instead of letting the graph capture '
                          'time the candidates (profilers distort those timings)')
     return ap.parse_args()
@@ -574,8 +575,9 @@ def run_batch(a, rank):
                                             record_format=fmt, flags=flags))
             r.update_scene(sd)
             recs.append(r)
-    raster_pin = {'auto': None, 'per-view': {'multi_view': 0}, 'per-view-32': {'multi_view': 0, 'warps_per_sm': 32},
-                  'multi-view': {'multi_view': 1}}[a.raster_config]
+    raster_pin = {'auto': None, 'per-view': {'multi_view': 0},
+                  'per-view-longest-first': {'multi_view': 0, 'lane_order': 1},
+                  'per-view-32': {'multi_view': 0, 'warps_per_sm': 32}, 'multi-view': {'multi_view': 1}}[a.raster_config]
     batch = oit.Batch(parallel_streams=8)
     batch.set_raster_config(raster_pin)
     batch.set_views([(r, m, h[2], 100) for r, m, h in zip(mixed, meshes, host)])
@@ -887,7 +889,8 @@ def main_batch(a, rank, world):
                                      'fragment-parallel COLOR pass, warp-aggregated node counter, atomicExch '
                                      'heads in HBM, no tile binning; list order not deterministic'},
         'autotuned_raster': dict(res['raster_cfg'], picked_by='oit_batch_render timing the candidate graphs on the '
-                                 'batch\'s frames (per-view launches at 36 and 32 warps per SM, multi-view launches)'),
+                                 'batch\'s frames (per-view launches at 36 and 32 warps per SM, views over the '
+                                 'streams in view order or longest first, multi-view launches)'),
         'resolve': resolve,
         'cpu_baseline': cpu_line,
         'cpu_baseline_fp32_omp': cpu_omp_line,

@@ -335,13 +335,18 @@ typedef struct oit_raster_config {
   uint32_t warps_per_sm;  /* register budget of the 1x linked-list, Simple, Loop64 and lock rasters:
                              36 resident warps per SM (56 registers, the default) or 32 (64 registers;
                              per-view launches only) */
+  int32_t lane_order;     /* how views are spread over the forked streams: 0 round-robin in view order;
+                             1 longest first: views in decreasing order of their frame time measured on
+                             the batch's first (one by one) frames, each to the stream with the least
+                             work so far */
 } oit_raster_config;
 
 /* Pins the batch's raster configuration; NULL (the default) lets the
  * autotuner capture the candidates (per-view launches at 36 and 32 warps per
- * SM, multi-view launches) when the graph is built, time them on the batch's
- * own frames and keep the fastest. The next oit_batch_render captures again.
- * Unknown values return OIT_ERR_INVALID_ARGUMENT. */
+ * SM, each with both lane orders, and multi-view launches) when the graph is
+ * built, time them on the batch's own frames and keep the fastest. The next
+ * oit_batch_render captures again. Unknown values return
+ * OIT_ERR_INVALID_ARGUMENT. */
 int oit_batch_set_raster_config(oit_batch* batch, const oit_raster_config* config);
 
 /* The raster configuration of the batch's current graph; OIT_ERR_STATE

@@ -185,7 +185,8 @@ def test_pinned_shape_validation():
 
 def test_raster_config_validation():
     batch = oit.Batch()
-    for cfg in ({'multi_view': 2}, {'warps_per_sm': 40}, {'multi_view': 1, 'warps_per_sm': 32}):
+    for cfg in ({'multi_view': 2}, {'warps_per_sm': 40}, {'multi_view': 1, 'warps_per_sm': 32}, {'lane_order': 2},
+                {'lane_order': -1}):
         with pytest.raises(oit.OitError) as e:
             batch.set_raster_config(cfg)
         assert e.value.status == oit.OIT_ERR_INVALID_ARGUMENT
@@ -193,4 +194,5 @@ def test_raster_config_validation():
         batch.raster_config()  # nothing captured yet
     assert e.value.status == oit.OIT_ERR_STATE
     batch.set_raster_config({'multi_view': 0, 'warps_per_sm': 32})
+    batch.set_raster_config({'multi_view': 0, 'lane_order': 1})
     batch.set_raster_config(None)

@@ -228,15 +228,17 @@ def test_cuda_graph_replay(engine, alg):
     assert r.get_error() == 0
 
 
-RASTER_CONFIGS = [{'multi_view': 0}, {'multi_view': 0, 'warps_per_sm': 32}, {'multi_view': 1}, None]
+RASTER_CONFIGS = [{'multi_view': 0}, {'multi_view': 0, 'warps_per_sm': 32}, {'multi_view': 0, 'lane_order': 1},
+                  {'multi_view': 1}, None]
 
 
 @pytest.mark.parametrize('raster_cfg', RASTER_CONFIGS)
 def test_batched_views_match_single_frames(engine, raster_cfg):
     """oit_batch_render (one CUDA graph, views on forked streams) gives every
     view the image its own oit_render_frame gives, with one raster launch per
-    view and pass (at either register budget), multi-view raster launches, or
-    the autotuner's pick of those."""
+    view and pass (at either register budget, views spread over the streams
+    in view order or longest first), multi-view raster launches, or the
+    autotuner's pick of those."""
     specs = [(1, 96, 80, 4, 12), (3, 160, 120, 16, 40), (1, 64, 64, 8, 8), (3, 128, 128, 32, 30),
              (0, 80, 60, 8, 20), (6, 96, 96, 8, 24)]
     views, refs, keep = [], [], []
@@ -257,9 +259,10 @@ def test_batched_views_match_single_frames(engine, raster_cfg):
             assert r.get_error() == 0
     got = batch.raster_config()
     if raster_cfg is None:
-        assert (got['multi_view'], got['warps_per_sm']) in ((0, 36), (0, 32), (1, 36))
+        assert (got['multi_view'], got['warps_per_sm'], got['lane_order']) in (
+            (0, 36, 0), (0, 36, 1), (0, 32, 0), (0, 32, 1), (1, 36, 0))
     else:
-        assert got == dict({'warps_per_sm': 36}, **raster_cfg)
+        assert got == dict({'warps_per_sm': 36, 'lane_order': 0}, **raster_cfg)
     assert batch.launch_count() >= len(specs) * 6
 
 

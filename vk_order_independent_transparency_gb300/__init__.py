@@ -95,7 +95,7 @@ class OitResolveShape(ctypes.Structure):
 
 
 class OitRasterConfig(ctypes.Structure):
-    _fields_ = [('multi_view', ctypes.c_int32), ('warps_per_sm', ctypes.c_uint32)]
+    _fields_ = [('multi_view', ctypes.c_int32), ('warps_per_sm', ctypes.c_uint32), ('lane_order', ctypes.c_int32)]
 
 
 class OitSceneDesc(ctypes.Structure):
@@ -523,18 +523,20 @@ class Batch:
 
     def set_raster_config(self, config):
         """Pins the tile-raster configuration ({'multi_view': 0|1,
-        'warps_per_sm': 36|32}) or, with None, lets the autotuner pick it."""
+        'warps_per_sm': 36|32, 'lane_order': 0|1}) or, with None, lets the
+        autotuner pick it."""
         if config is None:
             _check(self.lib.oit_batch_set_raster_config(self._b, None), 'oit_batch_set_raster_config')
             return
-        c = OitRasterConfig(int(config.get('multi_view', 0)), int(config.get('warps_per_sm', 36)))
+        c = OitRasterConfig(int(config.get('multi_view', 0)), int(config.get('warps_per_sm', 36)),
+                            int(config.get('lane_order', 0)))
         _check(self.lib.oit_batch_set_raster_config(self._b, ctypes.byref(c)), 'oit_batch_set_raster_config')
 
     def raster_config(self):
         """The current graph's tile-raster configuration as a dict."""
         c = OitRasterConfig()
         _check(self.lib.oit_batch_raster_config(self._b, ctypes.byref(c)), 'oit_batch_raster_config')
-        return {'multi_view': c.multi_view, 'warps_per_sm': c.warps_per_sm}
+        return {'multi_view': c.multi_view, 'warps_per_sm': c.warps_per_sm, 'lane_order': c.lane_order}
 
     def set_raster_mode(self, mode):
         """0 one raster launch per view and pass, 1 multi-view launches (both at

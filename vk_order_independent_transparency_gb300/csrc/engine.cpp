@@ -896,6 +896,9 @@ struct oit_batch {
   oit_raster_config raster_pin{};
   oit_raster_config raster_cfg{};
   bool raster_known = false;
+  // each view's frame time on the batch's first (one by one) frames: the
+  // longest-first lane order's weights
+  std::vector<float> view_ms;
   int num_sms = 0;
   cudaEvent_t rfork = nullptr, rjoin[2] = {nullptr, nullptr};
 
@@ -1243,8 +1246,30 @@ int batch_mv_rasters(const oit_view_frame* views, uint32_t n, cudaStream_t s, ui
 // multi_view, only up to its binning; the rasters then run as multi-view
 // launches), then the batched resolve. The caller has rendered plain frames
 // (buffers sized) and tuned the resolve.
+// The capture order of the views and the lane (forked stream) of each:
+// round-robin in view order, or longest first (decreasing measured frame
+// time, each view to the lane with the least work so far).
+void batch_lanes(const oit_batch* b, uint32_t n, int lane_order, std::vector<uint32_t>& order,
+                 std::vector<size_t>& lane) {
+  const size_t K = b->lanes.size();
+  order.resize(n);
+  lane.resize(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    order[i] = i;
+    lane[i] = i % K;
+  }
+  if (lane_order != 1 || b->view_ms.size() != n) return;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return b->view_ms[x] > b->view_ms[y]; });
+  std::vector<double> load(K, 0.0);
+  for (uint32_t i : order) {
+    const size_t k = (size_t)(std::min_element(load.begin(), load.end()) - load.begin());
+    lane[i] = k;
+    load[k] += b->view_ms[i];
+  }
+}
+
 int batch_capture(oit_batch* b, const oit_view_frame* views, uint32_t n, cudaStream_t s, bool multi_view,
-                  cudaGraphExec_t* exec, uint64_t* launches) {
+                  int lane_order, cudaGraphExec_t* exec, uint64_t* launches) {
   *exec = nullptr;
   OIT_TRY_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed), "capture");
   int r = OIT_OK;
@@ -1254,14 +1279,18 @@ int batch_capture(oit_batch* b, const oit_view_frame* views, uint32_t n, cudaStr
   uint64_t nodes = 0;
   b->ctxs.assign(n, nullptr);
   b->opaque_valid.assign(n, false);
-  for (uint32_t i = 0; i < n && e == cudaSuccess && r == OIT_OK; ++i) {
+  std::vector<uint32_t> order;
+  std::vector<size_t> lane;
+  batch_lanes(b, n, lane_order, order, lane);
+  for (uint32_t j = 0; j < n && e == cudaSuccess && r == OIT_OK; ++j) {
+    const uint32_t i = order[j];
     const oit_view_frame& v = views[i];
     oit_context* c = v.ctx;
     const uint64_t l0 = c->launches;
     c->graph_stats.clear();
     c->capturing = true;
     r = c->render_frame_body(view_mesh(v), view_tpo(v), v.percent_transparent, v.out_rgba8_device,
-                             b->lanes[i % K], !multi_view && !c->batch_resolvable(), !multi_view);
+                             b->lanes[lane[i]], !multi_view && !c->batch_resolvable(), !multi_view);
     c->capturing = false;
     nodes += c->launches - l0;
     c->launches = l0;
@@ -1598,26 +1627,64 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
   for (uint32_t i = 0; i < n; ++i) fit = views[i].ctx->graph_bins_fit() && fit;
   if (!fit || sig != b->sig) b->drop();
   if (!b->exec) {
-    // plain frames, one view after the other, size every buffer; views the
-    // batched resolve handles are resolved together afterwards
+    // plain frames, one view after the other, size every buffer (and time
+    // each view for the longest-first lane order); views the batched resolve
+    // handles are resolved together afterwards
+    std::vector<cudaEvent_t> marks(n + 1, nullptr);
+    auto free_marks = [&]() {
+      for (cudaEvent_t ev : marks)
+        if (ev) cudaEventDestroy(ev);
+    };
+    for (cudaEvent_t& ev : marks) {
+      const cudaError_t ce = cudaEventCreate(&ev);
+      if (ce != cudaSuccess) {
+        ev = nullptr;
+        free_marks();
+        return cuda_status(ce, "event");
+      }
+    }
     for (uint32_t i = 0; i < n; ++i) {
       const oit_view_frame& v = views[i];
-      int r = v.ctx->render_frame_body(view_mesh(v), view_tpo(v), v.percent_transparent,
-                                       v.out_rgba8_device, s, !v.ctx->batch_resolvable());
-      if (r != OIT_OK) return r;
+      cudaError_t ce = cudaEventRecord(marks[i], s);
+      int r = ce == cudaSuccess ? v.ctx->render_frame_body(view_mesh(v), view_tpo(v), v.percent_transparent,
+                                                            v.out_rgba8_device, s, !v.ctx->batch_resolvable())
+                                : cuda_status(ce, "event");
+      if (r != OIT_OK) {
+        free_marks();
+        return r;
+      }
+    }
+    {
+      const cudaError_t ce = cudaEventRecord(marks[n], s);
+      if (ce != cudaSuccess) {
+        free_marks();
+        return cuda_status(ce, "event");
+      }
     }
     int pr = batch_prepare_resolve(b, views, n);
     if (pr != OIT_OK) return pr;
     uint64_t scratch = 0;
     pr = b->r_tuned ? batch_resolve_launch(b, s, &scratch) : batch_autotune(b, s);
     if (pr != OIT_OK) return pr;
-    OIT_TRY_CUDA(cudaStreamSynchronize(s), "sync");
+    {
+      const cudaError_t ce = cudaStreamSynchronize(s);
+      if (ce == cudaSuccess) {
+        b->view_ms.assign(n, 0.0f);
+        for (uint32_t i = 0; i < n; ++i)
+          if (cudaEventElapsedTime(&b->view_ms[i], marks[i], marks[i + 1]) != cudaSuccess) b->view_ms[i] = 0.0f;
+      }
+      free_marks();
+      OIT_TRY_CUDA(ce, "sync");
+    }
     // the graph: as pinned, or each raster configuration (per-view launches at
-    // the default and at the 32-warp register budget, multi-view launches)
-    // captured and timed on these frames, the fastest kept
+    // the default and at the 32-warp register budget, each in both lane
+    // orders, multi-view launches) captured and timed on these frames, the
+    // fastest kept
     std::vector<oit_raster_config> cands;
     if (b->raster_pinned) cands.push_back(b->raster_pin);
-    else cands = {oit_raster_config{0, 0}, oit_raster_config{0, 32}, oit_raster_config{1, 0}};
+    else
+      cands = {oit_raster_config{0, 0, 0}, oit_raster_config{0, 0, 1}, oit_raster_config{0, 32, 0},
+               oit_raster_config{0, 32, 1}, oit_raster_config{1, 0, 0}};
     cudaGraphExec_t best = nullptr;
     uint64_t best_launches = 0;
     float best_ms = 1e30f;
@@ -1630,7 +1697,7 @@ int oit_batch_render(oit_batch* b, const oit_view_frame* views, uint32_t n, void
         saved[i] = views[i].ctx->raster_wpsm;
         views[i].ctx->raster_wpsm = (int)cfg.warps_per_sm;
       }
-      int r = batch_capture(b, views, n, s, cfg.multi_view == 1, &ex, &nodes);
+      int r = batch_capture(b, views, n, s, cfg.multi_view == 1, cfg.lane_order, &ex, &nodes);
       for (uint32_t i = 0; i < n; ++i) views[i].ctx->raster_wpsm = saved[i];
       if (r == OIT_OK && !b->raster_pinned) {
         float ms = 0.f;
@@ -1754,10 +1821,13 @@ int oit_batch_set_raster_config(oit_batch* b, const oit_raster_config* cfg) {
     if (cfg->multi_view != 0 && cfg->multi_view != 1) return OIT_ERR_INVALID_ARGUMENT;
     if (cfg->warps_per_sm != 0 && cfg->warps_per_sm != 32 && cfg->warps_per_sm != 36) return OIT_ERR_INVALID_ARGUMENT;
     if (cfg->multi_view && cfg->warps_per_sm == 32) return OIT_ERR_INVALID_ARGUMENT;
+    if (cfg->lane_order != 0 && cfg->lane_order != 1) return OIT_ERR_INVALID_ARGUMENT;
   }
   if (b->stream) OIT_TRY_CUDA(cudaStreamSynchronize(b->stream), "sync");
   b->raster_pinned = cfg != nullptr;
-  if (cfg) b->raster_pin = oit_raster_config{cfg->multi_view, cfg->warps_per_sm == 36 ? 0u : cfg->warps_per_sm};
+  if (cfg)
+    b->raster_pin =
+        oit_raster_config{cfg->multi_view, cfg->warps_per_sm == 36 ? 0u : cfg->warps_per_sm, cfg->lane_order};
   b->drop();  // captured again on the next render
   return OIT_OK;
 }
