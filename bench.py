@@ -578,7 +578,7 @@ def run_batch(a, rank):
     raster_pin = {'auto': None, 'per-view': {'multi_view': 0},
                   'per-view-longest-first': {'multi_view': 0, 'lane_order': 1},
                   'per-view-32': {'multi_view': 0, 'warps_per_sm': 32}, 'multi-view': {'multi_view': 1}}[a.raster_config]
-    batch = oit.Batch(parallel_streams=8)
+    batch = oit.Batch(parallel_streams=16)
     batch.set_raster_config(raster_pin)
     batch.set_views([(r, m, h[2], 100) for r, m, h in zip(mixed, meshes, host)])
 
@@ -637,7 +637,7 @@ def run_batch(a, rank):
                                          flags=oit.OIT_FLAG_HALF_COLOR | oit.OIT_FLAG_ARRIVAL_ORDER))
         ra.update_scene(oit.make_camera(vd['width'], vd['height']))
         arrival.append(ra)
-    batch_arr = oit.Batch(parallel_streams=8)
+    batch_arr = oit.Batch(parallel_streams=16)
     batch_arr.set_raster_config(raster_pin)
     batch_arr.set_views([(r, m, h[2], 100) for r, m, h in zip(arrival, meshes, host)])
     for _ in range(max(3, a.warmup)):
@@ -700,7 +700,7 @@ def run_batch(a, rank):
             for st, n in zip(starts[:-1], counts)]
         out_dev = torch.empty(int(out_at[-1]), dtype=torch.uint8, device='cuda')
         out_host = torch.empty(int(out_at[-1]), dtype=torch.uint8).pin_memory()
-        bt = oit.Batch(parallel_streams=8)
+        bt = oit.Batch(parallel_streams=16)
         bt.set_raster_config(raster_pin)
         bt.set_views([(r, m, 0, 100, out_dev.data_ptr() + int(o)) for r, m, o in zip(mixed, inst_views, out_at)])
         pipe.append(dict(scene=scene_dev, out=out_dev, host=out_host, batch=bt, meshes=inst_views,
@@ -863,7 +863,7 @@ def main_batch(a, rank, world):
         'data': 'synthetic: 64 seeded UV-sphere scenes, inputs resident in HBM',
         'config': dict(workload_dict(BATCH_WORKLOAD), views=len(res['views']), fragments_per_batch=res['frags'],
                        parallelism='replicas' if world > 1 else 'single',
-                       frame='all 64 views in one CUDA graph (binning on 8 parallel streams)',
+                       frame='all 64 views in one CUDA graph (views on 16 forked streams)',
                        l2='working set larger than L2, no flush'),
         'plain_fp32': {'value': round(plain, 3), 'unit': 'Mfragments/s', 'ms_per_step': round(t_plain / a.steps, 4),
                        'path': 'one oit_render_frame per view, RGBA32F records, no graph'},
