@@ -30,7 +30,7 @@ constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;  // 4096 elements per block
 constexpr int kRadixThreads = 256;
-constexpr int kRadixRounds = 16;
+constexpr int kRadixRounds = 8;
 constexpr int kRadixBits = 8;
 constexpr int kRadixBins = 1 << kRadixBits;
 
@@ -287,12 +287,12 @@ __device__ __forceinline__ uint32_t setup_clipped(const SetupParams& p, int S, u
 }
 
 // Triangles per block of the clip kernel (4 per thread) and of the emit
-// kernel (one per thread): the pair-count sums are per 1024 triangles.
-constexpr int kClipThreads = 256;
+// kernel (one per thread): the pair-count sums are per 512 triangles.
+constexpr int kClipThreads = 128;
 constexpr int kEmitItems = 4;
 constexpr int kEmitTile = kClipThreads * kEmitItems;
 
-// The marked triangles of each 1024-triangle block are clipped one by one;
+// The marked triangles of each 512-triangle block are clipped one by one;
 // with block_sums, the block's pair count (after clipping) is written there,
 // the first level of the pair-offset scan. pair_count is 16-byte aligned.
 __global__ void __launch_bounds__(kClipThreads) k_setup_clip(SetupParams p, int S, uint32_t* __restrict__ block_sums) {
@@ -478,7 +478,7 @@ __device__ __forceinline__ uint32_t emit_bbox(uint2 bb, uint32_t t, uint32_t til
   return j;
 }
 
-// The pairs of the block's 1024 triangles, one per thread: a triangle's
+// The pairs of the block's 512 triangles, one per thread: a triangle's
 // offset is the scanned block sum plus the exclusive prefix of the counts
 // before it in the block (written to pair_offset, which the bin-overflow walk
 // reads); it emits its first (or only) half's tiles, then the second half's
@@ -509,11 +509,11 @@ __global__ void __launch_bounds__(kEmitTile) k_emit(const uint32_t* __restrict__
 // ---------------------------------------------------------------------------
 // Stable LSD radix sort of (key, value) pairs, 8-bit digits.
 //
-// The pairs are cut into at most kSortBlocks chunks (multiples of 4096
+// The pairs are cut into at most kSortBlocks chunks (multiples of 2048
 // pairs). k_radix_hist counts each chunk's digits; k_radix_scatter derives
 // its chunk's output offset for every digit from those counts itself (the
 // digit's start over all chunks plus the counts of the chunks before it) and
-// moves the chunk 4096 pairs at a time: each warp ranks its 512 consecutive
+// moves the chunk 2048 pairs at a time: each warp ranks its 256 consecutive
 // pairs with its own shared-memory counters, so a sub-tile costs three block
 // barriers. Pairs keep their order within a digit: the sort is stable.
 // ---------------------------------------------------------------------------
@@ -522,7 +522,7 @@ __device__ __forceinline__ size_t pair_count_of(const uint32_t* total, size_t ca
   return t < capacity ? t : capacity;
 }
 
-constexpr int kSortSubTile = kRadixThreads * kRadixRounds;  // 4096 pairs: 8 warps x 16 rounds of 32
+constexpr int kSortSubTile = kRadixThreads * kRadixRounds;  // 2048 pairs: 8 warps x 8 rounds of 32
 constexpr int kSortWarps = kRadixThreads / 32;
 
 // Digit counts of chunk blockIdx.x, written digit-major per chunk:
@@ -595,7 +595,7 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t*
 #pragma unroll
     for (int k = 0; k < kRadixBins / 32; ++k) wcount[warp][lane + 32 * k] = 0;
     __syncwarp();
-    // this warp's 512 consecutive pairs of the sub-tile, 32 per round
+    // this warp's 256 consecutive pairs of the sub-tile, 32 per round
     const size_t wbase = sub + (size_t)warp * (32 * kRadixRounds);
     uint32_t key[kRadixRounds], val[kRadixRounds], dr[kRadixRounds];
 #pragma unroll
@@ -697,7 +697,7 @@ cudaError_t launch_fill_f4(float4* dst, float4 value, size_t count, cudaStream_t
 
 namespace {
 // k_setup, then k_setup_clip over the triangles it marked (and, with
-// block_sums, the pair count of every 1024-triangle block)
+// block_sums, the pair count of every 512-triangle block)
 cudaError_t launch_setup(const SetupParams& sp, uint32_t* block_sums, cudaStream_t s, uint64_t* launches) {
   const uint32_t n = sp.num_triangles;
   const int S = sp.samples > 1 ? sp.samples : 1;
@@ -710,7 +710,7 @@ cudaError_t launch_setup(const SetupParams& sp, uint32_t* block_sums, cudaStream
   return cudaGetLastError();
 }
 
-// Pairs per chunk of the radix sort: whole 4096-pair sub-tiles, at most
+// Pairs per chunk of the radix sort: whole 2048-pair sub-tiles, at most
 // kSortBlocks chunks.
 constexpr size_t kSortBlocks = 128;
 size_t sort_chunk(size_t capacity) {
@@ -733,7 +733,7 @@ cudaError_t bin_setup_only(const SetupParams& sp, cudaStream_t s, uint64_t* laun
   return launch_setup(sp, nullptr, s, launches);
 }
 
-// Binning, step 1: setup, clip, pair counts per 1024-triangle block and their
+// Binning, step 1: setup, clip, pair counts per 512-triangle block and their
 // exclusive scan (in b.scan_tmp, read by k_emit); the number of (tile,
 // triangle) pairs lands in b.total (device).
 cudaError_t bin_setup_scan(const SetupParams& sp, Bins& b, cudaStream_t s, uint64_t* launches) {
