@@ -525,12 +525,14 @@ __device__ __forceinline__ size_t pair_count_of(const uint32_t* total, size_t ca
 constexpr int kSortSubTile = kRadixThreads * kRadixRounds;  // 2048 pairs: 8 warps x 8 rounds of 32
 constexpr int kSortWarps = kRadixThreads / 32;
 
-// Digit counts of chunk blockIdx.x, written digit-major per chunk:
-// counts[chunk * 256 + digit]. One shared-memory atomic per distinct digit per
-// warp (tile ids of neighbouring pairs are mostly equal).
+// Digit counts of chunk blockIdx.x: counts[chunk * 256 + digit], or, with
+// digit_major (many chunks, scanned in place before the scatter),
+// counts[digit * gridDim.x + chunk]. One shared-memory atomic per distinct
+// digit per warp (tile ids of neighbouring pairs are mostly equal).
 __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t* __restrict__ keys,
                                                               const uint32_t* __restrict__ total, size_t capacity,
-                                                              int shift, size_t chunk, uint32_t* __restrict__ counts) {
+                                                              int shift, size_t chunk, bool digit_major,
+                                                              uint32_t* __restrict__ counts) {
   __shared__ uint32_t h[kRadixBins];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -552,7 +554,8 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t* __
     }
   }
   __syncthreads();
-  counts[(size_t)blockIdx.x * kRadixBins + threadIdx.x] = h[threadIdx.x];
+  if (digit_major) counts[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+  else counts[(size_t)blockIdx.x * kRadixBins + threadIdx.x] = h[threadIdx.x];
 }
 
 __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t* __restrict__ keys_in,
@@ -561,7 +564,7 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t*
                                                                  uint32_t* __restrict__ vals_out,
                                                                  const uint32_t* __restrict__ total, size_t capacity,
                                                                  int shift, size_t chunk, uint32_t nchunks,
-                                                                 const uint32_t* __restrict__ counts) {
+                                                                 bool scanned, const uint32_t* __restrict__ counts) {
   __shared__ uint32_t base[kRadixBins];             // output position of the chunk's next pair of each digit
   __shared__ uint32_t wcount[kSortWarps][kRadixBins];  // per warp: counts, then exclusive offsets in the sub-tile
   __shared__ uint32_t sub_total[kRadixBins];
@@ -571,7 +574,11 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t*
   const size_t n = pair_count_of(total, capacity);
   const size_t beg = (size_t)blockIdx.x * chunk;
   // this digit's pairs in all chunks, and in the chunks before this one
-  {
+  if (scanned) {
+    // the digit-major counts, scanned: this chunk's output offset per digit
+    base[threadIdx.x] = __ldg(&counts[(size_t)threadIdx.x * nchunks + blockIdx.x]);
+    __syncthreads();
+  } else {
     // 32 independent loads in flight per thread: the chunks' counts are read
     // by every block, so their latency, not their bytes, is the cost
     const uint32_t d = threadIdx.x;
@@ -710,10 +717,15 @@ cudaError_t launch_setup(const SetupParams& sp, uint32_t* block_sums, cudaStream
   return cudaGetLastError();
 }
 
-// Pairs per chunk of the radix sort: whole 2048-pair sub-tiles, at most
-// kSortBlocks chunks.
+// Pairs per chunk of the radix sort. Up to kSortDirectPairs pairs: whole
+// 2048-pair sub-tiles, at most kSortBlocks chunks, each scatter block summing
+// the counts of the chunks before it. Beyond: one sub-tile per chunk (every
+// block busy on a large view), the digit-major counts scanned in place.
 constexpr size_t kSortBlocks = 128;
+constexpr size_t kSortDirectPairs = 8u << 20;
+bool sort_scanned(size_t capacity) { return capacity > kSortDirectPairs; }
 size_t sort_chunk(size_t capacity) {
+  if (sort_scanned(capacity)) return kSortSubTile;
   const size_t per = (capacity + kSortBlocks - 1) / kSortBlocks;
   const size_t sub = (per + kSortSubTile - 1) / kSortSubTile * kSortSubTile;
   return sub > (size_t)kSortSubTile ? sub : (size_t)kSortSubTile;
@@ -763,11 +775,15 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles
   const size_t chunk = sort_chunk(b.capacity);
   const uint32_t nchunks = (uint32_t)std::max<size_t>((b.capacity + chunk - 1) / chunk, 1);
   uint32_t *kin = b.keys, *vin = b.tris, *kout = b.keys_alt, *vout = b.tris_alt;
+  const bool scanned = sort_scanned(b.capacity);
   for (int shift = 0; shift < key_bits; shift += kRadixBits) {
-    k_radix_hist<<<nchunks, kRadixThreads, 0, s>>>(kin, b.total, b.capacity, shift, chunk, b.hist);
+    k_radix_hist<<<nchunks, kRadixThreads, 0, s>>>(kin, b.total, b.capacity, shift, chunk, scanned, b.hist);
     ++*launches;
+    if (scanned && (e = scan_exclusive(b.hist, b.hist, (size_t)nchunks * kRadixBins, b.hist + (size_t)nchunks * kRadixBins,
+                                       nullptr, s, launches)) != cudaSuccess)
+      return e;
     k_radix_scatter<<<nchunks, kRadixThreads, 0, s>>>(kin, vin, kout, vout, b.total, b.capacity, shift, chunk,
-                                                      nchunks, b.hist);
+                                                      nchunks, scanned, b.hist);
     ++*launches;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     std::swap(kin, kout);
@@ -789,8 +805,12 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles
   return cudaGetLastError();
 }
 
-// Digit counts of at most kSortBlocks chunks.
-size_t radix_hist_words(size_t) { return kSortBlocks * kRadixBins; }
+// Digit counts of the chunks (and, for the scanned sort, its scan scratch).
+size_t radix_hist_words(size_t pairs) {
+  if (!sort_scanned(pairs)) return kSortBlocks * kRadixBins;
+  const size_t words = (pairs + kSortSubTile - 1) / kSortSubTile * kRadixBins;
+  return words + scan_scratch_words(words);
+}
 
 void srgb_host_tables(float* thr256, float* dec256) {
   static const float thr[256] = OIT_SRGB_THR_INIT;
