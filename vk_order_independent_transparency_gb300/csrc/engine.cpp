@@ -294,7 +294,7 @@ struct oit_context {
       OIT_TRY_CUDA(tris_alt.ensure(cap * 4), "alloc tris");
       pair_cap = cap;
     }
-    const size_t hist_words = std::max<size_t>(oit::radix_hist_words(pair_cap), 256);
+    const size_t hist_words = oit::radix_hist_words(pair_cap, true);
     OIT_TRY_CUDA(hist.ensure(hist_words * 4), "alloc hist");
     const size_t scan_words = oit::bin_scan_words(tri_cap);
     OIT_TRY_CUDA(scan_tmp.ensure(scan_words * 4), "alloc scan");
@@ -365,6 +365,9 @@ struct oit_context {
     b.hist = hist.as<uint32_t>();
     b.total = total.as<uint32_t>();
     b.capacity = pair_cap;
+    // measured: the 64-view batch 18.64 ms at 8M against 18.96 at 1M; a
+    // 2560x1440 MSAA-8 frame alone 6.38 ms at 1M against 6.51 at 8M
+    b.sort_direct_max = in_batch ? (8u << 20) : (1u << 20);
     return b;
   }
 
@@ -741,6 +744,7 @@ struct oit_context {
 
   // ---- CUDA graph of a whole frame (OIT_FLAG_CUDA_GRAPH) ----
   bool capturing = false;
+  bool in_batch = false;  // binning inside a batch graph, beside other views
   cudaGraphExec_t graph_exec = nullptr;
   uint64_t graph_sig = 0;
   uint64_t graph_launches = 0;
@@ -1289,9 +1293,11 @@ int batch_capture(oit_batch* b, const oit_view_frame* views, uint32_t n, cudaStr
     const uint64_t l0 = c->launches;
     c->graph_stats.clear();
     c->capturing = true;
+    c->in_batch = true;
     r = c->render_frame_body(view_mesh(v), view_tpo(v), v.percent_transparent, v.out_rgba8_device,
                              b->lanes[lane[i]], !multi_view && !c->batch_resolvable(), !multi_view);
     c->capturing = false;
+    c->in_batch = false;
     nodes += c->launches - l0;
     c->launches = l0;
     c->last_stream = s;

@@ -155,9 +155,9 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   // The rest holds the pairs (16 bytes each: keys, triangles, ping-pong), the
   // radix sort's digit counts and the pair-offset scan's words.
   const size_t left = a.cap - ((a.off + 255) & ~(size_t)255);
-  const size_t reserve = (radix_hist_words(0) + bin_scan_words(N)) * 4 + 6 * 256;  // + alignment of 6 regions
+  const size_t reserve = (radix_hist_words(0, false) + bin_scan_words(N)) * 4 + 6 * 256;  // + alignment of 6 regions
   size_t pair_cap = left > reserve ? ((left - reserve) / 16) & ~(size_t)4095 : 0;
-  const size_t hist_words = radix_hist_words(pair_cap);
+  const size_t hist_words = radix_hist_words(pair_cap, false);
   const size_t scan_n = bin_scan_words(N);
   Bins b{};
   b.keys = a.take<uint32_t>(pair_cap * 4);
@@ -173,6 +173,7 @@ extern "C" int oit_render_frame_noalloc(const oit_state* st, const oit_scene_dat
   b.pair_offset = pair_offset;
   b.total = words + 1;
   b.capacity = pair_cap;
+  b.sort_direct_max = ~(size_t)0;  // the arena holds the chunked sort's counts only
 
   // Calls share the arena and find the previous call's contents: clear what
   // must start at zero (error bits, pair count, node counter, fragment count).

@@ -73,6 +73,10 @@ struct Bins {
   size_t capacity;
   size_t scan_tmp_words;
   size_t hist_words;
+  // the radix sort keeps a view's pairs in at most 128 chunks up to this many
+  // pairs (a view sorted beside others: they fill the GPU), and beyond it
+  // spreads them over every block (a view sorted alone)
+  size_t sort_direct_max;
 };
 
 enum class Alg : int {
@@ -248,7 +252,8 @@ struct ResolveBatch {
 cudaError_t bin_setup_scan(const SetupParams& sp, Bins& b, cudaStream_t s, uint64_t* launches);
 cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles, uint32_t* error, cudaStream_t s,
                      uint64_t* launches);
-size_t radix_hist_words(size_t pairs);
+// with_scanned: room for the sort beyond sort_direct_max as well.
+size_t radix_hist_words(size_t pairs, bool with_scanned);
 // Triangle blocks of the clip and emit kernels, and the words of b.scan_tmp
 // (their pair counts, scanned in place, and the scan's scratch).
 size_t emit_blocks(size_t tris);

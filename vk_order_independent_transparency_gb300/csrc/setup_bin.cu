@@ -717,15 +717,14 @@ cudaError_t launch_setup(const SetupParams& sp, uint32_t* block_sums, cudaStream
   return cudaGetLastError();
 }
 
-// Pairs per chunk of the radix sort. Up to kSortDirectPairs pairs: whole
-// 2048-pair sub-tiles, at most kSortBlocks chunks, each scatter block summing
-// the counts of the chunks before it. Beyond: one sub-tile per chunk (every
-// block busy on a large view), the digit-major counts scanned in place.
+// Pairs per chunk of the radix sort. Up to direct_max pairs: whole 2048-pair
+// sub-tiles, at most kSortBlocks chunks, each scatter block summing the counts
+// of the chunks before it. Beyond: one sub-tile per chunk (every block busy),
+// the digit-major counts scanned in place.
 constexpr size_t kSortBlocks = 128;
-constexpr size_t kSortDirectPairs = 8u << 20;
-bool sort_scanned(size_t capacity) { return capacity > kSortDirectPairs; }
-size_t sort_chunk(size_t capacity) {
-  if (sort_scanned(capacity)) return kSortSubTile;
+bool sort_scanned(size_t capacity, size_t direct_max) { return capacity > direct_max; }
+size_t sort_chunk(size_t capacity, size_t direct_max) {
+  if (sort_scanned(capacity, direct_max)) return kSortSubTile;
   const size_t per = (capacity + kSortBlocks - 1) / kSortBlocks;
   const size_t sub = (per + kSortSubTile - 1) / kSortSubTile * kSortSubTile;
   return sub > (size_t)kSortSubTile ? sub : (size_t)kSortSubTile;
@@ -772,10 +771,10 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles
     ++*launches;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
-  const size_t chunk = sort_chunk(b.capacity);
+  const size_t chunk = sort_chunk(b.capacity, b.sort_direct_max);
   const uint32_t nchunks = (uint32_t)std::max<size_t>((b.capacity + chunk - 1) / chunk, 1);
   uint32_t *kin = b.keys, *vin = b.tris, *kout = b.keys_alt, *vout = b.tris_alt;
-  const bool scanned = sort_scanned(b.capacity);
+  const bool scanned = sort_scanned(b.capacity, b.sort_direct_max);
   for (int shift = 0; shift < key_bits; shift += kRadixBits) {
     k_radix_hist<<<nchunks, kRadixThreads, 0, s>>>(kin, b.total, b.capacity, shift, chunk, scanned, b.hist);
     ++*launches;
@@ -806,10 +805,11 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles
 }
 
 // Digit counts of the chunks (and, for the scanned sort, its scan scratch).
-size_t radix_hist_words(size_t pairs) {
-  if (!sort_scanned(pairs)) return kSortBlocks * kRadixBins;
+size_t radix_hist_words(size_t pairs, bool with_scanned) {
+  const size_t direct = kSortBlocks * kRadixBins;
+  if (!with_scanned) return direct;
   const size_t words = (pairs + kSortSubTile - 1) / kSortSubTile * kRadixBins;
-  return words + scan_scratch_words(words);
+  return std::max(direct, words + scan_scratch_words(words));
 }
 
 void srgb_host_tables(float* thr256, float* dec256) {
