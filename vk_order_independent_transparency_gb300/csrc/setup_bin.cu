@@ -291,7 +291,6 @@ __device__ __forceinline__ uint32_t setup_clipped(const SetupParams& p, int S, u
 constexpr int kClipThreads = 128;
 constexpr int kEmitItems = 4;
 constexpr int kEmitTile = kClipThreads * kEmitItems;
-static_assert(kEmitTile == 2 * 256, "k_emit clears and flushes its two chunks' digit counts one word per thread");
 
 // The marked triangles of each 512-triangle block are clipped one by one;
 // with block_sums, the block's pair count (after clipping) is written there,
@@ -456,24 +455,9 @@ cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, size_t n, uint32_t
 // ---------------------------------------------------------------------------
 // Pair emission: pair j of triangle t lands at pair_offset[t] + j.
 // ---------------------------------------------------------------------------
-// Digit counts of the radix sort's first pass, taken while the pairs are
-// written: the pair at `pos` lands in chunk pos / chunk; the block's first two
-// chunks count in shared memory (h0), any later one straight into `counts`.
-struct EmitCount {
-  uint32_t* h0;           // [2][256] shared
-  uint32_t* counts;       // the sort's chunk counts (zeroed before k_emit)
-  uint32_t chunk, nchunks, c_first;
-  bool digit_major;
-  __device__ __forceinline__ void add(uint32_t pos, uint32_t key) const {
-    const uint32_t c = pos / chunk, d = key & 255u;
-    if (c - c_first < 2u) atomicAdd(&h0[(c - c_first) * 256u + d], 1u);
-    else atomicAdd(&counts[digit_major ? (size_t)d * nchunks + c : (size_t)c * 256u + d], 1u);
-  }
-};
-
 __device__ __forceinline__ uint32_t emit_bbox(uint2 bb, uint32_t t, uint32_t tile_base, int tiles_x, uint32_t off,
                                               uint32_t j, uint32_t* __restrict__ keys, uint32_t* __restrict__ tris,
-                                              size_t capacity, const EmitCount& ec) {
+                                              size_t capacity) {
   const int bx0 = bb.x & 0xFFFF, by0 = bb.x >> 16, bx1 = bb.y & 0xFFFF, by1 = (bb.y >> 16) & 0x7FFF;
   if (bx0 > bx1 || by0 > by1) return j;
   const int tx0 = bx0 / kTile, ty0 = by0 / kTile, tx1 = bx1 / kTile, ty1 = by1 / kTile;
@@ -487,10 +471,8 @@ __device__ __forceinline__ uint32_t emit_bbox(uint2 bb, uint32_t t, uint32_t til
       if (pos >= capacity) return j;
       const int lx0 = max(bx0 - tx * kTile, 0), lx1 = min(bx1 - tx * kTile, kTile - 1);
       const uint32_t cols = (lx0 <= 7 ? 0x55u : 0u) | (lx1 >= 8 ? 0xAAu : 0u);
-      const uint32_t key = (tile_base + (uint32_t)(ty * tiles_x + tx)) | ((rows & cols) << kMaskShift);
-      keys[pos] = key;
+      keys[pos] = (tile_base + (uint32_t)(ty * tiles_x + tx)) | ((rows & cols) << kMaskShift);
       tris[pos] = t;
-      ec.add((uint32_t)pos, key);
     }
   }
   return j;
@@ -500,9 +482,7 @@ __device__ __forceinline__ uint32_t emit_bbox(uint2 bb, uint32_t t, uint32_t til
 // offset is the scanned block sum plus the exclusive prefix of the counts
 // before it in the block (written to pair_offset, which the bin-overflow walk
 // reads); it emits its first (or only) half's tiles, then the second half's
-// (record n + t) when the near-plane clip split it. The block's pairs are
-// consecutive, so the first radix pass's digit counts of the one or two chunks
-// they fall in add up in shared memory, then into `counts`.
+// (record n + t) when the near-plane clip split it.
 __global__ void __launch_bounds__(kEmitTile) k_emit(const uint32_t* __restrict__ pair_count,
                                                     uint32_t* __restrict__ pair_offset,
                                                     const uint32_t* __restrict__ block_offsets,
@@ -510,31 +490,20 @@ __global__ void __launch_bounds__(kEmitTile) k_emit(const uint32_t* __restrict__
                                                     uint32_t opaque_from, uint32_t num_tiles,
                                                     uint32_t* __restrict__ keys, uint32_t* __restrict__ tris,
                                                     size_t capacity, const uint32_t* __restrict__ total,
-                                                    uint32_t* err, uint32_t* __restrict__ counts, uint32_t chunk,
-                                                    uint32_t nchunks, bool digit_major) {
+                                                    uint32_t* err) {
   __shared__ uint32_t smem[64];
-  __shared__ uint32_t h0[2 * 256];
-  h0[threadIdx.x] = 0u;  // kEmitTile == 512 threads: one word each
   if (blockIdx.x == 0 && threadIdx.x == 0 && *total > capacity) atomicOr(err, 1u);  // OIT_DEVERR_BIN_OVERFLOW
   const uint32_t t = blockIdx.x * kEmitTile + threadIdx.x;
   const uint32_t c = t < n ? __ldg(&pair_count[t]) : 0u;
   uint32_t block_total;
-  const uint32_t block_first = block_offsets[blockIdx.x];
-  const uint32_t off = block_exclusive_scan(c, &block_total, smem) + block_first;  // also orders the h0 clears
-  const EmitCount ec{h0, counts, chunk, nchunks, block_first / chunk, digit_major};
-  if (t < n) {
-    pair_offset[t] = off;
-    if (c) {
-      const uint2 bb = bbox[t];
-      const uint32_t tile_base = t < opaque_from ? num_tiles : 0u;
-      const uint32_t j = emit_bbox(bb, t, tile_base, tiles_x, off, 0u, keys, tris, capacity, ec);
-      if (bb.y >> 31) emit_bbox(bbox[n + t], n + t, tile_base, tiles_x, off, j, keys, tris, capacity, ec);
-    }
-  }
-  __syncthreads();
-  const uint32_t v = h0[threadIdx.x];
-  const uint32_t ch = ec.c_first + threadIdx.x / 256u, d = threadIdx.x & 255u;
-  if (v && ch < nchunks) atomicAdd(&counts[digit_major ? (size_t)d * nchunks + ch : (size_t)ch * 256u + d], v);
+  const uint32_t off = block_exclusive_scan(c, &block_total, smem) + block_offsets[blockIdx.x];
+  if (t >= n) return;
+  pair_offset[t] = off;
+  if (!c) return;
+  const uint2 bb = bbox[t];
+  const uint32_t tile_base = t < opaque_from ? num_tiles : 0u;
+  const uint32_t j = emit_bbox(bb, t, tile_base, tiles_x, off, 0u, keys, tris, capacity);
+  if (bb.y >> 31) emit_bbox(bbox[n + t], n + t, tile_base, tiles_x, off, j, keys, tris, capacity);
 }
 
 // ---------------------------------------------------------------------------
@@ -795,25 +764,20 @@ cudaError_t bin_sort(const SetupParams& sp, Bins& b, int key_bits, int num_tiles
                      uint64_t* launches) {
   cudaError_t e;
   const uint32_t n = sp.num_triangles;
-  const size_t chunk = sort_chunk(b.capacity, b.sort_direct_max);
-  const uint32_t nchunks = (uint32_t)std::max<size_t>((b.capacity + chunk - 1) / chunk, 1);
-  const bool scanned = sort_scanned(b.capacity, b.sort_direct_max);
-  // the first pass's digit counts come from k_emit: start them at zero
-  if ((e = cudaMemsetAsync(b.hist, 0, (size_t)nchunks * kRadixBins * sizeof(uint32_t), s)) != cudaSuccess) return e;
   if (n > 0) {
     k_emit<<<(unsigned)emit_blocks(n), kEmitTile, 0, s>>>(sp.pair_count, b.pair_offset, b.scan_tmp, sp.bbox, n,
                                                           sp.tiles_x, sp.opaque_from, (uint32_t)sp.num_tiles, b.keys,
-                                                          b.tris, b.capacity, b.total, error, b.hist,
-                                                          (uint32_t)chunk, nchunks, scanned);
+                                                          b.tris, b.capacity, b.total, error);
     ++*launches;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
+  const size_t chunk = sort_chunk(b.capacity, b.sort_direct_max);
+  const uint32_t nchunks = (uint32_t)std::max<size_t>((b.capacity + chunk - 1) / chunk, 1);
   uint32_t *kin = b.keys, *vin = b.tris, *kout = b.keys_alt, *vout = b.tris_alt;
+  const bool scanned = sort_scanned(b.capacity, b.sort_direct_max);
   for (int shift = 0; shift < key_bits; shift += kRadixBits) {
-    if (shift > 0) {
-      k_radix_hist<<<nchunks, kRadixThreads, 0, s>>>(kin, b.total, b.capacity, shift, chunk, scanned, b.hist);
-      ++*launches;
-    }
+    k_radix_hist<<<nchunks, kRadixThreads, 0, s>>>(kin, b.total, b.capacity, shift, chunk, scanned, b.hist);
+    ++*launches;
     if (scanned && (e = scan_exclusive(b.hist, b.hist, (size_t)nchunks * kRadixBins, b.hist + (size_t)nchunks * kRadixBins,
                                        nullptr, s, launches)) != cudaSuccess)
       return e;
