@@ -101,8 +101,10 @@ def test_linked_list_overflow(engine):
 
 @pytest.mark.parametrize('prec', [0, 1])
 def test_weighted_accumulators(engine, prec):
-    """WBOIT accumulation vs FP64: FP32 within 1e-5 relative, FP16 (RGBA16F
-    emulation, rounding after every blend) within 2e-2 relative."""
+    """WBOIT accumulation vs FP64, bounds at about twice the values measured on
+    a GB300 (deterministic inputs): FP16 (RGBA16F emulation, rounding after
+    every blend) accumulation 1.52e-3 relative, revealage 3.1e-3; FP32
+    accumulation 4.5e-7, revealage 2.4e-7."""
     W, H = 128, 96
     v, i, tpo, sd = pu.scene(64, W, H, seed=4)
     g = pu.render_gpu(engine.OIT_WEIGHTED, W, H, v, i, tpo, sd, weighted_precision=prec)
@@ -110,10 +112,10 @@ def test_weighted_accumulators(engine, prec):
     acc_g, acc_o = g['accum'], o['accum']
     mask = np.abs(acc_o) > 1e-3
     rel = np.abs(acc_g - acc_o)[mask] / np.abs(acc_o)[mask]
-    tol = 1e-5 if prec == 1 else 2e-2
+    tol, rtol = (1e-6, 5e-7) if prec == 1 else (3e-3, 6.5e-3)
     assert rel.max() < tol, rel.max()
     rrel = np.abs(g['reveal'] - o['reveal']) / np.maximum(o['reveal'], 1e-3)
-    assert rrel.max() < tol * 10
+    assert rrel.max() < rtol, rrel.max()
     if prec == 1:
         pu.compare_images(g, o)
 
