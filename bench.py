@@ -112,7 +112,7 @@ def dtype_of(alg):
 # ---------------------------------------------------------------------------
 def _oracle_frame(args):
     """(fragments, seconds[, RGBA8 image]) of one oracle frame of a workload;
-    args = (workload, want_image[, oracle build: 'fp64' the checker, or
+    args = (workload, want_image[, oracle build: 'fp64' the FP64 oracle, or
     'fp32_omp' FP32 blending with OpenMP tile-parallel draws])."""
     wd, want_image = args[0], args[1]
     variant = args[2] if len(args) > 2 else 'fp64'

@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the GB300 order-independent-transparency engine.
- * TEST INFRASTRUCTURE ONLY (see oit_oracle.h): the checker for the CUDA
- * engine, never linked into or called by the product path.
+ * TEST INFRASTRUCTURE ONLY (see oit_oracle.h): the parity oracle for the
+ * CUDA engine, never linked into or called by the product path.
  *
  * Build with -ffp-contract=off: the float32 raster/shading sequence below is
  * the specification the CUDA rasteriser reproduces bit for bit, so no
@@ -9,7 +9,7 @@
  *
  * Reference files cited as path:line within nvpro-samples/vk_order_independent_transparency.
  *
- * Two builds of this file (oracle/Makefile): the checker (blending in FP64,
+ * Two builds of this file (oracle/Makefile): the oracle (blending in FP64,
  * single-threaded) and, as a CPU baseline only, OR_FP32 + OpenMP: blending in
  * FP32 and the draws split over screen tiles (every triangle is set up, binned
  * into 32x32 tiles in primitive order, and each thread rasterises whole tiles,

@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the GB300 order-independent-transparency engine.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker the parity tests,
+ * TEST INFRASTRUCTURE ONLY. This library is the oracle the parity tests,
  * the smoke check and the bench's CPU-baseline leg compare the CUDA engine
  * against; no product code path loads or calls it.
  *

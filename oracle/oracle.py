@@ -1,10 +1,10 @@
 """ctypes wrapper of the CPU oracle (liboit_oracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
-by bench.py's CPU-baseline leg as the checker; the engine never uses it.
+by bench.py's CPU-baseline leg as the parity oracle; the engine never uses it.
 variant='fp32_omp' loads the same source built with FP32 blending and
-OpenMP tile-parallel draws (liboit_oracle_fp32_omp.so): a CPU baseline, not
-the checker.
+OpenMP tile-parallel draws (liboit_oracle_fp32_omp.so): a CPU baseline, never
+used for parity.
 """
 import ctypes
 import os
