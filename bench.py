@@ -209,7 +209,7 @@ def weighted_precision(wd, width=None, height=None):
     import importlib.util
     import numpy as np
     import vk_order_independent_transparency_gb300 as oit
-    spec = importlib.util.spec_from_file_location('oit_checker_oracle', os.path.join(ROOT, 'oracle', 'oracle.py'))
+    spec = importlib.util.spec_from_file_location('oit_parity_oracle', os.path.join(ROOT, 'oracle', 'oracle.py'))
     orc = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(orc)
     v, i, tpo = oit.make_scene(wd['spheres'], seed=wd['seed'], radius_min=wd['radius_min'], radius_max=wd['radius_max'])

@@ -199,7 +199,7 @@ int oit_composite(oit_context* ctx, uint8_t* out_rgba8_device, void* stream);
  * colour target (main.cpp:548-558) in FP64, then the MSAA / supersample
  * resolve. Writes width*height premultiplied linear double4 colours to
  * out_linear_device and/or RGBA8 sRGB pixels to out_rgba8_device (either may
- * be NULL, not both). A checker of the FP32 resolve, not part of a frame: no
+ * be NULL, not both). Verification of the FP32 resolve, not part of a frame: no
  * counterpart in the reference, whose composite runs in FP32 shaders. */
 int oit_verify_composite_fp64(oit_context* ctx, double* out_linear_device, uint8_t* out_rgba8_device, void* stream);
 

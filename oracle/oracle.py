@@ -30,7 +30,7 @@ class OrParams(ctypes.Structure):
 
 def build():
     """Compiles the oracle with its Makefile (gcc, -ffp-contract=off): the
-    checker, then the FP32 + OpenMP baseline build, which is skipped (and its
+    FP64 oracle, then the FP32 + OpenMP baseline build, which is skipped (and its
     bench leg reported unavailable) where the compiler has no OpenMP."""
     subprocess.run(['make', '-s', '-C', HERE, 'liboit_oracle.so'], check=True)
     subprocess.run(['make', '-s', '-C', HERE, 'liboit_oracle_fp32_omp.so'], check=False)

@@ -1,5 +1,5 @@
 """The CPU baseline build of the oracle (FP32 blending, OpenMP tile-parallel
-draws): the same fragments and integer A-buffers as the FP64 checker, and
+draws): the same fragments and integer A-buffers as the FP64 oracle, and
 images within FP32 rounding of it. It is timed by bench.py beside the
 single-threaded FP64 oracle; it never checks the engine."""
 import numpy as np
@@ -22,7 +22,7 @@ def _frame(variant, alg, aa, pct, L, W=96, H=72):
 
 
 @pytest.mark.parametrize('alg,aa,pct,L', CASES)
-def test_fp32_omp_matches_checker(alg, aa, pct, L):
+def test_fp32_omp_matches_fp64_oracle(alg, aa, pct, L):
     import os
     orc.build()
     if not os.path.exists(orc.LIB_PATHS['fp32_omp']):
