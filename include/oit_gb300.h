@@ -390,6 +390,14 @@ int oit_batch_set_resolve_config(oit_batch* batch, uint32_t part, const oit_reso
  * the failure returns the error and leaves the context usable. */
 int oit_debug_fail_allocations(int32_t after);
 
+/* Testing aid for bounded waits: the context's next arrival-order frames
+ * (OIT_FLAG_ARRIVAL_ORDER) start with the tail-blend lock of colour-target
+ * element `element` already held, so a fragment that must tail-blend there
+ * gives up after its bounded spin, is not blended, and the frame raises
+ * OIT_DEVERR_TIMEOUT; the rest of the frame is unaffected. -1 releases it.
+ * OIT_ERR_INVALID_ARGUMENT for an element outside the colour target. */
+int oit_debug_hold_arrival_lock(oit_context* ctx, int32_t element);
+
 /* Synchronises the context's last stream and returns the device error bits
  * (OIT_DEVERR_*) accumulated since the last call, then clears them. */
 int oit_get_error(oit_context* ctx, uint32_t* device_error_bits);

@@ -94,6 +94,44 @@ def test_arrival_pool_overflow(engine):
     assert d.max() <= 1
 
 
+def test_arrival_lock_wait_times_out(engine):
+    """A tail-blend lock that nothing releases (held from the start of the
+    pass by the testing hook): the fragments that must blend at that pixel
+    give up after their bounded spin, the frame reports OIT_DEVERR_TIMEOUT
+    instead of hanging, the rest of the frame equals the oracle's composite of
+    the GPU's own lists and colour target, and the next frame, with the lock
+    released, renders without an error."""
+    W, H, L, npp = 96, 72, 4, 1
+    v, i, tpo, sd = pu.scene(24, W, H, seed=9, radius_min=0.1, radius_max=0.25)
+    P = W * H
+    r = engine.Renderer(engine.make_state(engine.OIT_LINKEDLIST, W, H,
+                                          **arrival_kw(oit_layers=L, nodes_per_pixel=npp)))
+    mesh = engine.DeviceMesh(v, i)
+    r.update_scene(sd)
+    r.render_frame(mesh, tpo, 100)
+    g = pu.collect(r, engine.OIT_LINKEDLIST)
+    assert g['error'] == 0
+    full = pu.render_oracle(engine.OIT_LINKEDLIST, W, H, v, i, tpo, sd, 100, oit_layers=L, nodes_per_pixel=64)
+    gl, ol = list_sets(g, full, P)
+    # the pixel that lost the most fragments to tail blending: its tail
+    # fragments meet the held lock on the next frame too
+    lost = [len(b) - len(a) for a, b in zip(gl, ol)]
+    px = int(np.argmax(lost))
+    assert lost[px] >= 3
+    r.debug_hold_arrival_lock(px)
+    r.render_frame(mesh, tpo, 100)
+    g = pu.collect(r, engine.OIT_LINKEDLIST)
+    assert g['error'] & engine.OIT_DEVERR_TIMEOUT
+    d = np.abs(g['image'].astype(np.int32) - replay_image(g, W, H, L, npp).astype(np.int32))
+    assert d.max() <= 1
+    r.debug_hold_arrival_lock(-1)
+    r.render_frame(mesh, tpo, 100)
+    g = pu.collect(r, engine.OIT_LINKEDLIST)
+    assert g['error'] == 0
+    with pytest.raises(engine.OitError):
+        r.debug_hold_arrival_lock(P)
+
+
 def test_arrival_unsupported_states(engine):
     import ctypes
     for alg, aa, fmt in ((engine.OIT_LOOP64, 0, 0), (engine.OIT_SIMPLE, 0, 0), (engine.OIT_LINKEDLIST, 1, 0),

@@ -55,7 +55,7 @@ EXPORTS = [
     'oit_profile_enable', 'oit_profile_read', 'oit_render_frame_noalloc',
     'oit_batch_create', 'oit_batch_destroy', 'oit_batch_render', 'oit_batch_launch_count',
     'oit_render_frame_instanced', 'oit_render_frame_instanced_host', 'oit_scene_generate_instanced',
-    'oit_batch_resolve', 'oit_batch_resolve_config', 'oit_batch_set_resolve_config', 'oit_debug_fail_allocations',
+    'oit_batch_resolve', 'oit_batch_resolve_config', 'oit_batch_set_resolve_config', 'oit_debug_fail_allocations', 'oit_debug_hold_arrival_lock',
     'oit_verify_composite_fp64', 'oit_batch_set_raster_config', 'oit_batch_raster_config',
 ]
 PROF_SECTIONS = ['opaque_bin', 'opaque_raster', 'transparent_bin', 'transparent_raster', 'composite']
@@ -172,6 +172,7 @@ def library():
         'oit_batch_resolve_config': (I, [P, U, ctypes.POINTER(OitResolveShape)]),
         'oit_batch_set_resolve_config': (I, [P, U, ctypes.POINTER(OitResolveShape)]),
         'oit_debug_fail_allocations': (I, [ctypes.c_int32]),
+        'oit_debug_hold_arrival_lock': (I, [P, ctypes.c_int32]),
         'oit_verify_composite_fp64': (I, [P, P, P, P]),
         'oit_batch_set_raster_config': (I, [P, ctypes.POINTER(OitRasterConfig)]),
         'oit_batch_raster_config': (I, [P, ctypes.POINTER(OitRasterConfig)]),
@@ -446,6 +447,11 @@ class Renderer:
         bits = ctypes.c_uint32()
         _check(self.lib.oit_get_error(self._ctx, ctypes.byref(bits)), 'oit_get_error')
         return bits.value
+
+    def debug_hold_arrival_lock(self, element):
+        """Testing aid: the next arrival-order frames start with this colour
+        element's tail-blend lock held (-1 releases it)."""
+        _check(self.lib.oit_debug_hold_arrival_lock(self._ctx, int(element)), 'oit_debug_hold_arrival_lock')
 
     def fragment_count(self):
         v = ctypes.c_uint64()

@@ -186,7 +186,7 @@ __global__ void k_arrival_init(ArrivalParams p) {
     const float4 c = p.has_opaque ? p.opaque_color[i] : p.background;
     store_color(p.color, p.color_half != 0, i, c);
     p.heads[i] = 0u;
-    p.locks[i] = 0u;
+    p.locks[i] = (int32_t)i == p.held_lock ? 1u : 0u;  // a held lock is never released
   }
 }
 

@@ -624,6 +624,7 @@ struct oit_context {
     a.counter = counter.as<uint32_t>();
     a.capacity = capacity;
     a.locks = auxdepth.as<uint32_t>();
+    a.held_lock = debug_held_lock;
     a.tail = st.tail_blend ? 1 : 0;
     a.error = err.as<uint32_t>();
     a.frag_count = frag.as<unsigned long long>();
@@ -744,7 +745,8 @@ struct oit_context {
 
   // ---- CUDA graph of a whole frame (OIT_FLAG_CUDA_GRAPH) ----
   bool capturing = false;
-  bool in_batch = false;  // binning inside a batch graph, beside other views
+  bool in_batch = false;
+  int32_t debug_held_lock = -1;  // oit_debug_hold_arrival_lock  // binning inside a batch graph, beside other views
   cudaGraphExec_t graph_exec = nullptr;
   uint64_t graph_sig = 0;
   uint64_t graph_launches = 0;
@@ -1878,6 +1880,13 @@ int oit_batch_resolve_config(oit_batch* b, uint32_t part, oit_resolve_shape* out
 int oit_debug_fail_allocations(int32_t after) {
   if (after < -1) return OIT_ERR_INVALID_ARGUMENT;
   g_fail_alloc_countdown.store(after);
+  return OIT_OK;
+}
+
+int oit_debug_hold_arrival_lock(oit_context* ctx, int32_t element) {
+  if (!ctx || element < -1 || (element >= 0 && (uint64_t)element >= ctx->P)) return OIT_ERR_INVALID_ARGUMENT;
+  ctx->debug_held_lock = element;
+  ctx->drop_graph();  // a captured frame holds the launch parameters
   return OIT_OK;
 }
 

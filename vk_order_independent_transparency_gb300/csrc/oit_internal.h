@@ -182,6 +182,7 @@ struct ArrivalParams {
   uint32_t* counter;
   uint32_t capacity;
   uint32_t* locks;               // [P] spin words (zeroed by the pass)
+  int32_t held_lock;             // testing aid: this element's lock starts held (-1: none)
   int tail;
   uint32_t* error;
   unsigned long long* frag_count;
