@@ -101,8 +101,8 @@ def test_arrival_lock_wait_times_out(engine):
     instead of hanging, the rest of the frame equals the oracle's composite of
     the GPU's own lists and colour target, and the next frame, with the lock
     released, renders without an error."""
-    W, H, L, npp = 96, 72, 4, 1
-    v, i, tpo, sd = pu.scene(24, W, H, seed=9, radius_min=0.1, radius_max=0.25)
+    W, H, L, npp = 96, 72, 4, 1  # 2.8 fragments per pixel: about two thirds tail-blend
+    v, i, tpo, sd = pu.scene(64, W, H, seed=9, radius_min=0.15, radius_max=0.3)
     P = W * H
     r = engine.Renderer(engine.make_state(engine.OIT_LINKEDLIST, W, H,
                                           **arrival_kw(oit_layers=L, nodes_per_pixel=npp)))
@@ -113,10 +113,11 @@ def test_arrival_lock_wait_times_out(engine):
     assert g['error'] == 0
     full = pu.render_oracle(engine.OIT_LINKEDLIST, W, H, v, i, tpo, sd, 100, oit_layers=L, nodes_per_pixel=64)
     gl, ol = list_sets(g, full, P)
-    # the pixel that lost the most fragments to tail blending: its tail
-    # fragments meet the held lock on the next frame too
-    lost = [len(b) - len(a) for a, b in zip(gl, ol)]
-    px = int(np.argmax(lost))
+    # a pixel that lost 3 to 5 fragments to tail blending: its tail fragments
+    # meet the held lock on the next frame too, and only a few wait there
+    lost = np.array([len(b) - len(a) for a, b in zip(gl, ol)])
+    some = np.nonzero((lost >= 3) & (lost <= 5))[0]
+    px = int(some[0]) if some.size else int(np.argmax(lost))
     assert lost[px] >= 3
     r.debug_hold_arrival_lock(px)
     r.render_frame(mesh, tpo, 100)
