@@ -67,12 +67,10 @@ struct Bins {
   uint32_t* tris_alt;     // radix-sort ping-pong buffers
   uint32_t* keys_alt;
   uint32_t* pair_offset;  // [num_triangles + 1]
-  uint32_t* scan_tmp;     // scan scratch
-  uint32_t* hist;         // radix histograms
+  uint32_t* scan_tmp;     // pair counts per 512-triangle block, scanned in place, then the scan's scratch
+  uint32_t* hist;         // the radix sort's digit counts per chunk (and the scanned sort's scratch)
   uint32_t* total;        // [1] number of pairs (device)
   size_t capacity;
-  size_t scan_tmp_words;
-  size_t hist_words;
   // the radix sort keeps a view's pairs in at most 128 chunks up to this many
   // pairs (a view sorted beside others: they fill the GPU), and beyond it
   // spreads them over every block (a view sorted alone)
