@@ -7,12 +7,16 @@
 //   k_setup       one thread per triangle: transform, cull, snap to 1/256 px,
 //                 bbox, interpolation constants (the raster specification);
 //   k_setup_clip  the same for the triangles that cross the near plane,
-//                 clipped into one or two;
-//   scan + emit   one (tile, triangle) pair per 16x16 tile the bbox touches,
-//                 written in triangle order; the key holds the tile id (bits
-//                 0-23) and the 8x4 micro-tiles the bbox overlaps (bits 24-31);
-//   radix sort    stable LSD sort of the pairs by tile id, so every tile's list
-//                 keeps primitive order (the mask bits ride along unsorted);
+//                 clipped into one or two; the pair count of every
+//                 512-triangle block;
+//   scan + emit   the blocks' pair counts scanned, then one (tile, triangle)
+//                 pair per 16x16 tile the bbox touches, written in triangle
+//                 order; the key holds the tile id (bits 0-23) and the 8x4
+//                 micro-tiles the bbox overlaps (bits 24-31);
+//   radix sort    stable LSD sort of the pairs by tile id, 8 bits a pass, in
+//                 chunks (digit counts, then a scatter with warp-private
+//                 ranks), so every tile's list keeps primitive order (the
+//                 mask bits ride along unsorted);
 //   k_tile_bounds begin/end of each tile's list (where the sorted tile id
 //                 changes).
 #include <algorithm>
