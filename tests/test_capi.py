@@ -141,3 +141,8 @@ def test_null_arguments(lib):
     assert lib.oit_update_scene(None, ctypes.byref(sd)) == oit.OIT_ERR_INVALID_ARGUMENT
     d = oit.OitSceneDesc(1, 0, 16, 32, 1.0, 0.1, 0.2)
     assert lib.oit_scene_generate(ctypes.byref(d), None, None) == oit.OIT_ERR_INVALID_ARGUMENT
+    assert lib.oit_debug_hold_arrival_lock(None, 0) == oit.OIT_ERR_INVALID_ARGUMENT
+    assert lib.oit_verify_composite_fp64(None, None, None, None) == oit.OIT_ERR_INVALID_ARGUMENT
+    assert lib.oit_batch_set_raster_config(None, None) == oit.OIT_ERR_INVALID_ARGUMENT
+    rc = oit.OitRasterConfig()
+    assert lib.oit_batch_raster_config(None, ctypes.byref(rc)) == oit.OIT_ERR_INVALID_ARGUMENT
